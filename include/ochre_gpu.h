@@ -1,0 +1,163 @@
+/*
+ * ochre_gpu.h — C ABI of the GB300 (sm_103a) implementation of ochre's
+ * path-rasterization hot path (glowcoil/ochre 0.2.0).
+ *
+ * The reference API is Rust (src/rasterizer.rs):
+ *     Rasterizer::new() -> Rasterizer                       rasterizer.rs:50
+ *     Rasterizer::move_to(&mut self, Vec2)                  rasterizer.rs:61
+ *     Rasterizer::line_to(&mut self, Vec2)                  rasterizer.rs:72
+ *     Rasterizer::command(&mut self, PathCmd)               rasterizer.rs:145
+ *     Rasterizer::fill(&mut self, &[PathCmd], Transform)    rasterizer.rs:161
+ *     Rasterizer::finish<B: TileBuilder>(self, &mut B)      rasterizer.rs:180
+ *     trait TileBuilder { tile(x, y, [u8; 64]); span(x, y, width) }  rasterizer.rs:12-22
+ * Rust enums and traits cannot cross a C ABI, so:
+ *   - PathCmd (path.rs:5-12) becomes a verb byte plus a float stream
+ *     (see ochre_verb and the table below);
+ *   - Transform (geom.rs:204-207) becomes 6 floats m0 m1 m2 m3 ox oy, the
+ *     row-major Mat2x2 followed by the offset;
+ *   - TileBuilder becomes two callbacks plus a user pointer;
+ *   - errors, which the Rust API cannot report (it is infallible), are
+ *     returned as an int status (ochre_status).
+ *
+ * Every function returns OCHRE_OK (0) or an ochre_status code.  A context is
+ * bound to one CUDA device and one stream; use one context per host thread.
+ * Output buffers returned in ochre_result are owned by the context and stay
+ * valid until the next rasterize/finish call on it or ochre_gpu_destroy.
+ */
+#ifndef OCHRE_GPU_H
+#define OCHRE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OCHRE_TILE_SIZE 8      /* TILE_SIZE, rasterizer.rs:4 (not configurable) */
+#define OCHRE_TOLERANCE 0.1f   /* TOLERANCE, rasterizer.rs:6 (device pixels) */
+
+typedef enum ochre_status {
+    OCHRE_OK = 0,
+    OCHRE_E_INVALID = 1,   /* malformed input (bad verb, short point stream, bad offsets, non-finite point) */
+    OCHRE_E_CAPACITY = 2,  /* a size limit of this implementation was exceeded (counts >= 2^30) */
+    OCHRE_E_CUDA = 3,      /* a CUDA runtime call failed */
+    OCHRE_E_TIMEOUT = 4,   /* a bounded device-side wait gave up (results are not valid) */
+    OCHRE_E_NOMEM = 5,     /* device or host allocation failed */
+    OCHRE_E_LIMIT = 6      /* a per-segment/per-line iteration cap was hit: the reference would not terminate */
+} ochre_status;
+
+/* PathCmd discriminants (path.rs:5-12).  Floats consumed per verb:
+ *   MOVE x y | LINE x y | QUADRATIC cx cy x y | CUBIC c1x c1y c2x c2y x y |
+ *   CONIC cx cy x y w | CLOSE (none) */
+typedef enum ochre_verb {
+    OCHRE_MOVE = 0,
+    OCHRE_LINE = 1,
+    OCHRE_QUADRATIC = 2,
+    OCHRE_CUBIC = 3,
+    OCHRE_CONIC = 4,
+    OCHRE_CLOSE = 5
+} ochre_verb;
+
+/* fill_flags bit: the fill's commands are already in device space and are
+ * not transformed (Rasterizer::command/move_to/line_to, rasterizer.rs:61-157). */
+#define OCHRE_FILL_RAW 1u
+
+/* A batch of independent rasterizers.  Raster r owns fills
+ * [raster_fill_off[r], raster_fill_off[r+1]) (one fill per raster when
+ * raster_fill_off is NULL); fill f owns commands
+ * [fill_cmd_off[f], fill_cmd_off[f+1]) and transform fill_xf[6f .. 6f+5].
+ * Equivalent to, per raster: Rasterizer::new(); fill(cmds_f, xf_f) for each
+ * of its fills in order; finish(builder).  Pointers are host pointers for
+ * ochre_gpu_rasterize and device pointers for ochre_gpu_rasterize_device. */
+typedef struct ochre_batch {
+    const uint8_t *verbs;
+    uint64_t n_cmds;
+    const float *pts;
+    uint64_t n_floats;
+    const uint32_t *fill_cmd_off;    /* n_fills + 1 */
+    const float *fill_xf;            /* 6 * n_fills */
+    const uint8_t *fill_flags;       /* n_fills, or NULL (all transformed) */
+    uint32_t n_fills;
+    const uint32_t *raster_fill_off; /* n_rasters + 1, or NULL */
+    uint32_t n_rasters;
+} ochre_batch;
+
+/* Output, in TileBuilder callback order per raster (rasterizer.rs:241, 263):
+ * tiles ascending by (y, x); a span follows the tile with index span_tile. */
+typedef struct ochre_result {
+    uint32_t n_tiles;
+    uint32_t n_spans;
+    const int16_t *tile_xy;          /* 2 per tile: x, y in pixels (multiples of 8) */
+    const uint8_t *tile_alpha;       /* 64 per tile, row-major 8x8 alpha mask */
+    const float *tile_cov;           /* 64 per tile: |accum + area| before quantisation, or NULL */
+    const int16_t *span_xy;          /* 2 per span */
+    const uint16_t *span_width;      /* 1 per span, pixels; height is always 8 */
+    const uint32_t *span_tile;       /* 1 per span: index of the tile it follows */
+    const uint32_t *raster_tile_off; /* n_rasters + 1 */
+    const uint32_t *raster_span_off; /* n_rasters + 1 */
+} ochre_result;
+
+/* Intermediate counts of the last run (for tests and profiling). */
+typedef struct ochre_stats {
+    uint64_t n_lines;      /* flattened line segments, including implicit closes */
+    uint64_t n_entries;    /* sort entries: tile bins + tile-row crossings */
+    uint64_t n_tiles;
+    uint64_t n_spans;
+    uint32_t key_bits;     /* significant bits of the tile sort key */
+    uint32_t sort_passes;
+} ochre_stats;
+
+typedef struct ochre_gpu_ctx ochre_gpu_ctx;
+
+#define OCHRE_CTX_WANT_COV 1u   /* also produce tile_cov */
+
+/* Create a context on `device` (CUDA ordinal).  flags: OCHRE_CTX_*. */
+int ochre_gpu_create(ochre_gpu_ctx **out, int device, uint32_t flags);
+void ochre_gpu_destroy(ochre_gpu_ctx *ctx);
+int ochre_gpu_set_flags(ochre_gpu_ctx *ctx, uint32_t flags);
+
+/* Batched fill+finish of many independent rasterizers (device pointers in
+ * `in`, results left in device memory owned by ctx).  `stream` is a
+ * cudaStream_t, or NULL for the context's own stream.  Replaces, per raster,
+ * Rasterizer::new/fill/finish (rasterizer.rs:50, 161-165, 180-268). */
+int ochre_gpu_rasterize_device(ochre_gpu_ctx *ctx, const ochre_batch *in, ochre_result *out, void *stream);
+
+/* Same with host buffers: copies the batch to the device, rasterizes and
+ * copies the result back into pinned host buffers owned by ctx. */
+int ochre_gpu_rasterize(ochre_gpu_ctx *ctx, const ochre_batch *in, ochre_result *out);
+
+int ochre_gpu_last_stats(const ochre_gpu_ctx *ctx, ochre_stats *out);
+
+/* Status text for a code. */
+const char *ochre_gpu_status_string(int status);
+
+/* ---- Single-rasterizer mirror of the Rust API -------------------------- */
+
+typedef struct ochre_rasterizer ochre_rasterizer;
+
+/* TileBuilder::tile / TileBuilder::span (rasterizer.rs:14, 21). */
+typedef void (*ochre_tile_fn)(void *user, int16_t x, int16_t y, const uint8_t data[64]);
+typedef void (*ochre_span_fn)(void *user, int16_t x, int16_t y, uint16_t width);
+
+/* Rasterizer::new (rasterizer.rs:50).  The rasterizer renders through ctx. */
+int ochre_rasterizer_new(ochre_gpu_ctx *ctx, ochre_rasterizer **out);
+/* Rasterizer::move_to / line_to (rasterizer.rs:61, 72): device-space points. */
+int ochre_rasterizer_move_to(ochre_rasterizer *r, float x, float y);
+int ochre_rasterizer_line_to(ochre_rasterizer *r, float x, float y);
+/* Rasterizer::command (rasterizer.rs:145): one PathCmd, device space. */
+int ochre_rasterizer_command(ochre_rasterizer *r, uint8_t verb, const float *floats);
+/* Rasterizer::fill (rasterizer.rs:161): a path under a transform (6 floats). */
+int ochre_rasterizer_fill(ochre_rasterizer *r, const uint8_t *verbs, size_t n_verbs,
+                          const float *pts, size_t n_floats, const float xf[6]);
+/* Rasterizer::finish (rasterizer.rs:180): rasterizes on the GPU, then calls
+ * tile/span in the reference's order.  Consumes (frees) the rasterizer, even
+ * on error. */
+int ochre_rasterizer_finish(ochre_rasterizer *r, ochre_tile_fn tile, ochre_span_fn span, void *user);
+/* Drop a rasterizer without finishing it. */
+void ochre_rasterizer_free(ochre_rasterizer *r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCHRE_GPU_H */

@@ -1,0 +1,412 @@
+// C ABI (include/ochre_gpu.h): contexts, orchestration of the kernel chain,
+// the host-buffer entry point and the single-rasterizer mirror of ochre's
+// Rust API (src/rasterizer.rs).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace ochre {
+
+cudaError_t DevBuf::ensure(size_t bytes) {
+    if (bytes <= cap && p != nullptr) return cudaSuccess;
+    if (bytes == 0) bytes = 16;
+    size_t want = cap ? cap : 256;
+    while (want < bytes) want *= 2;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, want);
+    if (e != cudaSuccess) {
+        // retry at the exact size before giving up
+        cudaGetLastError();
+        e = cudaMalloc(&q, bytes);
+        if (e != cudaSuccess) return e;
+        want = bytes;
+    }
+    if (p) cudaFree(p);
+    p = q;
+    cap = want;
+    return cudaSuccess;
+}
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+}
+cudaError_t HostBuf::ensure(size_t bytes) {
+    if (bytes <= cap && p != nullptr) return cudaSuccess;
+    if (bytes == 0) bytes = 16;
+    size_t want = cap ? cap : 256;
+    while (want < bytes) want *= 2;
+    void* q = nullptr;
+    cudaError_t e = cudaMallocHost(&q, want);
+    if (e != cudaSuccess) return e;
+    if (p) cudaFreeHost(p);
+    p = q;
+    cap = want;
+    return cudaSuccess;
+}
+void HostBuf::release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+}
+
+int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
+    OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_scalars.p, ctx->scalars.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
+    return OCHRE_OK;
+}
+
+int check_device_error(ochre_gpu_ctx* ctx) {
+    const uint32_t e = host_scalars(ctx)->err;
+    if (e & ERR_INVALID) return OCHRE_E_INVALID;
+    if (e & ERR_LIMIT) return OCHRE_E_LIMIT;
+    if (e & ERR_TIMEOUT) return OCHRE_E_TIMEOUT;
+    if (e & ERR_CAPACITY) return OCHRE_E_CAPACITY;
+    return OCHRE_OK;
+}
+
+// Host-side validation of the structural arrays of a host batch.
+static int validate_host(const ochre_batch* in) {
+    if (in->n_fills > 0 && (in->fill_cmd_off == nullptr || in->fill_xf == nullptr)) return OCHRE_E_INVALID;
+    if (in->n_cmds > 0 && (in->verbs == nullptr)) return OCHRE_E_INVALID;
+    if (in->n_floats > 0 && in->pts == nullptr) return OCHRE_E_INVALID;
+    if (in->n_cmds > MAX_COUNT || in->n_floats > 0xffffffffull) return OCHRE_E_CAPACITY;
+    if (in->n_rasters > MAX_RASTERS) return OCHRE_E_CAPACITY;
+    if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
+    if (in->n_fills == 0 && in->n_cmds != 0) return OCHRE_E_INVALID;
+    if (in->fill_cmd_off) {
+        if (in->fill_cmd_off[0] != 0 || in->fill_cmd_off[in->n_fills] != in->n_cmds) return OCHRE_E_INVALID;
+        for (uint32_t f = 0; f < in->n_fills; f++)
+            if (in->fill_cmd_off[f + 1] < in->fill_cmd_off[f]) return OCHRE_E_INVALID;
+    }
+    if (in->raster_fill_off) {
+        if (in->raster_fill_off[0] != 0 || in->raster_fill_off[in->n_rasters] != in->n_fills) return OCHRE_E_INVALID;
+        for (uint32_t r = 0; r < in->n_rasters; r++)
+            if (in->raster_fill_off[r + 1] < in->raster_fill_off[r]) return OCHRE_E_INVALID;
+    }
+    return OCHRE_OK;
+}
+
+static int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s) {
+    std::memset(out, 0, sizeof *out);
+    ctx->stats = ochre_stats{};
+    OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+    const uint32_t R = in->n_rasters;
+    OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
+    OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
+    if (R == 0) {
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->out_raster_tile_off.p, 0, 4, s));
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->out_raster_span_off.p, 0, 4, s));
+        out->raster_tile_off = ctx->out_raster_tile_off.as<uint32_t>();
+        out->raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
+        return OCHRE_OK;
+    }
+    uint32_t L = 0;
+    int st = stage_flatten(ctx, in, s, &L);
+    if (st != OCHRE_OK) return st;
+    uint64_t E = 0;
+    uint32_t bits = 0;
+    st = stage_bin(ctx, in, L, s, &E, &bits);
+    if (st != OCHRE_OK) return st;
+    uint32_t passes = 0;
+    st = stage_sort(ctx, E, bits, s, &passes);
+    if (st != OCHRE_OK) return st;
+    uint32_t T = 0, N = 0;
+    st = stage_tiles(ctx, in, E, s, &T, &N);
+    if (st != OCHRE_OK) return st;
+    ctx->stats.n_lines = L;
+    ctx->stats.n_entries = E;
+    ctx->stats.n_tiles = T;
+    ctx->stats.n_spans = N;
+    ctx->stats.key_bits = bits;
+    ctx->stats.sort_passes = passes;
+    out->n_tiles = T;
+    out->n_spans = N;
+    out->tile_xy = ctx->out_tile_xy.as<int16_t>();
+    out->tile_alpha = ctx->out_tile_alpha.as<uint8_t>();
+    out->tile_cov = (ctx->flags & OCHRE_CTX_WANT_COV) ? ctx->out_tile_cov.as<float>() : nullptr;
+    out->span_xy = ctx->out_span_xy.as<int16_t>();
+    out->span_width = ctx->out_span_w.as<uint16_t>();
+    out->span_tile = ctx->out_span_tile.as<uint32_t>();
+    out->raster_tile_off = ctx->out_raster_tile_off.as<uint32_t>();
+    out->raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
+    return OCHRE_OK;
+}
+
+}  // namespace ochre
+
+using namespace ochre;
+
+extern "C" {
+
+const char* ochre_gpu_status_string(int status) {
+    switch (status) {
+    case OCHRE_OK: return "ok";
+    case OCHRE_E_INVALID: return "invalid input";
+    case OCHRE_E_CAPACITY: return "size limit exceeded";
+    case OCHRE_E_CUDA: return "CUDA error";
+    case OCHRE_E_TIMEOUT: return "bounded device wait timed out";
+    case OCHRE_E_NOMEM: return "out of memory";
+    case OCHRE_E_LIMIT: return "iteration cap hit (input would not terminate in the reference)";
+    default: return "unknown status";
+    }
+}
+
+int ochre_gpu_create(ochre_gpu_ctx** out, int device, uint32_t flags) {
+    if (!out) return OCHRE_E_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return OCHRE_E_CUDA;
+    ochre_gpu_ctx* ctx = new (std::nothrow) ochre_gpu_ctx();
+    if (!ctx) return OCHRE_E_NOMEM;
+    ctx->device = device;
+    ctx->flags = flags;
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        ctx->scalars.ensure(sizeof(DevScalars)) != cudaSuccess ||
+        ctx->h_scalars.ensure(sizeof(DevScalars)) != cudaSuccess) {
+        ochre_gpu_destroy(ctx);
+        return OCHRE_E_CUDA;
+    }
+    *out = ctx;
+    return OCHRE_OK;
+}
+
+void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    DevBuf* dev[] = {&ctx->in_verbs, &ctx->in_pts, &ctx->in_fill_off, &ctx->in_fill_xf, &ctx->in_fill_flags,
+                     &ctx->in_raster_off, &ctx->cmd_foff, &ctx->cmd_mv, &ctx->cmd_ep, &ctx->cmd_line_off,
+                     &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->raster_bbox, &ctx->raster_keybase,
+                     &ctx->raster_empty, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
+                     &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_state,
+                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->out_tile_xy,
+                     &ctx->out_tile_alpha, &ctx->out_tile_cov, &ctx->out_span_xy, &ctx->out_span_w,
+                     &ctx->out_span_tile, &ctx->out_raster_tile_off, &ctx->out_raster_span_off};
+    for (DevBuf* b : dev) b->release();
+    HostBuf* host[] = {&ctx->h_scalars, &ctx->h_tile_xy, &ctx->h_tile_alpha, &ctx->h_tile_cov, &ctx->h_span_xy,
+                       &ctx->h_span_w, &ctx->h_span_tile, &ctx->h_raster_tile_off, &ctx->h_raster_span_off};
+    for (HostBuf* b : host) b->release();
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+int ochre_gpu_set_flags(ochre_gpu_ctx* ctx, uint32_t flags) {
+    if (!ctx) return OCHRE_E_INVALID;
+    ctx->flags = flags;
+    return OCHRE_OK;
+}
+
+int ochre_gpu_rasterize_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, void* stream) {
+    if (!ctx || !in || !out) return OCHRE_E_INVALID;
+    if (in->n_rasters > MAX_RASTERS || in->n_cmds > MAX_COUNT) return OCHRE_E_CAPACITY;
+    if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    return run_device(ctx, in, out, s);
+}
+
+int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out) {
+    if (!ctx || !in || !out) return OCHRE_E_INVALID;
+    int st = validate_host(in);
+    if (st != OCHRE_OK) return st;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
+    cudaStream_t s = ctx->own_stream;
+    // host -> device (one copy per array)
+    ochre_batch d = *in;
+    OCHRE_CUDA_TRY(ctx->in_verbs.ensure(in->n_cmds));
+    OCHRE_CUDA_TRY(ctx->in_pts.ensure(in->n_floats * 4));
+    OCHRE_CUDA_TRY(ctx->in_fill_off.ensure(((size_t)in->n_fills + 1) * 4));
+    OCHRE_CUDA_TRY(ctx->in_fill_xf.ensure((size_t)in->n_fills * 24));
+    if (in->n_cmds) OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_verbs.p, in->verbs, in->n_cmds, cudaMemcpyHostToDevice, s));
+    if (in->n_floats) OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_pts.p, in->pts, in->n_floats * 4, cudaMemcpyHostToDevice, s));
+    if (in->fill_cmd_off)
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_fill_off.p, in->fill_cmd_off, ((size_t)in->n_fills + 1) * 4,
+                                       cudaMemcpyHostToDevice, s));
+    else
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->in_fill_off.p, 0, 4, s));
+    if (in->n_fills)
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_fill_xf.p, in->fill_xf, (size_t)in->n_fills * 24, cudaMemcpyHostToDevice, s));
+    d.verbs = ctx->in_verbs.as<uint8_t>();
+    d.pts = ctx->in_pts.as<float>();
+    d.fill_cmd_off = ctx->in_fill_off.as<uint32_t>();
+    d.fill_xf = ctx->in_fill_xf.as<float>();
+    if (in->fill_flags) {
+        OCHRE_CUDA_TRY(ctx->in_fill_flags.ensure(in->n_fills));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_fill_flags.p, in->fill_flags, in->n_fills, cudaMemcpyHostToDevice, s));
+        d.fill_flags = ctx->in_fill_flags.as<uint8_t>();
+    }
+    if (in->raster_fill_off) {
+        OCHRE_CUDA_TRY(ctx->in_raster_off.ensure(((size_t)in->n_rasters + 1) * 4));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_raster_off.p, in->raster_fill_off, ((size_t)in->n_rasters + 1) * 4,
+                                       cudaMemcpyHostToDevice, s));
+        d.raster_fill_off = ctx->in_raster_off.as<uint32_t>();
+    }
+    ochre_result dr;
+    st = run_device(ctx, &d, &dr, s);
+    if (st != OCHRE_OK) return st;
+    // device -> pinned host
+    const size_t T = dr.n_tiles, N = dr.n_spans, R = in->n_rasters;
+    OCHRE_CUDA_TRY(ctx->h_tile_xy.ensure(T * 4));
+    OCHRE_CUDA_TRY(ctx->h_tile_alpha.ensure(T * 64));
+    OCHRE_CUDA_TRY(ctx->h_span_xy.ensure(N * 4));
+    OCHRE_CUDA_TRY(ctx->h_span_w.ensure(N * 2));
+    OCHRE_CUDA_TRY(ctx->h_span_tile.ensure(N * 4));
+    OCHRE_CUDA_TRY(ctx->h_raster_tile_off.ensure((R + 1) * 4));
+    OCHRE_CUDA_TRY(ctx->h_raster_span_off.ensure((R + 1) * 4));
+    if (T) {
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_tile_xy.p, dr.tile_xy, T * 4, cudaMemcpyDeviceToHost, s));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_tile_alpha.p, dr.tile_alpha, T * 64, cudaMemcpyDeviceToHost, s));
+    }
+    if (N) {
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_span_xy.p, dr.span_xy, N * 4, cudaMemcpyDeviceToHost, s));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_span_w.p, dr.span_width, N * 2, cudaMemcpyDeviceToHost, s));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_span_tile.p, dr.span_tile, N * 4, cudaMemcpyDeviceToHost, s));
+    }
+    OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_raster_tile_off.p, dr.raster_tile_off, (R + 1) * 4, cudaMemcpyDeviceToHost, s));
+    OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_raster_span_off.p, dr.raster_span_off, (R + 1) * 4, cudaMemcpyDeviceToHost, s));
+    if (dr.tile_cov && T) {
+        OCHRE_CUDA_TRY(ctx->h_tile_cov.ensure(T * 256));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_tile_cov.p, dr.tile_cov, T * 256, cudaMemcpyDeviceToHost, s));
+    }
+    OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
+    out->n_tiles = dr.n_tiles;
+    out->n_spans = dr.n_spans;
+    out->tile_xy = ctx->h_tile_xy.as<int16_t>();
+    out->tile_alpha = ctx->h_tile_alpha.as<uint8_t>();
+    out->tile_cov = (dr.tile_cov && T) ? ctx->h_tile_cov.as<float>() : nullptr;
+    out->span_xy = ctx->h_span_xy.as<int16_t>();
+    out->span_width = ctx->h_span_w.as<uint16_t>();
+    out->span_tile = ctx->h_span_tile.as<uint32_t>();
+    out->raster_tile_off = ctx->h_raster_tile_off.as<uint32_t>();
+    out->raster_span_off = ctx->h_raster_span_off.as<uint32_t>();
+    return OCHRE_OK;
+}
+
+int ochre_gpu_last_stats(const ochre_gpu_ctx* ctx, ochre_stats* out) {
+    if (!ctx || !out) return OCHRE_E_INVALID;
+    *out = ctx->stats;
+    return OCHRE_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Single-rasterizer mirror: buffers commands on the host like the Rust
+// Rasterizer buffers increments, then rasterizes on finish.
+// ---------------------------------------------------------------------------
+struct ochre_rasterizer {
+    ochre_gpu_ctx* ctx;
+    std::vector<uint8_t> verbs;
+    std::vector<float> pts;
+    std::vector<uint32_t> fill_off{0};
+    std::vector<float> xf;
+    std::vector<uint8_t> flags;
+    // A run of raw commands (move_to/line_to/command) is one untransformed fill.
+    bool open_raw = false;
+};
+
+static const float kIdentity[6] = {1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f};
+
+static void raw_cmd(ochre_rasterizer* r, uint8_t verb, const float* f, int nf) {
+    if (!r->open_raw) {
+        r->xf.insert(r->xf.end(), kIdentity, kIdentity + 6);
+        r->flags.push_back(OCHRE_FILL_RAW);
+        r->fill_off.push_back((uint32_t)r->verbs.size());
+        r->open_raw = true;
+    }
+    r->verbs.push_back(verb);
+    r->pts.insert(r->pts.end(), f, f + nf);
+    r->fill_off.back() = (uint32_t)r->verbs.size();
+}
+
+extern "C" {
+
+int ochre_rasterizer_new(ochre_gpu_ctx* ctx, ochre_rasterizer** out) {
+    if (!ctx || !out) return OCHRE_E_INVALID;
+    *out = new (std::nothrow) ochre_rasterizer();
+    if (!*out) return OCHRE_E_NOMEM;
+    (*out)->ctx = ctx;
+    return OCHRE_OK;
+}
+
+int ochre_rasterizer_move_to(ochre_rasterizer* r, float x, float y) {
+    if (!r) return OCHRE_E_INVALID;
+    const float f[2] = {x, y};
+    raw_cmd(r, OCHRE_MOVE, f, 2);
+    return OCHRE_OK;
+}
+
+int ochre_rasterizer_line_to(ochre_rasterizer* r, float x, float y) {
+    if (!r) return OCHRE_E_INVALID;
+    const float f[2] = {x, y};
+    raw_cmd(r, OCHRE_LINE, f, 2);
+    return OCHRE_OK;
+}
+
+int ochre_rasterizer_command(ochre_rasterizer* r, uint8_t verb, const float* floats) {
+    if (!r || verb > OCHRE_CLOSE) return OCHRE_E_INVALID;
+    const int nf = (int)floats_per_verb(verb);
+    if (nf && !floats) return OCHRE_E_INVALID;
+    raw_cmd(r, verb, floats, nf);
+    return OCHRE_OK;
+}
+
+int ochre_rasterizer_fill(ochre_rasterizer* r, const uint8_t* verbs, size_t n_verbs, const float* pts,
+                          size_t n_floats, const float xf[6]) {
+    if (!r || (n_verbs && !verbs) || (n_floats && !pts) || !xf) return OCHRE_E_INVALID;
+    size_t need = 0;
+    for (size_t i = 0; i < n_verbs; i++) {
+        if (verbs[i] > OCHRE_CLOSE) return OCHRE_E_INVALID;
+        need += floats_per_verb(verbs[i]);
+    }
+    if (need > n_floats) return OCHRE_E_INVALID;
+    r->open_raw = false;
+    r->verbs.insert(r->verbs.end(), verbs, verbs + n_verbs);
+    r->pts.insert(r->pts.end(), pts, pts + need);
+    r->xf.insert(r->xf.end(), xf, xf + 6);
+    r->flags.push_back(0);
+    r->fill_off.push_back((uint32_t)r->verbs.size());
+    return OCHRE_OK;
+}
+
+void ochre_rasterizer_free(ochre_rasterizer* r) { delete r; }
+
+int ochre_rasterizer_finish(ochre_rasterizer* r, ochre_tile_fn tile, ochre_span_fn span, void* user) {
+    if (!r) return OCHRE_E_INVALID;
+    ochre_batch b{};
+    b.verbs = r->verbs.data();
+    b.n_cmds = r->verbs.size();
+    b.pts = r->pts.data();
+    b.n_floats = r->pts.size();
+    b.fill_cmd_off = r->fill_off.data();
+    b.fill_xf = r->xf.data();
+    b.fill_flags = r->flags.data();
+    b.n_fills = (uint32_t)(r->fill_off.size() - 1);
+    const uint32_t raster_off[2] = {0, b.n_fills};
+    b.raster_fill_off = raster_off;
+    b.n_rasters = 1;
+    ochre_result res;
+    int st = ochre_gpu_rasterize(r->ctx, &b, &res);
+    if (st == OCHRE_OK) {
+        uint32_t s = 0;
+        for (uint32_t t = 0; t < res.n_tiles; t++) {
+            if (tile) tile(user, res.tile_xy[2 * t], res.tile_xy[2 * t + 1], res.tile_alpha + 64 * (size_t)t);
+            while (s < res.n_spans && res.span_tile[s] == t) {
+                if (span) span(user, res.span_xy[2 * s], res.span_xy[2 * s + 1], res.span_width[s]);
+                s++;
+            }
+        }
+    }
+    delete r;
+    return st;
+}
+
+}  // extern "C"

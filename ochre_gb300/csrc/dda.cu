@@ -1,0 +1,291 @@
+// Stage 2: line segments -> sort entries (pixel DDA binning).
+//
+// Reference: Rasterizer::line_to (rasterizer.rs:72-140) and the run-length
+// binning of finish (rasterizer.rs:185-208).
+//
+// Every line is walked by one thread with the reference's exact serial
+// recurrence.  Invariant used to make lines independent: at the start of
+// every line_to, tile_y_prev == div_euclid(floor(last.y) as i16, 8) — move_to
+// sets it that way (rasterizer.rs:68) and every walk ends by snapping to
+// floor(point) and updating tile_y_prev for that cell (rasterizer.rs:118-131).
+//
+// A walk produces two kinds of sort entries:
+//   * a *bin* per run of consecutive increment cells in one tile
+//     (value = entry index; the BinRec at that index holds the DDA state at
+//     the run's first cell so the tile kernel can replay it exactly);
+//   * a *crossing* per tile-row change (rasterizer.rs:123-131)
+//     (value = CROSS_TAG | raster << 8 | sign byte).
+// Keys order entries by (raster, tile_y, tile_x, kind) inside a compact key
+// space: key_base[raster] + ((ty - by0) * w + (tx - bx0)) * 2 + kind, with
+// the raster's tile bounding box (bx0, by0)..(bx1, by1) measured in the count
+// pass; kind 0 (crossing) sorts before kind 1 (bin) of the same tile.
+#include "common.cuh"
+#include "internal.h"
+#include "scan.cuh"
+
+namespace ochre {
+
+struct BBoxAcc {
+    int x0, y0, x1, y1;
+};
+
+__device__ __forceinline__ void bbox_add(BBoxAcc& b, int x, int y) {
+    const int tx = div8(x), ty = div8(y);
+    b.x0 = min(b.x0, tx);
+    b.y0 = min(b.y0, ty);
+    b.x1 = max(b.x1, tx);
+    b.y1 = max(b.y1, ty);
+}
+
+// Count bins and crossings of a line; extend its raster's tile bbox.
+__device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* capped) {
+    if (veq(a, p)) return 0u;
+    uint32_t nb = 0, nc = 0;
+    int ptx = 0x7fffffff, pty = 0x7fffffff;
+    const bool ok = walk_line(
+        a, p,
+        [&](const Walk&, const WalkState& s) {
+            const int tx = div8(s.x), ty = div8(s.y);
+            if (tx != ptx || ty != pty) { nb++; ptx = tx; pty = ty; }
+        },
+        [&](int, int, int) { nc++; },
+        [&](int x, int y) { bbox_add(bb, x, y); });
+    if (!ok) *capped = true;
+    return nb + nc;
+}
+
+// Entry counts folded into the entry-offset scan; the bbox is reduced per
+// raster across the warp (lines of a raster are contiguous) before the
+// atomics.
+struct LineCountIn {
+    const float4* lines;
+    const uint32_t* line_raster;
+    int4* bbox;
+    uint32_t* err;
+    uint64_t n;
+    __device__ __forceinline__ uint32_t operator()(uint64_t i) const {
+        const float4 l = lines[i];
+        BBoxAcc bb{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
+        bool capped = false;
+        const uint32_t c = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped);
+        if (capped) atomicOr(err, ERR_LIMIT);
+        if (bb.x0 <= bb.x1) {
+            int4* d = bbox + line_raster[i];
+            atomicMin(&d->x, bb.x0);
+            atomicMin(&d->y, bb.y0);
+            atomicMax(&d->z, bb.x1);
+            atomicMax(&d->w, bb.y1);
+        }
+        return c;
+    }
+};
+struct OffOut32 {
+    uint32_t* off;
+    __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
+};
+
+__global__ void k_bbox_init(int4* bbox, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) bbox[i] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
+}
+
+// Per-raster key space: w * h * 2 keys; rasters without increments get a
+// 1x1 box at tile (0,0) and one synthetic bin (finish pushes a bin at (0,0)
+// even when there are no increments, rasterizer.rs:194-208).
+struct RasterScan {
+    uint64_t ks;
+    uint32_t ne;
+    uint32_t pad;
+};
+struct OpRaster {
+    __device__ __forceinline__ RasterScan operator()(RasterScan a, RasterScan b) const {
+        return RasterScan{a.ks + b.ks, a.ne + b.ne, 0u};
+    }
+};
+struct RasterIn {
+    const int4* bbox;
+    __device__ __forceinline__ RasterScan operator()(uint64_t r) const {
+        const int4 b = bbox[r];
+        if (b.x > b.z) return RasterScan{2ull, 1u, 0u};
+        const uint64_t w = (uint64_t)(b.z - b.x + 1), h = (uint64_t)(b.w - b.y + 1);
+        return RasterScan{w * h * 2ull, 0u, 0u};
+    }
+};
+struct RasterOut {
+    int4* bbox;
+    uint64_t* key_base;
+    uint32_t* empty;   // 0: has increments; else 1 + rank among empty rasters
+    __device__ __forceinline__ void operator()(uint64_t r, RasterScan ex, RasterScan v) const {
+        key_base[r] = ex.ks;
+        if (v.ne) {
+            bbox[r] = make_int4(0, 0, 0, 0);
+            empty[r] = ex.ne + 1u;
+        } else {
+            empty[r] = 0u;
+        }
+    }
+};
+
+template <class K>
+__device__ __forceinline__ K make_key(uint64_t base, const int4& bb, int tx, int ty, uint32_t kind) {
+    const uint64_t w = (uint64_t)(bb.z - bb.x + 1);
+    return (K)(base + (((uint64_t)(ty - bb.y) * w + (uint64_t)(tx - bb.x)) << 1) + kind);
+}
+
+template <class K>
+__global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster,
+                            const uint32_t* __restrict__ ent_off, uint64_t n_lines,
+                            const int4* __restrict__ bbox, const uint64_t* __restrict__ key_base,
+                            K* __restrict__ keys, uint32_t* __restrict__ vals, BinRec* __restrict__ bins) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n_lines) return;
+    const float4 l = lines[i];
+    const V2 a = v2(l.x, l.y), p = v2(l.z, l.w);
+    if (veq(a, p)) return;
+    const uint32_t r = line_raster[i];
+    const int4 bb = bbox[r];
+    const uint64_t base = key_base[r];
+    uint32_t e = ent_off[i];
+    // open bin
+    int btx = 0x7fffffff, bty = 0x7fffffff;
+    uint32_t bcount = 0, bentry = 0;
+    BinRec rec;
+    auto flush = [&]() {
+        if (bcount) {
+            rec.n = bcount;
+            const uint4* s = reinterpret_cast<const uint4*>(&rec);
+            uint4* d = reinterpret_cast<uint4*>(bins + bentry);
+            d[0] = s[0];
+            d[1] = s[1];
+            keys[bentry] = make_key<K>(base, bb, btx, bty, 1u);
+            vals[bentry] = bentry;
+        }
+    };
+    walk_line(
+        a, p,
+        [&](const Walk&, const WalkState& s) {
+            const int tx = div8(s.x), ty = div8(s.y);
+            if (tx != btx || ty != bty) {
+                flush();
+                btx = tx;
+                bty = ty;
+                bcount = 0;
+                bentry = e++;
+                rec.line = (uint32_t)i;
+                rec.raster = r;
+                rec.x = (int16_t)s.x;
+                rec.y = (int16_t)s.y;
+                rec.row_t0 = s.row_t0;
+                rec.row_t1 = s.row_t1;
+                rec.col_t0 = s.col_t0;
+                rec.col_t1 = s.col_t1;
+            }
+            bcount++;
+        },
+        [&](int tx, int ty, int sign) {
+            const uint32_t c = e++;
+            keys[c] = make_key<K>(base, bb, tx, ty, 0u);
+            vals[c] = CROSS_TAG | (r << 8) | ((uint32_t)sign & 0xffu);
+        },
+        [&](int, int) {});
+    flush();
+}
+
+template <class K>
+__global__ void k_empty_emit(const uint32_t* __restrict__ empty, uint32_t n_rasters, uint32_t first_entry,
+                             const uint64_t* __restrict__ key_base, K* __restrict__ keys,
+                             uint32_t* __restrict__ vals, BinRec* __restrict__ bins) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rasters) return;
+    const uint32_t rank = empty[r];
+    if (!rank) return;
+    const uint32_t e = first_entry + rank - 1u;
+    BinRec rec;
+    rec.line = 0xffffffffu;
+    rec.raster = r;
+    rec.x = 0;
+    rec.y = 0;
+    rec.n = 0;
+    rec.row_t0 = rec.row_t1 = rec.col_t0 = rec.col_t1 = 0.0f;
+    bins[e] = rec;
+    keys[e] = (K)(key_base[r] + 1ull);
+    vals[e] = e;
+}
+
+int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaStream_t s, uint64_t* n_entries,
+              uint32_t* key_bits) {
+    DevScalars* ds = dev_scalars(ctx);
+    const uint32_t R = in->n_rasters;
+    *n_entries = 0;
+    *key_bits = 0;
+    if (R == 0) return OCHRE_OK;
+    if (R > MAX_RASTERS) return OCHRE_E_CAPACITY;
+    OCHRE_CUDA_TRY(ctx->raster_bbox.ensure((size_t)R * sizeof(int4)));
+    OCHRE_CUDA_TRY(ctx->raster_keybase.ensure((size_t)R * 8));
+    OCHRE_CUDA_TRY(ctx->raster_empty.ensure((size_t)R * 4));
+    k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(), R);
+    OCHRE_CUDA_TRY(cudaGetLastError());
+    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_line_ent, 0, sizeof(uint32_t), s));
+    if (n_lines) {
+        OCHRE_CUDA_TRY(ctx->line_ent_off.ensure((size_t)n_lines * 4));
+        OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<uint32_t>)));
+        OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+            n_lines, LineCountIn{ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->raster_bbox.as<int4>(),
+                                 &ds->err, n_lines},
+            OffOut32{ctx->line_ent_off.as<uint32_t>()}, OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket,
+            &ds->n_line_ent, &ds->err, s));
+    }
+    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(R) * sizeof(ScanStatus<RasterScan>)));
+    OCHRE_CUDA_TRY(launch_scan<RasterScan>(
+        R, RasterIn{ctx->raster_bbox.as<int4>()},
+        RasterOut{ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->raster_empty.as<uint32_t>()},
+        OpRaster{}, RasterScan{0, 0, 0}, ctx->scan_status.p, &ds->ticket,
+        reinterpret_cast<RasterScan*>(&ds->keyspace), &ds->err, s));
+    int st = read_scalars(ctx, s);
+    if (st != OCHRE_OK) return st;
+    st = check_device_error(ctx);
+    if (st != OCHRE_OK) return st;
+    const DevScalars* hs = host_scalars(ctx);
+    const uint64_t E = (uint64_t)hs->n_line_ent + hs->n_empty;
+    if (E > MAX_COUNT) return OCHRE_E_CAPACITY;
+    uint64_t K = hs->keyspace;
+    uint32_t bits = 1;
+    while (bits < 64 && (K - 1) >> bits) bits++;
+    *key_bits = bits;
+    *n_entries = E;
+    ctx->keys64 = bits > 32;
+    const size_t ksz = ctx->keys64 ? 8 : 4;
+    OCHRE_CUDA_TRY(ctx->keys.ensure(E * ksz));
+    OCHRE_CUDA_TRY(ctx->vals.ensure(E * 4));
+    OCHRE_CUDA_TRY(ctx->keys_alt.ensure(E * ksz));
+    OCHRE_CUDA_TRY(ctx->vals_alt.ensure(E * 4));
+    OCHRE_CUDA_TRY(ctx->bins.ensure(E * sizeof(BinRec)));
+    if (n_lines) {
+        const unsigned blocks = (unsigned)((n_lines + 127) / 128);
+        if (ctx->keys64)
+            k_line_emit<uint64_t><<<blocks, 128, 0, s>>>(
+                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
+                ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(),
+                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+        else
+            k_line_emit<uint32_t><<<blocks, 128, 0, s>>>(
+                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
+                ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(),
+                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+        OCHRE_CUDA_TRY(cudaGetLastError());
+    }
+    if (hs->n_empty) {
+        if (ctx->keys64)
+            k_empty_emit<uint64_t><<<(R + 255) / 256, 256, 0, s>>>(
+                ctx->raster_empty.as<uint32_t>(), R, hs->n_line_ent, ctx->raster_keybase.as<uint64_t>(),
+                ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+        else
+            k_empty_emit<uint32_t><<<(R + 255) / 256, 256, 0, s>>>(
+                ctx->raster_empty.as<uint32_t>(), R, hs->n_line_ent, ctx->raster_keybase.as<uint64_t>(),
+                ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+        OCHRE_CUDA_TRY(cudaGetLastError());
+    }
+    return OCHRE_OK;
+}
+
+}  // namespace ochre

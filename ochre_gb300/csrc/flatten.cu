@@ -1,0 +1,306 @@
+// Stage 1: commands -> line segments (flattening).
+//
+// Reference: Rasterizer::fill / command (rasterizer.rs:145-165),
+// PathCmd::transform (path.rs:16-37), PathCmd::flatten (path.rs:41-109),
+// and the implicit closing lines of move_to / finish (rasterizer.rs:62-64,
+// 181-183).
+//
+// A raster's line list is the sequence of its line_to calls.  Each command
+// contributes, in order:
+//   Move   : the closing line last -> first when last != first
+//   Line   : last -> point
+//   Quad   : n lines from the serial t recurrence (path.rs:52-57)
+//   Cubic  : n lines (path.rs:65-73)
+//   Conic  : 2 lines per subdivision leaf (path.rs:76-101)
+//   Close  : nothing (rasterizer.rs:154 ignores it)
+// plus, on the raster's last command, the final closing line of finish.
+// `last` for a command is the transformed end point of the most recent
+// earlier non-Close command of the raster (or (0,0)), `first` the point of
+// the most recent earlier Move (or (0,0)); both come from one scan.
+#include "common.cuh"
+#include "internal.h"
+#include "scan.cuh"
+
+namespace ochre {
+
+struct CmdScan {
+    uint32_t foff;   // exclusive sum of floats consumed
+    uint32_t mv;     // 1 + index of the most recent Move (0: none)
+    uint32_t ep;     // 1 + index of the most recent non-Close command (0: none)
+};
+struct OpCmd {
+    __device__ __forceinline__ CmdScan operator()(CmdScan a, CmdScan b) const {
+        return CmdScan{a.foff + b.foff, max(a.mv, b.mv), max(a.ep, b.ep)};
+    }
+};
+struct CmdIn {
+    const uint8_t* verbs;
+    uint32_t* err;
+    __device__ __forceinline__ CmdScan operator()(uint64_t i) const {
+        const uint8_t v = verbs[i];
+        if (v > V_CLOSE) atomicOr(err, ERR_INVALID);
+        const uint32_t id = (uint32_t)i + 1u;
+        return CmdScan{floats_per_verb(v), v == V_MOVE ? id : 0u, v <= V_CONIC ? id : 0u};
+    }
+};
+struct CmdOut {
+    uint32_t* foff;
+    uint32_t* mv;
+    uint32_t* ep;
+    __device__ __forceinline__ void operator()(uint64_t i, CmdScan ex, CmdScan) const {
+        foff[i] = ex.foff;
+        mv[i] = ex.mv;
+        ep[i] = ex.ep;
+    }
+};
+
+struct BatchView {
+    const uint8_t* verbs;
+    const float* pts;
+    const uint32_t* fill_off;
+    const float* fill_xf;
+    const uint8_t* fill_flags;
+    const uint32_t* raster_off;
+    uint32_t n_fills, n_rasters;
+    uint64_t n_cmds;
+    const uint32_t* cmd_foff;
+    const uint32_t* cmd_mv;
+    const uint32_t* cmd_ep;
+};
+
+// Everything a command's flattening depends on.
+struct CmdCtx {
+    uint8_t verb;
+    uint32_t raster;
+    bool last_of_raster;
+    V2 last, first;   // rasterizer state before the command
+    V2 pt[3];         // transformed points of the command
+    float w;          // conic weight
+    bool ok;
+};
+
+__device__ __forceinline__ uint32_t fill_of(const BatchView& b, uint32_t c) {
+    return upper_bound_u32(b.fill_off, b.n_fills + 1, c) - 1u;
+}
+
+// The transformed end point of command j (a non-Close command).
+__device__ __forceinline__ V2 endpoint_of(const BatchView& b, uint32_t j, uint32_t f_hint) {
+    const uint32_t f = j >= __ldg(b.fill_off + f_hint) ? f_hint : fill_of(b, j);
+    const uint8_t v = __ldg(b.verbs + j);
+    const float* fp = b.pts + __ldg(b.cmd_foff + j) + endpoint_float(v);
+    V2 p = v2(__ldg(fp), __ldg(fp + 1));
+    const bool raw = b.fill_flags != nullptr && (__ldg(b.fill_flags + f) & OCHRE_FILL_RAW);
+    if (!raw) p = xf_apply(b.fill_xf + 6 * (size_t)f, p);
+    return p;
+}
+
+__device__ CmdCtx load_cmd(const BatchView& b, uint32_t c) {
+    CmdCtx k;
+    k.ok = true;
+    k.verb = __ldg(b.verbs + c);
+    const uint32_t f = fill_of(b, c);
+    uint32_t r, rf0, rf1;
+    if (b.raster_off != nullptr) {
+        r = upper_bound_u32(b.raster_off, b.n_rasters + 1, f) - 1u;
+        rf0 = __ldg(b.raster_off + r);
+        rf1 = __ldg(b.raster_off + r + 1);
+    } else {
+        r = f;
+        rf0 = f;
+        rf1 = f + 1;
+    }
+    k.raster = r;
+    const uint32_t rc0 = __ldg(b.fill_off + rf0), rc1 = __ldg(b.fill_off + rf1);
+    k.last_of_raster = c + 1 == rc1;
+    const uint32_t ep = __ldg(b.cmd_ep + c), mv = __ldg(b.cmd_mv + c);
+    k.last = ep > rc0 ? endpoint_of(b, ep - 1u, f) : v2(0.0f, 0.0f);
+    if (mv > rc0) {
+        const uint32_t m = mv - 1u;
+        const uint32_t fm = m >= __ldg(b.fill_off + f) ? f : fill_of(b, m);
+        const float* fp = b.pts + __ldg(b.cmd_foff + m);
+        V2 p = v2(__ldg(fp), __ldg(fp + 1));
+        const bool raw = b.fill_flags != nullptr && (__ldg(b.fill_flags + fm) & OCHRE_FILL_RAW);
+        k.first = raw ? p : xf_apply(b.fill_xf + 6 * (size_t)fm, p);
+    } else {
+        k.first = v2(0.0f, 0.0f);
+    }
+    const bool raw = b.fill_flags != nullptr && (__ldg(b.fill_flags + f) & OCHRE_FILL_RAW);
+    const float* xf = b.fill_xf + 6 * (size_t)f;
+    const float* fp = b.pts + __ldg(b.cmd_foff + c);
+    const int np = k.verb == V_MOVE || k.verb == V_LINE ? 1 : k.verb == V_QUAD || k.verb == V_CONIC ? 2
+                 : k.verb == V_CUBIC ? 3 : 0;
+    for (int q = 0; q < 3; q++) {
+        if (q < np) {
+            V2 p = v2(__ldg(fp + 2 * q), __ldg(fp + 2 * q + 1));
+            if (!raw) p = xf_apply(xf, p);   // PathCmd::transform (path.rs:16-37)
+            if (!finite2(p)) k.ok = false;
+            k.pt[q] = p;
+        } else {
+            k.pt[q] = v2(0.0f, 0.0f);
+        }
+    }
+    k.w = k.verb == V_CONIC ? __ldg(fp + 4) : 0.0f;
+    if (k.verb == V_CONIC && !isfinite(k.w)) k.ok = false;
+    return k;
+}
+
+// Runs the flattening of one command, calling line(a, b) for each line_to
+// in order.  Returns false when a cap was hit.
+template <class Line>
+__device__ bool flatten_cmd(const CmdCtx& k, Line line) {
+    bool capped = false;
+    V2 prev = k.last;
+    auto to = [&](V2 p) { line(prev, p); prev = p; };
+    switch (k.verb) {
+    case V_MOVE:
+        if (!veq(k.last, k.first)) line(k.last, k.first);
+        break;
+    case V_LINE:
+        to(k.pt[0]);
+        break;
+    case V_QUAD: {
+        const float dt = quad_dt(k.last, k.pt[0], k.pt[1]);
+        float t = 0.0f;
+        uint32_t n = 0;
+        while (t < 1.0f) {
+            t = rmin(__fadd_rn(t, dt), 1.0f);
+            to(quad_point(t, k.last, k.pt[0], k.pt[1]));
+            if (++n >= FLATTEN_CAP) { capped = true; break; }
+        }
+        break;
+    }
+    case V_CUBIC: {
+        const float dt = cubic_dt(k.last, k.pt[0], k.pt[1], k.pt[2]);
+        float t = 0.0f;
+        uint32_t n = 0;
+        while (t < 1.0f) {
+            t = rmin(__fadd_rn(t, dt), 1.0f);
+            to(cubic_point(t, k.last, k.pt[0], k.pt[1], k.pt[2]));
+            if (++n >= FLATTEN_CAP) { capped = true; break; }
+        }
+        break;
+    }
+    case V_CONIC:
+        conic_flatten(k.last, k.pt[0], k.pt[1], k.w, &capped, to);
+        break;
+    default:
+        break;
+    }
+    if (k.last_of_raster) {
+        // finish(): line_to(first) when last != first (rasterizer.rs:181-183)
+        const V2 last_end = k.verb == V_CLOSE ? k.last : k.verb == V_CUBIC ? k.pt[2]
+                          : k.verb == V_MOVE || k.verb == V_LINE ? k.pt[0] : k.pt[1];
+        const V2 first_end = k.verb == V_MOVE ? k.pt[0] : k.first;
+        if (!veq(last_end, first_end)) line(last_end, first_end);
+    }
+    return !capped;
+}
+
+// Line count of one command (the count pass never materialises points for
+// curves: it only replays the t recurrence).
+__device__ uint32_t count_cmd(const CmdCtx& k, bool* capped) {
+    uint32_t n = 0;
+    switch (k.verb) {
+    case V_MOVE: n = veq(k.last, k.first) ? 0u : 1u; break;
+    case V_LINE: n = 1; break;
+    case V_QUAD: n = flatten_steps(quad_dt(k.last, k.pt[0], k.pt[1]), capped); break;
+    case V_CUBIC: n = flatten_steps(cubic_dt(k.last, k.pt[0], k.pt[1], k.pt[2]), capped); break;
+    case V_CONIC: conic_flatten(k.last, k.pt[0], k.pt[1], k.w, capped, [&](V2) { n++; }); break;
+    default: break;
+    }
+    if (k.last_of_raster) {
+        const V2 last_end = k.verb == V_CLOSE ? k.last : k.verb == V_CUBIC ? k.pt[2]
+                          : k.verb == V_MOVE || k.verb == V_LINE ? k.pt[0] : k.pt[1];
+        const V2 first_end = k.verb == V_MOVE ? k.pt[0] : k.first;
+        if (!veq(last_end, first_end)) n++;
+    }
+    return n;
+}
+
+// Line counts folded straight into the line-offset scan.
+struct CountIn {
+    BatchView b;
+    uint32_t* err;
+    __device__ __forceinline__ uint32_t operator()(uint64_t i) const {
+        const CmdCtx k = load_cmd(b, (uint32_t)i);
+        if (!k.ok) { atomicOr(err, ERR_INVALID); return 0u; }
+        bool capped = false;
+        const uint32_t n = count_cmd(k, &capped);
+        if (capped) atomicOr(err, ERR_LIMIT);
+        return n;
+    }
+};
+struct OffOut {
+    uint32_t* off;
+    __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
+};
+
+__global__ void k_cmd_emit(BatchView b, const uint32_t* __restrict__ line_off, uint32_t n_lines_cap,
+                           float4* __restrict__ lines, uint32_t* __restrict__ line_raster, uint32_t* err) {
+    const uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (c >= b.n_cmds) return;
+    const CmdCtx k = load_cmd(b, (uint32_t)c);
+    if (!k.ok) return;
+    uint32_t o = line_off[c];
+    flatten_cmd(k, [&](V2 a, V2 p) {
+        if (o < n_lines_cap) {
+            lines[o] = make_float4(a.x, a.y, p.x, p.y);
+            line_raster[o] = k.raster;
+        } else {
+            atomicOr(err, ERR_CAPACITY);
+        }
+        o++;
+    });
+}
+
+int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uint32_t* n_lines) {
+    const uint64_t n = in->n_cmds;
+    DevScalars* ds = dev_scalars(ctx);
+    *n_lines = 0;
+    if (n == 0) return OCHRE_OK;
+    OCHRE_CUDA_TRY(ctx->cmd_foff.ensure(n * 4));
+    OCHRE_CUDA_TRY(ctx->cmd_mv.ensure(n * 4));
+    OCHRE_CUDA_TRY(ctx->cmd_ep.ensure(n * 4));
+    OCHRE_CUDA_TRY(ctx->cmd_line_off.ensure(n * 4));
+    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n) * sizeof(ScanStatus<CmdScan>)));
+
+    CmdScan total_id{0, 0, 0};
+    OCHRE_CUDA_TRY(launch_scan<CmdScan>(n, CmdIn{in->verbs, &ds->err},
+                                        CmdOut{ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
+                                               ctx->cmd_ep.as<uint32_t>()},
+                                        OpCmd{}, total_id, ctx->scan_status.p, &ds->ticket,
+                                        reinterpret_cast<CmdScan*>(&ds->n_floats), &ds->err, s));
+
+    // The verbs must not consume more floats than the point stream holds:
+    // check before any kernel reads a point.
+    int st = read_scalars(ctx, s);
+    if (st != OCHRE_OK) return st;
+    const DevScalars* hs = host_scalars(ctx);
+    if (hs->n_floats > in->n_floats) return OCHRE_E_INVALID;
+    st = check_device_error(ctx);
+    if (st != OCHRE_OK) return st;
+
+    BatchView b{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
+                in->n_fills, in->n_rasters, n, ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
+                ctx->cmd_ep.as<uint32_t>()};
+    OCHRE_CUDA_TRY(launch_scan<uint32_t>(n, CountIn{b, &ds->err}, OffOut{ctx->cmd_line_off.as<uint32_t>()},
+                                         OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_lines,
+                                         &ds->err, s));
+    st = read_scalars(ctx, s);
+    if (st != OCHRE_OK) return st;
+    st = check_device_error(ctx);
+    if (st != OCHRE_OK) return st;
+    const uint32_t L = hs->n_lines;
+    *n_lines = L;
+    if (L == 0) return OCHRE_OK;
+    if (L > MAX_COUNT) return OCHRE_E_CAPACITY;
+    OCHRE_CUDA_TRY(ctx->lines.ensure((size_t)L * sizeof(float4)));
+    OCHRE_CUDA_TRY(ctx->line_raster.ensure((size_t)L * 4));
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    k_cmd_emit<<<blocks, 256, 0, s>>>(b, ctx->cmd_line_off.as<uint32_t>(), L, ctx->lines.as<float4>(),
+                                      ctx->line_raster.as<uint32_t>(), &ds->err);
+    OCHRE_CUDA_TRY(cudaGetLastError());
+    return OCHRE_OK;
+}
+
+}  // namespace ochre

@@ -1,0 +1,141 @@
+// Host-side internals shared by the translation units of libochre_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/ochre_gpu.h"
+
+namespace ochre {
+
+// Grow-only device buffer.
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    void release();
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Grow-only pinned host buffer.
+struct HostBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes);
+    void release();
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Device-resident scalars of one run (read back with one copy).
+struct DevScalars {
+    uint32_t err;          // ERR_* bits
+    uint32_t ticket;       // ticket counter for ticketed kernels
+    uint32_t n_floats;     // floats the verbs consume (command scan total .foff)
+    uint32_t cmd_mv_tot;   // unused totals of the command scan
+    uint32_t cmd_ep_tot;
+    uint32_t n_lines;      // total lines
+    uint32_t n_line_ent;   // entries produced by lines
+    uint32_t pad0;
+    uint64_t keyspace;     // total key space (raster scan .ks)
+    uint32_t n_empty;      // rasters without increments (raster scan .ne)
+    uint32_t pad1;
+    uint32_t n_tiles;
+    uint32_t n_spans;
+    uint32_t sort_ticket;
+    uint32_t pad2;
+};
+
+// Entry value tag for tile-row crossings: 1 | raster (23 bits) | sign byte.
+constexpr uint32_t CROSS_TAG = 0x80000000u;
+constexpr uint32_t MAX_RASTERS = 1u << 23;
+constexpr uint64_t MAX_COUNT = (1ull << 30) - 1;   // lines, entries, tiles
+
+// Per-bin replay record: DDA state at the first cell of a run of cells that
+// share one tile (32 bytes).
+struct BinRec {
+    uint32_t line;       // line index, 0xffffffff for the empty-raster tile
+    uint32_t raster;
+    int16_t x, y;        // first cell of the run
+    uint32_t n;          // cells in the run
+    float row_t0, row_t1, col_t0, col_t1;
+};
+static_assert(sizeof(BinRec) == 32, "BinRec must be 32 bytes");
+
+struct TileInfo {
+    int32_t raster;
+    int32_t tx, ty;
+    uint32_t head;       // first bin entry of the tile in the sorted entries
+    uint32_t nbins;
+    int32_t lwind;       // tile-row crossing signs between the previous tile and this one
+};
+
+// Look-back state of the per-tile prefix chains (row carry and winding).
+struct TileState {
+    uint32_t rflag, wflag;
+    float ragg[8];
+    float rinc[8];
+    int32_t wagg, winc;
+};
+
+}  // namespace ochre
+
+struct ochre_gpu_ctx {
+    int device = 0;
+    uint32_t flags = 0;
+    cudaStream_t own_stream = nullptr;
+
+    // device copies of a host batch (ochre_gpu_rasterize)
+    ochre::DevBuf in_verbs, in_pts, in_fill_off, in_fill_xf, in_fill_flags, in_raster_off;
+    // per command
+    ochre::DevBuf cmd_foff, cmd_mv, cmd_ep, cmd_line_off;
+    // per line
+    ochre::DevBuf lines, line_raster, line_ent_off;
+    // per raster
+    ochre::DevBuf raster_bbox, raster_keybase, raster_empty;
+    // sort entries
+    ochre::DevBuf keys, vals, keys_alt, vals_alt, bins;
+    ochre::DevBuf sort_hist, sort_lookback;
+    // tiles
+    ochre::DevBuf tile_head, tile_info, tile_state, span_flag, span_val;
+    // scan workspace
+    ochre::DevBuf scan_status;
+    ochre::DevBuf scalars;   // DevScalars
+    // device outputs
+    ochre::DevBuf out_tile_xy, out_tile_alpha, out_tile_cov, out_span_xy, out_span_w, out_span_tile,
+        out_raster_tile_off, out_raster_span_off;
+    // pinned host
+    ochre::HostBuf h_scalars;
+    ochre::HostBuf h_tile_xy, h_tile_alpha, h_tile_cov, h_span_xy, h_span_w, h_span_tile, h_raster_tile_off,
+        h_raster_span_off;
+
+    ochre_stats stats{};
+    int keys64 = 0;          // last run used 64-bit keys
+};
+
+namespace ochre {
+
+// Stage launchers (each returns an ochre_status).
+int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uint32_t* n_lines);
+int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaStream_t s, uint64_t* n_entries,
+              uint32_t* key_bits);
+int stage_sort(ochre_gpu_ctx* ctx, uint64_t n_entries, uint32_t key_bits, cudaStream_t s, uint32_t* passes);
+int stage_tiles(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t n_entries, cudaStream_t s, uint32_t* n_tiles,
+                uint32_t* n_spans);
+
+// Read the device scalars into ctx->h_scalars (synchronises the stream).
+int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);
+inline DevScalars* dev_scalars(ochre_gpu_ctx* ctx) { return ctx->scalars.as<DevScalars>(); }
+inline DevScalars* host_scalars(ochre_gpu_ctx* ctx) { return ctx->h_scalars.as<DevScalars>(); }
+int check_device_error(ochre_gpu_ctx* ctx);
+
+#define OCHRE_CUDA_TRY(expr)                                   \
+    do {                                                       \
+        cudaError_t e_ = (expr);                               \
+        if (e_ != cudaSuccess) {                               \
+            return e_ == cudaErrorMemoryAllocation ? OCHRE_E_NOMEM : OCHRE_E_CUDA; \
+        }                                                      \
+    } while (0)
+
+}  // namespace ochre

@@ -1,0 +1,135 @@
+// Single-pass device-wide exclusive scan with decoupled look-back.
+//
+// Generic over the value type T (a trivially copyable struct of 32-bit
+// words), the associative operator, the input functor in(i) -> T and the
+// output functor out(i, exclusive_prefix, own_value).  Tiles are numbered by
+// an atomic ticket taken when a block starts, so a block only ever waits on
+// blocks that are already resident; every wait is bounded (SPIN_LIMIT) and a
+// timeout sets ERR_TIMEOUT instead of hanging.
+#pragma once
+
+#include "common.cuh"
+
+namespace ochre {
+
+template <class T>
+struct ScanStatus {
+    uint32_t flag;   // 0: nothing yet, 1: aggregate published, 2: inclusive prefix published
+    uint32_t pad;
+    T agg;
+    T inc;
+};
+
+template <int BLOCK, int ITEMS, class T, class Op, class In, class Out>
+__global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, In in, Out out, Op op, T identity,
+                                                 ScanStatus<T>* status, uint32_t* ticket, T* total,
+                                                 uint32_t* err) {
+    constexpr int WARPS = BLOCK / 32;
+    __shared__ uint32_t s_tile;
+    __shared__ T s_warp[WARPS];
+    __shared__ T s_prefix;
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = (uint64_t)tile * (BLOCK * ITEMS) + (uint64_t)threadIdx.x * ITEMS;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    T v[ITEMS];
+    T acc = identity;
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+        const uint64_t i = base + k;
+        v[k] = i < n ? in(i) : identity;
+        acc = op(acc, v[k]);
+    }
+    // warp inclusive scan of per-thread aggregates
+    T inc = acc;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const T o = shfl_up_T(inc, d);
+        if (lane >= d) inc = op(o, inc);
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        T w = lane < WARPS ? s_warp[lane] : identity;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const T o = shfl_up_T(w, d);
+            if (lane >= d) w = op(o, w);
+        }
+        // w = inclusive over warps; turn into exclusive per warp
+        const T ex = shfl_up_T(w, 1);
+        const T tile_agg = shfl_idx_T(w, WARPS - 1);
+        if (lane < WARPS) s_warp[lane] = lane == 0 ? identity : ex;
+        if (lane == 0) {
+            T prefix = identity;
+            ScanStatus<T>* me = status + tile;
+            if (tile == 0) {
+                st_words(&me->inc, tile_agg);
+                __threadfence();
+                st_release(&me->flag, 2u);
+            } else {
+                st_words(&me->agg, tile_agg);
+                __threadfence();
+                st_release(&me->flag, 1u);
+                int64_t j = (int64_t)tile - 1;
+                long long spins = 0;
+                while (j >= 0) {
+                    const uint32_t f = ld_acquire(&status[j].flag);
+                    if (f == 0u) {
+                        if (++spins > SPIN_LIMIT) { atomicOr(err, ERR_TIMEOUT); break; }
+                        if (spins > 64) __nanosleep(64);
+                        continue;
+                    }
+                    if (f == 2u) { prefix = op(ld_words(&status[j].inc), prefix); break; }
+                    prefix = op(ld_words(&status[j].agg), prefix);
+                    --j;
+                }
+                st_words(&me->inc, op(prefix, tile_agg));
+                __threadfence();
+                st_release(&me->flag, 2u);
+            }
+            s_prefix = prefix;
+            const uint64_t tile_end = (uint64_t)(tile + 1) * (BLOCK * ITEMS);
+            if (tile_end >= n && total != nullptr) *total = op(prefix, tile_agg);
+        }
+    }
+    __syncthreads();
+    // exclusive prefix of this thread's first item
+    T ex_lane = shfl_up_T(inc, 1);
+    if (lane == 0) ex_lane = identity;
+    T run = op(op(s_prefix, s_warp[warp]), ex_lane);
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+        const uint64_t i = base + k;
+        if (i < n) out(i, run, v[k]);
+        run = op(run, v[k]);
+    }
+}
+
+struct OpSumU32 {
+    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a + b; }
+};
+
+// Launch helper.  `status` must hold at least scan_tiles(n) entries and,
+// together with `ticket`, be zeroed on `stream` before the launch (done here).
+constexpr int SCAN_BLOCK = 256;
+constexpr int SCAN_ITEMS = 8;
+inline uint64_t scan_tiles(uint64_t n) { return (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS); }
+
+template <class T, class Op, class In, class Out>
+cudaError_t launch_scan(uint64_t n, In in, Out out, Op op, T identity, void* status, uint32_t* ticket, T* total,
+                        uint32_t* err, cudaStream_t stream) {
+    const uint64_t tiles = scan_tiles(n);
+    if (tiles == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(status, 0, tiles * sizeof(ScanStatus<T>), stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
+    if (e != cudaSuccess) return e;
+    k_scan<SCAN_BLOCK, SCAN_ITEMS, T, Op, In, Out><<<(unsigned)tiles, SCAN_BLOCK, 0, stream>>>(
+        n, in, out, op, identity, reinterpret_cast<ScanStatus<T>*>(status), ticket, total, err);
+    return cudaGetLastError();
+}
+
+}  // namespace ochre

@@ -1,0 +1,241 @@
+// Stage 3: stable LSD radix sort of (key, value) pairs, onesweep style.
+//
+// Reference counterpart: the two sort_unstable_by_key calls of finish
+// (rasterizer.rs:209, 211).  The reference's sorts are unstable, so the f32
+// accumulation order inside a tile is unspecified there; this sort is stable,
+// which makes the GPU result deterministic.
+//
+// One upfront kernel histograms every 8-bit digit of every pass; each pass
+// then ranks a tile of keys in shared memory (per-warp counters with
+// __match_any_sync for stable ranks), publishes its per-digit counts and
+// resolves its global offsets by decoupled look-back over earlier tiles
+// (bounded spins), and scatters through shared memory so that runs of equal
+// digits leave as contiguous writes.
+#include "common.cuh"
+#include "internal.h"
+
+#include <utility>
+#include <vector>
+
+namespace ochre {
+
+constexpr int SORT_BLOCK = 256;   // one thread per digit in the offset phase
+constexpr int SORT_WARPS = SORT_BLOCK / 32;
+constexpr int SORT_ITEMS = 15;
+constexpr int SORT_TILE = SORT_BLOCK * SORT_ITEMS;
+constexpr uint32_t LB_AGG = 1u << 30, LB_INC = 2u << 30, LB_MASK = (1u << 30) - 1u;
+
+template <class K>
+__global__ void __launch_bounds__(256) k_sort_hist(const K* __restrict__ keys, uint64_t n, int passes,
+                                                   uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[8][256];
+    for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&sh[0][0])[i] = 0u;
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const K k = keys[i];
+        for (int p = 0; p < passes; p++) atomicAdd(&sh[p][(uint32_t)(k >> (8 * p)) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * 256; i += blockDim.x) {
+        const uint32_t v = (&sh[0][0])[i];
+        if (v) atomicAdd(hist + i, v);
+    }
+}
+
+// Exclusive scan of each pass's 256 counts (one block per pass).
+__global__ void k_sort_offsets(const uint32_t* __restrict__ hist, uint32_t* __restrict__ off) {
+    __shared__ uint32_t s[256];
+    const int p = blockIdx.x, d = threadIdx.x;
+    s[d] = hist[p * 256 + d];
+    __syncthreads();
+    for (int k = 1; k < 256; k <<= 1) {
+        const uint32_t v = d >= k ? s[d - k] : 0u;
+        __syncthreads();
+        s[d] += v;
+        __syncthreads();
+    }
+    off[p * 256 + d] = s[d] - hist[p * 256 + d];
+}
+
+template <class K>
+__global__ void __launch_bounds__(SORT_BLOCK) k_onesweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                                                         K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
+                                                         uint64_t n, int shift, const uint32_t* __restrict__ digit_off,
+                                                         uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    K* s_keys = reinterpret_cast<K*>(smem);
+    uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + SORT_TILE);
+    uint32_t* s_whist = s_vals + SORT_TILE;            // [SORT_WARPS][256]
+    uint32_t* s_tile_excl = s_whist + SORT_WARPS * 256; // [256]
+    uint32_t* s_gbase = s_tile_excl + 256;              // [256]
+    uint32_t* s_misc = s_gbase + 256;                   // [0]: tile id
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_misc[0] = atomicAdd(ticket, 1u);
+    for (int i = lane; i < 256; i += 32) s_whist[warp * 256 + i] = 0u;
+    __syncthreads();
+    const uint32_t tile = s_misc[0];
+    const uint64_t tile_base = (uint64_t)tile * SORT_TILE;
+    const uint64_t warp_base = tile_base + (uint64_t)warp * 32 * SORT_ITEMS;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+
+    K key[SORT_ITEMS];
+    uint32_t val[SORT_ITEMS];
+    uint32_t rank[SORT_ITEMS];
+    uint32_t dig[SORT_ITEMS];
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        const uint64_t i = warp_base + (uint64_t)k * 32 + lane;
+        const bool valid = i < n;
+        key[k] = valid ? keys_in[i] : (K)0;
+        val[k] = valid ? vals_in[i] : 0u;
+        const uint32_t d = valid ? ((uint32_t)(key[k] >> shift) & 255u) : 256u;
+        dig[k] = d;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        uint32_t b = 0;
+        if (lane == leader && d < 256u) {
+            b = s_whist[warp * 256 + d];
+            s_whist[warp * 256 + d] = b + __popc(peers);
+        }
+        b = __shfl_sync(0xffffffffu, b, leader);
+        rank[k] = b + __popc(peers & lt_mask);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // one thread per digit: exclusive over warps, tile count, look-back
+    {
+        const int d = threadIdx.x;
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < SORT_WARPS; w++) {
+            const uint32_t c = s_whist[w * 256 + d];
+            s_whist[w * 256 + d] = run;
+            run += c;
+        }
+        uint32_t* my = lookback + (size_t)tile * 256 + d;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            st_release(my, LB_INC | run);
+        } else {
+            st_release(my, LB_AGG | run);
+            int64_t j = (int64_t)tile - 1;
+            long long spins = 0;
+            while (j >= 0) {
+                const uint32_t v = ld_acquire(lookback + (size_t)j * 256 + d);
+                const uint32_t f = v & ~LB_MASK;
+                if (f == 0u) {
+                    if (++spins > SPIN_LIMIT) { atomicOr(err, ERR_TIMEOUT); break; }
+                    if (spins > 64) __nanosleep(64);
+                    continue;
+                }
+                excl += v & LB_MASK;
+                if (f == LB_INC) break;
+                --j;
+            }
+            st_release(my, LB_INC | (excl + run));
+        }
+        s_gbase[d] = digit_off[d] + excl;
+        // block exclusive scan of run over digits -> tile-local digit starts
+        s_tile_excl[d] = run;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        // 256 values, 8 per lane
+        uint32_t v[8], sum = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) { v[q] = s_tile_excl[lane * 8 + q]; sum += v[q]; }
+        uint32_t inc = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        uint32_t run = inc - sum;
+#pragma unroll
+        for (int q = 0; q < 8; q++) { s_tile_excl[lane * 8 + q] = run; run += v[q]; }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        const uint32_t d = dig[k];
+        if (d < 256u) {
+            const uint32_t pos = s_tile_excl[d] + s_whist[warp * 256 + d] + rank[k];
+            s_keys[pos] = key[k];
+            s_vals[pos] = val[k];
+        }
+    }
+    __syncthreads();
+    const uint64_t remain = n - tile_base;
+    const int cnt = remain < (uint64_t)SORT_TILE ? (int)remain : SORT_TILE;
+    for (int i = threadIdx.x; i < cnt; i += SORT_BLOCK) {
+        const K k = s_keys[i];
+        const uint32_t d = (uint32_t)(k >> shift) & 255u;
+        const uint32_t g = s_gbase[d] + ((uint32_t)i - s_tile_excl[d]);
+        keys_out[g] = k;
+        vals_out[g] = s_vals[i];
+    }
+}
+
+template <class K>
+static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStream_t s, uint32_t* passes_done) {
+    DevScalars* ds = dev_scalars(ctx);
+    const int passes = (int)((key_bits + 7) / 8);
+    const uint64_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
+    OCHRE_CUDA_TRY(ctx->sort_hist.ensure((size_t)passes * 256 * 4 * 2));
+    OCHRE_CUDA_TRY(ctx->sort_lookback.ensure((size_t)tiles * 256 * 4));
+    uint32_t* hist = ctx->sort_hist.as<uint32_t>();
+    uint32_t* off = hist + passes * 256;
+    OCHRE_CUDA_TRY(cudaMemsetAsync(hist, 0, (size_t)passes * 256 * 4, s));
+    K* kin = ctx->keys.as<K>();
+    uint32_t* vin = ctx->vals.as<uint32_t>();
+    K* kout = ctx->keys_alt.as<K>();
+    uint32_t* vout = ctx->vals_alt.as<uint32_t>();
+    {
+        int blocks = (int)((n + 255) / 256);
+        if (blocks > 152 * 8) blocks = 152 * 8;
+        k_sort_hist<K><<<blocks, 256, 0, s>>>(kin, n, passes, hist);
+        OCHRE_CUDA_TRY(cudaGetLastError());
+        k_sort_offsets<<<passes, 256, 0, s>>>(hist, off);
+        OCHRE_CUDA_TRY(cudaGetLastError());
+    }
+    const size_t smem = (size_t)SORT_TILE * (sizeof(K) + 4) + (SORT_WARPS * 256 + 256 + 256 + 4) * 4;
+    OCHRE_CUDA_TRY(cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // Skip passes whose digit is constant over all keys (one bucket holds n).
+    std::vector<uint32_t> h_hist((size_t)passes * 256);
+    OCHRE_CUDA_TRY(cudaMemcpyAsync(h_hist.data(), hist, h_hist.size() * 4, cudaMemcpyDeviceToHost, s));
+    OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
+    uint32_t done = 0;
+    for (int p = 0; p < passes; p++) {
+        bool trivial = false;
+        for (int d = 0; d < 256; d++)
+            if (h_hist[(size_t)p * 256 + d] == n) trivial = true;
+        if (trivial) continue;
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->sort_lookback.p, 0, (size_t)tiles * 256 * 4, s));
+        OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->sort_ticket, 0, 4, s));
+        k_onesweep<K><<<(unsigned)tiles, SORT_BLOCK, smem, s>>>(kin, vin, kout, vout, n, 8 * p, off + p * 256,
+                                                                ctx->sort_lookback.as<uint32_t>(), &ds->sort_ticket,
+                                                                &ds->err);
+        OCHRE_CUDA_TRY(cudaGetLastError());
+        K* tk = kin; kin = kout; kout = tk;
+        uint32_t* tv = vin; vin = vout; vout = tv;
+        done++;
+    }
+    if (kin != ctx->keys.as<K>()) {
+        // leave the sorted result in ctx->keys / ctx->vals
+        std::swap(ctx->keys, ctx->keys_alt);
+        std::swap(ctx->vals, ctx->vals_alt);
+    }
+    *passes_done = done;
+    return OCHRE_OK;
+}
+
+int stage_sort(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStream_t s, uint32_t* passes) {
+    *passes = 0;
+    if (n <= 1) return OCHRE_OK;
+    return ctx->keys64 ? sort_impl<uint64_t>(ctx, n, key_bits, s, passes)
+                       : sort_impl<uint32_t>(ctx, n, key_bits, s, passes);
+}
+
+}  // namespace ochre

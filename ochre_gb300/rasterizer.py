@@ -1,0 +1,369 @@
+"""Python mirror of ochre's public API over the C ABI.
+
+``Vec2``, ``Mat2x2``, ``Transform`` (src/geom.rs), ``PathCmd`` (src/path.rs:5-12),
+``TileBuilder`` and ``Rasterizer`` (src/rasterizer.rs:12-268) keep the
+reference's names, argument meaning and call order; rasterization runs on the
+GPU through libochre_gpu.so.  ``GpuContext`` exposes the batched entry points
+(many independent rasterizers per call) used by the benchmark.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .batch import (CLOSE, CONIC, CUBIC, FLOATS_PER_VERB, IDENTITY, LINE, MOVE, QUADRATIC, Batch,
+                    BatchBuilder)
+
+TILE_SIZE = 8  # src/rasterizer.rs:4
+
+
+# ---------------------------------------------------------------------------
+# geom.rs
+# ---------------------------------------------------------------------------
+@dataclass(frozen=True)
+class Vec2:
+    x: float
+    y: float
+
+
+@dataclass(frozen=True)
+class Mat2x2:
+    """Row-major 2x2 matrix (geom.rs:133)."""
+    m: tuple
+
+    @staticmethod
+    def new(a: float, b: float, c: float, d: float) -> "Mat2x2":
+        return Mat2x2((a, b, c, d))
+
+    @staticmethod
+    def id() -> "Mat2x2":
+        return Mat2x2((1.0, 0.0, 0.0, 1.0))
+
+    @staticmethod
+    def scale(s: float) -> "Mat2x2":
+        return Mat2x2((s, 0.0, 0.0, s))
+
+    @staticmethod
+    def rotate(angle: float) -> "Mat2x2":
+        """geom.rs:152-154: [cos, sin, -sin, cos] (evaluated in f32)."""
+        a = np.float32(angle)
+        c, s = float(np.cos(a)), float(np.sin(a))
+        return Mat2x2((c, s, -s, c))
+
+
+@dataclass(frozen=True)
+class Transform:
+    matrix: Mat2x2
+    offset: Vec2
+
+    @staticmethod
+    def new(matrix: Mat2x2, offset: Vec2) -> "Transform":
+        return Transform(matrix, offset)
+
+    @staticmethod
+    def id() -> "Transform":
+        return Transform(Mat2x2.id(), Vec2(0.0, 0.0))
+
+    @staticmethod
+    def translate(x: float, y: float) -> "Transform":
+        return Transform(Mat2x2.id(), Vec2(x, y))
+
+    @staticmethod
+    def scale(s: float) -> "Transform":
+        return Transform(Mat2x2.scale(s), Vec2(0.0, 0.0))
+
+    @staticmethod
+    def rotate(angle: float) -> "Transform":
+        return Transform(Mat2x2.rotate(angle), Vec2(0.0, 0.0))
+
+    def then(self, t: "Transform") -> "Transform":
+        """geom.rs:252-257, in f32."""
+        f = np.float32
+        a, b = [f(v) for v in t.matrix.m], [f(v) for v in self.matrix.m]
+        m = (a[0] * b[0] + a[1] * b[2], a[0] * b[1] + a[1] * b[3], a[2] * b[0] + a[3] * b[2], a[2] * b[1] + a[3] * b[3])
+        ox, oy = f(self.offset.x), f(self.offset.y)
+        o = (a[0] * ox + a[1] * oy + f(t.offset.x), a[2] * ox + a[3] * oy + f(t.offset.y))
+        return Transform(Mat2x2(tuple(float(v) for v in m)), Vec2(float(o[0]), float(o[1])))
+
+    def as_array(self) -> np.ndarray:
+        return np.array([*self.matrix.m, self.offset.x, self.offset.y], dtype=np.float32)
+
+
+# ---------------------------------------------------------------------------
+# path.rs
+# ---------------------------------------------------------------------------
+@dataclass(frozen=True)
+class PathCmd:
+    """One path command: use the constructors Move/Line/Quadratic/Cubic/Conic/Close."""
+    verb: int
+    floats: tuple = ()
+
+    @staticmethod
+    def Move(p: Vec2) -> "PathCmd":
+        return PathCmd(MOVE, (p.x, p.y))
+
+    @staticmethod
+    def Line(p: Vec2) -> "PathCmd":
+        return PathCmd(LINE, (p.x, p.y))
+
+    @staticmethod
+    def Quadratic(c: Vec2, p: Vec2) -> "PathCmd":
+        return PathCmd(QUADRATIC, (c.x, c.y, p.x, p.y))
+
+    @staticmethod
+    def Cubic(c1: Vec2, c2: Vec2, p: Vec2) -> "PathCmd":
+        return PathCmd(CUBIC, (c1.x, c1.y, c2.x, c2.y, p.x, p.y))
+
+    @staticmethod
+    def Conic(c: Vec2, p: Vec2, w: float) -> "PathCmd":
+        return PathCmd(CONIC, (c.x, c.y, p.x, p.y, w))
+
+    @staticmethod
+    def Close() -> "PathCmd":
+        return PathCmd(CLOSE, ())
+
+
+def encode_path(path: Sequence[PathCmd]) -> tuple[np.ndarray, np.ndarray]:
+    verbs = np.array([c.verb for c in path], dtype=np.uint8)
+    pts = np.array([v for c in path for v in c.floats], dtype=np.float32)
+    return verbs, pts
+
+
+# ---------------------------------------------------------------------------
+# rasterizer.rs
+# ---------------------------------------------------------------------------
+class TileBuilder:
+    """rasterizer.rs:12-22.  Subclass and override tile() and span()."""
+
+    def tile(self, x: int, y: int, data: bytes) -> None:  # pragma: no cover - interface
+        raise NotImplementedError
+
+    def span(self, x: int, y: int, width: int) -> None:  # pragma: no cover - interface
+        raise NotImplementedError
+
+
+_default_ctx: Optional["GpuContext"] = None
+
+
+def default_context() -> "GpuContext":
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = GpuContext(0)
+    return _default_ctx
+
+
+class Rasterizer:
+    """rasterizer.rs:40-268: Rasterizer::new / move_to / line_to / command /
+    fill / finish.  Commands are buffered on the host; finish() rasterizes on
+    the GPU and calls the builder in the reference's order."""
+
+    def __init__(self, ctx: Optional["GpuContext"] = None):
+        self._ctx = ctx or default_context()
+        L = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(L.ochre_rasterizer_new(self._ctx.handle, ctypes.byref(h)), "Rasterizer::new")
+        self._h = h
+
+    @staticmethod
+    def new(ctx: Optional["GpuContext"] = None) -> "Rasterizer":
+        return Rasterizer(ctx)
+
+    def _live(self):
+        if self._h is None:
+            raise RuntimeError("Rasterizer used after finish()")
+        return self._h
+
+    def move_to(self, point: Vec2) -> None:
+        _lib.check(_lib.load().ochre_rasterizer_move_to(self._live(), point.x, point.y), "move_to")
+
+    def line_to(self, point: Vec2) -> None:
+        _lib.check(_lib.load().ochre_rasterizer_line_to(self._live(), point.x, point.y), "line_to")
+
+    def command(self, cmd: PathCmd) -> None:
+        f = (ctypes.c_float * max(1, len(cmd.floats)))(*cmd.floats)
+        _lib.check(_lib.load().ochre_rasterizer_command(self._live(), cmd.verb, f), "command")
+
+    def fill(self, path: Sequence[PathCmd], transform: Transform) -> None:
+        verbs, pts = encode_path(path)
+        xf = transform.as_array()
+        _lib.check(_lib.load().ochre_rasterizer_fill(
+            self._live(), verbs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), len(verbs),
+            pts.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(pts),
+            xf.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "fill")
+
+    def finish(self, builder: TileBuilder) -> None:
+        h = self._live()
+        self._h = None  # finish consumes the rasterizer
+        errors = []
+
+        def on_tile(_user, x, y, data):
+            try:
+                builder.tile(int(x), int(y), ctypes.string_at(data, 64))
+            except BaseException as e:  # pragma: no cover - surfaced below
+                errors.append(e)
+
+        def on_span(_user, x, y, w):
+            try:
+                builder.span(int(x), int(y), int(w))
+            except BaseException as e:  # pragma: no cover
+                errors.append(e)
+
+        st = _lib.load().ochre_rasterizer_finish(h, _lib.TILE_FN(on_tile), _lib.SPAN_FN(on_span), None)
+        if errors:
+            raise errors[0]
+        _lib.check(st, "finish")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.ochre_rasterizer_free(h)
+            self._h = None
+
+
+# ---------------------------------------------------------------------------
+# Batched entry points
+# ---------------------------------------------------------------------------
+def _c_batch(verbs_p, n_cmds, pts_p, n_floats, off_p, xf_p, flags_p, n_fills, roff_p, n_rasters) -> _lib.Batch:
+    b = _lib.Batch()
+    b.verbs, b.n_cmds, b.pts, b.n_floats = verbs_p, n_cmds, pts_p, n_floats
+    b.fill_cmd_off, b.fill_xf, b.fill_flags, b.n_fills = off_p, xf_p, flags_p, n_fills
+    b.raster_fill_off, b.n_rasters = roff_p, n_rasters
+    return b
+
+
+class DeviceBatch:
+    """A Batch resident in device memory (torch CUDA tensors as storage)."""
+
+    def __init__(self, batch: Batch, device: int = 0):
+        import torch
+        dev = torch.device("cuda", device)
+        self.batch = batch
+        t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)
+        self.verbs = t(batch.verbs if len(batch.verbs) else np.zeros(1, np.uint8), np.uint8)
+        self.pts = t(batch.pts if len(batch.pts) else np.zeros(1, np.float32), np.float32)
+        self.fill_off = t(batch.fill_cmd_off.astype(np.int32), np.int32)
+        self.fill_xf = t(batch.fill_xf.reshape(-1) if batch.n_fills else np.zeros(6, np.float32), np.float32)
+        self.fill_flags = t(batch.fill_flags, np.uint8) if batch.fill_flags is not None else None
+        self.raster_off = (t(batch.raster_fill_off.astype(np.int32), np.int32)
+                           if batch.raster_fill_off is not None else None)
+        self.c = _c_batch(self.verbs.data_ptr(), batch.n_cmds, self.pts.data_ptr(), len(batch.pts),
+                          self.fill_off.data_ptr(), self.fill_xf.data_ptr(),
+                          self.fill_flags.data_ptr() if self.fill_flags is not None else None,
+                          batch.n_fills, self.raster_off.data_ptr() if self.raster_off is not None else None,
+                          batch.n_rasters)
+
+    def input_bytes(self) -> int:
+        return self.batch.input_bytes()
+
+
+def _np_from(ptr, dtype, count):
+    if count == 0 or not ptr:
+        return np.zeros(0, dtype=dtype)
+    buf = (ctypes.c_char * (count * np.dtype(dtype).itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype).copy()
+
+
+class GpuContext:
+    """One libochre_gpu context (device + stream + buffers)."""
+
+    def __init__(self, device: int = 0, want_cov: bool = False):
+        L = _lib.load()
+        h = ctypes.c_void_p()
+        _lib.check(L.ochre_gpu_create(ctypes.byref(h), int(device), _lib.CTX_WANT_COV if want_cov else 0),
+                   "ochre_gpu_create")
+        self.handle = h
+        self.device = device
+        self.want_cov = want_cov
+
+    def set_want_cov(self, on: bool) -> None:
+        _lib.check(_lib.load().ochre_gpu_set_flags(self.handle, _lib.CTX_WANT_COV if on else 0))
+        self.want_cov = on
+
+    def close(self) -> None:
+        if self.handle is not None:
+            _lib.load().ochre_gpu_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def rasterize(self, batch: Batch) -> dict:
+        """Host buffers in, host arrays out (copies the batch to the device,
+        rasterizes, copies results back)."""
+        keep = []
+
+        def p(a, dt):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a.ctypes.data
+
+        c = _c_batch(p(batch.verbs, np.uint8), batch.n_cmds, p(batch.pts, np.float32), len(batch.pts),
+                     p(batch.fill_cmd_off, np.uint32), p(batch.fill_xf, np.float32), p(batch.fill_flags, np.uint8),
+                     batch.n_fills, p(batch.raster_fill_off, np.uint32), batch.n_rasters)
+        r = _lib.Result()
+        _lib.check(_lib.load().ochre_gpu_rasterize(self.handle, ctypes.byref(c), ctypes.byref(r)), "rasterize")
+        return self._result_to_numpy(r, batch.n_rasters)
+
+    def rasterize_device(self, dbatch: DeviceBatch, stream: Optional[int] = None) -> _lib.Result:
+        """Device buffers in, device result (pointers owned by the context)."""
+        r = _lib.Result()
+        _lib.check(_lib.load().ochre_gpu_rasterize_device(self.handle, ctypes.byref(dbatch.c), ctypes.byref(r),
+                                                          stream), "rasterize_device")
+        return r
+
+    def device_result_to_numpy(self, r: _lib.Result, n_rasters: int) -> dict:
+        import torch
+        out = {}
+        T, N = r.n_tiles, r.n_spans
+
+        def get(ptr, dtype, count):
+            if count == 0 or not ptr:
+                return np.zeros(0, dtype=dtype)
+            host = np.empty(count, dtype=dtype)
+            cudart = torch.cuda.cudart()
+            err = cudart.cudaMemcpy(host.ctypes.data, ptr, host.nbytes, 2)  # DeviceToHost
+            if int(err) != 0:
+                raise RuntimeError(f"cudaMemcpy failed ({err})")
+            return host
+
+        out["tile_xy"] = get(r.tile_xy, np.int16, 2 * T).reshape(T, 2)
+        out["tile_alpha"] = get(r.tile_alpha, np.uint8, 64 * T).reshape(T, 64)
+        if r.tile_cov:
+            out["tile_cov"] = get(r.tile_cov, np.float32, 64 * T).reshape(T, 64)
+        out["span_xy"] = get(r.span_xy, np.int16, 2 * N).reshape(N, 2)
+        out["span_w"] = get(r.span_width, np.uint16, N)
+        out["span_tile"] = get(r.span_tile, np.uint32, N)
+        out["raster_tile_off"] = get(r.raster_tile_off, np.uint32, n_rasters + 1).astype(np.uint64)
+        out["raster_span_off"] = get(r.raster_span_off, np.uint32, n_rasters + 1).astype(np.uint64)
+        return out
+
+    @staticmethod
+    def _result_to_numpy(r: _lib.Result, n_rasters: int) -> dict:
+        T, N = r.n_tiles, r.n_spans
+        out = {
+            "tile_xy": _np_from(r.tile_xy, np.int16, 2 * T).reshape(T, 2),
+            "tile_alpha": _np_from(r.tile_alpha, np.uint8, 64 * T).reshape(T, 64),
+            "span_xy": _np_from(r.span_xy, np.int16, 2 * N).reshape(N, 2),
+            "span_w": _np_from(r.span_width, np.uint16, N),
+            "span_tile": _np_from(r.span_tile, np.uint32, N),
+            "raster_tile_off": _np_from(r.raster_tile_off, np.uint32, n_rasters + 1).astype(np.uint64),
+            "raster_span_off": _np_from(r.raster_span_off, np.uint32, n_rasters + 1).astype(np.uint64),
+        }
+        if r.tile_cov:
+            out["tile_cov"] = _np_from(r.tile_cov, np.float32, 64 * T).reshape(T, 64)
+        return out
+
+    def stats(self) -> dict:
+        s = _lib.Stats()
+        _lib.check(_lib.load().ochre_gpu_last_stats(self.handle, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in _lib.Stats._fields_}

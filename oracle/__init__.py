@@ -1,0 +1,151 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper over ``ochre_oracle.c``, a strict-f32 CPU restatement of ochre
+0.2.0's rasterizer (``src/rasterizer.rs``, ``src/path.rs``, ``src/geom.rs``).
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use it, as the checker; the product never imports it.
+
+Parity with the reference: UNPINNED.  The reference is a Rust crate that
+cannot be built here (no rustc/cargo) and ships no tests or golden vectors.
+The restatement is cross-checked against an independent numpy-float32
+restatement (``tests/oracle_py.py``) and hand-derived known answers.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_LIB_PATH = os.path.join(_BUILD, "libochre_oracle.so")
+
+CFLAGS = ["-O3", "-ffp-contract=off", "-fno-fast-math", "-fexcess-precision=standard",
+          "-fno-strict-aliasing", "-std=c11", "-fPIC", "-shared", "-pthread"]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle into oracle/_build/libochre_oracle.so."""
+    src = os.path.join(_HERE, "ochre_oracle.c")
+    hdr = os.path.join(_HERE, "ochre_oracle.h")
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+        return _LIB_PATH
+    os.makedirs(_BUILD, exist_ok=True)
+    tmp = _LIB_PATH + f".tmp{os.getpid()}"
+    cmd = ["gcc", *CFLAGS, "-o", tmp, src, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+class _Batch(ctypes.Structure):
+    _fields_ = [
+        ("verbs", ctypes.c_void_p), ("n_cmds", ctypes.c_uint64),
+        ("pts", ctypes.c_void_p), ("n_floats", ctypes.c_uint64),
+        ("fill_cmd_off", ctypes.c_void_p), ("fill_xf", ctypes.c_void_p),
+        ("fill_flags", ctypes.c_void_p), ("n_fills", ctypes.c_uint32),
+        ("raster_fill_off", ctypes.c_void_p), ("n_rasters", ctypes.c_uint32),
+    ]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [
+        ("n_rasters", ctypes.c_uint32),
+        ("n_tiles", ctypes.c_uint64), ("n_spans", ctypes.c_uint64), ("n_lines", ctypes.c_uint64),
+        ("tile_xy", ctypes.c_void_p), ("tile_alpha", ctypes.c_void_p), ("tile_cov", ctypes.c_void_p),
+        ("span_xy", ctypes.c_void_p), ("span_w", ctypes.c_void_p), ("span_tile", ctypes.c_void_p),
+        ("raster_tile_off", ctypes.c_void_p), ("raster_span_off", ctypes.c_void_p),
+        ("raster_line_off", ctypes.c_void_p), ("raster_stats", ctypes.c_void_p),
+        ("lines", ctypes.c_void_p), ("line_ninc", ctypes.c_void_p),
+        ("error_raster", ctypes.c_uint32),
+    ]
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = build()
+        lib = ctypes.CDLL(path)
+        lib.ochre_oracle_run.argtypes = [ctypes.POINTER(_Batch), ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.POINTER(_Result))]
+        lib.ochre_oracle_run.restype = ctypes.c_int
+        lib.ochre_oracle_free.argtypes = [ctypes.POINTER(_Result)]
+        lib.ochre_oracle_free.restype = None
+        _lib = lib
+    return _lib
+
+
+def _copy(ptr, dtype, count):
+    if count == 0 or not ptr:
+        return np.zeros(0, dtype=dtype)
+    buf = (ctypes.c_char * (count * np.dtype(dtype).itemsize)).from_address(ptr)
+    return np.frombuffer(buf, dtype=dtype).copy()
+
+
+def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = False) -> dict:
+    """Rasterize every raster of ``batch`` on the CPU.
+
+    ``batch`` has the attributes of ``ochre_gb300.batch.Batch`` (numpy arrays
+    in the C-ABI layout).  Returns a dict of numpy arrays in the same layout as
+    the GPU result plus per-raster statistics.
+    """
+    lib = _load()
+    keep = []
+
+    def p(a, dtype):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(a)
+        return a.ctypes.data
+
+    b = _Batch()
+    b.verbs = p(batch.verbs, np.uint8)
+    b.n_cmds = len(batch.verbs)
+    b.pts = p(batch.pts, np.float32)
+    b.n_floats = len(batch.pts)
+    b.fill_cmd_off = p(batch.fill_cmd_off, np.uint32)
+    b.fill_xf = p(batch.fill_xf, np.float32)
+    b.fill_flags = p(batch.fill_flags, np.uint8)
+    b.n_fills = len(batch.fill_cmd_off) - 1
+    b.raster_fill_off = p(batch.raster_fill_off, np.uint32)
+    b.n_rasters = batch.n_rasters
+    flags = (1 if want_cov else 0) | (2 if capture_lines else 0)
+    res_p = ctypes.POINTER(_Result)()
+    st = lib.ochre_oracle_run(ctypes.byref(b), int(threads), flags, ctypes.byref(res_p))
+    if not res_p:
+        raise RuntimeError(f"oracle failed with status {st}")
+    try:
+        r = res_p.contents
+        nr, nt, ns, nl = r.n_rasters, r.n_tiles, r.n_spans, r.n_lines
+        out = {
+            "status": st,
+            "tile_xy": _copy(r.tile_xy, np.int16, 2 * nt).reshape(nt, 2),
+            "tile_alpha": _copy(r.tile_alpha, np.uint8, 64 * nt).reshape(nt, 64),
+            "span_xy": _copy(r.span_xy, np.int16, 2 * ns).reshape(ns, 2),
+            "span_w": _copy(r.span_w, np.uint16, ns),
+            "span_tile": _copy(r.span_tile, np.uint32, ns),
+            "raster_tile_off": _copy(r.raster_tile_off, np.uint64, nr + 1),
+            "raster_span_off": _copy(r.raster_span_off, np.uint64, nr + 1),
+            "raster_stats": _copy(r.raster_stats, np.uint64, 3 * nr).reshape(nr, 3),
+        }
+        if want_cov:
+            out["tile_cov"] = _copy(r.tile_cov, np.float32, 64 * nt).reshape(nt, 64)
+        if capture_lines:
+            out["lines"] = _copy(r.lines, np.float32, 4 * nl).reshape(nl, 4)
+            out["line_ninc"] = _copy(r.line_ninc, np.uint32, nl)
+            out["raster_line_off"] = _copy(r.raster_line_off, np.uint64, nr + 1)
+        return out
+    finally:
+        lib.ochre_oracle_free(res_p)
+
+
+if __name__ == "__main__":  # pragma: no cover
+    print(build(force="--force" in sys.argv))

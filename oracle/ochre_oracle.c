@@ -1,0 +1,674 @@
+/*
+ * ORACLE — test infrastructure only.
+ *
+ * A CPU restatement, in strict IEEE-754 single precision, of ochre 0.2.0's
+ * path rasterizer (glowcoil/ochre).  It is the checker for the CUDA path in
+ * ochre_gb300/csrc and the timed CPU baseline in bench.py ("kind": "port").
+ * Nothing in the product links or calls it.
+ *
+ * Parity status: UNPINNED by the reference itself.  The reference is Rust
+ * (no rustc/cargo on these machines) and ships no tests, golden vectors or
+ * recorded outputs (its only executable example, examples/basic.rs, prints
+ * and asserts nothing).  The restatement is cross-checked against an
+ * independent pure-Python restatement (tests/oracle_py.py) and against
+ * hand-derived known answers (tests/test_oracle.py).
+ *
+ * Build: see oracle/build_oracle.py (gcc -O2 -ffp-contract=off -fno-fast-math
+ * -fexcess-precision=standard): Rust never contracts a*b+c into an FMA, and
+ * aarch64 gcc does by default, so contraction must be off for bit parity.
+ *
+ * Line-by-line sources (paths inside the ochre crate):
+ *   geom.rs:19-21   dot            geom.rs:38-40  length
+ *   geom.rs:50-52   lerp           geom.rs:170-178 Mat2x2 * Vec2
+ *   geom.rs:260-262 Transform::apply
+ *   path.rs:16-37   PathCmd::transform   path.rs:41-109 PathCmd::flatten
+ *   rasterizer.rs:61-69  move_to   rasterizer.rs:72-140 line_to
+ *   rasterizer.rs:145-157 command  rasterizer.rs:161-165 fill
+ *   rasterizer.rs:180-268 finish
+ */
+#include "ochre_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* Rust scalar semantics (the casts and min/max used by the reference) */
+/* ------------------------------------------------------------------ */
+
+/* `f as i16`: truncate toward zero, saturate, NaN -> 0. */
+static int16_t f2i16(float v) {
+    if (v != v) return 0;
+    if (v <= -32768.0f) return -32768;
+    if (v >= 32767.0f) return 32767;
+    return (int16_t)v;
+}
+
+/* `f as u8`: truncate toward zero, saturate, NaN -> 0. */
+static uint8_t f2u8(float v) {
+    if (v != v) return 0;
+    if (v <= 0.0f) return 0;
+    if (v >= 255.0f) return 255;
+    return (uint8_t)v;
+}
+
+/* `f32::signum(v) as i16`: +0 and +inf give 1, -0 and -inf give -1,
+ * NaN gives NaN which casts to 0. */
+static int16_t signum_i16(float v) {
+    if (v != v) return 0;
+    return signbit(v) ? -1 : 1;
+}
+
+/* i16::wrapping_div_euclid(8): floor division for a positive divisor. */
+static int16_t div8(int16_t v) {
+    int q = (int)v / 8;
+    if ((int)v % 8 < 0) q -= 1;
+    return (int16_t)q;
+}
+
+/* f32::min / f32::max return the non-NaN operand, as fminf / fmaxf do. */
+static float rmin(float a, float b) { return fminf(a, b); }
+static float rmax(float a, float b) { return fmaxf(a, b); }
+
+/* ------------------------------------------------------------------ */
+/* geom.rs                                                             */
+/* ------------------------------------------------------------------ */
+typedef struct { float x, y; } vec2;
+
+static vec2 v2(float x, float y) { vec2 r = {x, y}; return r; }
+static vec2 vadd(vec2 a, vec2 b) { return v2(a.x + b.x, a.y + b.y); }
+static vec2 vsub(vec2 a, vec2 b) { return v2(a.x - b.x, a.y - b.y); }
+static vec2 vscale(float s, vec2 a) { return v2(s * a.x, s * a.y); }
+static int veq(vec2 a, vec2 b) { return a.x == b.x && a.y == b.y; }
+static float vlength(vec2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+/* lerp(t, a, b) = (1 - t) * a + t * b */
+static vec2 vlerp(float t, vec2 a, vec2 b) {
+    return vadd(vscale(1.0f - t, a), vscale(t, b));
+}
+/* Transform::apply: matrix * v + offset, matrix row-major [m0 m1; m2 m3]. */
+static vec2 xf_apply(const float *xf, vec2 v) {
+    vec2 m = v2(xf[0] * v.x + xf[1] * v.y, xf[2] * v.x + xf[3] * v.y);
+    return vadd(m, v2(xf[4], xf[5]));
+}
+
+/* ------------------------------------------------------------------ */
+/* rasterizer.rs                                                       */
+/* ------------------------------------------------------------------ */
+#define TILE 8
+#define TOLERANCE 0.1f
+
+typedef struct { int16_t x, y; float area, height; } increment;
+typedef struct { int16_t tile_x, tile_y; int8_t sign; } tile_increment;
+
+typedef struct {
+    increment *inc; size_t n_inc, cap_inc;
+    tile_increment *tinc; size_t n_tinc, cap_tinc;
+    vec2 first, last;
+    int16_t tile_y_prev;
+    /* statistics and safety */
+    uint64_t n_lines;        /* line_to calls that walked (point != last) */
+    int error;               /* nonzero: an iteration cap was hit */
+    /* optional line capture (intermediate parity) */
+    float *lines; size_t n_lines_cap_used, cap_lines;
+    uint32_t *line_ninc;
+    int capture_lines;
+} rasterizer;
+
+/* Iteration caps: the reference would loop (or allocate) without bound on
+ * such inputs; the oracle stops and reports instead. */
+#define WALK_CAP (1u << 20)
+#define FLATTEN_CAP (1u << 20)
+#define CONIC_DEPTH_CAP 64
+
+static int push_inc(rasterizer *r, increment v) {
+    if (r->n_inc == r->cap_inc) {
+        size_t c = r->cap_inc ? r->cap_inc * 2 : 256;
+        increment *p = (increment *)realloc(r->inc, c * sizeof *p);
+        if (!p) { r->error = OCHRE_ORACLE_E_NOMEM; return 0; }
+        r->inc = p; r->cap_inc = c;
+    }
+    r->inc[r->n_inc++] = v;
+    return 1;
+}
+
+static int push_tinc(rasterizer *r, tile_increment v) {
+    if (r->n_tinc == r->cap_tinc) {
+        size_t c = r->cap_tinc ? r->cap_tinc * 2 : 64;
+        tile_increment *p = (tile_increment *)realloc(r->tinc, c * sizeof *p);
+        if (!p) { r->error = OCHRE_ORACLE_E_NOMEM; return 0; }
+        r->tinc = p; r->cap_tinc = c;
+    }
+    r->tinc[r->n_tinc++] = v;
+    return 1;
+}
+
+static void capture_line(rasterizer *r, vec2 a, vec2 b, uint32_t ninc) {
+    if (!r->capture_lines) return;
+    if (r->n_lines_cap_used == r->cap_lines) {
+        size_t c = r->cap_lines ? r->cap_lines * 2 : 256;
+        float *p = (float *)realloc(r->lines, c * 4 * sizeof(float));
+        uint32_t *q = (uint32_t *)realloc(r->line_ninc, c * sizeof(uint32_t));
+        if (!p || !q) { r->error = OCHRE_ORACLE_E_NOMEM; free(p); return; }
+        r->lines = p; r->line_ninc = q; r->cap_lines = c;
+    }
+    float *d = r->lines + 4 * r->n_lines_cap_used;
+    d[0] = a.x; d[1] = a.y; d[2] = b.x; d[3] = b.y;
+    r->line_ninc[r->n_lines_cap_used++] = ninc;
+}
+
+static void rasterizer_init(rasterizer *r) {
+    memset(r, 0, sizeof *r);
+    r->first = v2(0.0f, 0.0f);
+    r->last = v2(0.0f, 0.0f);
+    r->tile_y_prev = 0;
+}
+
+static void rasterizer_free(rasterizer *r) {
+    free(r->inc); free(r->tinc); free(r->lines); free(r->line_ninc);
+}
+
+static void line_to(rasterizer *r, vec2 point);
+
+/* rasterizer.rs:61-69 */
+static void move_to(rasterizer *r, vec2 point) {
+    if (!veq(r->last, r->first)) line_to(r, r->first);
+    r->first = point;
+    r->last = point;
+    r->tile_y_prev = div8(f2i16(floorf(point.y)));
+}
+
+/* rasterizer.rs:72-140: the pixel DDA. */
+static void line_to(rasterizer *r, vec2 point) {
+    vec2 last = r->last;
+    size_t inc_before = r->n_inc;
+    int walked = 0;
+    if (!veq(point, last)) {
+        walked = 1;
+        int16_t x_dir = signum_i16(point.x - last.x);
+        int16_t y_dir = signum_i16(point.y - last.y);
+        float dtdx = 1.0f / (point.x - last.x);
+        float dtdy = 1.0f / (point.y - last.y);
+        int16_t x = f2i16(floorf(last.x));
+        int16_t y = f2i16(floorf(last.y));
+        float row_t0 = 0.0f, col_t0 = 0.0f;
+        float row_t1, col_t1;
+        if (last.y == point.y) {
+            row_t1 = INFINITY;
+        } else {
+            float next_y = point.y > last.y ? (float)(int16_t)(y + 1) : (float)y;
+            row_t1 = rmin(dtdy * (next_y - last.y), 1.0f);
+        }
+        if (last.x == point.x) {
+            col_t1 = INFINITY;
+        } else {
+            float next_x = point.x > last.x ? (float)(int16_t)(x + 1) : (float)x;
+            col_t1 = rmin(dtdx * (next_x - last.x), 1.0f);
+        }
+        float x_step = fabsf(dtdx);
+        float y_step = fabsf(dtdy);
+
+        uint32_t iters = 0;
+        for (;;) {
+            float t0 = rmax(row_t0, col_t0);
+            float t1 = rmin(row_t1, col_t1);
+            vec2 p0 = vadd(vscale(1.0f - t0, last), vscale(t0, point));
+            vec2 p1 = vadd(vscale(1.0f - t1, last), vscale(t1, point));
+            float height = p1.y - p0.y;
+            float right = (float)(int16_t)(x + 1);
+            float area = 0.5f * height * ((right - p0.x) + (right - p1.x));
+            increment inc = {x, y, area, height};
+            if (!push_inc(r, inc)) return;
+
+            if (row_t1 < col_t1) {
+                row_t0 = row_t1;
+                row_t1 = rmin(row_t1 + y_step, 1.0f);
+                y = (int16_t)(y + y_dir);
+            } else {
+                col_t0 = col_t1;
+                col_t1 = rmin(col_t1 + x_step, 1.0f);
+                x = (int16_t)(x + x_dir);
+            }
+
+            int done = row_t0 == 1.0f || col_t0 == 1.0f;
+            if (done) {
+                x = f2i16(floorf(point.x));
+                y = f2i16(floorf(point.y));
+            }
+
+            int16_t tile_y = div8(y);
+            if (tile_y != r->tile_y_prev) {
+                tile_increment ti;
+                ti.tile_x = div8(x);
+                ti.tile_y = r->tile_y_prev < tile_y ? r->tile_y_prev : tile_y;
+                ti.sign = (int8_t)(int16_t)(tile_y - r->tile_y_prev);
+                if (!push_tinc(r, ti)) return;
+                r->tile_y_prev = tile_y;
+            }
+
+            if (done) break;
+            if (++iters >= WALK_CAP) { r->error = OCHRE_ORACLE_E_LIMIT; break; }
+        }
+        r->n_lines++;
+    }
+    capture_line(r, last, point, walked ? (uint32_t)(r->n_inc - inc_before) : 0u);
+    r->last = point;
+}
+
+/* path.rs:76-101 */
+static void flatten_conic(rasterizer *r, vec2 last, vec2 control, vec2 point, float weight,
+                          float t0, float t1, vec2 p0, vec2 p1, int depth) {
+    float t = 0.5f * (t0 + t1);
+    vec2 wc = vscale(weight, control);
+    vec2 p01 = vlerp(t, last, wc);
+    vec2 p12 = vlerp(t, wc, point);
+    float denom = (1.0f - t) * (1.0f - t) + 2.0f * t * (1.0f - t) * weight + t * t;
+    vec2 midpoint = vscale(1.0f / denom, vlerp(t, p01, p12));
+    float err = vlength(vsub(midpoint, vscale(0.5f, vadd(p0, p1))));
+    if (err > TOLERANCE) {
+        if (depth >= CONIC_DEPTH_CAP) { r->error = OCHRE_ORACLE_E_LIMIT; return; }
+        flatten_conic(r, last, control, point, weight, t0, t, p0, midpoint, depth + 1);
+        flatten_conic(r, last, control, point, weight, t, t1, midpoint, p1, depth + 1);
+    } else {
+        line_to(r, midpoint);
+        line_to(r, p1);
+    }
+}
+
+/* rasterizer.rs:145-157 with path.rs:41-109 inlined (the callback only
+ * dispatches Move and Line; Close is ignored). `last` is the rasterizer's
+ * last point at the time of the call. */
+static void command(rasterizer *r, uint8_t verb, const vec2 *p, float weight) {
+    vec2 last = r->last;
+    switch (verb) {
+    case OCHRE_ORACLE_MOVE:
+        move_to(r, p[0]);
+        break;
+    case OCHRE_ORACLE_LINE:
+        line_to(r, p[0]);
+        break;
+    case OCHRE_ORACLE_QUADRATIC: {
+        vec2 control = p[0], point = p[1];
+        float dt = sqrtf((4.0f * TOLERANCE) / vlength(vadd(vsub(last, vscale(2.0f, control)), point)));
+        float t = 0.0f;
+        uint32_t n = 0;
+        while (t < 1.0f) {
+            t = rmin(t + dt, 1.0f);
+            vec2 p01 = vlerp(t, last, control);
+            vec2 p12 = vlerp(t, control, point);
+            line_to(r, vlerp(t, p01, p12));
+            if (++n >= FLATTEN_CAP) { r->error = OCHRE_ORACLE_E_LIMIT; break; }
+        }
+        break;
+    }
+    case OCHRE_ORACLE_CUBIC: {
+        vec2 c1 = p[0], c2 = p[1], point = p[2];
+        vec2 a = vadd(vsub(vadd(vscale(-1.0f, last), vscale(3.0f, c1)), vscale(3.0f, c2)), point);
+        vec2 b = vscale(3.0f, vadd(vsub(last, vscale(2.0f, c1)), c2));
+        float conc = rmax(vlength(b), vlength(vadd(a, b)));
+        float dt = sqrtf((sqrtf(8.0f) * TOLERANCE) / conc);
+        float t = 0.0f;
+        uint32_t n = 0;
+        while (t < 1.0f) {
+            t = rmin(t + dt, 1.0f);
+            vec2 p01 = vlerp(t, last, c1);
+            vec2 p12 = vlerp(t, c1, c2);
+            vec2 p23 = vlerp(t, c2, point);
+            vec2 p012 = vlerp(t, p01, p12);
+            vec2 p123 = vlerp(t, p12, p23);
+            line_to(r, vlerp(t, p012, p123));
+            if (++n >= FLATTEN_CAP) { r->error = OCHRE_ORACLE_E_LIMIT; break; }
+        }
+        break;
+    }
+    case OCHRE_ORACLE_CONIC:
+        flatten_conic(r, last, p[0], p[1], weight, 0.0f, 1.0f, last, p[1], 0);
+        break;
+    default: /* Close */
+        break;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* finish (rasterizer.rs:180-268) into a collecting builder            */
+/* ------------------------------------------------------------------ */
+typedef struct { int16_t tile_x, tile_y; size_t start, end; } bin;
+
+static int cmp_bin(const void *a, const void *b) {
+    const bin *x = (const bin *)a, *y = (const bin *)b;
+    if (x->tile_y != y->tile_y) return x->tile_y < y->tile_y ? -1 : 1;
+    if (x->tile_x != y->tile_x) return x->tile_x < y->tile_x ? -1 : 1;
+    /* Any order is a valid outcome of the reference's unstable sort; take
+     * emission order so the oracle is deterministic. */
+    return x->start < y->start ? -1 : (x->start > y->start);
+}
+
+typedef struct { tile_increment t; size_t idx; } tinc_ix;
+static int cmp_tinc(const void *a, const void *b) {
+    const tinc_ix *x = (const tinc_ix *)a, *y = (const tinc_ix *)b;
+    if (x->t.tile_y != y->t.tile_y) return x->t.tile_y < y->t.tile_y ? -1 : 1;
+    if (x->t.tile_x != y->t.tile_x) return x->t.tile_x < y->t.tile_x ? -1 : 1;
+    return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+typedef struct {
+    int16_t *tile_xy; uint8_t *tile_alpha; float *tile_cov;
+    size_t n_tiles, cap_tiles;
+    int16_t *span_xy; uint16_t *span_w; uint32_t *span_tile;
+    size_t n_spans, cap_spans;
+    int want_cov;
+    int error;
+} collector;
+
+static void coll_tile(collector *c, int16_t x, int16_t y, const uint8_t *data, const float *cov) {
+    if (c->n_tiles == c->cap_tiles) {
+        size_t n = c->cap_tiles ? c->cap_tiles * 2 : 64;
+        int16_t *a = (int16_t *)realloc(c->tile_xy, n * 2 * sizeof(int16_t));
+        if (a) c->tile_xy = a;
+        uint8_t *b = (uint8_t *)realloc(c->tile_alpha, n * 64);
+        if (b) c->tile_alpha = b;
+        if (!a || !b) { c->error = OCHRE_ORACLE_E_NOMEM; return; }
+        if (c->want_cov) {
+            float *f = (float *)realloc(c->tile_cov, n * 64 * sizeof(float));
+            if (!f) { c->error = OCHRE_ORACLE_E_NOMEM; return; }
+            c->tile_cov = f;
+        }
+        c->cap_tiles = n;
+    }
+    c->tile_xy[2 * c->n_tiles] = x;
+    c->tile_xy[2 * c->n_tiles + 1] = y;
+    memcpy(c->tile_alpha + 64 * c->n_tiles, data, 64);
+    if (c->want_cov) memcpy(c->tile_cov + 64 * c->n_tiles, cov, 64 * sizeof(float));
+    c->n_tiles++;
+}
+
+static void coll_span(collector *c, int16_t x, int16_t y, uint16_t w) {
+    if (c->n_spans == c->cap_spans) {
+        size_t n = c->cap_spans ? c->cap_spans * 2 : 16;
+        int16_t *a = (int16_t *)realloc(c->span_xy, n * 2 * sizeof(int16_t));
+        if (a) c->span_xy = a;
+        uint16_t *b = (uint16_t *)realloc(c->span_w, n * sizeof(uint16_t));
+        if (b) c->span_w = b;
+        uint32_t *d = (uint32_t *)realloc(c->span_tile, n * sizeof(uint32_t));
+        if (d) c->span_tile = d;
+        if (!a || !b || !d) { c->error = OCHRE_ORACLE_E_NOMEM; return; }
+        c->cap_spans = n;
+    }
+    c->span_xy[2 * c->n_spans] = x;
+    c->span_xy[2 * c->n_spans + 1] = y;
+    c->span_w[c->n_spans] = w;
+    c->span_tile[c->n_spans] = (uint32_t)(c->n_tiles - 1); /* follows the last tile */
+    c->n_spans++;
+}
+
+static void finish(rasterizer *r, collector *out) {
+    if (!veq(r->last, r->first)) line_to(r, r->first);
+
+    size_t cap = 16, nb = 0;
+    bin *bins = (bin *)malloc(cap * sizeof(bin));
+    if (!bins) { out->error = OCHRE_ORACLE_E_NOMEM; return; }
+    bin b = {0, 0, 0, 0};
+    if (r->n_inc > 0) {
+        b.tile_x = div8(r->inc[0].x);
+        b.tile_y = div8(r->inc[0].y);
+    }
+    for (size_t i = 0; i < r->n_inc; i++) {
+        int16_t tx = div8(r->inc[i].x), ty = div8(r->inc[i].y);
+        if (tx != b.tile_x || ty != b.tile_y) {
+            if (nb == cap) { cap *= 2; bin *p = (bin *)realloc(bins, cap * sizeof(bin)); if (!p) { free(bins); out->error = OCHRE_ORACLE_E_NOMEM; return; } bins = p; }
+            bins[nb++] = b;
+            b.tile_x = tx; b.tile_y = ty; b.start = i; b.end = i;
+        }
+        b.end += 1;
+    }
+    if (nb == cap) { cap *= 2; bin *p = (bin *)realloc(bins, cap * sizeof(bin)); if (!p) { free(bins); out->error = OCHRE_ORACLE_E_NOMEM; return; } bins = p; }
+    bins[nb++] = b;
+    qsort(bins, nb, sizeof(bin), cmp_bin);
+
+    tinc_ix *ti = (tinc_ix *)malloc((r->n_tinc ? r->n_tinc : 1) * sizeof(tinc_ix));
+    if (!ti) { free(bins); out->error = OCHRE_ORACLE_E_NOMEM; return; }
+    for (size_t i = 0; i < r->n_tinc; i++) { ti[i].t = r->tinc[i]; ti[i].idx = i; }
+    qsort(ti, r->n_tinc, sizeof(tinc_ix), cmp_tinc);
+
+    float areas[64] = {0}, heights[64] = {0}, prev[8] = {0}, next[8] = {0};
+    size_t tinc_i = 0;
+    long long winding = 0;
+
+    for (size_t i = 0; i < nb; i++) {
+        bin bn = bins[i];
+        for (size_t k = bn.start; k < bn.end; k++) {
+            const increment *inc = &r->inc[k];
+            unsigned x = (unsigned)(uint16_t)inc->x & 7u; /* (x as usize).rem_euclid(8) */
+            unsigned y = (unsigned)(uint16_t)inc->y & 7u;
+            areas[y * 8 + x] += inc->area;
+            heights[y * 8 + x] += inc->height;
+        }
+        if (i + 1 == nb || bins[i + 1].tile_x != bn.tile_x || bins[i + 1].tile_y != bn.tile_y) {
+            uint8_t tile[64];
+            float cov[64];
+            for (int y = 0; y < 8; y++) {
+                float accum = prev[y];
+                for (int x = 0; x < 8; x++) {
+                    float c = fabsf(accum + areas[y * 8 + x]);
+                    cov[y * 8 + x] = c;
+                    tile[y * 8 + x] = f2u8(rmin(c * 256.0f, 255.0f));
+                    accum += heights[y * 8 + x];
+                }
+                next[y] = accum;
+            }
+            coll_tile(out, (int16_t)(bn.tile_x * 8), (int16_t)(bn.tile_y * 8), tile, cov);
+
+            memset(areas, 0, sizeof areas);
+            memset(heights, 0, sizeof heights);
+            if (i + 1 < nb && bins[i + 1].tile_y == bn.tile_y) memcpy(prev, next, sizeof prev);
+            else memset(prev, 0, sizeof prev);
+            memset(next, 0, sizeof next);
+
+            if (i + 1 < nb && bins[i + 1].tile_y == bn.tile_y && bins[i + 1].tile_x > bn.tile_x + 1) {
+                while (tinc_i < r->n_tinc) {
+                    tile_increment t = ti[tinc_i].t;
+                    if (t.tile_y > bn.tile_y || (t.tile_y == bn.tile_y && t.tile_x > bn.tile_x)) break;
+                    winding += t.sign;
+                    tinc_i++;
+                }
+                if (winding != 0) {
+                    int16_t width = (int16_t)(bins[i + 1].tile_x - bn.tile_x - 1);
+                    coll_span(out, (int16_t)((bn.tile_x + 1) * 8), (int16_t)(bn.tile_y * 8),
+                              (uint16_t)((uint16_t)width * 8u));
+                }
+            }
+        }
+    }
+    free(bins);
+    free(ti);
+}
+
+/* ------------------------------------------------------------------ */
+/* Batch driver: each raster is Rasterizer::new -> fill* -> finish      */
+/* ------------------------------------------------------------------ */
+static const int FLOATS_PER_VERB[6] = {2, 2, 4, 6, 5, 0};
+
+typedef struct {
+    collector c;
+    uint64_t n_lines, n_inc, n_tinc;
+    float *lines; uint32_t *line_ninc; size_t n_cap_lines;
+    int error;
+} raster_out;
+
+static void run_raster(const ochre_oracle_batch *bt, const uint64_t *cmd_float_off, uint32_t ri,
+                       int want_cov, int capture, raster_out *ro) {
+    rasterizer r;
+    rasterizer_init(&r);
+    r.capture_lines = capture;
+    memset(&ro->c, 0, sizeof ro->c);
+    ro->c.want_cov = want_cov;
+    uint32_t f0 = bt->raster_fill_off ? bt->raster_fill_off[ri] : ri;
+    uint32_t f1 = bt->raster_fill_off ? bt->raster_fill_off[ri + 1] : ri + 1;
+    for (uint32_t f = f0; f < f1 && !r.error; f++) {
+        const float *xf = bt->fill_xf + 6 * (size_t)f;
+        int raw = bt->fill_flags ? (bt->fill_flags[f] & 1) : 0;
+        for (uint32_t c = bt->fill_cmd_off[f]; c < bt->fill_cmd_off[f + 1] && !r.error; c++) {
+            uint8_t verb = bt->verbs[c];
+            const float *fp = bt->pts + cmd_float_off[c];
+            vec2 p[3];
+            float w = 0.0f;
+            int np = 0;
+            switch (verb) {
+            case OCHRE_ORACLE_MOVE: case OCHRE_ORACLE_LINE: np = 1; break;
+            case OCHRE_ORACLE_QUADRATIC: np = 2; break;
+            case OCHRE_ORACLE_CUBIC: np = 3; break;
+            case OCHRE_ORACLE_CONIC: np = 2; w = fp[4]; break;
+            default: np = 0; break;
+            }
+            for (int k = 0; k < np; k++) {
+                p[k] = v2(fp[2 * k], fp[2 * k + 1]);
+                if (!raw) p[k] = xf_apply(xf, p[k]); /* PathCmd::transform, path.rs:16-37 */
+            }
+            command(&r, verb, p, w);
+        }
+    }
+    if (!r.error) finish(&r, &ro->c);
+    ro->n_lines = r.n_lines;
+    ro->n_inc = r.n_inc;
+    ro->n_tinc = r.n_tinc;
+    ro->error = r.error ? r.error : ro->c.error;
+    if (capture) {
+        ro->lines = r.lines; ro->line_ninc = r.line_ninc; ro->n_cap_lines = r.n_lines_cap_used;
+        r.lines = NULL; r.line_ninc = NULL;
+    }
+    rasterizer_free(&r);
+}
+
+typedef struct {
+    const ochre_oracle_batch *bt;
+    const uint64_t *cmd_float_off;
+    raster_out *outs;
+    atomic_uint next;
+    int want_cov, capture;
+} pool_ctx;
+
+static void *worker(void *arg) {
+    pool_ctx *pc = (pool_ctx *)arg;
+    for (;;) {
+        unsigned ri = atomic_fetch_add(&pc->next, 1u);
+        if (ri >= pc->bt->n_rasters) break;
+        run_raster(pc->bt, pc->cmd_float_off, ri, pc->want_cov, pc->capture, &pc->outs[ri]);
+    }
+    return NULL;
+}
+
+static int validate(const ochre_oracle_batch *bt, uint64_t **off_out) {
+    uint64_t *off = (uint64_t *)malloc((bt->n_cmds + 1) * sizeof(uint64_t));
+    if (!off) return OCHRE_ORACLE_E_NOMEM;
+    uint64_t acc = 0;
+    for (uint64_t c = 0; c < bt->n_cmds; c++) {
+        if (bt->verbs[c] > 5) { free(off); return OCHRE_ORACLE_E_INVALID; }
+        off[c] = acc;
+        acc += (uint64_t)FLOATS_PER_VERB[bt->verbs[c]];
+    }
+    off[bt->n_cmds] = acc;
+    if (acc > bt->n_floats) { free(off); return OCHRE_ORACLE_E_INVALID; }
+    if (bt->fill_cmd_off[0] != 0 || bt->fill_cmd_off[bt->n_fills] != bt->n_cmds) { free(off); return OCHRE_ORACLE_E_INVALID; }
+    *off_out = off;
+    return 0;
+}
+
+int ochre_oracle_run(const ochre_oracle_batch *bt, int threads, int flags, ochre_oracle_result **res_out) {
+    *res_out = NULL;
+    uint64_t *off = NULL;
+    int st = validate(bt, &off);
+    if (st) return st;
+    raster_out *outs = (raster_out *)calloc(bt->n_rasters ? bt->n_rasters : 1, sizeof(raster_out));
+    if (!outs) { free(off); return OCHRE_ORACLE_E_NOMEM; }
+    int want_cov = (flags & OCHRE_ORACLE_WANT_COV) != 0;
+    int capture = (flags & OCHRE_ORACLE_CAPTURE_LINES) != 0;
+
+    if (threads <= 1) {
+        for (uint32_t ri = 0; ri < bt->n_rasters; ri++) run_raster(bt, off, ri, want_cov, capture, &outs[ri]);
+    } else {
+        pool_ctx pc;
+        pc.bt = bt; pc.cmd_float_off = off; pc.outs = outs; pc.want_cov = want_cov; pc.capture = capture;
+        atomic_init(&pc.next, 0u);
+        pthread_t *th = (pthread_t *)malloc((size_t)threads * sizeof(pthread_t));
+        int started = 0;
+        for (int i = 0; th && i < threads; i++) {
+            if (pthread_create(&th[i], NULL, worker, &pc) == 0) started++;
+        }
+        if (started == 0) worker(&pc);
+        for (int i = 0; i < started; i++) pthread_join(th[i], NULL);
+        free(th);
+    }
+    free(off);
+
+    /* Concatenate per-raster outputs in raster order. */
+    ochre_oracle_result *res = (ochre_oracle_result *)calloc(1, sizeof *res);
+    if (!res) { st = OCHRE_ORACLE_E_NOMEM; goto cleanup; }
+    res->n_rasters = bt->n_rasters;
+    res->raster_tile_off = (uint64_t *)calloc(bt->n_rasters + 1, sizeof(uint64_t));
+    res->raster_span_off = (uint64_t *)calloc(bt->n_rasters + 1, sizeof(uint64_t));
+    res->raster_line_off = (uint64_t *)calloc(bt->n_rasters + 1, sizeof(uint64_t));
+    res->raster_stats = (uint64_t *)calloc(3 * (size_t)bt->n_rasters + 1, sizeof(uint64_t));
+    if (!res->raster_tile_off || !res->raster_span_off || !res->raster_line_off || !res->raster_stats) { st = OCHRE_ORACLE_E_NOMEM; goto cleanup; }
+    uint64_t nt = 0, ns = 0, nl = 0;
+    for (uint32_t ri = 0; ri < bt->n_rasters; ri++) {
+        if (outs[ri].error && !st) { st = outs[ri].error; res->error_raster = ri; }
+        res->raster_tile_off[ri] = nt; res->raster_span_off[ri] = ns; res->raster_line_off[ri] = nl;
+        nt += outs[ri].c.n_tiles; ns += outs[ri].c.n_spans; nl += outs[ri].n_cap_lines;
+        res->raster_stats[3 * ri] = outs[ri].n_lines;
+        res->raster_stats[3 * ri + 1] = outs[ri].n_inc;
+        res->raster_stats[3 * ri + 2] = outs[ri].n_tinc;
+    }
+    res->raster_tile_off[bt->n_rasters] = nt;
+    res->raster_span_off[bt->n_rasters] = ns;
+    res->raster_line_off[bt->n_rasters] = nl;
+    res->n_tiles = nt; res->n_spans = ns; res->n_lines = nl;
+    res->tile_xy = (int16_t *)malloc((nt ? nt : 1) * 2 * sizeof(int16_t));
+    res->tile_alpha = (uint8_t *)malloc((nt ? nt : 1) * 64);
+    res->tile_cov = want_cov ? (float *)malloc((nt ? nt : 1) * 64 * sizeof(float)) : NULL;
+    res->span_xy = (int16_t *)malloc((ns ? ns : 1) * 2 * sizeof(int16_t));
+    res->span_w = (uint16_t *)malloc((ns ? ns : 1) * sizeof(uint16_t));
+    res->span_tile = (uint32_t *)malloc((ns ? ns : 1) * sizeof(uint32_t));
+    res->lines = capture ? (float *)malloc((nl ? nl : 1) * 4 * sizeof(float)) : NULL;
+    res->line_ninc = capture ? (uint32_t *)malloc((nl ? nl : 1) * sizeof(uint32_t)) : NULL;
+    if (!res->tile_xy || !res->tile_alpha || (want_cov && !res->tile_cov) || !res->span_xy || !res->span_w ||
+        !res->span_tile || (capture && (!res->lines || !res->line_ninc))) { st = OCHRE_ORACLE_E_NOMEM; goto cleanup; }
+    for (uint32_t ri = 0; ri < bt->n_rasters; ri++) {
+        collector *c = &outs[ri].c;
+        uint64_t t0 = res->raster_tile_off[ri], s0 = res->raster_span_off[ri], l0 = res->raster_line_off[ri];
+        if (c->n_tiles) {
+            memcpy(res->tile_xy + 2 * t0, c->tile_xy, c->n_tiles * 2 * sizeof(int16_t));
+            memcpy(res->tile_alpha + 64 * t0, c->tile_alpha, c->n_tiles * 64);
+            if (want_cov) memcpy(res->tile_cov + 64 * t0, c->tile_cov, c->n_tiles * 64 * sizeof(float));
+        }
+        for (size_t s = 0; s < c->n_spans; s++) {
+            res->span_xy[2 * (s0 + s)] = c->span_xy[2 * s];
+            res->span_xy[2 * (s0 + s) + 1] = c->span_xy[2 * s + 1];
+            res->span_w[s0 + s] = c->span_w[s];
+            res->span_tile[s0 + s] = (uint32_t)(t0 + c->span_tile[s]);
+        }
+        if (capture && outs[ri].n_cap_lines) {
+            memcpy(res->lines + 4 * l0, outs[ri].lines, outs[ri].n_cap_lines * 4 * sizeof(float));
+            memcpy(res->line_ninc + l0, outs[ri].line_ninc, outs[ri].n_cap_lines * sizeof(uint32_t));
+        }
+    }
+cleanup:
+    for (uint32_t ri = 0; ri < bt->n_rasters; ri++) {
+        free(outs[ri].c.tile_xy); free(outs[ri].c.tile_alpha); free(outs[ri].c.tile_cov);
+        free(outs[ri].c.span_xy); free(outs[ri].c.span_w); free(outs[ri].c.span_tile);
+        free(outs[ri].lines); free(outs[ri].line_ninc);
+    }
+    free(outs);
+    if (st && st != OCHRE_ORACLE_E_LIMIT && res) { ochre_oracle_free(res); res = NULL; }
+    *res_out = res;
+    return st;
+}
+
+void ochre_oracle_free(ochre_oracle_result *r) {
+    if (!r) return;
+    free(r->tile_xy); free(r->tile_alpha); free(r->tile_cov);
+    free(r->span_xy); free(r->span_w); free(r->span_tile);
+    free(r->raster_tile_off); free(r->raster_span_off); free(r->raster_line_off); free(r->raster_stats);
+    free(r->lines); free(r->line_ninc);
+    free(r);
+}

@@ -1,0 +1,73 @@
+/*
+ * ORACLE — test infrastructure only (CPU restatement of ochre 0.2.0's
+ * rasterizer; see ochre_oracle.c).  Parity with the reference: unpinned
+ * (the Rust reference cannot be built here and ships no golden vectors).
+ */
+#ifndef OCHRE_ORACLE_H
+#define OCHRE_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* PathCmd discriminants (path.rs:5-12); same numbering as the C-ABI. */
+enum {
+    OCHRE_ORACLE_MOVE = 0,
+    OCHRE_ORACLE_LINE = 1,
+    OCHRE_ORACLE_QUADRATIC = 2,
+    OCHRE_ORACLE_CUBIC = 3,
+    OCHRE_ORACLE_CONIC = 4,
+    OCHRE_ORACLE_CLOSE = 5,
+};
+
+enum {
+    OCHRE_ORACLE_E_INVALID = 1,
+    OCHRE_ORACLE_E_NOMEM = 5,
+    OCHRE_ORACLE_E_LIMIT = 6,
+};
+
+enum {
+    OCHRE_ORACLE_WANT_COV = 1,      /* also return |accum + area| per tile pixel */
+    OCHRE_ORACLE_CAPTURE_LINES = 2, /* also return every line_to segment */
+};
+
+/* Same layout as the product's ochre_batch (host pointers). */
+typedef struct ochre_oracle_batch {
+    const uint8_t *verbs;
+    uint64_t n_cmds;
+    const float *pts;
+    uint64_t n_floats;
+    const uint32_t *fill_cmd_off;    /* n_fills + 1 */
+    const float *fill_xf;            /* 6 per fill */
+    const uint8_t *fill_flags;       /* bit0: commands are not transformed; may be NULL */
+    uint32_t n_fills;
+    const uint32_t *raster_fill_off; /* n_rasters + 1; NULL means one fill per raster */
+    uint32_t n_rasters;
+} ochre_oracle_batch;
+
+typedef struct ochre_oracle_result {
+    uint32_t n_rasters;
+    uint64_t n_tiles, n_spans, n_lines;
+    int16_t *tile_xy;        /* 2 per tile */
+    uint8_t *tile_alpha;     /* 64 per tile */
+    float *tile_cov;         /* 64 per tile, or NULL */
+    int16_t *span_xy;        /* 2 per span */
+    uint16_t *span_w;
+    uint32_t *span_tile;     /* global index of the tile the span follows */
+    uint64_t *raster_tile_off, *raster_span_off, *raster_line_off; /* n_rasters + 1 */
+    uint64_t *raster_stats;  /* 3 per raster: walked lines, increments, tile increments */
+    float *lines;            /* 4 per captured line (x0, y0, x1, y1), or NULL */
+    uint32_t *line_ninc;     /* increments per captured line */
+    uint32_t error_raster;
+} ochre_oracle_result;
+
+int ochre_oracle_run(const ochre_oracle_batch *batch, int threads, int flags, ochre_oracle_result **out);
+void ochre_oracle_free(ochre_oracle_result *r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,52 @@
+"""Comparison of a GPU result with the oracle's (test infrastructure).
+
+The bar: tile positions, tile counts per raster, span positions/widths and
+the tile each span follows are bit-exact; every alpha byte is within 1 LSB
+(the reference's unstable sorts leave the f32 summation order inside a tile
+unspecified, so 1 LSB is the tightest meaningful bound).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+ALPHA_TOL_LSB = 1
+
+
+def compare(gpu: dict, ref: dict, n_rasters: int) -> dict:
+    """Raises AssertionError on any structural mismatch or alpha > 1 LSB;
+    returns diff statistics."""
+    for k in ("raster_tile_off", "raster_span_off"):
+        g = np.asarray(gpu[k], dtype=np.int64)
+        r = np.asarray(ref[k], dtype=np.int64)
+        assert g.shape == r.shape == (n_rasters + 1,), (k, g.shape, r.shape)
+        if not np.array_equal(g, r):
+            bad = int(np.flatnonzero(g != r)[0])
+            raise AssertionError(f"{k} differs first at raster {bad}: gpu {g[bad]} oracle {r[bad]}")
+    assert gpu["tile_xy"].shape == ref["tile_xy"].shape, (gpu["tile_xy"].shape, ref["tile_xy"].shape)
+    if not np.array_equal(gpu["tile_xy"], ref["tile_xy"]):
+        bad = int(np.flatnonzero(np.any(gpu["tile_xy"] != ref["tile_xy"], axis=1))[0])
+        raise AssertionError(f"tile position differs at tile {bad}: gpu {gpu['tile_xy'][bad]} oracle {ref['tile_xy'][bad]}")
+    for k in ("span_xy", "span_w", "span_tile"):
+        g, r = np.asarray(gpu[k]), np.asarray(ref[k])
+        assert g.shape == r.shape, (k, g.shape, r.shape)
+        if not np.array_equal(g.astype(np.int64), r.astype(np.int64)):
+            bad = int(np.flatnonzero((g != r).reshape(len(g), -1).any(axis=1))[0])
+            raise AssertionError(f"{k} differs at span {bad}: gpu {g[bad]} oracle {r[bad]}")
+    ga = gpu["tile_alpha"].astype(np.int16)
+    ra = ref["tile_alpha"].astype(np.int16)
+    d = np.abs(ga - ra)
+    max_lsb = int(d.max()) if d.size else 0
+    if max_lsb > ALPHA_TOL_LSB:
+        t, c = np.unravel_index(int(np.argmax(d)), d.shape)
+        raise AssertionError(f"alpha differs by {max_lsb} LSB at tile {t} cell {c} "
+                             f"(gpu {ga[t, c]} oracle {ra[t, c]}, tile at {ref['tile_xy'][t]})")
+    stats = {
+        "tiles": int(len(ra)),
+        "spans": int(len(ref["span_w"])),
+        "max_lsb": max_lsb,
+        "diff_fraction": float((d > 0).mean()) if d.size else 0.0,
+    }
+    if "tile_cov" in gpu and "tile_cov" in ref:
+        e = np.abs(gpu["tile_cov"].astype(np.float64) - ref["tile_cov"].astype(np.float64))
+        stats["cov_max_abs_vs_oracle_f32"] = float(e.max()) if e.size else 0.0
+    return stats

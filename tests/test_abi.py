@@ -1,0 +1,57 @@
+"""CPU tests of the C-ABI library: it builds for sm_103a, loads, and exports
+every entry point include/ochre_gpu.h declares (no compute without a GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from ochre_gb300 import _lib, build
+from ochre_gb300 import batch as B
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", h)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            src = re.sub(r"//[^\n]*", "", src)
+            names |= set(re.findall(r"\b(ochre_\w+)\s*\(", src))
+    return {n for n in names if not n.endswith("_fn")}
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    path = build.build()
+    assert os.path.exists(path)
+    lib = ctypes.CDLL(path)
+    declared = _declared()
+    assert "ochre_gpu_rasterize" in declared and "ochre_rasterizer_finish" in declared
+    missing = [n for n in sorted(declared) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(_lib.EXPORTS) <= declared
+
+
+def test_status_strings_without_gpu():
+    assert _lib.status_string(_lib.OK) == "ok"
+    assert "invalid" in _lib.status_string(_lib.E_INVALID)
+
+
+def test_header_constants_match_python():
+    src = open(os.path.join(ROOT, "include", "ochre_gpu.h")).read()
+    for name, val in [("OCHRE_MOVE", B.MOVE), ("OCHRE_LINE", B.LINE), ("OCHRE_QUADRATIC", B.QUADRATIC),
+                      ("OCHRE_CUBIC", B.CUBIC), ("OCHRE_CONIC", B.CONIC), ("OCHRE_CLOSE", B.CLOSE)]:
+        assert re.search(rf"{name}\s*=\s*{val}\b", src), name
+    assert re.search(r"OCHRE_FILL_RAW\s+1u", src)
+    assert re.search(r"OCHRE_TILE_SIZE\s+8\b", src)
+
+
+def test_create_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from ochre_gb300 import GpuContext
+    with pytest.raises(_lib.OchreError):
+        GpuContext(0)

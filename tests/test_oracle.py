@@ -1,0 +1,132 @@
+"""CPU tests of the oracle: pinned against hand-derived answers of the
+reference's semantics, against an independent Python restatement, and against
+the committed golden fixtures."""
+import numpy as np
+import pytest
+
+import oracle
+import oracle_py
+from golden.make_golden import NAMES, load
+from ochre_gb300 import workloads as W
+
+
+def _raster(r, i):
+    t0, t1 = int(r["raster_tile_off"][i]), int(r["raster_tile_off"][i + 1])
+    s0, s1 = int(r["raster_span_off"][i]), int(r["raster_span_off"][i + 1])
+    return (r["tile_xy"][t0:t1], r["tile_alpha"][t0:t1], r["span_xy"][s0:s1], r["span_w"][s0:s1],
+            r["span_tile"][s0:s1] - t0)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_reproduces_golden(name):
+    b, exp = load(name)
+    r = oracle.run(b, want_cov=True)
+    assert r["status"] == 0
+    for k, v in exp.items():
+        assert np.array_equal(r[k], v), k
+
+
+def test_known_answer_empty_raster():
+    # rasterizer.rs:194-208: no increments -> one all-zero tile at (0, 0)
+    from ochre_gb300.batch import BatchBuilder
+    b = BatchBuilder().begin_raster().build()
+    r = oracle.run(b)
+    assert r["tile_xy"].tolist() == [[0, 0]]
+    assert not r["tile_alpha"].any()
+    assert len(r["span_w"]) == 0
+
+
+def test_known_answer_pixel_square():
+    # Square (1,1)-(3,3): the right edge pushes area +1 per cell at x=3, the
+    # left edge -1 at x=1; accum = -1 between them -> |.| = 1 -> 255.
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    b = BatchBuilder().fill([MOVE, LINE, LINE, LINE, CLOSE], [1, 1, 3, 1, 3, 3, 1, 3], raw=True).build()
+    r = oracle.run(b)
+    expect = np.zeros((8, 8), np.uint8)
+    expect[1:3, 1:3] = 255
+    assert r["tile_xy"].tolist() == [[0, 0]]
+    assert np.array_equal(r["tile_alpha"][0].reshape(8, 8), expect)
+
+
+def test_known_answer_rectangle_spans():
+    # Rectangle x 4..60, y 4..28: tile rows 0 and 3 are crossed by the
+    # horizontal edges (zero-height increments still create tiles); rows 1, 2
+    # hold only the left (tile 0) and right (tile 7) edge tiles.  Crossings of
+    # tile-row boundaries: left edge (going up) -1 at tile_x 0, right edge
+    # (going down) +1 at tile_x 7; the winding after tile (0, ty) is -1, so a
+    # span of 6 tiles (48 px) follows tile 0 on rows 1 and 2.
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    b = BatchBuilder().fill([MOVE, LINE, LINE, LINE, CLOSE], [4, 4, 60, 4, 60, 28, 4, 28]).build()
+    r = oracle.run(b)
+    xy, alpha, sxy, sw, st = _raster(r, 0)
+    expect_tiles = ([(8 * i, 0) for i in range(8)] + [(0, 8), (56, 8), (0, 16), (56, 16)]
+                    + [(8 * i, 24) for i in range(8)])
+    assert [tuple(t) for t in xy.tolist()] == expect_tiles
+    assert sxy.tolist() == [[8, 8], [8, 16]]
+    assert sw.tolist() == [48, 48]
+    assert st.tolist() == [8, 10]
+    left = alpha[8].reshape(8, 8)
+    right = alpha[9].reshape(8, 8)
+    assert np.array_equal(left, np.tile([0, 0, 0, 0, 255, 255, 255, 255], (8, 1)))
+    assert np.array_equal(right, np.tile([255, 255, 255, 255, 0, 0, 0, 0], (8, 1)))
+
+
+def test_known_answer_half_pixel_edge():
+    # A vertical edge at x = 2.5 from y=0 down to y=8 and back along x = 0:
+    # cell x=2 gets area 0.5*h*((3-2.5)+(3-2.5)) = 0.5 per row -> |-1 + 0.5|
+    # ... with accum -1 from the left edge: coverage 0.5 -> 128.
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    b = BatchBuilder().fill([MOVE, LINE, LINE, LINE, CLOSE], [0, 0, 2.5, 0, 2.5, 8, 0, 8], raw=True).build()
+    r = oracle.run(b)
+    a = r["tile_alpha"][0].reshape(8, 8)
+    assert np.array_equal(a, np.tile([255, 255, 128, 0, 0, 0, 0, 0], (8, 1)))
+
+
+@pytest.mark.parametrize("gen,kw", [
+    (W.readme_path, {}),
+    (W.cubic_boxes, dict(n_paths=2)),
+    (W.glyph_run, dict(n_paths=12)),
+    (W.uneven_mix, dict(n_paths=3, max_seg=40)),
+    (W.diff_scenes, dict(n_scenes=1, min_paths=3, max_paths=3, max_seg=12)),
+])
+def test_oracle_matches_python_restatement(gen, kw):
+    b = gen(**kw)
+    r = oracle.run(b)
+    for i in range(b.n_rasters):
+        tiles, spans, ninc = oracle_py.rasterize(oracle_py.commands_of_batch(b, i))
+        xy, alpha, sxy, sw, st = _raster(r, i)
+        assert [tuple(t) for t in xy.tolist()] == [t[:2] for t in tiles]
+        assert np.array_equal(alpha, np.array([np.frombuffer(t[2], np.uint8) for t in tiles]).reshape(-1, 64))
+        assert [(int(a), int(c), int(w), int(t)) for (a, c), w, t in zip(sxy.tolist(), sw, st)] == spans
+        assert int(r["raster_stats"][i, 1]) == ninc
+
+
+def test_edge_cases_match_python_restatement():
+    import edge_cases
+    b, names = edge_cases.edge_batch()
+    r = oracle.run(b)
+    for i, name in enumerate(names):
+        tiles, spans, _ = oracle_py.rasterize(oracle_py.commands_of_batch(b, i))
+        xy, alpha, sxy, sw, st = _raster(r, i)
+        assert [tuple(t) for t in xy.tolist()] == [t[:2] for t in tiles], name
+        assert np.array_equal(alpha, np.array([np.frombuffer(t[2], np.uint8) for t in tiles]).reshape(-1, 64)), name
+        assert len(spans) == len(sw), name
+
+
+def test_oracle_threads_agree():
+    b = W.glyph_run(n_paths=300)
+    r1 = oracle.run(b, threads=1)
+    r4 = oracle.run(b, threads=4)
+    for k in ("tile_xy", "tile_alpha", "span_xy", "span_w", "span_tile", "raster_tile_off"):
+        assert np.array_equal(r1[k], r4[k]), k
+
+
+def test_oracle_line_capture_counts():
+    b = W.cubic_boxes(n_paths=3)
+    r = oracle.run(b, capture_lines=True)
+    # every line ends where the next one starts within a raster
+    for i in range(b.n_rasters):
+        l0, l1 = int(r["raster_line_off"][i]), int(r["raster_line_off"][i + 1])
+        L = r["lines"][l0:l1]
+        assert np.array_equal(L[1:, :2], L[:-1, 2:])
+    assert int(r["line_ninc"].sum()) == int(r["raster_stats"][:, 1].sum())

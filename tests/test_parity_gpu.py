@@ -1,0 +1,160 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle.
+
+Tile/span structure must be bit-exact and alpha within 1 LSB (compare.py).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from compare import compare
+from golden.make_golden import NAMES, load
+from ochre_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_golden_host_path(gpu_ctx, name):
+    b, exp = load(name)
+    gpu_ctx.set_want_cov(True)
+    try:
+        got = gpu_ctx.rasterize(b)
+    finally:
+        gpu_ctx.set_want_cov(False)
+    st = compare(got, exp, b.n_rasters)
+    # pre-quantisation coverage vs the oracle's f32 coverage (summation order only)
+    assert st["cov_max_abs_vs_oracle_f32"] < 1e-3, st
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_golden_device_path(gpu_ctx, name):
+    from ochre_gb300 import DeviceBatch
+    b, exp = load(name)
+    db = DeviceBatch(b)
+    r = gpu_ctx.rasterize_device(db)
+    got = gpu_ctx.device_result_to_numpy(r, b.n_rasters)
+    compare(got, exp, b.n_rasters)
+
+
+@pytest.mark.parametrize("gen,kw", [
+    (W.cubic_boxes, dict(n_paths=60)),
+    (W.glyph_run, dict(n_paths=3000)),
+    (W.uneven_mix, dict(n_paths=150)),
+    (W.diff_union, dict()),
+    (W.diff_scenes, dict(n_scenes=6)),
+])
+def test_workload_parity(gpu_ctx, gen, kw):
+    b = gen(**kw)
+    ref = oracle.run(b, threads=8)
+    got = gpu_ctx.rasterize(b)
+    st = compare(got, ref, b.n_rasters)
+    assert st["diff_fraction"] < 0.01, st
+
+
+def test_line_and_entry_counts_match_oracle(gpu_ctx):
+    b = W.cubic_boxes(n_paths=5)
+    ref = oracle.run(b, capture_lines=True)
+    gpu_ctx.rasterize(b)
+    s = gpu_ctx.stats()
+    assert s["n_lines"] == len(ref["lines"])
+    assert s["n_tiles"] == len(ref["tile_xy"])
+
+
+def test_readme_through_rasterizer_api():
+    from ochre_gb300 import PathCmd, Rasterizer, TileBuilder, Transform, Vec2
+
+    class Collect(TileBuilder):
+        def __init__(self):
+            self.events = []
+
+        def tile(self, x, y, data):
+            self.events.append(("tile", x, y, bytes(data)))
+
+        def span(self, x, y, width):
+            self.events.append(("span", x, y, width))
+
+    r = Rasterizer()
+    r.fill([
+        PathCmd.Move(Vec2(400.0, 300.0)),
+        PathCmd.Quadratic(Vec2(500.0, 200.0), Vec2(400.0, 100.0)),
+        PathCmd.Cubic(Vec2(350.0, 150.0), Vec2(100.0, 250.0), Vec2(400.0, 300.0)),
+        PathCmd.Close(),
+    ], Transform.id())
+    c = Collect()
+    r.finish(c)
+    ref = oracle.run(W.readme_path())
+    tiles = [e for e in c.events if e[0] == "tile"]
+    assert [(e[1], e[2]) for e in tiles] == [tuple(t) for t in ref["tile_xy"].tolist()]
+    a = np.array([np.frombuffer(e[3], np.uint8) for e in tiles]).astype(int)
+    assert np.abs(a - ref["tile_alpha"].astype(int)).max() <= 1
+    # callback order: each span right after the tile it follows
+    order, ti = [], -1
+    for e in c.events:
+        if e[0] == "tile":
+            ti += 1
+        else:
+            order.append((ti, e[1], e[2], e[3]))
+    assert order == [(int(t), int(x), int(y), int(w)) for t, (x, y), w in
+                     zip(ref["span_tile"], ref["span_xy"].tolist(), ref["span_w"])]
+
+
+def test_raw_commands_and_multiple_fills():
+    from ochre_gb300 import PathCmd, Rasterizer, TileBuilder, Transform, Vec2, Mat2x2
+    from ochre_gb300.batch import BatchBuilder, CUBIC, LINE, MOVE, QUADRATIC, CLOSE
+
+    class Collect(TileBuilder):
+        def __init__(self):
+            self.tiles, self.spans = [], []
+
+        def tile(self, x, y, data):
+            self.tiles.append((x, y, bytes(data)))
+
+        def span(self, x, y, w):
+            self.spans.append((x, y, w))
+
+    xf = Transform.new(Mat2x2.new(1.5, 0.25, -0.3, 1.2), Vec2(40.0, 30.0))
+    r = Rasterizer()
+    r.move_to(Vec2(3.5, 3.5))
+    r.line_to(Vec2(70.25, 9.75))
+    r.command(PathCmd.Quadratic(Vec2(90.0, 40.0), Vec2(40.0, 60.0)))
+    r.fill([PathCmd.Line(Vec2(10.0, 10.0)), PathCmd.Cubic(Vec2(30.0, -20.0), Vec2(60.0, 40.0), Vec2(0.0, 30.0)),
+            PathCmd.Close()], xf)
+    c = Collect()
+    r.finish(c)
+    bb = BatchBuilder()
+    bb.fill([MOVE, LINE, QUADRATIC], [3.5, 3.5, 70.25, 9.75, 90.0, 40.0, 40.0, 60.0], raw=True)
+    bb.fill([LINE, CUBIC, CLOSE], [10.0, 10.0, 30.0, -20.0, 60.0, 40.0, 0.0, 30.0], xf.as_array())
+    ref = oracle.run(bb.build())
+    assert [(t[0], t[1]) for t in c.tiles] == [tuple(t) for t in ref["tile_xy"].tolist()]
+    assert c.spans == [(int(x), int(y), int(w)) for (x, y), w in zip(ref["span_xy"].tolist(), ref["span_w"])]
+
+
+def test_empty_batch_and_empty_rasterizer(gpu_ctx):
+    from ochre_gb300.batch import BatchBuilder
+    b = BatchBuilder().begin_raster().begin_raster().build()
+    got = gpu_ctx.rasterize(b)
+    assert got["tile_xy"].tolist() == [[0, 0], [0, 0]]
+    assert not got["tile_alpha"].any()
+    assert got["raster_tile_off"].tolist() == [0, 1, 2]
+
+
+def test_invalid_inputs_are_reported(gpu_ctx):
+    from ochre_gb300 import _lib
+    b = W.readme_path()
+    bad = b.pts.copy()
+    bad[3] = np.inf
+    b2 = type(b)(b.verbs, bad, b.fill_cmd_off, b.fill_xf, None, None, 1)
+    with pytest.raises(_lib.OchreError) as e:
+        gpu_ctx.rasterize(b2)
+    assert e.value.status == _lib.E_INVALID
+    # the context stays usable
+    got = gpu_ctx.rasterize(b)
+    compare(got, oracle.run(b), 1)
+
+
+def test_deterministic(gpu_ctx):
+    b = W.glyph_run(n_paths=2000, seed=11)
+    r1 = gpu_ctx.rasterize(b)
+    r2 = gpu_ctx.rasterize(b)
+    for k in r1:
+        assert np.array_equal(r1[k], r2[k]), k
