@@ -1,0 +1,370 @@
+"""Benchmark of the GB300 rasterization path (ochre Rasterizer::fill -> finish).
+
+Workload (default): the glyph-like text run — 100,000 independent closed
+paths of 8-40 quadratics over 1-3 contours under random affine transforms on
+a 4096x4096 canvas (seeded synthetic data, one rasterizer per path).  A step
+rasterizes the whole batch: every path's flatten -> DDA binning -> sort ->
+tile coverage -> spans, producing the tiles and spans of every path.
+
+  value  : paths/s with the batch resident in HBM (CUDA events on the
+           launching stream; L2 flushed between timed steps).
+  e2e    : paths/s through the host C-ABI entry point (ochre_gpu_rasterize)
+           from pinned host buffers, H2D of the inputs and D2H of all tiles
+           and spans inside the timed region.
+  --impl reference : the reference's CPU algorithm (the oracle restatement,
+           all host threads) on the same workload.
+
+Multi-GPU: paths are independent, so each rank rasterizes its own batch
+(weak scaling, no collective on the data path); value = all paths / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "tiles/s & paths/s batched vs plain GPU at ≤1 LSB alpha; fwd+bwd scenes/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+def make_workload(name: str, n: int, seed: int):
+    from ochre_gb300 import workloads as W
+    if name == "glyph_run":
+        return W.glyph_run(n_paths=n, seed=seed)
+    if name == "cubic_boxes":
+        return W.cubic_boxes(n_paths=n, seed=seed)
+    if name == "uneven_mix":
+        return W.uneven_mix(n_paths=n, seed=seed)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def output_bytes(n_tiles: int, n_spans: int, n_rasters: int) -> int:
+    """Compulsory output: 68 B per tile (64 alpha + 2 x i16 position), 6 B per
+    span (i16 x, i16 y, u16 width)."""
+    return 68 * n_tiles + 6 * n_spans
+
+
+def kernel_bytes(name: str, st: dict, batch) -> int:
+    """Bytes each kernel of the chain must move for its job (every input array
+    read once, every output array written once).  Used as the roofline
+    numerator of the dominant kernel."""
+    C, R = batch.n_cmds, batch.n_rasters
+    L, E, T, B, N = st["n_lines"], st["n_entries"], st["n_tiles"], st["n_bins"], st["n_spans"]
+    kb = 8 if st["key_bits"] > 32 else 4
+    if name == "cmd_scan":
+        return C * 1 + C * 12
+    if name == "flatten_count_scan":
+        return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 12 + C * 4
+    if name == "flatten_emit":
+        return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 16 + L * 20
+    if name == "dda_count_scan":
+        return L * 20 + L * 4 + R * 16
+    if name == "dda_emit":
+        return L * 28 + R * 24 + E * (kb + 4) + B * 32
+    if name == "sort_onesweep":
+        return 2 * E * (kb + 4)
+    if name == "sort_hist":
+        return E * kb
+    if name == "tile_head_scan":
+        return E * (kb + 4) + T * 4
+    if name == "tile_info":
+        return T * 4 + T * (kb + 4 + 32) + T * 24 + R * 4
+    if name == "tile_coverage":
+        return B * (4 + 32 + 16) + T * 24 * 2 + T * 68 + T * 12
+    if name == "span_scan":
+        return T * 4 + T * 8 + N * 10 + R * 4
+    return 0
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int, path: str):
+        self.path = path
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(batch, reps: int = 3) -> dict:
+    import numpy as np
+    import oracle
+    threads = os.cpu_count() or 1
+    with np.errstate(all="ignore"):
+        oracle.run(batch, threads=threads)  # warm
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            oracle.run(batch, threads=threads)
+        dt = (time.perf_counter() - t0) / reps
+    return {"value": batch.n_rasters / dt, "unit": "paths/s", "cores": threads, "kind": "port",
+            "sample": f"the full workload ({batch.n_rasters} paths) x {reps} repetitions, "
+                      f"oracle/ochre_oracle.c on {threads} threads"}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def reduce_max(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import numpy as np
+    import oracle
+    batch = make_workload(args.workload, args.n_paths, args.seed)
+    threads = os.cpu_count() or 1
+    with np.errstate(all="ignore"):
+        for _ in range(args.warmup):
+            oracle.run(batch, threads=threads)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r = oracle.run(batch, threads=threads)
+        dt = time.perf_counter() - t0
+    n_tiles = int(len(r["tile_xy"]))
+    value = batch.n_rasters * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "n_paths": batch.n_rasters, "seed": args.seed},
+        "tiles_per_s": n_tiles * args.steps / dt,
+        "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
+                         "sample": f"the full workload ({batch.n_rasters} paths) per step, "
+                                   f"oracle/ochre_oracle.c (strict-f32 restatement of the reference) on {threads} threads"},
+        "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    from ochre_gb300 import DeviceBatch, GpuContext
+
+    torch.cuda.set_device(local)
+    batch = make_workload(args.workload, args.n_paths, args.seed + 1000 * rank)
+    ctx = GpuContext(local)
+    db = DeviceBatch(batch, local)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 126 MB L2
+
+    for _ in range(max(3, args.warmup)):
+        ctx.rasterize_device(db, sp)
+    torch.cuda.synchronize()
+    st = ctx.stats()
+
+    # ---- timed: device-resident inputs ----
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks_path = os.path.join(ROOT, "gpurun_out", f"bench_clocks_r{rank}.csv") if os.path.isdir(
+        os.path.join(ROOT, "gpurun_out")) else f"/tmp/bench_clocks_r{rank}.csv"
+    barrier(ws)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    with ClockSampler(local, clocks_path) as clk:
+        for i in range(args.steps):
+            flush.fill_(i & 0xff)
+            ev[i][0].record(stream)
+            ctx.rasterize_device(db, sp)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    wall = time.perf_counter() - wall0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(step_ms) / 1000.0
+    dev_s_max = reduce_max(dev_s, ws)
+    launches = st["n_launches"] * args.steps
+
+    # ---- per-kernel profile (separate, untimed pass) ----
+    ctx.set_profile(True)
+    flush.fill_(1)
+    torch.cuda.synchronize()
+    ctx.rasterize_device(db, sp)
+    torch.cuda.synchronize()
+    prof = ctx.timings()
+    ctx.set_profile(False)
+    per = {}
+    for name, ms in prof:
+        d = per.setdefault(name, [0.0, 0])
+        d[0] += ms
+        d[1] += 1
+    total_k = sum(v[0] for v in per.values())
+    kernels = sorted(({"kernel": k, "ms": v[0], "launches": v[1], "share": v[0] / total_k if total_k else 0.0}
+                      for k, v in per.items()), key=lambda x: -x["ms"])
+    dom = kernels[0]
+    peaks, peak_kind = load_peaks()
+    peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+    dom_bytes = kernel_bytes(dom["kernel"], st, batch) / max(1, dom["launches"])
+    dom_ms = dom["ms"] / max(1, dom["launches"])
+    achieved = dom_bytes / (dom_ms / 1000.0) / 1e9 if dom_ms > 0 else 0.0
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get(dom["kernel"])
+
+    # ---- e2e: host C-ABI entry, pinned host inputs, H2D + D2H in the timed region ----
+    def pinned(a):
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t.numpy()
+
+    from ochre_gb300.batch import Batch
+    hb = Batch(pinned(batch.verbs), pinned(batch.pts), pinned(batch.fill_cmd_off), pinned(batch.fill_xf),
+               None if batch.fill_flags is None else pinned(batch.fill_flags),
+               None if batch.raster_fill_off is None else pinned(batch.raster_fill_off), batch.n_rasters)
+    h2d = (hb.verbs.nbytes + hb.pts.nbytes + hb.fill_cmd_off.nbytes + hb.fill_xf.nbytes
+           + (0 if hb.fill_flags is None else hb.fill_flags.nbytes)
+           + (0 if hb.raster_fill_off is None else hb.raster_fill_off.nbytes))
+    for _ in range(2):
+        res = ctx.rasterize(hb)
+    n_t, n_s = len(res["tile_xy"]), len(res["span_w"])
+    d2h = n_t * 68 + n_s * 10 + 2 * 4 * (batch.n_rasters + 1)
+    e2e_steps = max(1, min(args.steps, 10))
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.rasterize(hb)
+    e2e_s = reduce_max((time.perf_counter() - t0) / e2e_steps, ws)
+
+    if rank != 0:
+        ctx.close()
+        return
+    n_paths_all = batch.n_rasters * ws
+    value = n_paths_all * args.steps / dev_s_max
+    cpu = cpu_baseline(batch) if ws == 1 else None
+    comp_in = batch.input_bytes()
+    comp_out = output_bytes(st["n_tiles"], st["n_spans"], batch.n_rasters)
+    path_gbs = (comp_in + comp_out) / (dev_s / args.steps) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "n_paths_per_gpu": batch.n_rasters, "seed": args.seed,
+                   "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                   "l2": "flushed (256 MiB write) between timed steps, outside the events",
+                   "tiles_per_step": st["n_tiles"], "spans_per_step": st["n_spans"], "lines_per_step": st["n_lines"],
+                   "sort_entries_per_step": st["n_entries"], "key_bits": st["key_bits"],
+                   "sort_passes": st["sort_passes"]},
+        "tiles_per_s": st["n_tiles"] * ws * args.steps / dev_s_max,
+        "wall_s_timed_region": wall,
+        "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,
+                     "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+        "path_roofline": {"compulsory_bytes_per_step": comp_in + comp_out, "achieved_gbs": path_gbs,
+                          "frac": path_gbs / peak, "note": "input verbs+points+transforms and 68 B/tile + 6 B/span"},
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="glyph_run")
+    ap.add_argument("--n-paths", type=int, default=100_000)
+    ap.add_argument("--seed", type=int, default=2)
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        from ochre_gb300 import build
+        build.build()
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

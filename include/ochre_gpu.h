@@ -106,11 +106,21 @@ typedef struct ochre_stats {
     uint64_t n_spans;
     uint32_t key_bits;     /* significant bits of the tile sort key */
     uint32_t sort_passes;
+    uint32_t n_launches;   /* kernels launched by the run */
+    uint32_t pad;
+    uint64_t n_bins;       /* sort entries that are tile bins (runs of cells in one tile) */
 } ochre_stats;
+
+/* Device time of one kernel launch of the last run (OCHRE_CTX_PROFILE). */
+typedef struct ochre_kernel_time {
+    const char *name;      /* static string naming the kernel */
+    float ms;
+} ochre_kernel_time;
 
 typedef struct ochre_gpu_ctx ochre_gpu_ctx;
 
 #define OCHRE_CTX_WANT_COV 1u   /* also produce tile_cov */
+#define OCHRE_CTX_PROFILE 2u    /* time every kernel launch with CUDA events */
 
 /* Create a context on `device` (CUDA ordinal).  flags: OCHRE_CTX_*. */
 int ochre_gpu_create(ochre_gpu_ctx **out, int device, uint32_t flags);
@@ -128,6 +138,10 @@ int ochre_gpu_rasterize_device(ochre_gpu_ctx *ctx, const ochre_batch *in, ochre_
 int ochre_gpu_rasterize(ochre_gpu_ctx *ctx, const ochre_batch *in, ochre_result *out);
 
 int ochre_gpu_last_stats(const ochre_gpu_ctx *ctx, ochre_stats *out);
+
+/* Per-launch device times of the last run (needs OCHRE_CTX_PROFILE): writes
+ * up to `cap` entries and the total count to *n. */
+int ochre_gpu_last_timings(const ochre_gpu_ctx *ctx, ochre_kernel_time *out, uint32_t cap, uint32_t *n);
 
 /* Status text for a code. */
 const char *ochre_gpu_status_string(int status);

@@ -14,10 +14,11 @@ from . import build as _build
 
 OK, E_INVALID, E_CAPACITY, E_CUDA, E_TIMEOUT, E_NOMEM, E_LIMIT = range(7)
 CTX_WANT_COV = 1
+CTX_PROFILE = 2
 
 EXPORTS = [
     "ochre_gpu_create", "ochre_gpu_destroy", "ochre_gpu_set_flags", "ochre_gpu_rasterize_device",
-    "ochre_gpu_rasterize", "ochre_gpu_last_stats", "ochre_gpu_status_string",
+    "ochre_gpu_rasterize", "ochre_gpu_last_stats", "ochre_gpu_last_timings", "ochre_gpu_status_string",
     "ochre_rasterizer_new", "ochre_rasterizer_move_to", "ochre_rasterizer_line_to",
     "ochre_rasterizer_command", "ochre_rasterizer_fill", "ochre_rasterizer_finish", "ochre_rasterizer_free",
 ]
@@ -53,7 +54,12 @@ class Stats(ctypes.Structure):
     _fields_ = [
         ("n_lines", ctypes.c_uint64), ("n_entries", ctypes.c_uint64), ("n_tiles", ctypes.c_uint64),
         ("n_spans", ctypes.c_uint64), ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32),
+        ("n_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("n_bins", ctypes.c_uint64),
     ]
+
+
+class KernelTime(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("ms", ctypes.c_float)]
 
 
 TILE_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int16, ctypes.c_int16, ctypes.POINTER(ctypes.c_uint8))
@@ -85,6 +91,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_gpu_rasterize_device.argtypes = [vp, ctypes.POINTER(Batch), ctypes.POINTER(Result), vp]
         L.ochre_gpu_rasterize.argtypes = [vp, ctypes.POINTER(Batch), ctypes.POINTER(Result)]
         L.ochre_gpu_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+        L.ochre_gpu_last_timings.argtypes = [vp, ctypes.POINTER(KernelTime), u32, ctypes.POINTER(u32)]
         L.ochre_gpu_status_string.argtypes = [ctypes.c_int]
         L.ochre_gpu_status_string.restype = ctypes.c_char_p
         L.ochre_rasterizer_new.argtypes = [vp, ctypes.POINTER(vp)]
@@ -98,6 +105,31 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_rasterizer_free.restype = None
         _lib = L
         return L
+
+
+_cudart = None
+
+
+def memcpy_d2h(dst: int, src: int, nbytes: int) -> None:
+    """Synchronous device-to-host copy through the CUDA runtime the library
+    itself links (test and inspection helper)."""
+    global _cudart
+    if _cudart is None:
+        load()
+        for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+            try:
+                _cudart = ctypes.CDLL(name)
+                break
+            except OSError:
+                continue
+        if _cudart is None:
+            raise RuntimeError("libcudart not found")
+        _cudart.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+        _cudart.cudaDeviceSynchronize.argtypes = []
+    _cudart.cudaDeviceSynchronize()
+    err = _cudart.cudaMemcpy(dst, src, nbytes, 2)  # cudaMemcpyDeviceToHost
+    if err != 0:
+        raise RuntimeError(f"cudaMemcpy failed with error {err}")
 
 
 def status_string(status: int) -> str:

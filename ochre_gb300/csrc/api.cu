@@ -62,6 +62,43 @@ int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
     return OCHRE_OK;
 }
 
+void prof_begin(ochre_gpu_ctx* ctx, const char* name, cudaStream_t s) {
+    ctx->launches++;
+    if (!(ctx->flags & OCHRE_CTX_PROFILE)) return;
+    if (ctx->prof_used == ctx->prof.size()) {
+        ochre_gpu_ctx::Prof p{name, nullptr, nullptr};
+        if (cudaEventCreate(&p.a) != cudaSuccess || cudaEventCreate(&p.b) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        ctx->prof.push_back(p);
+    }
+    ochre_gpu_ctx::Prof& p = ctx->prof[ctx->prof_used];
+    p.name = name;
+    cudaEventRecord(p.a, s);
+}
+
+void prof_end(ochre_gpu_ctx* ctx, cudaStream_t s) {
+    if (!(ctx->flags & OCHRE_CTX_PROFILE) || ctx->prof_used >= ctx->prof.size()) return;
+    cudaEventRecord(ctx->prof[ctx->prof_used].b, s);
+    ctx->prof_used++;
+}
+
+// Converts the recorded event pairs of the finished run into timings.
+static void collect_timings(ochre_gpu_ctx* ctx, cudaStream_t s) {
+    ctx->timings.clear();
+    if (!(ctx->flags & OCHRE_CTX_PROFILE) || ctx->prof_used == 0) return;
+    cudaStreamSynchronize(s);
+    for (uint32_t i = 0; i < ctx->prof_used; i++) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, ctx->prof[i].a, ctx->prof[i].b) != cudaSuccess) {
+            cudaGetLastError();
+            ms = -1.0f;
+        }
+        ctx->timings.push_back(ochre_kernel_time{ctx->prof[i].name, ms});
+    }
+}
+
 int check_device_error(ochre_gpu_ctx* ctx) {
     const uint32_t e = host_scalars(ctx)->err;
     if (e & ERR_INVALID) return OCHRE_E_INVALID;
@@ -96,6 +133,9 @@ static int validate_host(const ochre_batch* in) {
 static int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s) {
     std::memset(out, 0, sizeof *out);
     ctx->stats = ochre_stats{};
+    ctx->prof_used = 0;
+    ctx->launches = 0;
+    ctx->timings.clear();
     OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
     const uint32_t R = in->n_rasters;
     OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
@@ -126,6 +166,8 @@ static int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* o
     ctx->stats.n_spans = N;
     ctx->stats.key_bits = bits;
     ctx->stats.sort_passes = passes;
+    ctx->stats.n_launches = ctx->launches;
+    collect_timings(ctx, s);
     out->n_tiles = T;
     out->n_spans = N;
     out->tile_xy = ctx->out_tile_xy.as<int16_t>();
@@ -194,6 +236,10 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
     HostBuf* host[] = {&ctx->h_scalars, &ctx->h_tile_xy, &ctx->h_tile_alpha, &ctx->h_tile_cov, &ctx->h_span_xy,
                        &ctx->h_span_w, &ctx->h_span_tile, &ctx->h_raster_tile_off, &ctx->h_raster_span_off};
     for (HostBuf* b : host) b->release();
+    for (auto& p : ctx->prof) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -287,6 +333,14 @@ int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result*
     out->span_tile = ctx->h_span_tile.as<uint32_t>();
     out->raster_tile_off = ctx->h_raster_tile_off.as<uint32_t>();
     out->raster_span_off = ctx->h_raster_span_off.as<uint32_t>();
+    return OCHRE_OK;
+}
+
+int ochre_gpu_last_timings(const ochre_gpu_ctx* ctx, ochre_kernel_time* out, uint32_t cap, uint32_t* n) {
+    if (!ctx || !n || (cap && !out)) return OCHRE_E_INVALID;
+    const uint32_t m = (uint32_t)ctx->timings.size();
+    for (uint32_t i = 0; i < m && i < cap; i++) out[i] = ctx->timings[i];
+    *n = m;
     return OCHRE_OK;
 }
 

@@ -223,24 +223,24 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_CUDA_TRY(ctx->raster_bbox.ensure((size_t)R * sizeof(int4)));
     OCHRE_CUDA_TRY(ctx->raster_keybase.ensure((size_t)R * 8));
     OCHRE_CUDA_TRY(ctx->raster_empty.ensure((size_t)R * 4));
-    k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(), R);
+    OCHRE_LAUNCH(ctx, "bbox_init", s, k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(), R));
     OCHRE_CUDA_TRY(cudaGetLastError());
     OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_line_ent, 0, sizeof(uint32_t), s));
     if (n_lines) {
         OCHRE_CUDA_TRY(ctx->line_ent_off.ensure((size_t)n_lines * 4));
         OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<uint32_t>)));
-        OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+        OCHRE_LAUNCH(ctx, "dda_count_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
             n_lines, LineCountIn{ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->raster_bbox.as<int4>(),
                                  &ds->err, n_lines},
             OffOut32{ctx->line_ent_off.as<uint32_t>()}, OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket,
-            &ds->n_line_ent, &ds->err, s));
+            &ds->n_line_ent, &ds->err, s)));
     }
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(R) * sizeof(ScanStatus<RasterScan>)));
-    OCHRE_CUDA_TRY(launch_scan<RasterScan>(
+    OCHRE_LAUNCH(ctx, "raster_key_scan", s, OCHRE_CUDA_TRY(launch_scan<RasterScan>(
         R, RasterIn{ctx->raster_bbox.as<int4>()},
         RasterOut{ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->raster_empty.as<uint32_t>()},
         OpRaster{}, RasterScan{0, 0, 0}, ctx->scan_status.p, &ds->ticket,
-        reinterpret_cast<RasterScan*>(&ds->keyspace), &ds->err, s));
+        reinterpret_cast<RasterScan*>(&ds->keyspace), &ds->err, s)));
     int st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
     st = check_device_error(ctx);
@@ -263,26 +263,26 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     if (n_lines) {
         const unsigned blocks = (unsigned)((n_lines + 127) / 128);
         if (ctx->keys64)
-            k_line_emit<uint64_t><<<blocks, 128, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<blocks, 128, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
                 ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(),
-                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
         else
-            k_line_emit<uint32_t><<<blocks, 128, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<blocks, 128, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
                 ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(),
-                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
         OCHRE_CUDA_TRY(cudaGetLastError());
     }
     if (hs->n_empty) {
         if (ctx->keys64)
-            k_empty_emit<uint64_t><<<(R + 255) / 256, 256, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "empty_emit", s, k_empty_emit<uint64_t><<<(R + 255) / 256, 256, 0, s>>>(
                 ctx->raster_empty.as<uint32_t>(), R, hs->n_line_ent, ctx->raster_keybase.as<uint64_t>(),
-                ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+                ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
         else
-            k_empty_emit<uint32_t><<<(R + 255) / 256, 256, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "empty_emit", s, k_empty_emit<uint32_t><<<(R + 255) / 256, 256, 0, s>>>(
                 ctx->raster_empty.as<uint32_t>(), R, hs->n_line_ent, ctx->raster_keybase.as<uint64_t>(),
-                ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>());
+                ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
         OCHRE_CUDA_TRY(cudaGetLastError());
     }
     return OCHRE_OK;

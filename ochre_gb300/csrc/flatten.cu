@@ -265,11 +265,11 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n) * sizeof(ScanStatus<CmdScan>)));
 
     CmdScan total_id{0, 0, 0};
-    OCHRE_CUDA_TRY(launch_scan<CmdScan>(n, CmdIn{in->verbs, &ds->err},
+    OCHRE_LAUNCH(ctx, "cmd_scan", s, OCHRE_CUDA_TRY(launch_scan<CmdScan>(n, CmdIn{in->verbs, &ds->err},
                                         CmdOut{ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
                                                ctx->cmd_ep.as<uint32_t>()},
                                         OpCmd{}, total_id, ctx->scan_status.p, &ds->ticket,
-                                        reinterpret_cast<CmdScan*>(&ds->n_floats), &ds->err, s));
+                                        reinterpret_cast<CmdScan*>(&ds->n_floats), &ds->err, s)));
 
     // The verbs must not consume more floats than the point stream holds:
     // check before any kernel reads a point.
@@ -283,9 +283,9 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
     BatchView b{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                 in->n_fills, in->n_rasters, n, ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
                 ctx->cmd_ep.as<uint32_t>()};
-    OCHRE_CUDA_TRY(launch_scan<uint32_t>(n, CountIn{b, &ds->err}, OffOut{ctx->cmd_line_off.as<uint32_t>()},
+    OCHRE_LAUNCH(ctx, "flatten_count_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(n, CountIn{b, &ds->err}, OffOut{ctx->cmd_line_off.as<uint32_t>()},
                                          OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_lines,
-                                         &ds->err, s));
+                                         &ds->err, s)));
     st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
     st = check_device_error(ctx);
@@ -297,8 +297,8 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
     OCHRE_CUDA_TRY(ctx->lines.ensure((size_t)L * sizeof(float4)));
     OCHRE_CUDA_TRY(ctx->line_raster.ensure((size_t)L * 4));
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    k_cmd_emit<<<blocks, 256, 0, s>>>(b, ctx->cmd_line_off.as<uint32_t>(), L, ctx->lines.as<float4>(),
-                                      ctx->line_raster.as<uint32_t>(), &ds->err);
+    OCHRE_LAUNCH(ctx, "flatten_emit", s, k_cmd_emit<<<blocks, 256, 0, s>>>(b, ctx->cmd_line_off.as<uint32_t>(), L, ctx->lines.as<float4>(),
+                                      ctx->line_raster.as<uint32_t>(), &ds->err));
     OCHRE_CUDA_TRY(cudaGetLastError());
     return OCHRE_OK;
 }

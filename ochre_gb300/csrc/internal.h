@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include "../../include/ochre_gpu.h"
 
@@ -41,10 +42,10 @@ struct DevScalars {
     uint64_t keyspace;     // total key space (raster scan .ks)
     uint32_t n_empty;      // rasters without increments (raster scan .ne)
     uint32_t pad1;
-    uint32_t n_tiles;
+    uint32_t n_tiles;      // tile-head scan total .heads
+    uint32_t n_bins;       // tile-head scan total .bins
     uint32_t n_spans;
     uint32_t sort_ticket;
-    uint32_t pad2;
 };
 
 // Entry value tag for tile-row crossings: 1 | raster (23 bits) | sign byte.
@@ -54,7 +55,7 @@ constexpr uint64_t MAX_COUNT = (1ull << 30) - 1;   // lines, entries, tiles
 
 // Per-bin replay record: DDA state at the first cell of a run of cells that
 // share one tile (32 bytes).
-struct BinRec {
+struct alignas(16) BinRec {
     uint32_t line;       // line index, 0xffffffff for the empty-raster tile
     uint32_t raster;
     int16_t x, y;        // first cell of the run
@@ -112,6 +113,17 @@ struct ochre_gpu_ctx {
 
     ochre_stats stats{};
     int keys64 = 0;          // last run used 64-bit keys
+
+    // Tracing: every kernel launch of a run is counted; with OCHRE_CTX_PROFILE
+    // each one is also bracketed by a pair of CUDA events on its stream.
+    struct Prof {
+        const char* name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Prof> prof;
+    uint32_t prof_used = 0;
+    uint32_t launches = 0;
+    std::vector<ochre_kernel_time> timings;
 };
 
 namespace ochre {
@@ -129,6 +141,17 @@ int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);
 inline DevScalars* dev_scalars(ochre_gpu_ctx* ctx) { return ctx->scalars.as<DevScalars>(); }
 inline DevScalars* host_scalars(ochre_gpu_ctx* ctx) { return ctx->h_scalars.as<DevScalars>(); }
 int check_device_error(ochre_gpu_ctx* ctx);
+void prof_begin(ochre_gpu_ctx* ctx, const char* name, cudaStream_t s);
+void prof_end(ochre_gpu_ctx* ctx, cudaStream_t s);
+
+// Counts (and, when profiling, times) one launch site: the statements in
+// `...` must enqueue exactly the work to attribute to `name`.
+#define OCHRE_LAUNCH(ctx, name, s, ...)      \
+    do {                                      \
+        ::ochre::prof_begin(ctx, name, s);    \
+        __VA_ARGS__;                          \
+        ::ochre::prof_end(ctx, s);            \
+    } while (0)
 
 #define OCHRE_CUDA_TRY(expr)                                   \
     do {                                                       \

@@ -195,9 +195,9 @@ static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStre
     {
         int blocks = (int)((n + 255) / 256);
         if (blocks > 152 * 8) blocks = 152 * 8;
-        k_sort_hist<K><<<blocks, 256, 0, s>>>(kin, n, passes, hist);
+        OCHRE_LAUNCH(ctx, "sort_hist", s, k_sort_hist<K><<<blocks, 256, 0, s>>>(kin, n, passes, hist));
         OCHRE_CUDA_TRY(cudaGetLastError());
-        k_sort_offsets<<<passes, 256, 0, s>>>(hist, off);
+        OCHRE_LAUNCH(ctx, "sort_offsets", s, k_sort_offsets<<<passes, 256, 0, s>>>(hist, off));
         OCHRE_CUDA_TRY(cudaGetLastError());
     }
     const size_t smem = (size_t)SORT_TILE * (sizeof(K) + 4) + (SORT_WARPS * 256 + 256 + 256 + 4) * 4;
@@ -214,9 +214,9 @@ static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStre
         if (trivial) continue;
         OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->sort_lookback.p, 0, (size_t)tiles * 256 * 4, s));
         OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->sort_ticket, 0, 4, s));
-        k_onesweep<K><<<(unsigned)tiles, SORT_BLOCK, smem, s>>>(kin, vin, kout, vout, n, 8 * p, off + p * 256,
+        OCHRE_LAUNCH(ctx, "sort_onesweep", s, k_onesweep<K><<<(unsigned)tiles, SORT_BLOCK, smem, s>>>(kin, vin, kout, vout, n, 8 * p, off + p * 256,
                                                                 ctx->sort_lookback.as<uint32_t>(), &ds->sort_ticket,
-                                                                &ds->err);
+                                                                &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());
         K* tk = kin; kin = kout; kout = tk;
         uint32_t* tv = vin; vin = vout; vout = tv;

@@ -21,19 +21,30 @@
 
 namespace ochre {
 
+// Tile heads: the first bin entry of every run of equal keys.  The scan also
+// counts bin entries (statistics only).
+struct HeadScan {
+    uint32_t heads;
+    uint32_t bins;
+};
+struct OpHead {
+    __device__ __forceinline__ HeadScan operator()(HeadScan a, HeadScan b) const {
+        return HeadScan{a.heads + b.heads, a.bins + b.bins};
+    }
+};
 template <class K>
 struct HeadIn {
     const K* keys;
     const uint32_t* vals;
-    __device__ __forceinline__ uint32_t operator()(uint64_t i) const {
-        if (vals[i] & CROSS_TAG) return 0u;
-        return (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+    __device__ __forceinline__ HeadScan operator()(uint64_t i) const {
+        if (vals[i] & CROSS_TAG) return HeadScan{0u, 0u};
+        return HeadScan{(i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u, 1u};
     }
 };
 struct HeadOut {
     uint32_t* head;
-    __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t v) const {
-        if (v) head[ex] = (uint32_t)i;
+    __device__ __forceinline__ void operator()(uint64_t i, HeadScan ex, HeadScan v) const {
+        if (v.heads) head[ex.heads] = (uint32_t)i;
     }
 };
 
@@ -263,10 +274,10 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     DevScalars* ds = dev_scalars(ctx);
     const uint32_t R = in->n_rasters;
     OCHRE_CUDA_TRY(ctx->tile_head.ensure(E * 4));
-    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(E) * sizeof(ScanStatus<uint32_t>)));
-    OCHRE_CUDA_TRY(launch_scan<uint32_t>(E, HeadIn<K>{ctx->keys.as<K>(), ctx->vals.as<uint32_t>()},
-                                         HeadOut{ctx->tile_head.as<uint32_t>()}, OpSumU32{}, 0u, ctx->scan_status.p,
-                                         &ds->ticket, &ds->n_tiles, &ds->err, s));
+    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(E) * sizeof(ScanStatus<HeadScan>)));
+    OCHRE_LAUNCH(ctx, "tile_head_scan", s, OCHRE_CUDA_TRY(launch_scan<HeadScan>(E, HeadIn<K>{ctx->keys.as<K>(), ctx->vals.as<uint32_t>()},
+                                         HeadOut{ctx->tile_head.as<uint32_t>()}, OpHead{}, HeadScan{0u, 0u}, ctx->scan_status.p,
+                                         &ds->ticket, reinterpret_cast<HeadScan*>(&ds->n_tiles), &ds->err, s)));
     int st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
     const uint32_t T = host_scalars(ctx)->n_tiles;
@@ -281,32 +292,33 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     if (want_cov) OCHRE_CUDA_TRY(ctx->out_tile_cov.ensure((size_t)T * 64 * 4));
     OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
     OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
-    k_tile_info<K><<<(T + 255) / 256, 256, 0, s>>>(ctx->keys.as<K>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(),
+    OCHRE_LAUNCH(ctx, "tile_info", s, k_tile_info<K><<<(T + 255) / 256, 256, 0, s>>>(ctx->keys.as<K>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(),
                                                    ctx->tile_head.as<uint32_t>(), T, E, R, ctx->tile_info.as<TileInfo>(),
-                                                   ctx->out_raster_tile_off.as<uint32_t>());
+                                                   ctx->out_raster_tile_off.as<uint32_t>()));
     OCHRE_CUDA_TRY(cudaGetLastError());
     OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)T * sizeof(TileState), s));
     OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->ticket, 0, 4, s));
-    k_tile_cov<<<(T + COV_WARPS - 1) / COV_WARPS, COV_WARPS * 32, 0, s>>>(
+    OCHRE_LAUNCH(ctx, "tile_coverage", s, k_tile_cov<<<(T + COV_WARPS - 1) / COV_WARPS, COV_WARPS * 32, 0, s>>>(
         ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(), T,
         ctx->tile_state.as<TileState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
         ctx->out_tile_alpha.as<uint8_t>(), want_cov ? ctx->out_tile_cov.as<float>() : nullptr,
-        ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(), &ds->err);
+        ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(), &ds->err));
     OCHRE_CUDA_TRY(cudaGetLastError());
     // Spans: compact in tile order.  Capacity: at most one span per tile.
     OCHRE_CUDA_TRY(ctx->out_span_xy.ensure((size_t)T * 4));
     OCHRE_CUDA_TRY(ctx->out_span_w.ensure((size_t)T * 2));
     OCHRE_CUDA_TRY(ctx->out_span_tile.ensure((size_t)T * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(T) * sizeof(ScanStatus<uint32_t>)));
-    OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+    OCHRE_LAUNCH(ctx, "span_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
         T, SpanIn{ctx->span_flag.as<uint32_t>()},
         SpanOut{ctx->span_val.as<uint64_t>(), ctx->tile_info.as<TileInfo>(), T, R, ctx->out_span_xy.as<uint32_t>(),
                 ctx->out_span_w.as<uint16_t>(), ctx->out_span_tile.as<uint32_t>(),
                 ctx->out_raster_span_off.as<uint32_t>()},
-        OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_spans, &ds->err, s));
+        OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_spans, &ds->err, s)));
     st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
     *n_spans_out = host_scalars(ctx)->n_spans;
+    ctx->stats.n_bins = host_scalars(ctx)->n_bins;
     return check_device_error(ctx);
 }
 

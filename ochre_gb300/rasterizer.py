@@ -271,18 +271,34 @@ def _np_from(ptr, dtype, count):
 class GpuContext:
     """One libochre_gpu context (device + stream + buffers)."""
 
-    def __init__(self, device: int = 0, want_cov: bool = False):
+    def __init__(self, device: int = 0, want_cov: bool = False, profile: bool = False):
         L = _lib.load()
         h = ctypes.c_void_p()
-        _lib.check(L.ochre_gpu_create(ctypes.byref(h), int(device), _lib.CTX_WANT_COV if want_cov else 0),
-                   "ochre_gpu_create")
+        self.want_cov = want_cov
+        self.profile = profile
+        _lib.check(L.ochre_gpu_create(ctypes.byref(h), int(device), self._flags()), "ochre_gpu_create")
         self.handle = h
         self.device = device
-        self.want_cov = want_cov
+
+    def _flags(self) -> int:
+        return (_lib.CTX_WANT_COV if self.want_cov else 0) | (_lib.CTX_PROFILE if self.profile else 0)
 
     def set_want_cov(self, on: bool) -> None:
-        _lib.check(_lib.load().ochre_gpu_set_flags(self.handle, _lib.CTX_WANT_COV if on else 0))
         self.want_cov = on
+        _lib.check(_lib.load().ochre_gpu_set_flags(self.handle, self._flags()))
+
+    def set_profile(self, on: bool) -> None:
+        self.profile = on
+        _lib.check(_lib.load().ochre_gpu_set_flags(self.handle, self._flags()))
+
+    def timings(self) -> list:
+        """[(kernel name, ms)] of the last run (needs profile=True)."""
+        n = ctypes.c_uint32()
+        L = _lib.load()
+        _lib.check(L.ochre_gpu_last_timings(self.handle, None, 0, ctypes.byref(n)))
+        arr = (_lib.KernelTime * max(1, n.value))()
+        _lib.check(L.ochre_gpu_last_timings(self.handle, arr, n.value, ctypes.byref(n)))
+        return [(arr[i].name.decode(), float(arr[i].ms)) for i in range(n.value)]
 
     def close(self) -> None:
         if self.handle is not None:
@@ -322,7 +338,6 @@ class GpuContext:
         return r
 
     def device_result_to_numpy(self, r: _lib.Result, n_rasters: int) -> dict:
-        import torch
         out = {}
         T, N = r.n_tiles, r.n_spans
 
@@ -330,10 +345,7 @@ class GpuContext:
             if count == 0 or not ptr:
                 return np.zeros(0, dtype=dtype)
             host = np.empty(count, dtype=dtype)
-            cudart = torch.cuda.cudart()
-            err = cudart.cudaMemcpy(host.ctypes.data, ptr, host.nbytes, 2)  # DeviceToHost
-            if int(err) != 0:
-                raise RuntimeError(f"cudaMemcpy failed ({err})")
+            _lib.memcpy_d2h(host.ctypes.data, ptr, host.nbytes)
             return host
 
         out["tile_xy"] = get(r.tile_xy, np.int16, 2 * T).reshape(T, 2)
@@ -366,4 +378,4 @@ class GpuContext:
     def stats(self) -> dict:
         s = _lib.Stats()
         _lib.check(_lib.load().ochre_gpu_last_stats(self.handle, ctypes.byref(s)))
-        return {k: getattr(s, k) for k, _ in _lib.Stats._fields_}
+        return {k: getattr(s, k) for k, _ in _lib.Stats._fields_ if k != "pad"}
