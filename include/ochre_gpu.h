@@ -143,6 +143,43 @@ int ochre_gpu_last_stats(const ochre_gpu_ctx *ctx, ochre_stats *out);
  * up to `cap` entries and the total count to *n. */
 int ochre_gpu_last_timings(const ochre_gpu_ctx *ctx, ochre_kernel_time *out, uint32_t cap, uint32_t *n);
 
+/* ---- Rasterization without device allocation --------------------------
+ * No counterpart in the reference (which allocates freely on the CPU).
+ * For callers that may not allocate GPU memory once they are running:
+ * hosts that reserve all device memory at start-up (cudaMalloc/cudaFree
+ * synchronise the device and can stall a frame), or that run next to another
+ * allocator owning the device memory.  Same chain and results as
+ * ochre_gpu_rasterize_device (device pointers in `in`), but every
+ * intermediate buffer comes from one static device array of
+ * OCHRE_NOALLOC_SCRATCH_BYTES held by each GPU that loads the library, and
+ * results go to the caller's buffers.  Calls no cudaMalloc/cudaFree.
+ *   - Returns OCHRE_E_CAPACITY when the batch's intermediates do not fit the
+ *     array (roughly up to ~100k lines / ~150k tiles) or a caller buffer is
+ *     too small; span_capacity must be >= the tile count (a span follows at
+ *     most one tile), raster offsets need n_rasters + 1 entries.
+ *   - The first call on each device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture.
+ *   - All calls share the array: calls that overlap on the GPU race (host
+ *     threads are serialised).  `stream` is a cudaStream_t (NULL: default). */
+#define OCHRE_NOALLOC_SCRATCH_BYTES (32u << 20)
+
+typedef struct ochre_output_buffers {
+    int16_t *tile_xy;           /* 2 * tile_capacity */
+    uint8_t *tile_alpha;        /* 64 * tile_capacity */
+    uint32_t tile_capacity;
+    int16_t *span_xy;           /* 2 * span_capacity */
+    uint16_t *span_width;       /* span_capacity */
+    uint32_t *span_tile;        /* span_capacity */
+    uint32_t span_capacity;
+    uint32_t *raster_tile_off;  /* n_rasters + 1 */
+    uint32_t *raster_span_off;  /* n_rasters + 1 */
+    uint32_t n_tiles;           /* written on success */
+    uint32_t n_spans;           /* written on success */
+} ochre_output_buffers;
+
+int ochre_gpu_rasterize_noalloc(const ochre_batch *in, ochre_output_buffers *out, void *stream);
+
 /* Status text for a code. */
 const char *ochre_gpu_status_string(int status);
 

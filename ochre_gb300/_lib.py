@@ -21,6 +21,7 @@ EXPORTS = [
     "ochre_gpu_rasterize", "ochre_gpu_last_stats", "ochre_gpu_last_timings", "ochre_gpu_status_string",
     "ochre_rasterizer_new", "ochre_rasterizer_move_to", "ochre_rasterizer_line_to",
     "ochre_rasterizer_command", "ochre_rasterizer_fill", "ochre_rasterizer_finish", "ochre_rasterizer_free",
+    "ochre_gpu_rasterize_noalloc",
 ]
 
 
@@ -55,6 +56,17 @@ class Stats(ctypes.Structure):
         ("n_lines", ctypes.c_uint64), ("n_entries", ctypes.c_uint64), ("n_tiles", ctypes.c_uint64),
         ("n_spans", ctypes.c_uint64), ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32),
         ("n_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("n_bins", ctypes.c_uint64),
+    ]
+
+
+class OutputBuffers(ctypes.Structure):
+    """ochre_output_buffers: caller-provided device outputs of
+    ochre_gpu_rasterize_noalloc."""
+    _fields_ = [
+        ("tile_xy", ctypes.c_void_p), ("tile_alpha", ctypes.c_void_p), ("tile_capacity", ctypes.c_uint32),
+        ("span_xy", ctypes.c_void_p), ("span_width", ctypes.c_void_p), ("span_tile", ctypes.c_void_p),
+        ("span_capacity", ctypes.c_uint32), ("raster_tile_off", ctypes.c_void_p),
+        ("raster_span_off", ctypes.c_void_p), ("n_tiles", ctypes.c_uint32), ("n_spans", ctypes.c_uint32),
     ]
 
 
@@ -103,6 +115,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_rasterizer_finish.argtypes = [vp, TILE_FN, SPAN_FN, vp]
         L.ochre_rasterizer_free.argtypes = [vp]
         L.ochre_rasterizer_free.restype = None
+        L.ochre_gpu_rasterize_noalloc.argtypes = [ctypes.POINTER(Batch), ctypes.POINTER(OutputBuffers), vp]
         _lib = L
         return L
 

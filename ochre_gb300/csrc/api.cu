@@ -15,6 +15,21 @@ namespace ochre {
 
 cudaError_t DevBuf::ensure(size_t bytes) {
     if (bytes <= cap && p != nullptr) return cudaSuccess;
+    if (fixed) {
+        if (arena != nullptr) arena->overflow = true;
+        return cudaErrorMemoryAllocation;
+    }
+    if (arena != nullptr) {
+        const size_t need = (bytes + 255) & ~(size_t)255;
+        if (arena->used + need > arena->size) {
+            arena->overflow = true;
+            return cudaErrorMemoryAllocation;
+        }
+        p = arena->base + arena->used;
+        cap = need;
+        arena->used += need;
+        return cudaSuccess;
+    }
     if (bytes == 0) bytes = 16;
     size_t want = cap ? cap : 256;
     while (want < bytes) want *= 2;
@@ -33,7 +48,7 @@ cudaError_t DevBuf::ensure(size_t bytes) {
     return cudaSuccess;
 }
 void DevBuf::release() {
-    if (p) cudaFree(p);
+    if (p && arena == nullptr && !fixed) cudaFree(p);
     p = nullptr;
     cap = 0;
 }
@@ -130,7 +145,7 @@ static int validate_host(const ochre_batch* in) {
     return OCHRE_OK;
 }
 
-static int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s) {
+int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s) {
     std::memset(out, 0, sizeof *out);
     ctx->stats = ochre_stats{};
     ctx->prof_used = 0;

@@ -11,10 +11,22 @@
 
 namespace ochre {
 
-// Grow-only device buffer.
+// Bump region that DevBufs in arena mode carve from instead of cudaMalloc.
+struct Arena {
+    char* base = nullptr;
+    size_t size = 0;
+    size_t used = 0;
+    bool overflow = false;   // a request did not fit
+};
+
+// Grow-only device buffer.  With `arena` set it never calls cudaMalloc: it
+// carves from the arena; with `fixed` set it only accepts requests that fit
+// the preset storage.
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
+    Arena* arena = nullptr;
+    bool fixed = false;
     cudaError_t ensure(size_t bytes);
     void release();
     template <class T> T* as() const { return static_cast<T*>(p); }
@@ -135,6 +147,9 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
 int stage_sort(ochre_gpu_ctx* ctx, uint64_t n_entries, uint32_t key_bits, cudaStream_t s, uint32_t* passes);
 int stage_tiles(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t n_entries, cudaStream_t s, uint32_t* n_tiles,
                 uint32_t* n_spans);
+
+// The whole chain for one batch (device pointers), results in ctx buffers.
+int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s);
 
 // Read the device scalars into ctx->h_scalars (synchronises the stream).
 int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);

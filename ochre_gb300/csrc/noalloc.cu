@@ -1,0 +1,119 @@
+// Rasterization for callers that must not allocate device memory.
+//
+// Some hosts budget all GPU memory up front and forbid driver allocations
+// afterwards: renderers that reserve their memory at start-up because
+// cudaMalloc/cudaFree synchronise the device and can stall a frame, and
+// applications where another framework's allocator owns the device memory.
+// ochre_gpu_rasterize_noalloc runs the same chain as
+// ochre_gpu_rasterize_device but takes every intermediate buffer from one
+// file-scope device array (OCHRE_NOALLOC_SCRATCH_BYTES) and writes results
+// into buffers the caller provides.  It calls no cudaMalloc, cudaFree or
+// other allocating routine.
+//
+// The array is shared by every call and keeps the previous call's contents;
+// each stage clears what must start at zero (scan and sort look-back state,
+// tickets, device scalars) before it runs.  Calls that overlap on the GPU
+// (for example on two streams) race on the array; calls from several host
+// threads are serialised by a mutex.
+#include <mutex>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace {
+
+constexpr size_t kScratchBytes = OCHRE_NOALLOC_SCRATCH_BYTES;
+constexpr int kMaxDevices = 64;
+
+// The scratch itself.  Host code must not pass `g_scratch` to a kernel: in
+// host code the name is a host-side stand-in, so the device address is looked
+// up once per device with cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+void* g_scratch_addr[kMaxDevices];
+bool g_scratch_ready[kMaxDevices];
+ochre::DevScalars g_host_scalars;  // host copy of the run's device scalars
+std::mutex g_mutex;
+
+void use_arena(ochre::DevBuf& b, ochre::Arena* a) {
+    b.p = nullptr;
+    b.cap = 0;
+    b.arena = a;
+    b.fixed = false;
+}
+
+void use_caller(ochre::DevBuf& b, void* p, size_t bytes, ochre::Arena* a) {
+    b.p = p;
+    b.cap = p ? bytes : 0;
+    b.arena = a;   // only to report overflow
+    b.fixed = true;
+}
+
+}  // namespace
+
+extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_buffers* out, void* stream) {
+    if (in == nullptr || out == nullptr) return OCHRE_E_INVALID;
+    if (out->tile_xy == nullptr || out->tile_alpha == nullptr || out->span_xy == nullptr ||
+        out->span_width == nullptr || out->span_tile == nullptr || out->raster_tile_off == nullptr ||
+        out->raster_span_off == nullptr)
+        return OCHRE_E_INVALID;
+    out->n_tiles = 0;
+    out->n_spans = 0;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return OCHRE_E_CUDA;
+    if (dev < 0 || dev >= kMaxDevices) return OCHRE_E_CAPACITY;
+    if (!g_scratch_ready[dev]) {
+        // One-time set-up on this device (the device is current here).
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            return OCHRE_E_CUDA;
+        }
+        g_scratch_addr[dev] = p;
+        g_scratch_ready[dev] = true;
+    }
+
+    ochre::Arena arena;
+    arena.base = static_cast<char*>(g_scratch_addr[dev]);
+    arena.size = kScratchBytes;
+
+    ochre_gpu_ctx ctx;
+    ctx.device = dev;
+    ctx.flags = 0;
+    ctx.own_stream = static_cast<cudaStream_t>(stream);
+    ochre::DevBuf* internal[] = {&ctx.in_verbs, &ctx.in_pts, &ctx.in_fill_off, &ctx.in_fill_xf,
+                                 &ctx.in_fill_flags, &ctx.in_raster_off, &ctx.cmd_foff, &ctx.cmd_mv, &ctx.cmd_ep,
+                                 &ctx.cmd_line_off, &ctx.lines, &ctx.line_raster, &ctx.line_ent_off,
+                                 &ctx.raster_bbox, &ctx.raster_keybase, &ctx.raster_empty, &ctx.keys, &ctx.vals,
+                                 &ctx.keys_alt, &ctx.vals_alt, &ctx.bins, &ctx.sort_hist, &ctx.sort_lookback,
+                                 &ctx.tile_head, &ctx.tile_info, &ctx.tile_state, &ctx.span_flag, &ctx.span_val,
+                                 &ctx.scan_status, &ctx.scalars, &ctx.out_tile_cov};
+    for (ochre::DevBuf* b : internal) use_arena(*b, &arena);
+    const size_t R1 = (size_t)in->n_rasters + 1;
+    use_caller(ctx.out_tile_xy, out->tile_xy, (size_t)out->tile_capacity * 4, &arena);
+    use_caller(ctx.out_tile_alpha, out->tile_alpha, (size_t)out->tile_capacity * 64, &arena);
+    use_caller(ctx.out_span_xy, out->span_xy, (size_t)out->span_capacity * 4, &arena);
+    use_caller(ctx.out_span_w, out->span_width, (size_t)out->span_capacity * 2, &arena);
+    use_caller(ctx.out_span_tile, out->span_tile, (size_t)out->span_capacity * 4, &arena);
+    use_caller(ctx.out_raster_tile_off, out->raster_tile_off, R1 * 4, &arena);
+    use_caller(ctx.out_raster_span_off, out->raster_span_off, R1 * 4, &arena);
+    if (ctx.scalars.ensure(sizeof(ochre::DevScalars)) != cudaSuccess) return OCHRE_E_CAPACITY;
+    ctx.h_scalars.p = &g_host_scalars;
+    ctx.h_scalars.cap = sizeof(g_host_scalars);
+
+    if (in->n_rasters > ochre::MAX_RASTERS || in->n_cmds > ochre::MAX_COUNT) return OCHRE_E_CAPACITY;
+    if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
+    ochre_result res;
+    int st = ochre::run_device(&ctx, in, &res, ctx.own_stream);
+    if (st != OCHRE_OK && arena.overflow) st = OCHRE_E_CAPACITY;
+    if (st == OCHRE_OK) {
+        out->n_tiles = res.n_tiles;
+        out->n_spans = res.n_spans;
+    }
+    // ctx's buffers point into the arena or at the caller's memory: nothing
+    // to release.
+    ctx.h_scalars.p = nullptr;
+    return st;
+}

@@ -15,7 +15,6 @@
 #include "internal.h"
 
 #include <utility>
-#include <vector>
 
 namespace ochre {
 
@@ -203,8 +202,8 @@ static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStre
     const size_t smem = (size_t)SORT_TILE * (sizeof(K) + 4) + (SORT_WARPS * 256 + 256 + 256 + 4) * 4;
     OCHRE_CUDA_TRY(cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // Skip passes whose digit is constant over all keys (one bucket holds n).
-    std::vector<uint32_t> h_hist((size_t)passes * 256);
-    OCHRE_CUDA_TRY(cudaMemcpyAsync(h_hist.data(), hist, h_hist.size() * 4, cudaMemcpyDeviceToHost, s));
+    uint32_t h_hist[8 * 256];
+    OCHRE_CUDA_TRY(cudaMemcpyAsync(h_hist, hist, (size_t)passes * 256 * 4, cudaMemcpyDeviceToHost, s));
     OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
     uint32_t done = 0;
     for (int p = 0; p < passes; p++) {
