@@ -84,12 +84,15 @@ def kernel_bytes(name: str, st: dict, batch) -> int:
         return E * kb
     if name == "tile_head_scan":
         return E * (kb + 4) + T * 4
-    if name == "tile_info":
-        return T * 4 + T * (kb + 4 + 32) + T * 24 + R * 4
+    if name == "tile_info_wind_scan":
+        return T * 4 + T * (kb + 4 + 32) + T * 32 + R * 4
     if name == "tile_coverage":
-        return B * (4 + 32 + 16) + T * 24 * 2 + T * 68 + T * 12
+        return B * (4 + 32 + 16) + T * 32 + T * 68 + T * 12
     if name == "span_scan":
         return T * 4 + T * 8 + N * 10 + R * 4
+    if name == "raster_fused":
+        # the whole path in one kernel: compulsory input + output bytes
+        return batch.input_bytes() + 4 * (batch.n_fills + 1) + 68 * T + 10 * N + 8 * (R + 1)
     return 0
 
 
@@ -297,15 +300,33 @@ def run_ours(args, ws, rank, local):
            + (0 if hb.fill_flags is None else hb.fill_flags.nbytes)
            + (0 if hb.raster_fill_off is None else hb.raster_fill_off.nbytes))
     for _ in range(2):
-        res = ctx.rasterize(hb)
-    n_t, n_s = len(res["tile_xy"]), len(res["span_w"])
+        res = ctx.rasterize_raw(hb)
+    n_t, n_s = res.n_tiles, res.n_spans
     d2h = n_t * 68 + n_s * 10 + 2 * 4 * (batch.n_rasters + 1)
     e2e_steps = max(1, min(args.steps, 10))
     barrier(ws)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        ctx.rasterize(hb)
+        ctx.rasterize_raw(hb)
     e2e_s = reduce_max((time.perf_counter() - t0) / e2e_steps, ws)
+
+    # ---- the general kernel chain on the same batch (the plain GPU method) ----
+    ctx.set_chain_only(True)
+    for _ in range(2):
+        ctx.rasterize_device(db, sp)
+    chain_st = ctx.stats()
+    torch.cuda.synchronize()
+    chain_ms = []
+    for i in range(max(3, min(args.steps, 10))):
+        flush.fill_(i & 0xff)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.rasterize_device(db, sp)
+        b.record(stream)
+        torch.cuda.synchronize()
+        chain_ms.append(a.elapsed_time(b))
+    ctx.set_chain_only(False)
+    chain_step_ms = sum(chain_ms) / len(chain_ms)
 
     if rank != 0:
         ctx.close()
@@ -334,6 +355,10 @@ def run_ours(args, ws, rank, local):
         "path_roofline": {"compulsory_bytes_per_step": comp_in + comp_out, "achieved_gbs": path_gbs,
                           "frac": path_gbs / peak, "note": "input verbs+points+transforms and 68 B/tile + 6 B/span"},
         "kernels": kernels,
+        "path": "fused" if st.get("fused") else "chain",
+        "plain_chain": {"value": batch.n_rasters * ws / (chain_step_ms / 1000.0), "unit": "paths/s",
+                        "ms_per_step": chain_step_ms, "launches_per_step": chain_st["n_launches"],
+                        "note": "general flatten/DDA/sort/tile chain on the same batch"},
         "cpu_baseline": cpu,
         "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s},

@@ -109,6 +109,8 @@ typedef struct ochre_stats {
     uint32_t n_launches;   /* kernels launched by the run */
     uint32_t pad;
     uint64_t n_bins;       /* sort entries that are tile bins (runs of cells in one tile) */
+    uint32_t fused;        /* 1: the fused small-raster kernel handled the batch, 0: the general chain */
+    uint32_t pad2;
 } ochre_stats;
 
 /* Device time of one kernel launch of the last run (OCHRE_CTX_PROFILE). */
@@ -121,6 +123,7 @@ typedef struct ochre_gpu_ctx ochre_gpu_ctx;
 
 #define OCHRE_CTX_WANT_COV 1u   /* also produce tile_cov */
 #define OCHRE_CTX_PROFILE 2u    /* time every kernel launch with CUDA events */
+#define OCHRE_CTX_CHAIN_ONLY 4u /* always use the general kernel chain (no fused small-raster path) */
 
 /* Create a context on `device` (CUDA ordinal).  flags: OCHRE_CTX_*. */
 int ochre_gpu_create(ochre_gpu_ctx **out, int device, uint32_t flags);

@@ -15,6 +15,7 @@ from . import build as _build
 OK, E_INVALID, E_CAPACITY, E_CUDA, E_TIMEOUT, E_NOMEM, E_LIMIT = range(7)
 CTX_WANT_COV = 1
 CTX_PROFILE = 2
+CTX_CHAIN_ONLY = 4
 
 EXPORTS = [
     "ochre_gpu_create", "ochre_gpu_destroy", "ochre_gpu_set_flags", "ochre_gpu_rasterize_device",
@@ -56,6 +57,7 @@ class Stats(ctypes.Structure):
         ("n_lines", ctypes.c_uint64), ("n_entries", ctypes.c_uint64), ("n_tiles", ctypes.c_uint64),
         ("n_spans", ctypes.c_uint64), ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32),
         ("n_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("n_bins", ctypes.c_uint64),
+        ("fused", ctypes.c_uint32), ("pad2", ctypes.c_uint32),
     ]
 
 

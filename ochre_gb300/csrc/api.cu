@@ -162,25 +162,36 @@ int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cud
         out->raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
         return OCHRE_OK;
     }
-    uint32_t L = 0;
-    int st = stage_flatten(ctx, in, s, &L);
-    if (st != OCHRE_OK) return st;
-    uint64_t E = 0;
-    uint32_t bits = 0;
-    st = stage_bin(ctx, in, L, s, &E, &bits);
-    if (st != OCHRE_OK) return st;
-    uint32_t passes = 0;
-    st = stage_sort(ctx, E, bits, s, &passes);
-    if (st != OCHRE_OK) return st;
     uint32_t T = 0, N = 0;
-    st = stage_tiles(ctx, in, E, s, &T, &N);
-    if (st != OCHRE_OK) return st;
-    ctx->stats.n_lines = L;
-    ctx->stats.n_entries = E;
+    bool handled = false;
+    int st = OCHRE_OK;
+    if (!(ctx->flags & OCHRE_CTX_CHAIN_ONLY)) {
+        st = stage_fused(ctx, in, s, &handled, &T, &N);
+        if (st != OCHRE_OK) return st;
+    }
+    if (handled) {
+        ctx->stats.fused = 1;
+    } else {
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+        uint32_t L = 0;
+        st = stage_flatten(ctx, in, s, &L);
+        if (st != OCHRE_OK) return st;
+        uint64_t E = 0;
+        uint32_t bits = 0;
+        st = stage_bin(ctx, in, L, s, &E, &bits);
+        if (st != OCHRE_OK) return st;
+        uint32_t passes = 0;
+        st = stage_sort(ctx, E, bits, s, &passes);
+        if (st != OCHRE_OK) return st;
+        st = stage_tiles(ctx, in, E, s, &T, &N);
+        if (st != OCHRE_OK) return st;
+        ctx->stats.n_lines = L;
+        ctx->stats.n_entries = E;
+        ctx->stats.key_bits = bits;
+        ctx->stats.sort_passes = passes;
+    }
     ctx->stats.n_tiles = T;
     ctx->stats.n_spans = N;
-    ctx->stats.key_bits = bits;
-    ctx->stats.sort_passes = passes;
     ctx->stats.n_launches = ctx->launches;
     collect_timings(ctx, s);
     out->n_tiles = T;
@@ -244,7 +255,8 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
                      &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->raster_bbox, &ctx->raster_keybase,
                      &ctx->raster_empty, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_state,
-                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->out_tile_xy,
+                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain,
+                     &ctx->out_tile_xy,
                      &ctx->out_tile_alpha, &ctx->out_tile_cov, &ctx->out_span_xy, &ctx->out_span_w,
                      &ctx->out_span_tile, &ctx->out_raster_tile_off, &ctx->out_raster_span_off};
     for (DevBuf* b : dev) b->release();

@@ -58,6 +58,10 @@ struct DevScalars {
     uint32_t n_bins;       // tile-head scan total .bins
     uint32_t n_spans;
     uint32_t sort_ticket;
+    uint32_t fused_fallback;  // fused path: some raster did not fit
+    uint32_t fused_tiles;     // fused path totals
+    uint32_t fused_spans;
+    uint32_t pad3;
 };
 
 // Entry value tag for tile-row crossings: 1 | raster (23 bits) | sign byte.
@@ -81,15 +85,18 @@ struct TileInfo {
     int32_t tx, ty;
     uint32_t head;       // first bin entry of the tile in the sorted entries
     uint32_t nbins;
-    int32_t lwind;       // tile-row crossing signs between the previous tile and this one
+    int32_t wind;        // tile-row crossing winding at this tile (inclusive, per raster)
+    uint32_t row_head;   // 1 if the tile starts its (raster, tile_y) row
+    uint32_t pad;
 };
 
-// Look-back state of the per-tile prefix chains (row carry and winding).
-struct TileState {
-    uint32_t rflag, wflag;
-    float ragg[8];
-    float rinc[8];
-    int32_t wagg, winc;
+// Look-back state of one block of tiles for the row-carry chain: the row
+// sums (8 pixel rows) of the block's last row segment.
+struct TileBlockState {
+    uint32_t flag;       // 0: none, 1: aggregate (block continues one row), 2: inclusive
+    uint32_t pad;
+    float agg[8];
+    float inc[8];
 };
 
 }  // namespace ochre
@@ -111,10 +118,12 @@ struct ochre_gpu_ctx {
     ochre::DevBuf keys, vals, keys_alt, vals_alt, bins;
     ochre::DevBuf sort_hist, sort_lookback;
     // tiles
-    ochre::DevBuf tile_head, tile_info, tile_state, span_flag, span_val;
+    ochre::DevBuf tile_head, tile_info, tile_state, span_flag, span_val;   // tile_state: TileBlockState
     // scan workspace
     ochre::DevBuf scan_status;
     ochre::DevBuf scalars;   // DevScalars
+    ochre::DevBuf fused_chain;   // fused path: per-raster look-back slots
+    uint32_t fused_tile_cap = 0; // fused path: output capacity guess (tiles)
     // device outputs
     ochre::DevBuf out_tile_xy, out_tile_alpha, out_tile_cov, out_span_xy, out_span_w, out_span_tile,
         out_raster_tile_off, out_raster_span_off;
@@ -146,6 +155,8 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
               uint32_t* key_bits);
 int stage_sort(ochre_gpu_ctx* ctx, uint64_t n_entries, uint32_t key_bits, cudaStream_t s, uint32_t* passes);
 int stage_tiles(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t n_entries, cudaStream_t s, uint32_t* n_tiles,
+                uint32_t* n_spans);
+int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
                 uint32_t* n_spans);
 
 // The whole chain for one batch (device pointers), results in ctx buffers.

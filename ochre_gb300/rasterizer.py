@@ -271,17 +271,23 @@ def _np_from(ptr, dtype, count):
 class GpuContext:
     """One libochre_gpu context (device + stream + buffers)."""
 
-    def __init__(self, device: int = 0, want_cov: bool = False, profile: bool = False):
+    def __init__(self, device: int = 0, want_cov: bool = False, profile: bool = False, chain_only: bool = False):
         L = _lib.load()
         h = ctypes.c_void_p()
         self.want_cov = want_cov
         self.profile = profile
+        self.chain_only = chain_only
         _lib.check(L.ochre_gpu_create(ctypes.byref(h), int(device), self._flags()), "ochre_gpu_create")
         self.handle = h
         self.device = device
 
     def _flags(self) -> int:
-        return (_lib.CTX_WANT_COV if self.want_cov else 0) | (_lib.CTX_PROFILE if self.profile else 0)
+        return ((_lib.CTX_WANT_COV if self.want_cov else 0) | (_lib.CTX_PROFILE if self.profile else 0)
+                | (_lib.CTX_CHAIN_ONLY if self.chain_only else 0))
+
+    def set_chain_only(self, on: bool) -> None:
+        self.chain_only = on
+        _lib.check(_lib.load().ochre_gpu_set_flags(self.handle, self._flags()))
 
     def set_want_cov(self, on: bool) -> None:
         self.want_cov = on
@@ -314,6 +320,12 @@ class GpuContext:
     def rasterize(self, batch: Batch) -> dict:
         """Host buffers in, host arrays out (copies the batch to the device,
         rasterizes, copies results back)."""
+        r = self.rasterize_raw(batch)
+        return self._result_to_numpy(r, batch.n_rasters)
+
+    def rasterize_raw(self, batch: Batch) -> _lib.Result:
+        """ochre_gpu_rasterize itself: results stay in the context's pinned
+        host buffers (valid until the next call)."""
         keep = []
 
         def p(a, dt):
@@ -328,7 +340,7 @@ class GpuContext:
                      batch.n_fills, p(batch.raster_fill_off, np.uint32), batch.n_rasters)
         r = _lib.Result()
         _lib.check(_lib.load().ochre_gpu_rasterize(self.handle, ctypes.byref(c), ctypes.byref(r)), "rasterize")
-        return self._result_to_numpy(r, batch.n_rasters)
+        return r
 
     def rasterize_device(self, dbatch: DeviceBatch, stream: Optional[int] = None) -> _lib.Result:
         """Device buffers in, device result (pointers owned by the context)."""
@@ -378,4 +390,4 @@ class GpuContext:
     def stats(self) -> dict:
         s = _lib.Stats()
         _lib.check(_lib.load().ochre_gpu_last_stats(self.handle, ctypes.byref(s)))
-        return {k: getattr(s, k) for k, _ in _lib.Stats._fields_ if k != "pad"}
+        return {k: getattr(s, k) for k, _ in _lib.Stats._fields_ if not k.startswith("pad")}

@@ -23,6 +23,20 @@ def gpu_ctx():
     ctx.close()
 
 
+@pytest.fixture(scope="session")
+def gpu_ctx_chain():
+    """A context forced onto the general kernel chain (no fused path)."""
+    from ochre_gb300 import GpuContext
+    ctx = GpuContext(0, chain_only=True)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(params=["fused", "chain"])
+def any_ctx(request):
+    return request.getfixturevalue("gpu_ctx" if request.param == "fused" else "gpu_ctx_chain")
+
+
 @pytest.fixture(autouse=True)
 def _quiet_numpy():
     with np.errstate(all="ignore"):

@@ -14,25 +14,25 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name", NAMES)
-def test_golden_host_path(gpu_ctx, name):
+def test_golden_host_path(any_ctx, name):
     b, exp = load(name)
-    gpu_ctx.set_want_cov(True)
+    any_ctx.set_want_cov(True)
     try:
-        got = gpu_ctx.rasterize(b)
+        got = any_ctx.rasterize(b)
     finally:
-        gpu_ctx.set_want_cov(False)
+        any_ctx.set_want_cov(False)
     st = compare(got, exp, b.n_rasters)
     # pre-quantisation coverage vs the oracle's f32 coverage (summation order only)
     assert st["cov_max_abs_vs_oracle_f32"] < 1e-3, st
 
 
 @pytest.mark.parametrize("name", NAMES)
-def test_golden_device_path(gpu_ctx, name):
+def test_golden_device_path(any_ctx, name):
     from ochre_gb300 import DeviceBatch
     b, exp = load(name)
     db = DeviceBatch(b)
-    r = gpu_ctx.rasterize_device(db)
-    got = gpu_ctx.device_result_to_numpy(r, b.n_rasters)
+    r = any_ctx.rasterize_device(db)
+    got = any_ctx.device_result_to_numpy(r, b.n_rasters)
     compare(got, exp, b.n_rasters)
 
 
@@ -43,19 +43,19 @@ def test_golden_device_path(gpu_ctx, name):
     (W.diff_union, dict()),
     (W.diff_scenes, dict(n_scenes=6)),
 ])
-def test_workload_parity(gpu_ctx, gen, kw):
+def test_workload_parity(any_ctx, gen, kw):
     b = gen(**kw)
     ref = oracle.run(b, threads=8)
-    got = gpu_ctx.rasterize(b)
+    got = any_ctx.rasterize(b)
     st = compare(got, ref, b.n_rasters)
     assert st["diff_fraction"] < 0.01, st
 
 
-def test_line_and_entry_counts_match_oracle(gpu_ctx):
+def test_line_and_entry_counts_match_oracle(gpu_ctx_chain):
     b = W.cubic_boxes(n_paths=5)
     ref = oracle.run(b, capture_lines=True)
-    gpu_ctx.rasterize(b)
-    s = gpu_ctx.stats()
+    gpu_ctx_chain.rasterize(b)
+    s = gpu_ctx_chain.stats()
     assert s["n_lines"] == len(ref["lines"])
     assert s["n_tiles"] == len(ref["tile_xy"])
 
@@ -129,32 +129,54 @@ def test_raw_commands_and_multiple_fills():
     assert c.spans == [(int(x), int(y), int(w)) for (x, y), w in zip(ref["span_xy"].tolist(), ref["span_w"])]
 
 
-def test_empty_batch_and_empty_rasterizer(gpu_ctx):
+def test_empty_batch_and_empty_rasterizer(any_ctx):
     from ochre_gb300.batch import BatchBuilder
     b = BatchBuilder().begin_raster().begin_raster().build()
-    got = gpu_ctx.rasterize(b)
+    got = any_ctx.rasterize(b)
     assert got["tile_xy"].tolist() == [[0, 0], [0, 0]]
     assert not got["tile_alpha"].any()
     assert got["raster_tile_off"].tolist() == [0, 1, 2]
 
 
-def test_invalid_inputs_are_reported(gpu_ctx):
+def test_invalid_inputs_are_reported(any_ctx):
     from ochre_gb300 import _lib
     b = W.readme_path()
     bad = b.pts.copy()
     bad[3] = np.inf
     b2 = type(b)(b.verbs, bad, b.fill_cmd_off, b.fill_xf, None, None, 1)
     with pytest.raises(_lib.OchreError) as e:
-        gpu_ctx.rasterize(b2)
+        any_ctx.rasterize(b2)
     assert e.value.status == _lib.E_INVALID
     # the context stays usable
-    got = gpu_ctx.rasterize(b)
+    got = any_ctx.rasterize(b)
     compare(got, oracle.run(b), 1)
 
 
-def test_deterministic(gpu_ctx):
+def test_repeatable(any_ctx):
+    """Two runs: identical structure; alpha may differ by the f32 summation
+    order of shared-memory atomics (<= 1 LSB, the parity bound)."""
     b = W.glyph_run(n_paths=2000, seed=11)
-    r1 = gpu_ctx.rasterize(b)
-    r2 = gpu_ctx.rasterize(b)
+    r1 = any_ctx.rasterize(b)
+    r2 = any_ctx.rasterize(b)
     for k in r1:
-        assert np.array_equal(r1[k], r2[k]), k
+        if k == "tile_alpha":
+            assert np.abs(r1[k].astype(int) - r2[k].astype(int)).max() <= 1
+        else:
+            assert np.array_equal(r1[k], r2[k]), k
+
+
+def test_fused_path_taken_for_glyphs_and_chain_for_big_paths(gpu_ctx):
+    gpu_ctx.rasterize(W.glyph_run(n_paths=500))
+    assert gpu_ctx.stats()["fused"] == 1
+    gpu_ctx.rasterize(W.cubic_boxes(n_paths=3))
+    assert gpu_ctx.stats()["fused"] == 0
+
+
+def test_full_size_glyph_run_matches_oracle(gpu_ctx):
+    """The bench workload at full size (100,000 paths), fused path."""
+    b = W.glyph_run(n_paths=100_000)
+    ref = oracle.run(b, threads=16)
+    got = gpu_ctx.rasterize(b)
+    assert gpu_ctx.stats()["fused"] == 1
+    st = compare(got, ref, b.n_rasters)
+    assert st["diff_fraction"] < 1e-3, st
