@@ -232,6 +232,10 @@ def run_ours(args, ws, rank, local):
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 126 MB L2
+    # launch shapes: the project's autotuner on a sample of this workload
+    from ochre_gb300 import autotune
+    sample = make_workload(args.workload, min(args.n_paths, 20_000), args.seed + 7)
+    tuned = autotune.tune(ctx, fused_sample=sample)
 
     for _ in range(max(3, args.warmup)):
         ctx.rasterize_device(db, sp)
@@ -346,7 +350,8 @@ def run_ours(args, ws, rank, local):
                    "l2": "flushed (256 MiB write) between timed steps, outside the events",
                    "tiles_per_step": st["n_tiles"], "spans_per_step": st["n_spans"], "lines_per_step": st["n_lines"],
                    "sort_entries_per_step": st["n_entries"], "key_bits": st["key_bits"],
-                   "sort_passes": st["sort_passes"]},
+                   "sort_passes": st["sort_passes"], "launch_shape": tuned["choice"],
+                   "autotune_ms": tuned["ms"]},
         "tiles_per_s": st["n_tiles"] * ws * args.steps / dev_s_max,
         "wall_s_timed_region": wall,
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,

@@ -183,6 +183,15 @@ typedef struct ochre_output_buffers {
 
 int ochre_gpu_rasterize_noalloc(const ochre_batch *in, ochre_output_buffers *out, void *stream);
 
+/* Launch-shape tunables, chosen per GPU by the project's autotuner
+ * (ochre_gb300/autotune.py) and applied per context:
+ *   "fused_threads"          threads per raster in the fused kernel: 64 | 128
+ *   "fused_chunk"            tiles accumulated per pass in the fused kernel: 16 | 32
+ *   "chain_tiles_per_warp"   tiles per warp in the chain's coverage kernel: 4 | 8 | 16
+ * Results do not depend on them (beyond the 1 LSB alpha bound). */
+int ochre_gpu_set_tunable(ochre_gpu_ctx *ctx, const char *name, int value);
+int ochre_gpu_get_tunable(const ochre_gpu_ctx *ctx, const char *name, int *value);
+
 /* Status text for a code. */
 const char *ochre_gpu_status_string(int status);
 

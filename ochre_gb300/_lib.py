@@ -22,7 +22,7 @@ EXPORTS = [
     "ochre_gpu_rasterize", "ochre_gpu_last_stats", "ochre_gpu_last_timings", "ochre_gpu_status_string",
     "ochre_rasterizer_new", "ochre_rasterizer_move_to", "ochre_rasterizer_line_to",
     "ochre_rasterizer_command", "ochre_rasterizer_fill", "ochre_rasterizer_finish", "ochre_rasterizer_free",
-    "ochre_gpu_rasterize_noalloc",
+    "ochre_gpu_rasterize_noalloc", "ochre_gpu_set_tunable", "ochre_gpu_get_tunable",
 ]
 
 
@@ -118,6 +118,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_rasterizer_free.argtypes = [vp]
         L.ochre_rasterizer_free.restype = None
         L.ochre_gpu_rasterize_noalloc.argtypes = [ctypes.POINTER(Batch), ctypes.POINTER(OutputBuffers), vp]
+        L.ochre_gpu_set_tunable.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
+        L.ochre_gpu_get_tunable.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         _lib = L
         return L
 

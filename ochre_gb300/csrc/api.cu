@@ -371,6 +371,32 @@ int ochre_gpu_last_timings(const ochre_gpu_ctx* ctx, ochre_kernel_time* out, uin
     return OCHRE_OK;
 }
 
+int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
+    if (!ctx || !name) return OCHRE_E_INVALID;
+    if (!std::strcmp(name, "fused_threads")) {
+        if (value != 64 && value != 128) return OCHRE_E_INVALID;
+        ctx->tune_fused_threads = value;
+    } else if (!std::strcmp(name, "fused_chunk")) {
+        if (value != 16 && value != 32) return OCHRE_E_INVALID;
+        ctx->tune_fused_chunk = value;
+    } else if (!std::strcmp(name, "chain_tiles_per_warp")) {
+        if (value != 4 && value != 8 && value != 16) return OCHRE_E_INVALID;
+        ctx->tune_chain_tiles_per_warp = value;
+    } else {
+        return OCHRE_E_INVALID;
+    }
+    return OCHRE_OK;
+}
+
+int ochre_gpu_get_tunable(const ochre_gpu_ctx* ctx, const char* name, int* value) {
+    if (!ctx || !name || !value) return OCHRE_E_INVALID;
+    if (!std::strcmp(name, "fused_threads")) *value = ctx->tune_fused_threads;
+    else if (!std::strcmp(name, "fused_chunk")) *value = ctx->tune_fused_chunk;
+    else if (!std::strcmp(name, "chain_tiles_per_warp")) *value = ctx->tune_chain_tiles_per_warp;
+    else return OCHRE_E_INVALID;
+    return OCHRE_OK;
+}
+
 int ochre_gpu_last_stats(const ochre_gpu_ctx* ctx, ochre_stats* out) {
     if (!ctx || !out) return OCHRE_E_INVALID;
     *out = ctx->stats;

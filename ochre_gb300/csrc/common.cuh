@@ -279,8 +279,10 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
 __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-// Word-wise copies of a trivially copyable T through relaxed accesses; the
-// flag word that guards them is written with release / read with acquire.
+// Look-back slots publish data with relaxed stores followed by a release
+// store of the flag; readers acquire the flag, then read the data relaxed.
+// The release/acquire pair orders the data, so no separate fence is needed.
+// Word-wise copies of a trivially copyable T through relaxed accesses.
 template <class T>
 __device__ __forceinline__ void st_words(T* dst, const T& v) {
     static_assert(sizeof(T) % 4 == 0, "T must be a multiple of 4 bytes");

@@ -32,20 +32,20 @@
 
 namespace ochre {
 
-constexpr int FUSED_THREADS = 64;
-constexpr int F_WARPS = FUSED_THREADS / 32;
-constexpr int F_CMAX = FUSED_THREADS;   // commands per raster
+// Kernel shape (template parameters, chosen by the autotuner):
+//   THREADS  threads per raster (= max commands per raster), 64 or 128;
+//   CHUNK    tiles accumulated per pass (shared accumulators of CHUNK x 512 B).
 constexpr int F_LMAX = 256;             // lines per raster
 constexpr int GDIM = 32;                // grid side in tiles (one bitmap word per row)
-constexpr int F_TMAX = 2 * FUSED_THREADS;   // touched tiles per raster
+constexpr int F_TMAX = 128;             // touched tiles per raster
 constexpr int F_XMAX = 256;             // tile-row crossings per raster
-constexpr int CHUNK = 16;               // tiles accumulated per pass
 
+template <int THREADS, int CHUNK>
 struct FusedSmem {
     float4 lines[F_LMAX];
     float acc[CHUNK][128];         // [tile][64 area | 64 height]
     uint32_t cross[F_XMAX];        // grid tile << 16 | sign (i16)
-    V2 ep[F_CMAX];                 // transformed end point (or Move point) per command
+    V2 ep[THREADS];                // transformed end point (or Move point) per command
     uint16_t line_g0[F_LMAX], line_g1[F_LMAX];   // grid-tile range of each line's cells
     uint16_t tile_g[F_TMAX];       // tile slot -> grid tile (row-major order)
     uint32_t touched[GDIM];        // one word per grid row
@@ -53,7 +53,7 @@ struct FusedSmem {
     float rs[CHUNK][8];
     float carry[CHUNK][8];
     float pend[8];                 // running carry of the row continuing into the next chunk
-    int32_t warp_tmp[F_WARPS][4];
+    int32_t warp_tmp[THREADS / 32][4];
     uint32_t raster;
     uint32_t flag;                 // per-raster fallback
     uint32_t n_cross;
@@ -71,7 +71,8 @@ struct Chain {
     uint32_t pad[3];
 };
 
-// ---- block-wide scans over FUSED_THREADS threads (one value each) ----
+// ---- block-wide scans over WARPS * 32 threads (one value each) ----
+template <int WARPS>
 __device__ __forceinline__ int block_excl_sum(int v, int& total, int32_t (*tmp)[4]) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int inc = v;
@@ -85,7 +86,7 @@ __device__ __forceinline__ int block_excl_sum(int v, int& total, int32_t (*tmp)[
     __syncthreads();
     int base = 0, tot = 0;
 #pragma unroll
-    for (int k = 0; k < F_WARPS; k++) {
+    for (int k = 0; k < WARPS; k++) {
         const int t = tmp[k][0];
         if (k < w) base += t;
         tot += t;
@@ -94,6 +95,7 @@ __device__ __forceinline__ int block_excl_sum(int v, int& total, int32_t (*tmp)[
     return base + inc - v;
 }
 // exclusive max-scan (values >= -1), identity -1
+template <int WARPS>
 __device__ __forceinline__ int block_excl_max(int v, int& incl_last, int32_t (*tmp)[4]) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int inc = v;
@@ -107,7 +109,7 @@ __device__ __forceinline__ int block_excl_max(int v, int& incl_last, int32_t (*t
     __syncthreads();
     int base = -1, tot = -1;
 #pragma unroll
-    for (int k = 0; k < F_WARPS; k++) {
+    for (int k = 0; k < WARPS; k++) {
         const int t = tmp[k][1];
         if (k < w) base = max(base, t);
         tot = max(tot, t);
@@ -130,12 +132,10 @@ __device__ __forceinline__ void chain_resolve(Chain* slots, uint32_t r, uint32_t
         if (r == 0) {
             st_relaxed(&me->inc[0], a0);
             st_relaxed(&me->inc[1], a1);
-            __threadfence();
             st_release(&me->flag, 2u);
         } else {
             st_relaxed(&me->agg[0], a0);
             st_relaxed(&me->agg[1], a1);
-            __threadfence();
             st_release(&me->flag, 1u);
         }
     }
@@ -179,7 +179,6 @@ __device__ __forceinline__ void chain_resolve(Chain* slots, uint32_t r, uint32_t
     if (lane == 0) {
         st_relaxed(&me->inc[0], p0 + a0);
         st_relaxed(&me->inc[1], p1 + a1);
-        __threadfence();
         st_release(&me->flag, 2u);
     }
 }
@@ -212,8 +211,12 @@ struct FusedArgs {
 
 __device__ __forceinline__ V2 load_pt(const float* p) { return v2(__ldg(p), __ldg(p + 1)); }
 
-__global__ void __launch_bounds__(FUSED_THREADS) k_raster_fused(FusedArgs A) {
-    __shared__ FusedSmem S;
+template <int THREADS, int CHUNK>
+__global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
+    constexpr int FUSED_THREADS = THREADS;
+    constexpr int F_WARPS = THREADS / 32;
+    constexpr int F_CMAX = THREADS;   // commands per raster
+    __shared__ FusedSmem<THREADS, CHUNK> S;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     for (;;) {
         if (tid == 0) {
@@ -239,7 +242,7 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_raster_fused(FusedArgs A) {
             const int i = base + tid;
             const uint8_t v = i < n_cmd ? __ldg(A.verbs + c0 + i) : V_CLOSE;
             int t;
-            block_excl_sum((int)floats_per_verb(v), t, S.warp_tmp);
+            block_excl_sum<F_WARPS>((int)floats_per_verb(v), t, S.warp_tmp);
             nf_total += t;
         }
         if (wid == 0) {
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_raster_fused(FusedArgs A) {
             const bool active = tid < n_cmd;
             verb = active ? __ldg(A.verbs + c0 + tid) : V_CLOSE;
             int tot;
-            const int foff = block_excl_sum((int)floats_per_verb(verb), tot, S.warp_tmp);
+            const int foff = block_excl_sum<F_WARPS>((int)floats_per_verb(verb), tot, S.warp_tmp);
             bool ok = true;
             if (active) {
                 uint32_t f = f0;
@@ -294,8 +297,8 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_raster_fused(FusedArgs A) {
             // last: endpoint of the most recent earlier non-Close command;
             // first: point of the most recent earlier Move.
             int ep_last, mv_last;
-            const int ep_ex = block_excl_max(active && verb != V_CLOSE ? tid : -1, ep_last, S.warp_tmp);
-            const int mv_ex = block_excl_max(active && verb == V_MOVE ? tid : -1, mv_last, S.warp_tmp);
+            const int ep_ex = block_excl_max<F_WARPS>(active && verb != V_CLOSE ? tid : -1, ep_last, S.warp_tmp);
+            const int mv_ex = block_excl_max<F_WARPS>(active && verb == V_MOVE ? tid : -1, mv_last, S.warp_tmp);
             if (active) {
                 last = ep_ex >= 0 ? S.ep[ep_ex] : v2(0, 0);
                 first = mv_ex >= 0 ? S.ep[mv_ex] : v2(0, 0);
@@ -327,7 +330,7 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_raster_fused(FusedArgs A) {
         int n_lines = 0;
         int loff = 0;
         if (!bail) {
-            loff = block_excl_sum(n_lines_cmd, n_lines, S.warp_tmp);
+            loff = block_excl_sum<F_WARPS>(n_lines_cmd, n_lines, S.warp_tmp);
             if (n_lines > F_LMAX) bail = true;
         }
         if (!bail && tid < n_cmd) {
@@ -511,7 +514,7 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_raster_fused(FusedArgs A) {
                     }
                 }
             }
-            const int srank = block_excl_sum(my, n_spans, S.warp_tmp);
+            const int srank = block_excl_sum<F_WARPS>(my, n_spans, S.warp_tmp);
             if (wid == 0) {
                 uint32_t p0, p1;
                 chain_resolve(A.co, r, (uint32_t)n_tiles, (uint32_t)n_spans, A.err, p0, p1);
@@ -651,6 +654,22 @@ __global__ void __launch_bounds__(FUSED_THREADS) k_raster_fused(FusedArgs A) {
     }
 }
 
+// One launch of a kernel shape: a persistent grid of (SMs x resident CTAs).
+template <int T, int C>
+static int launch_fused(ochre_gpu_ctx* ctx, const FusedArgs& a, cudaStream_t s) {
+    static int grid = 0;
+    if (grid == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster_fused<T, C>, T, 0);
+        grid = sms * (per > 0 ? per : 1);
+    }
+    OCHRE_LAUNCH(ctx, "raster_fused", s, k_raster_fused<T, C><<<grid, T, 0, s>>>(a));
+    OCHRE_CUDA_TRY(cudaGetLastError());
+    return OCHRE_OK;
+}
+
 // Runs the fused kernel over the whole batch.  *handled is false when some
 // raster does not fit (the caller then runs the general chain).
 int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
@@ -662,14 +681,6 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
     OCHRE_CUDA_TRY(ctx->fused_chain.ensure((size_t)R * 2 * sizeof(Chain)));
     Chain* cf = ctx->fused_chain.as<Chain>();
     Chain* co = cf + R;
-    static int grid = 0;
-    if (grid == 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster_fused, FUSED_THREADS, 0);
-        grid = sms * (per > 0 ? per : 1);
-    }
     // capacity guess: the last run's totals, else 48 tiles per raster; with
     // caller-provided (fixed) outputs, their capacity
     const bool fixed_out = ctx->out_tile_xy.fixed;
@@ -721,8 +732,15 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         a.span_tile = ctx->out_span_tile.as<uint32_t>();
         a.raster_tile_off = ctx->out_raster_tile_off.as<uint32_t>();
         a.raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
-        OCHRE_LAUNCH(ctx, "raster_fused", s, k_raster_fused<<<grid, FUSED_THREADS, 0, s>>>(a));
-        OCHRE_CUDA_TRY(cudaGetLastError());
+        int st0 = OCHRE_OK;
+        switch (ctx->tune_fused_threads * 1000 + ctx->tune_fused_chunk) {
+        case 64016: st0 = launch_fused<64, 16>(ctx, a, s); break;
+        case 64032: st0 = launch_fused<64, 32>(ctx, a, s); break;
+        case 128016: st0 = launch_fused<128, 16>(ctx, a, s); break;
+        case 128032: st0 = launch_fused<128, 32>(ctx, a, s); break;
+        default: return OCHRE_E_INVALID;
+        }
+        if (st0 != OCHRE_OK) return st0;
         int st = read_scalars(ctx, s);
         if (st != OCHRE_OK) return st;
         const DevScalars* hs = host_scalars(ctx);

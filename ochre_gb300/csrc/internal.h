@@ -135,6 +135,11 @@ struct ochre_gpu_ctx {
     ochre_stats stats{};
     int keys64 = 0;          // last run used 64-bit keys
 
+    // Launch-shape tunables (ochre_gpu_set_tunable; chosen by the autotuner).
+    int tune_fused_threads = 64;
+    int tune_fused_chunk = 16;
+    int tune_chain_tiles_per_warp = 8;
+
     // Tracing: every kernel launch of a run is counted; with OCHRE_CTX_PROFILE
     // each one is also bracketed by a pair of CUDA events on its stream.
     struct Prof {

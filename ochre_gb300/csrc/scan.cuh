@@ -67,11 +67,9 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, In in, Out out, Op o
             ScanStatus<T>* me = status + tile;
             if (tile == 0) {
                 st_words(&me->inc, tile_agg);
-                __threadfence();
                 st_release(&me->flag, 2u);
             } else {
                 st_words(&me->agg, tile_agg);
-                __threadfence();
                 st_release(&me->flag, 1u);
                 int64_t j = (int64_t)tile - 1;
                 long long spins = 0;
@@ -87,7 +85,6 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, In in, Out out, Op o
                     --j;
                 }
                 st_words(&me->inc, op(prefix, tile_agg));
-                __threadfence();
                 st_release(&me->flag, 2u);
             }
             s_prefix = prefix;

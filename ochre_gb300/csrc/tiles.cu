@@ -211,11 +211,9 @@ __global__ void __launch_bounds__(128) k_tile_cov(
         TileBlockState* me = state + blk;
         if (!one_segment) {
             for (int y = 0; y < 8; y++) st_relaxed(reinterpret_cast<uint32_t*>(&me->inc[y]), __float_as_uint(seg[y]));
-            __threadfence();
             st_release(&me->flag, 2u);
         } else {
             for (int y = 0; y < 8; y++) st_relaxed(reinterpret_cast<uint32_t*>(&me->agg[y]), __float_as_uint(seg[y]));
-            __threadfence();
             st_release(&me->flag, 1u);
         }
     }
@@ -241,7 +239,6 @@ __global__ void __launch_bounds__(128) k_tile_cov(
                 TileBlockState* me = state + blk;
                 for (int y = 0; y < 8; y++)
                     st_relaxed(reinterpret_cast<uint32_t*>(&me->inc[y]), __float_as_uint(c[y] + seg[y]));
-                __threadfence();
                 st_release(&me->flag, 2u);
             }
         }
@@ -321,7 +318,19 @@ struct SpanOut {
     }
 };
 
-constexpr int TILES_PER_WARP = 8;
+// One launch of the coverage kernel with TPW tiles per warp (4 warps per CTA).
+template <int TPW>
+static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, bool want_cov, cudaStream_t s) {
+    DevScalars* ds = dev_scalars(ctx);
+    const uint32_t blocks = (T + TPW - 1) / TPW;
+    cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)blocks * sizeof(TileBlockState), s);
+    cudaMemsetAsync(&ds->ticket, 0, 4, s);
+    k_tile_cov<TPW><<<(blocks + 3) / 4, 128, 0, s>>>(
+        ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(), T,
+        ctx->tile_state.as<TileBlockState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
+        ctx->out_tile_alpha.as<uint8_t>(), want_cov ? ctx->out_tile_cov.as<float>() : nullptr,
+        ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(), &ds->err);
+}
 
 template <class K>
 static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cudaStream_t s, uint32_t* n_tiles_out,
@@ -339,7 +348,7 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     if (st != OCHRE_OK) return st;
     const uint32_t T = host_scalars(ctx)->n_tiles;
     *n_tiles_out = T;
-    const uint32_t blocks = (T + TILES_PER_WARP - 1) / TILES_PER_WARP;
+    const uint32_t blocks = (T + 3) / 4;   // >= blocks of the smallest tiles-per-warp shape
     OCHRE_CUDA_TRY(ctx->tile_info.ensure((size_t)T * sizeof(TileInfo)));
     OCHRE_CUDA_TRY(ctx->tile_state.ensure((size_t)blocks * sizeof(TileBlockState)));
     OCHRE_CUDA_TRY(ctx->span_flag.ensure((size_t)T * 4));
@@ -359,15 +368,12 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
                                ctx->out_raster_tile_off.as<uint32_t>()},
                      InfoOut{ctx->tile_info.as<TileInfo>()}, OpWind{}, WindScan{0, 0u}, ctx->scan_status.p,
                      &ds->ticket, static_cast<WindScan*>(nullptr), &ds->err, s)));
-    OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)blocks * sizeof(TileBlockState), s));
-    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->ticket, 0, 4, s));
-    OCHRE_LAUNCH(ctx, "tile_coverage", s,
-                 k_tile_cov<TILES_PER_WARP><<<(blocks + 3) / 4, 128, 0, s>>>(
-                     ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(),
-                     ctx->tile_info.as<TileInfo>(), T, ctx->tile_state.as<TileBlockState>(), &ds->ticket,
-                     ctx->out_tile_xy.as<uint32_t>(), ctx->out_tile_alpha.as<uint8_t>(),
-                     want_cov ? ctx->out_tile_cov.as<float>() : nullptr, ctx->span_flag.as<uint32_t>(),
-                     ctx->span_val.as<uint64_t>(), &ds->err));
+    switch (ctx->tune_chain_tiles_per_warp) {
+    case 4: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<4>(ctx, T, want_cov, s)); break;
+    case 8: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<8>(ctx, T, want_cov, s)); break;
+    case 16: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<16>(ctx, T, want_cov, s)); break;
+    default: return OCHRE_E_INVALID;
+    }
     OCHRE_CUDA_TRY(cudaGetLastError());
     // Spans: compact in tile order.  Capacity: at most one span per tile.
     OCHRE_CUDA_TRY(ctx->out_span_xy.ensure((size_t)T * 4));

@@ -280,6 +280,14 @@ class GpuContext:
         _lib.check(L.ochre_gpu_create(ctypes.byref(h), int(device), self._flags()), "ochre_gpu_create")
         self.handle = h
         self.device = device
+        # launch shapes chosen earlier by the autotuner on this GPU, if any
+        try:
+            from . import autotune
+            params = autotune.cached(device)
+        except Exception:
+            params = None
+        if params:
+            autotune.apply(self, params)
 
     def _flags(self) -> int:
         return ((_lib.CTX_WANT_COV if self.want_cov else 0) | (_lib.CTX_PROFILE if self.profile else 0)
