@@ -332,6 +332,26 @@ def run_ours(args, ws, rank, local):
     ctx.set_chain_only(False)
     chain_step_ms = sum(chain_ms) / len(chain_ms)
 
+    # ---- parity on a sample of this workload (the bar of the metric) ----
+    parity = None
+    if rank == 0:
+        import numpy as np
+        import oracle
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from compare import compare
+        from ochre_gb300 import batch as B
+        samp = B.subset(batch, list(range(0, batch.n_rasters, max(1, batch.n_rasters // 2000))))
+        ctx.set_want_cov(True)
+        got = ctx.rasterize(samp)
+        ctx.set_want_cov(False)
+        with np.errstate(all="ignore"):
+            ref = oracle.run(samp, threads=os.cpu_count() or 1)
+            cst = compare(got, ref, samp.n_rasters)
+            e64 = oracle.tile_cov_error_vs_fp64(samp, got["tile_xy"], got["tile_cov"], got["raster_tile_off"])
+        parity = {"sample_paths": samp.n_rasters, "tiles_spans_exact": True, "alpha_max_lsb": cst["max_lsb"],
+                  "alpha_diff_fraction": cst["diff_fraction"], "cov_err_vs_fp64_max": e64["max_abs"],
+                  "cov_err_vs_fp64_mean": e64["mean_abs"]}
+
     if rank != 0:
         ctx.close()
         return
@@ -360,6 +380,7 @@ def run_ours(args, ws, rank, local):
         "path_roofline": {"compulsory_bytes_per_step": comp_in + comp_out, "achieved_gbs": path_gbs,
                           "frac": path_gbs / peak, "note": "input verbs+points+transforms and 68 B/tile + 6 B/span"},
         "kernels": kernels,
+        "parity": parity,
         "path": "fused" if st.get("fused") else "chain",
         "plain_chain": {"value": batch.n_rasters * ws / (chain_step_ms / 1000.0), "unit": "paths/s",
                         "ms_per_step": chain_step_ms, "launches_per_step": chain_st["n_launches"],

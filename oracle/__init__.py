@@ -78,6 +78,9 @@ def _load():
         lib.ochre_oracle_run.restype = ctypes.c_int
         lib.ochre_oracle_free.argtypes = [ctypes.POINTER(_Result)]
         lib.ochre_oracle_free.restype = None
+        lib.ochre_oracle_cov64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                           ctypes.c_void_p]
+        lib.ochre_oracle_cov64.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -145,6 +148,53 @@ def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = F
         return out
     finally:
         lib.ochre_oracle_free(res_p)
+
+
+def cov64(lines: np.ndarray, raster_line_off: np.ndarray, rects: np.ndarray) -> list:
+    """FP64 analytic coverage |sum| of f32 lines (from run(capture_lines=True))
+    over one pixel rectangle (x0, y0, w, h) per raster; returns one [h, w]
+    float64 image per raster."""
+    lib = _load()
+    lines = np.ascontiguousarray(lines, dtype=np.float32)
+    off = np.ascontiguousarray(raster_line_off, dtype=np.uint64)
+    rects = np.ascontiguousarray(rects, dtype=np.int32).reshape(-1, 4)
+    n = len(rects)
+    total = int((rects[:, 2].astype(np.int64) * rects[:, 3]).sum())
+    out = np.zeros(max(total, 1), dtype=np.float64)
+    st = lib.ochre_oracle_cov64(lines.ctypes.data, off.ctypes.data, n, rects.ctypes.data, out.ctypes.data)
+    if st:
+        raise RuntimeError(f"oracle cov64 failed with status {st}")
+    imgs, b = [], 0
+    for x0, y0, w, h in rects:
+        imgs.append(out[b:b + w * h].reshape(h, w))
+        b += w * h
+    return imgs
+
+
+def tile_cov_error_vs_fp64(batch, gpu_tile_xy, gpu_tile_cov, gpu_raster_tile_off) -> dict:
+    """Pre-quantisation coverage error of a result (per-tile |accum + area|,
+    64 per tile) against the FP64 analytic coverage of the same f32 lines, at
+    every tile pixel.  Returns max / mean absolute error."""
+    ref = run(batch, capture_lines=True)
+    R = batch.n_rasters
+    rects = np.zeros((R, 4), np.int32)
+    for r in range(R):
+        t0, t1 = int(gpu_raster_tile_off[r]), int(gpu_raster_tile_off[r + 1])
+        xy = gpu_tile_xy[t0:t1].astype(np.int64)
+        rects[r] = (xy[:, 0].min(), xy[:, 1].min(), xy[:, 0].max() - xy[:, 0].min() + 8,
+                    xy[:, 1].max() - xy[:, 1].min() + 8)
+    imgs = cov64(ref["lines"], ref["raster_line_off"], rects)
+    errs = []
+    for r in range(R):
+        t0, t1 = int(gpu_raster_tile_off[r]), int(gpu_raster_tile_off[r + 1])
+        x0, y0 = rects[r, 0], rects[r, 1]
+        img = imgs[r]
+        for t in range(t0, t1):
+            tx, ty = int(gpu_tile_xy[t, 0]) - x0, int(gpu_tile_xy[t, 1]) - y0
+            block = img[ty:ty + 8, tx:tx + 8].reshape(64)
+            errs.append(np.abs(gpu_tile_cov[t].astype(np.float64) - block))
+    e = np.concatenate(errs) if errs else np.zeros(1)
+    return {"max_abs": float(e.max()), "mean_abs": float(e.mean()), "pixels": int(e.size)}
 
 
 if __name__ == "__main__":  # pragma: no cover

@@ -13,7 +13,7 @@
  * independent pure-Python restatement (tests/oracle_py.py) and against
  * hand-derived known answers (tests/test_oracle.py).
  *
- * Build: see oracle/build_oracle.py (gcc -O2 -ffp-contract=off -fno-fast-math
+ * Build: oracle/__init__.py build() (gcc -O3 -ffp-contract=off -fno-fast-math
  * -fexcess-precision=standard): Rust never contracts a*b+c into an FMA, and
  * aarch64 gcc does by default, so contraction must be off for bit parity.
  *
@@ -671,4 +671,91 @@ void ochre_oracle_free(ochre_oracle_result *r) {
     free(r->raster_tile_off); free(r->raster_span_off); free(r->raster_line_off); free(r->raster_stats);
     free(r->lines); free(r->line_ninc);
     free(r);
+}
+
+
+/* ------------------------------------------------------------------ */
+/* FP64 analytic coverage of the f32 lines                             */
+/* ------------------------------------------------------------------ */
+/* For each raster: the same f32 line segments the reference rasterizes
+ * (line_to calls, captured by ochre_oracle_run), clipped exactly against the
+ * pixel grid in double precision.  Each piece inside cell (cx, cy) adds
+ * area = 0.5*h*((cx+1-p0.x)+(cx+1-p1.x)) and height h = p1.y - p0.y, the
+ * quantities rasterizer.rs:102-104 computes in f32 from the DDA's serial
+ * crossing parameters; here every crossing parameter is computed directly.
+ * Coverage before quantisation is |sum of heights left of the pixel on its
+ * row + area of the pixel| (rasterizer.rs:232-239), written for the pixels
+ * of the rectangle [x0, x0+w) x [y0, y0+h); heights of pieces left of the
+ * rectangle are carried in. */
+static int cmp_double(const void *a, const void *b) {
+    double x = *(const double *)a, y = *(const double *)b;
+    return x < y ? -1 : x > y;
+}
+
+int ochre_oracle_cov64(const float *lines, const uint64_t *raster_line_off, uint32_t n_rasters,
+                       const int32_t *rect /* 4 per raster: x0 y0 w h */, double *out) {
+    size_t base = 0;
+    for (uint32_t r = 0; r < n_rasters; r++) {
+        const int x0 = rect[4 * r], y0 = rect[4 * r + 1], w = rect[4 * r + 2], h = rect[4 * r + 3];
+        double *img = out + base;
+        size_t npx = (size_t)w * (size_t)h;
+        double *hsum = (double *)calloc(npx ? npx : 1, sizeof(double));
+        double *left = (double *)calloc(h ? (size_t)h : 1, sizeof(double));
+        if (!hsum || !left) { free(hsum); free(left); return OCHRE_ORACLE_E_NOMEM; }
+        for (size_t i = 0; i < npx; i++) img[i] = 0.0;
+        for (uint64_t l = raster_line_off[r]; l < raster_line_off[r + 1]; l++) {
+            const double ax = lines[4 * l], ay = lines[4 * l + 1], bx = lines[4 * l + 2], by = lines[4 * l + 3];
+            if (ax == bx && ay == by) continue;
+            const double dx = bx - ax, dy = by - ay;
+            /* crossing parameters with every integer x and y between the ends */
+            long fx0 = (long)floor(fmin(ax, bx)), fx1 = (long)floor(fmax(ax, bx));
+            long fy0 = (long)floor(fmin(ay, by)), fy1 = (long)floor(fmax(ay, by));
+            size_t cap = (size_t)(fx1 - fx0 + fy1 - fy0 + 4);
+            double *ts = (double *)malloc(cap * sizeof(double));
+            if (!ts) { free(hsum); free(left); return OCHRE_ORACLE_E_NOMEM; }
+            size_t nt = 0;
+            ts[nt++] = 0.0;
+            if (dx != 0.0)
+                for (long k = fx0 + 1; k <= fx1; k++) {
+                    double t = ((double)k - ax) / dx;
+                    if (t > 0.0 && t < 1.0) ts[nt++] = t;
+                }
+            if (dy != 0.0)
+                for (long k = fy0 + 1; k <= fy1; k++) {
+                    double t = ((double)k - ay) / dy;
+                    if (t > 0.0 && t < 1.0) ts[nt++] = t;
+                }
+            ts[nt++] = 1.0;
+            qsort(ts, nt, sizeof(double), cmp_double);
+            for (size_t i = 0; i + 1 < nt; i++) {
+                const double t0 = ts[i], t1 = ts[i + 1];
+                if (t1 <= t0) continue;
+                const double tm = 0.5 * (t0 + t1);
+                const long cx = (long)floor(ax + tm * dx), cy = (long)floor(ay + tm * dy);
+                const double p0x = ax + t0 * dx, p0y = ay + t0 * dy, p1x = ax + t1 * dx, p1y = ay + t1 * dy;
+                const double hh = p1y - p0y;
+                const double right = (double)(cx + 1);
+                const double aa = 0.5 * hh * ((right - p0x) + (right - p1x));
+                const long py = cy - y0, px = cx - x0;
+                if (py < 0 || py >= h) continue;
+                if (px < 0) { left[py] += hh; continue; }
+                if (px >= w) continue;
+                img[(size_t)py * w + px] += aa;
+                hsum[(size_t)py * w + px] += hh;
+            }
+            free(ts);
+        }
+        for (int y = 0; y < h; y++) {
+            double acc = left[y];
+            for (int x = 0; x < w; x++) {
+                double v = acc + img[(size_t)y * w + x];
+                acc += hsum[(size_t)y * w + x];
+                img[(size_t)y * w + x] = fabs(v);
+            }
+        }
+        free(hsum);
+        free(left);
+        base += npx;
+    }
+    return 0;
 }

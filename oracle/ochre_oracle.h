@@ -65,6 +65,12 @@ typedef struct ochre_oracle_result {
 } ochre_oracle_result;
 
 int ochre_oracle_run(const ochre_oracle_batch *batch, int threads, int flags, ochre_oracle_result **out);
+
+/* FP64 analytic coverage |sum| of the given f32 lines (4 floats each),
+ * rasters delimited by raster_line_off, over one pixel rectangle per raster
+ * (x0, y0, w, h); images are concatenated row-major into `out`. */
+int ochre_oracle_cov64(const float *lines, const uint64_t *raster_line_off, uint32_t n_rasters,
+                       const int32_t *rect, double *out);
 void ochre_oracle_free(ochre_oracle_result *r);
 
 #ifdef __cplusplus

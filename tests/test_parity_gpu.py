@@ -180,3 +180,26 @@ def test_full_size_glyph_run_matches_oracle(gpu_ctx):
     assert gpu_ctx.stats()["fused"] == 1
     st = compare(got, ref, b.n_rasters)
     assert st["diff_fraction"] < 1e-3, st
+
+
+@pytest.mark.parametrize("name,gen,kw,bound", [
+    ("cubic_boxes", W.cubic_boxes, dict(n_paths=20), 2e-3),
+    ("glyph_run", W.glyph_run, dict(n_paths=2000), 2e-3),
+    ("uneven_mix", W.uneven_mix, dict(n_paths=40), 0.1),
+    ("diff_union", W.diff_union, dict(n_paths=128), 2e-3),
+    ("diff_scenes", W.diff_scenes, dict(n_scenes=2, max_paths=64), 2e-3),
+])
+def test_coverage_error_vs_fp64(any_ctx, name, gen, kw, bound):
+    """Pre-quantisation f32 coverage against the FP64 analytic area of the same
+    lines.  The bound for the uneven mix is loose on purpose: its long closing
+    lines (up to ~8000 px) drift in the reference's serial f32 DDA, which the
+    GPU reproduces bit for bit; the oracle shows the same error."""
+    b = gen(**kw)
+    any_ctx.set_want_cov(True)
+    try:
+        got = any_ctx.rasterize(b)
+    finally:
+        any_ctx.set_want_cov(False)
+    e = oracle.tile_cov_error_vs_fp64(b, got["tile_xy"], got["tile_cov"], got["raster_tile_off"])
+    print(name, e)
+    assert e["max_abs"] < bound, e
