@@ -146,6 +146,30 @@ int ochre_gpu_last_stats(const ochre_gpu_ctx *ctx, ochre_stats *out);
  * up to `cap` entries and the total count to *n. */
 int ochre_gpu_last_timings(const ochre_gpu_ctx *ctx, ochre_kernel_time *out, uint32_t cap, uint32_t *n);
 
+/* ---- Differentiable fill -------------------------------------------------
+ * Extends the reference's forward model (rasterizer.rs:180-268) with dense
+ * coverage images and a hand-written backward pass.  Raster r renders into a
+ * w x h canvas (origin (0,0)) at offset r*w*h of the image buffers; pixel
+ * coverage is min(|accum + area|, 1) inside boundary tiles (the value the
+ * reference quantises, rasterizer.rs:235), 1 inside spans, 0 elsewhere.
+ * All pointers are device pointers; `stream` is a cudaStream_t or NULL. */
+int ochre_gpu_render_coverage(ochre_gpu_ctx *ctx, const ochre_batch *in, uint32_t w, uint32_t h, float *cov,
+                              void *stream);
+
+/* loss = sum (cov - target)^2 (written as one double), dl_dcov = 2 (cov - target)
+ * (may be NULL). */
+int ochre_gpu_l2_loss(ochre_gpu_ctx *ctx, const float *cov, const float *target, uint64_t n, double *loss,
+                      float *dl_dcov, void *stream);
+
+/* Backward of ochre_gpu_render_coverage: from dL/d(coverage) (same layout),
+ * writes dL/d(pts) (one value per input float, in the input (pre-transform)
+ * space; conic weights get 0) and dL/d(transform) (6 per fill: m0 m1 m2 m3
+ * ox oy).  The tile and line lists are recomputed, not stored.  Segment
+ * counts, visited cells and tiles are held fixed (they are piecewise
+ * constant in the inputs). */
+int ochre_gpu_fill_backward(ochre_gpu_ctx *ctx, const ochre_batch *in, uint32_t w, uint32_t h,
+                            const float *dl_dcov, float *dl_dpts, float *dl_dxf, void *stream);
+
 /* ---- Rasterization without device allocation --------------------------
  * No counterpart in the reference (which allocates freely on the CPU).
  * For callers that may not allocate GPU memory once they are running:

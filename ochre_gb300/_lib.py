@@ -23,6 +23,7 @@ EXPORTS = [
     "ochre_rasterizer_new", "ochre_rasterizer_move_to", "ochre_rasterizer_line_to",
     "ochre_rasterizer_command", "ochre_rasterizer_fill", "ochre_rasterizer_finish", "ochre_rasterizer_free",
     "ochre_gpu_rasterize_noalloc", "ochre_gpu_set_tunable", "ochre_gpu_get_tunable",
+    "ochre_gpu_render_coverage", "ochre_gpu_l2_loss", "ochre_gpu_fill_backward",
 ]
 
 
@@ -119,6 +120,9 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_rasterizer_free.restype = None
         L.ochre_gpu_rasterize_noalloc.argtypes = [ctypes.POINTER(Batch), ctypes.POINTER(OutputBuffers), vp]
         L.ochre_gpu_set_tunable.argtypes = [vp, ctypes.c_char_p, ctypes.c_int]
+        L.ochre_gpu_render_coverage.argtypes = [vp, ctypes.POINTER(Batch), u32, u32, vp, vp]
+        L.ochre_gpu_l2_loss.argtypes = [vp, vp, vp, ctypes.c_uint64, vp, vp, vp]
+        L.ochre_gpu_fill_backward.argtypes = [vp, ctypes.POINTER(Batch), u32, u32, vp, vp, vp, vp]
         L.ochre_gpu_get_tunable.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         _lib = L
         return L

@@ -100,7 +100,7 @@ void prof_end(ochre_gpu_ctx* ctx, cudaStream_t s) {
 }
 
 // Converts the recorded event pairs of the finished run into timings.
-static void collect_timings(ochre_gpu_ctx* ctx, cudaStream_t s) {
+void collect_timings(ochre_gpu_ctx* ctx, cudaStream_t s) {
     ctx->timings.clear();
     if (!(ctx->flags & OCHRE_CTX_PROFILE) || ctx->prof_used == 0) return;
     cudaStreamSynchronize(s);
@@ -256,6 +256,7 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
                      &ctx->raster_empty, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_state,
                      &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain,
+                     &ctx->grad_g, &ctx->grad_gs, &ctx->grad_left, &ctx->grad_line, &ctx->grad_pts,
                      &ctx->out_tile_xy,
                      &ctx->out_tile_alpha, &ctx->out_tile_cov, &ctx->out_span_xy, &ctx->out_span_w,
                      &ctx->out_span_tile, &ctx->out_raster_tile_off, &ctx->out_raster_span_off};

@@ -69,12 +69,19 @@ struct LineCountIn {
         bool capped = false;
         const uint32_t c = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped);
         if (capped) atomicOr(err, ERR_LIMIT);
-        if (bb.x0 <= bb.x1) {
-            int4* d = bbox + line_raster[i];
-            atomicMin(&d->x, bb.x0);
-            atomicMin(&d->y, bb.y0);
-            atomicMax(&d->z, bb.x1);
-            atomicMax(&d->w, bb.y1);
+        // lanes of one raster (contiguous lines) reduce first; the group's
+        // leader updates the raster's box only where it grows
+        const uint32_t r = line_raster[i];
+        const unsigned grp = __match_any_sync(__activemask(), r);
+        const int x0 = __reduce_min_sync(grp, bb.x0), y0 = __reduce_min_sync(grp, bb.y0);
+        const int x1 = __reduce_max_sync(grp, bb.x1), y1 = __reduce_max_sync(grp, bb.y1);
+        if ((int)(threadIdx.x & 31) == __ffs(grp) - 1 && x0 <= x1) {
+            int4* d = bbox + r;
+            const int4 cur = ld_words(d);
+            if (x0 < cur.x) atomicMin(&d->x, x0);
+            if (y0 < cur.y) atomicMin(&d->y, y0);
+            if (x1 > cur.z) atomicMax(&d->z, x1);
+            if (y1 > cur.w) atomicMax(&d->w, y1);
         }
         return c;
     }

@@ -135,6 +135,10 @@ struct ochre_gpu_ctx {
     ochre_stats stats{};
     int keys64 = 0;          // last run used 64-bit keys
 
+    bool cov_signed = false;   // tile_cov holds accum + area (signed) instead of |accum + area|
+    // differentiable path scratch
+    ochre::DevBuf grad_g, grad_gs, grad_left, grad_line, grad_pts;
+
     // Launch-shape tunables (ochre_gpu_set_tunable; chosen by the autotuner).
     int tune_fused_threads = 64;
     int tune_fused_chunk = 16;
@@ -174,6 +178,8 @@ inline DevScalars* host_scalars(ochre_gpu_ctx* ctx) { return ctx->h_scalars.as<D
 int check_device_error(ochre_gpu_ctx* ctx);
 void prof_begin(ochre_gpu_ctx* ctx, const char* name, cudaStream_t s);
 void prof_end(ochre_gpu_ctx* ctx, cudaStream_t s);
+// Converts the event pairs recorded since the last reset into ctx->timings.
+void collect_timings(ochre_gpu_ctx* ctx, cudaStream_t s);
 
 // Counts (and, when profiling, times) one launch site: the statements in
 // `...` must enqueue exactly the work to attribute to `name`.

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
     const TileInfo* __restrict__ info, uint32_t n_tiles, TileBlockState* state, uint32_t* ticket,
     uint32_t* __restrict__ out_xy, uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov,
-    uint32_t* __restrict__ span_flag, uint64_t* __restrict__ span_val, uint32_t* err) {
+    uint32_t* __restrict__ span_flag, uint64_t* __restrict__ span_val, uint32_t* err, bool cov_signed) {
     constexpr int WARPS = 4;
     __shared__ float s_acc[WARPS][CH][128];   // [tile][0..63 area, 64..127 height]
     __shared__ uint32_t s_head[WARPS][CH];
@@ -268,14 +268,18 @@ __global__ void __launch_bounds__(128) k_tile_cov(
         if ((lane & 3) == 0) excl = 0.0f;
         const float rowsum = __shfl_sync(0xffffffffu, incl, (lane & ~3) | 3);
         const float acc0 = carry + excl;
-        const float cov0 = fabsf(acc0 + a0);
+        const float sum0 = acc0 + a0;
+        const float cov0 = fabsf(sum0);
         const float acc1 = acc0 + h0;
-        const float cov1 = fabsf(acc1 + a1);
+        const float sum1 = acc1 + a1;
+        const float cov1 = fabsf(sum1);
         const uint32_t t = t0 + i;
         const uint32_t al0 = f2u8(rmin(cov0 * 256.0f, 255.0f));
         const uint32_t al1 = f2u8(rmin(cov1 * 256.0f, 255.0f));
         reinterpret_cast<uint16_t*>(out_alpha + (size_t)t * 64)[lane] = (uint16_t)(al0 | (al1 << 8));
-        if (out_cov) reinterpret_cast<float2*>(out_cov + (size_t)t * 64)[lane] = make_float2(cov0, cov1);
+        if (out_cov)
+            reinterpret_cast<float2*>(out_cov + (size_t)t * 64)[lane] =
+                cov_signed ? make_float2(sum0, sum1) : make_float2(cov0, cov1);
         carry = carry + rowsum;
         if (lane == i) {
             out_xy[t] = (uint32_t)(uint16_t)(int16_t)(ti.tx * 8) | ((uint32_t)(uint16_t)(int16_t)(ti.ty * 8) << 16);
@@ -329,7 +333,7 @@ static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, bool want_cov, cudaS
         ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(), T,
         ctx->tile_state.as<TileBlockState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
         ctx->out_tile_alpha.as<uint8_t>(), want_cov ? ctx->out_tile_cov.as<float>() : nullptr,
-        ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(), &ds->err);
+        ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(), &ds->err, ctx->cov_signed);
 }
 
 template <class K>

@@ -395,6 +395,50 @@ class GpuContext:
             out["tile_cov"] = _np_from(r.tile_cov, np.float32, 64 * T).reshape(T, 64)
         return out
 
+    # ---- differentiable fill (device tensors as storage) ----
+    def _torch_stream(self, stream: Optional[int]) -> int:
+        import torch
+        return stream if stream is not None else torch.cuda.current_stream(self.device).cuda_stream
+
+    def render_coverage(self, dbatch: DeviceBatch, w: int, h: int, out=None, stream: Optional[int] = None):
+        """Dense coverage images [n_rasters, h, w] (float32 CUDA tensor),
+        min(|accum + area|, 1) at boundary-tile pixels, 1 in spans, else 0.
+        Runs on torch's current stream unless ``stream`` is given."""
+        import torch
+        stream = self._torch_stream(stream)
+        if out is None:
+            out = torch.empty((dbatch.batch.n_rasters, h, w), dtype=torch.float32, device=f"cuda:{self.device}")
+        _lib.check(_lib.load().ochre_gpu_render_coverage(self.handle, ctypes.byref(dbatch.c), w, h,
+                                                         out.data_ptr(), stream), "render_coverage")
+        return out
+
+    def l2_loss(self, cov, target, dl_dcov=None, stream: Optional[int] = None):
+        """(loss tensor [1] float64, dl_dcov) on the device: sum (cov - target)^2
+        and, when ``dl_dcov`` is given, 2 (cov - target) written into it."""
+        import torch
+        stream = self._torch_stream(stream)
+        loss = torch.empty(1, dtype=torch.float64, device=cov.device)
+        _lib.check(_lib.load().ochre_gpu_l2_loss(self.handle, cov.data_ptr(), target.data_ptr(), cov.numel(),
+                                                 loss.data_ptr(), dl_dcov.data_ptr() if dl_dcov is not None else None,
+                                                 stream), "l2_loss")
+        return loss, dl_dcov
+
+    def fill_backward(self, dbatch: DeviceBatch, w: int, h: int, dl_dcov, dl_dpts=None, dl_dxf=None,
+                      stream: Optional[int] = None):
+        """dL/d(points) [n_floats] and dL/d(transforms) [n_fills, 6] (CUDA tensors)
+        from dL/d(coverage) [n_rasters, h, w]."""
+        import torch
+        stream = self._torch_stream(stream)
+        dev = dl_dcov.device
+        if dl_dpts is None:
+            dl_dpts = torch.empty(max(1, len(dbatch.batch.pts)), dtype=torch.float32, device=dev)
+        if dl_dxf is None:
+            dl_dxf = torch.empty((max(1, dbatch.batch.n_fills), 6), dtype=torch.float32, device=dev)
+        _lib.check(_lib.load().ochre_gpu_fill_backward(self.handle, ctypes.byref(dbatch.c), w, h,
+                                                       dl_dcov.data_ptr(), dl_dpts.data_ptr(), dl_dxf.data_ptr(),
+                                                       stream), "fill_backward")
+        return dl_dpts, dl_dxf
+
     def stats(self) -> dict:
         s = _lib.Stats()
         _lib.check(_lib.load().ochre_gpu_last_stats(self.handle, ctypes.byref(s)))

@@ -81,6 +81,15 @@ def _load():
         lib.ochre_oracle_cov64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
                                            ctypes.c_void_p]
         lib.ochre_oracle_cov64.restype = ctypes.c_int
+        lib.ochre_oracle_seg_counts.argtypes = [ctypes.POINTER(_Batch), ctypes.c_void_p]
+        lib.ochre_oracle_seg_counts.restype = ctypes.c_int
+        lib.ochre_oracle_diff64.argtypes = [ctypes.POINTER(_Batch), ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+                                            ctypes.c_void_p]
+        lib.ochre_oracle_diff64.restype = ctypes.c_int
+        lib.ochre_oracle_backward64.argtypes = [ctypes.POINTER(_Batch), ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        lib.ochre_oracle_backward64.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -92,14 +101,7 @@ def _copy(ptr, dtype, count):
     return np.frombuffer(buf, dtype=dtype).copy()
 
 
-def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = False) -> dict:
-    """Rasterize every raster of ``batch`` on the CPU.
-
-    ``batch`` has the attributes of ``ochre_gb300.batch.Batch`` (numpy arrays
-    in the C-ABI layout).  Returns a dict of numpy arrays in the same layout as
-    the GPU result plus per-raster statistics.
-    """
-    lib = _load()
+def _as_batch(batch):
     keep = []
 
     def p(a, dtype):
@@ -120,6 +122,18 @@ def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = F
     b.n_fills = len(batch.fill_cmd_off) - 1
     b.raster_fill_off = p(batch.raster_fill_off, np.uint32)
     b.n_rasters = batch.n_rasters
+    return b, keep
+
+
+def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = False) -> dict:
+    """Rasterize every raster of ``batch`` on the CPU.
+
+    ``batch`` has the attributes of ``ochre_gb300.batch.Batch`` (numpy arrays
+    in the C-ABI layout).  Returns a dict of numpy arrays in the same layout as
+    the GPU result plus per-raster statistics.
+    """
+    lib = _load()
+    b, keep = _as_batch(batch)
     flags = (1 if want_cov else 0) | (2 if capture_lines else 0)
     res_p = ctypes.POINTER(_Result)()
     st = lib.ochre_oracle_run(ctypes.byref(b), int(threads), flags, ctypes.byref(res_p))
@@ -195,6 +209,78 @@ def tile_cov_error_vs_fp64(batch, gpu_tile_xy, gpu_tile_cov, gpu_raster_tile_off
             errs.append(np.abs(gpu_tile_cov[t].astype(np.float64) - block))
     e = np.concatenate(errs) if errs else np.zeros(1)
     return {"max_abs": float(e.max()), "mean_abs": float(e.mean()), "pixels": int(e.size)}
+
+
+def seg_counts(batch) -> np.ndarray:
+    """Lines the f32 flattening gives each command (0 for non-curves)."""
+    lib = _load()
+    b, keep = _as_batch(batch)
+    out = np.zeros(max(len(batch.verbs), 1), np.uint32)
+    st = lib.ochre_oracle_seg_counts(ctypes.byref(b), out.ctypes.data)
+    if st:
+        raise RuntimeError(f"oracle seg_counts failed with status {st}")
+    return out[:len(batch.verbs)]
+
+
+def diff64(batch, w: int, h: int, target: np.ndarray, counts=None, grad: bool = True):
+    """FP64 differentiable model: returns (loss, dL/dpts, dL/dxf) for a
+    ``w`` x ``h`` canvas per raster against ``target`` ([R, h, w]); line
+    counts of curves are held at ``counts`` (default: the f32 flattening's)."""
+    lib = _load()
+    b, keep = _as_batch(batch)
+    counts = seg_counts(batch) if counts is None else np.ascontiguousarray(counts, np.uint32)
+    target = np.ascontiguousarray(target, np.float64)
+    assert target.size == batch.n_rasters * w * h
+    loss = ctypes.c_double()
+    dpts = np.zeros(max(len(batch.pts), 1), np.float64)
+    dxf = np.zeros(max(6 * (len(batch.fill_cmd_off) - 1), 1), np.float64)
+    st = lib.ochre_oracle_diff64(ctypes.byref(b), counts.ctypes.data if counts.size else None, int(w), int(h),
+                                 target.ctypes.data, ctypes.byref(loss),
+                                 dpts.ctypes.data if grad else None, dxf.ctypes.data if grad else None)
+    if st:
+        raise RuntimeError(f"oracle diff64 failed with status {st}")
+    return loss.value, dpts[:len(batch.pts)], dxf[:6 * (len(batch.fill_cmd_off) - 1)].reshape(-1, 6)
+
+
+def backward64(batch, w: int, h: int, dl_ds: np.ndarray, counts=None):
+    """FP64 backward of the same model from a given dL/dS image ([R, h, w]);
+    returns (dL/dpts, dL/dxf)."""
+    lib = _load()
+    b, keep = _as_batch(batch)
+    counts = seg_counts(batch) if counts is None else np.ascontiguousarray(counts, np.uint32)
+    g = np.ascontiguousarray(dl_ds, np.float64)
+    assert g.size == batch.n_rasters * w * h
+    dpts = np.zeros(max(len(batch.pts), 1), np.float64)
+    dxf = np.zeros(max(6 * (len(batch.fill_cmd_off) - 1), 1), np.float64)
+    st = lib.ochre_oracle_backward64(ctypes.byref(b), counts.ctypes.data if counts.size else None, int(w), int(h),
+                                     g.ctypes.data, dpts.ctypes.data, dxf.ctypes.data)
+    if st:
+        raise RuntimeError(f"oracle backward64 failed with status {st}")
+    return dpts[:len(batch.pts)], dxf[:6 * (len(batch.fill_cmd_off) - 1)].reshape(-1, 6)
+
+
+def coverage_image(batch, w: int, h: int) -> np.ndarray:
+    """f32 model coverage min(|accum + area|, 1) of each raster on a w x h
+    canvas at the origin, from the f32 restatement (tiles) and its spans."""
+    ref = run(batch, want_cov=True)
+    R = batch.n_rasters
+    img = np.zeros((R, h + 8, w + 8), np.float32)
+    for r in range(R):
+        t0, t1 = int(ref["raster_tile_off"][r]), int(ref["raster_tile_off"][r + 1])
+        for t in range(t0, t1):
+            x, y = int(ref["tile_xy"][t, 0]), int(ref["tile_xy"][t, 1])
+            if x <= -8 or y <= -8 or x >= w or y >= h:
+                continue
+            blk = np.minimum(np.abs(ref["tile_cov"][t].reshape(8, 8)), 1.0)
+            xs, ys = max(x, 0), max(y, 0)
+            img[r, ys:y + 8, xs:x + 8] = blk[ys - y:, xs - x:]
+        s0, s1 = int(ref["raster_span_off"][r]), int(ref["raster_span_off"][r + 1])
+        for s in range(s0, s1):
+            x, y, sw = int(ref["span_xy"][s, 0]), int(ref["span_xy"][s, 1]), int(ref["span_w"][s])
+            if y <= -8 or y >= h or x + sw <= 0 or x >= w:
+                continue
+            img[r, max(y, 0):y + 8, max(x, 0):min(x + sw, w)] = 1.0
+    return img[:, :h, :w].copy()
 
 
 if __name__ == "__main__":  # pragma: no cover

@@ -759,3 +759,495 @@ int ochre_oracle_cov64(const float *lines, const uint64_t *raster_line_off, uint
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* Differentiable model in double precision                           */
+/* ------------------------------------------------------------------ */
+/* The model of ochre_gb300's differentiable fill, restated in double:
+ * coverage c = min(|S|, 1) on a w x h canvas per raster, S from the exact
+ * clipping of the path's edges (as ochre_oracle_cov64), loss = sum (c - t)^2.
+ * The discrete structure is held fixed: every curve keeps the number of
+ * lines the f32 flattening gives it (path.rs:52-57, 65-73), with parameters
+ * t_j = min(j dt, 1) (t_n = 1); closing lines (rasterizer.rs:62-64,
+ * 181-183) are always present, zero-length when the contour is closed. */
+typedef struct { double x, y; } dv2;
+typedef struct { dv2 a, b; } dedge;
+typedef struct { int64_t cmd; int pt; } pref;   /* a device-space point: command, point index; cmd < 0: constant */
+
+static dv2 dxf_apply(const float *xf, dv2 v) {
+    dv2 r = {(double)xf[0] * v.x + (double)xf[1] * v.y + (double)xf[4],
+             (double)xf[2] * v.x + (double)xf[3] * v.y + (double)xf[5]};
+    return r;
+}
+static int npts_of(uint8_t v) { return v == 0 || v == 1 ? 1 : v == 2 || v == 4 ? 2 : v == 3 ? 3 : 0; }
+static int endpt_of(uint8_t v) { return v == 3 ? 2 : (v == 2 || v == 4) ? 1 : 0; }
+
+int ochre_oracle_seg_counts(const ochre_oracle_batch *bt, uint32_t *counts) {
+    uint64_t *off = NULL;
+    int st = validate(bt, &off);
+    if (st) return st;
+    for (uint32_t ri = 0; ri < bt->n_rasters; ri++) {
+        uint32_t f0 = bt->raster_fill_off ? bt->raster_fill_off[ri] : ri;
+        uint32_t f1 = bt->raster_fill_off ? bt->raster_fill_off[ri + 1] : ri + 1;
+        vec2 last = v2(0.0f, 0.0f);
+        for (uint32_t f = f0; f < f1; f++) {
+            const float *xf = bt->fill_xf + 6 * (size_t)f;
+            int raw = bt->fill_flags ? (bt->fill_flags[f] & 1) : 0;
+            for (uint32_t c = bt->fill_cmd_off[f]; c < bt->fill_cmd_off[f + 1]; c++) {
+                uint8_t verb = bt->verbs[c];
+                const float *fp = bt->pts + off[c];
+                vec2 p[3];
+                for (int k = 0; k < npts_of(verb); k++) {
+                    p[k] = v2(fp[2 * k], fp[2 * k + 1]);
+                    if (!raw) p[k] = xf_apply(xf, p[k]);
+                }
+                uint32_t n = 0;
+                if (verb == 2 || verb == 3) {
+                    float dt;
+                    if (verb == 2) {
+                        dt = sqrtf((4.0f * TOLERANCE) / vlength(vadd(vsub(last, vscale(2.0f, p[0])), p[1])));
+                    } else {
+                        vec2 a = vadd(vsub(vadd(vscale(-1.0f, last), vscale(3.0f, p[0])), vscale(3.0f, p[1])), p[2]);
+                        vec2 b = vscale(3.0f, vadd(vsub(last, vscale(2.0f, p[0])), p[1]));
+                        float conc = rmax(vlength(b), vlength(vadd(a, b)));
+                        dt = sqrtf((sqrtf(8.0f) * TOLERANCE) / conc);
+                    }
+                    float t = 0.0f;
+                    while (t < 1.0f && n < FLATTEN_CAP) { t = rmin(t + dt, 1.0f); n++; }
+                }
+                counts[c] = n;
+                if (verb <= 4) last = p[endpt_of(verb)];
+            }
+        }
+    }
+    free(off);
+    return 0;
+}
+
+/* exact clipping of one edge; calls piece(cx, cy, p0, p1, kind0, kind1, bnd0, bnd1)
+ * where kind = 0 endpoint, 1 vertical boundary x = bnd, 2 horizontal y = bnd */
+typedef void (*piece_fn)(void *u, long cx, long cy, dv2 p0, dv2 p1, int k0, double b0, int k1, double b1);
+
+typedef struct { double t; int kind; double bnd; } tcross;
+
+/* Pieces of the edge A -> B, one per pixel cell on its way, each with the
+ * kinds of its two ends (start, end, or the pixel boundary crossed), in
+ * exact arithmetic.  The cell sequence is that of the reference's walk
+ * (rasterizer.rs:72-121) without rounding: it starts in floor(A), a crossing
+ * of a vertical boundary moves one column, of a horizontal one one row,
+ * simultaneous crossings take the column first (the walk's tie rule), and a
+ * crossing exactly at B still moves into floor(B).  Pieces may have zero
+ * length (an end point on a boundary, or a pass through a pixel corner). */
+static int cmp_tcross_kind(const void *a, const void *b) {
+    const tcross *x = (const tcross *)a, *y = (const tcross *)b;
+    if (x->t != y->t) return x->t < y->t ? -1 : 1;
+    return x->kind - y->kind;   /* vertical (1) before horizontal (2) */
+}
+
+static int clip_edge(dv2 A, dv2 B, piece_fn fn, void *u) {
+    const double dx = B.x - A.x, dy = B.y - A.y;
+    const long ax = (long)floor(A.x), ay = (long)floor(A.y), bx = (long)floor(B.x), by = (long)floor(B.y);
+    const size_t cap = (size_t)(labs(bx - ax) + labs(by - ay) + 2);
+    tcross *ts = (tcross *)malloc(cap * sizeof(tcross));
+    if (!ts) return OCHRE_ORACLE_E_NOMEM;
+    size_t n = 0;
+    if (dx > 0.0)
+        for (long k = ax + 1; k <= bx; k++) { ts[n].t = ((double)k - A.x) / dx; ts[n].kind = 1; ts[n].bnd = (double)k; n++; }
+    else if (dx < 0.0)
+        for (long k = ax; k > bx; k--) { ts[n].t = ((double)k - A.x) / dx; ts[n].kind = 1; ts[n].bnd = (double)k; n++; }
+    if (dy > 0.0)
+        for (long k = ay + 1; k <= by; k++) { ts[n].t = ((double)k - A.y) / dy; ts[n].kind = 2; ts[n].bnd = (double)k; n++; }
+    else if (dy < 0.0)
+        for (long k = ay; k > by; k--) { ts[n].t = ((double)k - A.y) / dy; ts[n].kind = 2; ts[n].bnd = (double)k; n++; }
+    qsort(ts, n, sizeof(tcross), cmp_tcross_kind);
+    long cx = ax, cy = ay;
+    dv2 p0 = A;
+    int k0 = 0;
+    double b0 = 0.0;
+    for (size_t i = 0; i <= n; i++) {
+        dv2 p1 = B;
+        int k1 = 0;
+        double b1 = 0.0;
+        if (i < n) {
+            const double t = ts[i].t;
+            p1.x = A.x + t * dx;
+            p1.y = A.y + t * dy;
+            k1 = ts[i].kind;
+            b1 = ts[i].bnd;
+            if (k1 == 1) p1.x = b1; else p1.y = b1;
+        }
+        fn(u, cx, cy, p0, p1, k0, b0, k1, b1);
+        if (i < n) {
+            if (k1 == 1) cx += dx > 0.0 ? 1 : -1;
+            else cy += dy > 0.0 ? 1 : -1;
+        }
+        p0 = p1;
+        k0 = k1;
+        b0 = b1;
+    }
+    free(ts);
+    return 0;
+}
+
+typedef struct {
+    int W, H;
+    double *area, *hgt, *left;   /* forward accumulation */
+    const double *g, *G, *gleft; /* backward: dL/dS, suffix sums, row totals */
+    dv2 A, B;                    /* current edge */
+    dv2 dA, dB;
+} diffctx;
+
+static void fwd_piece(void *u, long cx, long cy, dv2 p0, dv2 p1, int k0, double b0, int k1, double b1) {
+    (void)k0; (void)b0; (void)k1; (void)b1;
+    diffctx *d = (diffctx *)u;
+    if (cy < 0 || cy >= d->H) return;
+    const double h = p1.y - p0.y;
+    if (cx < 0) { d->left[cy] += h; return; }
+    if (cx >= d->W) return;
+    const double right = (double)(cx + 1);
+    d->area[(size_t)cy * d->W + cx] += 0.5 * h * ((right - p0.x) + (right - p1.x));
+    d->hgt[(size_t)cy * d->W + cx] += h;
+}
+
+static void lookup(const diffctx *d, long cx, long cy, double *g, double *G) {
+    *g = 0.0; *G = 0.0;
+    if (cy < 0 || cy >= d->H) return;
+    if (cx < 0) { *G = d->gleft[cy]; return; }
+    if (cx >= d->W) return;
+    *g = d->g[(size_t)cy * d->W + cx];
+    *G = d->G[(size_t)cy * d->W + cx];
+}
+
+/* dL/d(A, B) of a point on the edge given by its kind (see clip_edge) */
+static void chain_point(diffctx *d, int kind, double bnd, int is_end, double gx, double gy) {
+    const dv2 A = d->A, B = d->B;
+    const double D = B.x - A.x, E = B.y - A.y;
+    if (kind == 0) {
+        if (is_end) { d->dB.x += gx; d->dB.y += gy; }
+        else { d->dA.x += gx; d->dA.y += gy; }
+    } else if (kind == 1) {
+        const double s = (bnd - A.x) / D;
+        d->dA.y += gy * (1.0 - s);
+        d->dB.y += gy * s;
+        d->dA.x += gy * E * (s - 1.0) / D;
+        d->dB.x += gy * (-E * s / D);
+    } else {
+        const double u = (bnd - A.y) / E;
+        d->dA.x += gx * (1.0 - u);
+        d->dB.x += gx * u;
+        d->dA.y += gx * D * (u - 1.0) / E;
+        d->dB.y += gx * (-D * u / E);
+    }
+}
+
+static void bwd_piece(void *u, long cx, long cy, dv2 p0, dv2 p1, int k0, double b0, int k1, double b1) {
+    diffctx *d = (diffctx *)u;
+    double g, G;
+    lookup(d, cx, cy, &g, &G);
+    if (g == 0.0 && G == 0.0) return;
+    const double h = p1.y - p0.y;
+    const double right = (double)(cx + 1);
+    const double m = 0.5 * ((right - p0.x) + (right - p1.x));
+    chain_point(d, k0, b0, 0, -0.5 * h * g, -m * g - G);
+    chain_point(d, k1, b1, 1, -0.5 * h * g, m * g + G);
+}
+
+/* Edges of one raster in the model, with the points they depend on. */
+typedef struct {
+    dedge *e; size_t n, cap;
+    pref *ra, *rb;          /* per edge: point refs of A and B when they are plain points (closing lines, lines) */
+} edges_t;
+
+static int push_edge(edges_t *E, dv2 a, dv2 b, pref ra, pref rb) {
+    if (E->n == E->cap) {
+        size_t c = E->cap ? E->cap * 2 : 256;
+        dedge *p = (dedge *)realloc(E->e, c * sizeof(dedge));
+        pref *qa = (pref *)realloc(E->ra, c * sizeof(pref));
+        pref *qb = (pref *)realloc(E->rb, c * sizeof(pref));
+        if (p) E->e = p;
+        if (qa) E->ra = qa;
+        if (qb) E->rb = qb;
+        if (!p || !qa || !qb) return OCHRE_ORACLE_E_NOMEM;
+        E->cap = c;
+    }
+    E->e[E->n].a = a; E->e[E->n].b = b;
+    E->ra[E->n] = ra; E->rb[E->n] = rb;
+    E->n++;
+    return 0;
+}
+
+static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, const double *target,
+                       const double *dl_ds, double *loss_out, double *dpts, double *dxf) {
+    uint64_t *off = NULL;
+    int st = validate(bt, &off);
+    if (st) return st;
+    const size_t npx = (size_t)W * (size_t)H;
+    double *area = (double *)malloc(npx * sizeof(double));
+    double *hgt = (double *)malloc(npx * sizeof(double));
+    double *gimg = (double *)malloc(npx * sizeof(double));
+    double *Gimg = (double *)malloc(npx * sizeof(double));
+    double *left = (double *)malloc((size_t)H * sizeof(double));
+    double *gleft = (double *)malloc((size_t)H * sizeof(double));
+    double *dp = (double *)calloc(bt->n_floats ? bt->n_floats : 1, sizeof(double));   /* device-space point grads */
+    if (!area || !hgt || !gimg || !Gimg || !left || !gleft || !dp) { st = OCHRE_ORACLE_E_NOMEM; goto done; }
+    if (dpts) for (uint64_t i = 0; i < bt->n_floats; i++) dpts[i] = 0.0;
+    if (dxf) for (uint32_t i = 0; i < 6 * bt->n_fills; i++) dxf[i] = 0.0;
+    double loss = 0.0;
+    for (uint32_t ri = 0; ri < bt->n_rasters && !st; ri++) {
+        uint32_t f0 = bt->raster_fill_off ? bt->raster_fill_off[ri] : ri;
+        uint32_t f1 = bt->raster_fill_off ? bt->raster_fill_off[ri + 1] : ri + 1;
+        edges_t E = {0};
+        /* per command: first own edge, own edge count */
+        uint64_t c0 = bt->fill_cmd_off[f0], c1 = bt->fill_cmd_off[f1];
+        size_t ncmd = (size_t)(c1 - c0);
+        size_t *e_first = (size_t *)malloc((ncmd + 1) * sizeof(size_t));
+        dv2 *cpts = (dv2 *)malloc((ncmd ? ncmd : 1) * 3 * sizeof(dv2));
+        if (!e_first || !cpts) { free(e_first); free(cpts); st = OCHRE_ORACLE_E_NOMEM; break; }
+        dv2 last = {0.0, 0.0}, first = {0.0, 0.0};
+        pref last_ref = {-1, 0}, first_ref = {-1, 0};
+        /* ---- edges ---- */
+        for (uint32_t f = f0; f < f1 && !st; f++) {
+            const float *xf = bt->fill_xf + 6 * (size_t)f;
+            int raw = bt->fill_flags ? (bt->fill_flags[f] & 1) : 0;
+            for (uint64_t c = bt->fill_cmd_off[f]; c < bt->fill_cmd_off[f + 1]; c++) {
+                const size_t li = (size_t)(c - c0);
+                uint8_t verb = bt->verbs[c];
+                const float *fp = bt->pts + off[c];
+                dv2 *p = cpts + 3 * li;
+                for (int k = 0; k < npts_of(verb); k++) {
+                    dv2 v = {fp[2 * k], fp[2 * k + 1]};
+                    p[k] = raw ? v : dxf_apply(xf, v);
+                }
+                e_first[li] = E.n;
+                pref self0 = {(int64_t)c, 0}, none = {-1, 0};
+                if (verb == 0) {
+                    st = push_edge(&E, last, first, last_ref, first_ref);
+                    first = p[0]; last = p[0];
+                    first_ref = self0; last_ref = self0;
+                } else if (verb == 1) {
+                    st = push_edge(&E, last, p[0], last_ref, self0);
+                    last = p[0]; last_ref = self0;
+                } else if (verb == 2 || verb == 3) {
+                    const uint32_t n = counts[c];
+                    double dt;
+                    if (verb == 2) {
+                        dv2 v = {last.x - 2.0 * p[0].x + p[1].x, last.y - 2.0 * p[0].y + p[1].y};
+                        dt = sqrt(0.4 / sqrt(v.x * v.x + v.y * v.y));
+                    } else {
+                        dv2 b = {3.0 * (last.x - 2.0 * p[0].x + p[1].x), 3.0 * (last.y - 2.0 * p[0].y + p[1].y)};
+                        dv2 ab = {2.0 * last.x - 3.0 * p[0].x + p[2].x, 2.0 * last.y - 3.0 * p[0].y + p[2].y};
+                        double conc = fmax(sqrt(b.x * b.x + b.y * b.y), sqrt(ab.x * ab.x + ab.y * ab.y));
+                        dt = sqrt(sqrt(8.0) * 0.1 / conc);
+                    }
+                    dv2 prev = last;
+                    for (uint32_t j = 1; j <= n && !st; j++) {
+                        double t = j == n ? 1.0 : fmin((double)j * dt, 1.0), u = 1.0 - t;
+                        dv2 q;
+                        if (verb == 2) {
+                            q.x = u * u * last.x + 2.0 * u * t * p[0].x + t * t * p[1].x;
+                            q.y = u * u * last.y + 2.0 * u * t * p[0].y + t * t * p[1].y;
+                        } else {
+                            q.x = u * u * u * last.x + 3.0 * u * u * t * p[0].x + 3.0 * u * t * t * p[1].x + t * t * t * p[2].x;
+                            q.y = u * u * u * last.y + 3.0 * u * u * t * p[0].y + 3.0 * u * t * t * p[1].y + t * t * t * p[2].y;
+                        }
+                        st = push_edge(&E, prev, q, none, none);
+                        prev = q;
+                    }
+                    last = p[verb == 2 ? 1 : 2];
+                    last_ref.cmd = (int64_t)c; last_ref.pt = verb == 2 ? 1 : 2;
+                } else if (verb == 4) {
+                    st = OCHRE_ORACLE_E_INVALID;   /* conics are outside the differentiable model */
+                }
+            }
+        }
+        e_first[ncmd] = E.n;
+        if (!st) st = push_edge(&E, last, first, last_ref, first_ref);   /* finish's closing line */
+        /* ---- forward ---- */
+        diffctx d;
+        memset(&d, 0, sizeof d);
+        d.W = W; d.H = H; d.area = area; d.hgt = hgt; d.left = left;
+        for (size_t i = 0; i < npx; i++) { area[i] = 0.0; hgt[i] = 0.0; }
+        for (int y = 0; y < H; y++) left[y] = 0.0;
+        for (size_t e = 0; e < E.n && !st; e++)
+            if (!(E.e[e].a.x == E.e[e].b.x && E.e[e].a.y == E.e[e].b.y)) st = clip_edge(E.e[e].a, E.e[e].b, fwd_piece, &d);
+        const double *tgt = target ? target + (size_t)ri * npx : NULL;
+        for (int y = 0; y < H && !tgt; y++)
+            for (int x = 0; x < W; x++) gimg[(size_t)y * W + x] = dl_ds[(size_t)ri * npx + (size_t)y * W + x];
+        for (int y = 0; y < H && tgt; y++) {
+            double acc = left[y];
+            for (int x = 0; x < W; x++) {
+                const size_t i = (size_t)y * W + x;
+                const double S = acc + area[i];
+                acc += hgt[i];
+                const double c = fmin(fabs(S), 1.0);
+                loss += (c - tgt[i]) * (c - tgt[i]);
+                const double gc = 2.0 * (c - tgt[i]);
+                gimg[i] = fabs(S) < 1.0 ? (S > 0.0 ? gc : S < 0.0 ? -gc : 0.0) : 0.0;
+            }
+        }
+        if (dpts || dxf) {
+            /* suffix sums of dL/dS to the right of each pixel, and row totals */
+            for (int y = 0; y < H; y++) {
+                double s = 0.0;
+                for (int x = W - 1; x >= 0; x--) {
+                    Gimg[(size_t)y * W + x] = s;
+                    s += gimg[(size_t)y * W + x];
+                }
+                gleft[y] = s;
+            }
+            d.g = gimg; d.G = Gimg; d.gleft = gleft;
+            dv2 *gA = (dv2 *)calloc(E.n ? E.n : 1, sizeof(dv2));
+            dv2 *gB = (dv2 *)calloc(E.n ? E.n : 1, sizeof(dv2));
+            if (!gA || !gB) { free(gA); free(gB); st = OCHRE_ORACLE_E_NOMEM; }
+            for (size_t e = 0; e < E.n && !st; e++) {
+                d.A = E.e[e].a; d.B = E.e[e].b;
+                d.dA.x = d.dA.y = d.dB.x = d.dB.y = 0.0;
+                if (d.A.x == d.B.x && d.A.y == d.B.y) {
+                    double g, G;
+                    const long cx = (long)floor(d.B.x), cy = (long)floor(d.B.y);
+                    lookup(&d, cx, cy, &g, &G);
+                    const double dy = ((double)(cx + 1) - d.B.x) * g + G;
+                    d.dA.y = -dy; d.dB.y = dy;
+                } else {
+                    st = clip_edge(d.A, d.B, bwd_piece, &d);
+                }
+                gA[e] = d.dA; gB[e] = d.dB;
+            }
+            /* flatten adjoint: edge end points back to device-space points */
+#define ADDP(ref, vx, vy) do { if ((ref).cmd >= 0) { dp[off[(ref).cmd] + 2 * (ref).pt] += (vx); dp[off[(ref).cmd] + 2 * (ref).pt + 1] += (vy); } } while (0)
+            last_ref.cmd = -1; first_ref.cmd = -1;
+            dv2 lastp = {0.0, 0.0};
+            for (size_t li = 0; li < ncmd && !st; li++) {
+                const uint64_t c = c0 + li;
+                const uint8_t verb = bt->verbs[c];
+                const size_t e0 = e_first[li], e1 = e_first[li + 1];
+                const dv2 *p = cpts + 3 * li;
+                pref self0 = {(int64_t)c, 0};
+                if (verb == 0) {
+                    ADDP(E.ra[e0], gA[e0].x, gA[e0].y);
+                    ADDP(E.rb[e0], gB[e0].x, gB[e0].y);
+                    first_ref = self0; last_ref = self0; lastp = p[0];
+                } else if (verb == 1) {
+                    ADDP(E.ra[e0], gA[e0].x, gA[e0].y);
+                    ADDP(E.rb[e0], gB[e0].x, gB[e0].y);
+                    last_ref = self0; lastp = p[0];
+                } else if (verb == 2 || verb == 3) {
+                    const int cubic = verb == 3;
+                    const size_t n = e1 - e0;
+                    const dv2 P0 = lastp, P1 = p[0], P2 = p[1], P3 = cubic ? p[2] : p[1];
+                    double dt, S = 0.0;
+                    dv2 g[4] = {{gA[e0].x, gA[e0].y}, {0, 0}, {0, 0}, {0, 0}};
+                    if (!cubic) {
+                        dv2 v = {P0.x - 2.0 * P1.x + P2.x, P0.y - 2.0 * P1.y + P2.y};
+                        dt = sqrt(0.4 / sqrt(v.x * v.x + v.y * v.y));
+                    } else {
+                        dv2 b = {3.0 * (P0.x - 2.0 * P1.x + P2.x), 3.0 * (P0.y - 2.0 * P1.y + P2.y)};
+                        dv2 ab = {2.0 * P0.x - 3.0 * P1.x + P3.x, 2.0 * P0.y - 3.0 * P1.y + P3.y};
+                        dt = sqrt(sqrt(8.0) * 0.1 / fmax(sqrt(b.x * b.x + b.y * b.y), sqrt(ab.x * ab.x + ab.y * ab.y)));
+                    }
+                    for (size_t j = 1; j <= n; j++) {
+                        const double t = j == n ? 1.0 : fmin((double)j * dt, 1.0), u = 1.0 - t;
+                        dv2 dq = gB[e0 + j - 1];
+                        if (j < n) { dq.x += gA[e0 + j].x; dq.y += gA[e0 + j].y; }
+                        dv2 dc;
+                        if (cubic) {
+                            const double b0 = u * u * u, b1 = 3 * u * u * t, b2 = 3 * u * t * t, b3 = t * t * t;
+                            g[0].x += b0 * dq.x; g[0].y += b0 * dq.y; g[1].x += b1 * dq.x; g[1].y += b1 * dq.y;
+                            g[2].x += b2 * dq.x; g[2].y += b2 * dq.y; g[3].x += b3 * dq.x; g[3].y += b3 * dq.y;
+                            dc.x = 3 * u * u * (P1.x - P0.x) + 6 * u * t * (P2.x - P1.x) + 3 * t * t * (P3.x - P2.x);
+                            dc.y = 3 * u * u * (P1.y - P0.y) + 6 * u * t * (P2.y - P1.y) + 3 * t * t * (P3.y - P2.y);
+                        } else {
+                            const double b0 = u * u, b1 = 2 * u * t, b2 = t * t;
+                            g[0].x += b0 * dq.x; g[0].y += b0 * dq.y; g[1].x += b1 * dq.x; g[1].y += b1 * dq.y;
+                            g[2].x += b2 * dq.x; g[2].y += b2 * dq.y;
+                            dc.x = 2 * u * (P1.x - P0.x) + 2 * t * (P2.x - P1.x);
+                            dc.y = 2 * u * (P1.y - P0.y) + 2 * t * (P2.y - P1.y);
+                        }
+                        if (j < n && (double)j * dt < 1.0) S += (double)j * (dc.x * dq.x + dc.y * dq.y);
+                    }
+                    if (S != 0.0 && isfinite(dt)) {
+                        if (cubic) {
+                            dv2 b = {3.0 * (P0.x - 2.0 * P1.x + P2.x), 3.0 * (P0.y - 2.0 * P1.y + P2.y)};
+                            dv2 ab = {2.0 * P0.x - 3.0 * P1.x + P3.x, 2.0 * P0.y - 3.0 * P1.y + P3.y};
+                            const double lb = sqrt(b.x * b.x + b.y * b.y), lab = sqrt(ab.x * ab.x + ab.y * ab.y);
+                            const double conc = fmax(lb, lab), k1 = S * (-0.5 * dt / conc);
+                            if (lb >= lab && lb > 0.0) {
+                                const dv2 u1 = {k1 * b.x / lb, k1 * b.y / lb};
+                                g[0].x += 3 * u1.x; g[0].y += 3 * u1.y; g[1].x -= 6 * u1.x; g[1].y -= 6 * u1.y;
+                                g[2].x += 3 * u1.x; g[2].y += 3 * u1.y;
+                            } else if (lab > 0.0) {
+                                const dv2 u1 = {k1 * ab.x / lab, k1 * ab.y / lab};
+                                g[0].x += 2 * u1.x; g[0].y += 2 * u1.y; g[1].x -= 3 * u1.x; g[1].y -= 3 * u1.y;
+                                g[3].x += u1.x; g[3].y += u1.y;
+                            }
+                        } else {
+                            const dv2 v = {P0.x - 2.0 * P1.x + P2.x, P0.y - 2.0 * P1.y + P2.y};
+                            const double len2 = v.x * v.x + v.y * v.y;
+                            if (len2 > 0.0) {
+                                const double k1 = S * (-0.5 * dt / len2);
+                                g[0].x += k1 * v.x; g[0].y += k1 * v.y; g[1].x -= 2 * k1 * v.x; g[1].y -= 2 * k1 * v.y;
+                                g[2].x += k1 * v.x; g[2].y += k1 * v.y;
+                            }
+                        }
+                    }
+                    ADDP(last_ref, g[0].x, g[0].y);
+                    pref r1 = {(int64_t)c, 0}, r2 = {(int64_t)c, 1}, r3 = {(int64_t)c, 2};
+                    ADDP(r1, g[1].x, g[1].y);
+                    ADDP(r2, g[2].x, g[2].y);
+                    if (cubic) ADDP(r3, g[3].x, g[3].y);
+                    last_ref.cmd = (int64_t)c; last_ref.pt = cubic ? 2 : 1; lastp = cubic ? p[2] : p[1];
+                }
+            }
+            {
+                const size_t e = E.n - 1;   /* finish's closing line */
+                ADDP(E.ra[e], gA[e].x, gA[e].y);
+                ADDP(E.rb[e], gB[e].x, gB[e].y);
+            }
+#undef ADDP
+            free(gA); free(gB);
+        }
+        free(E.e); free(E.ra); free(E.rb); free(e_first); free(cpts);
+    }
+    /* transform adjoint */
+    if (!st && (dpts || dxf)) {
+        for (uint32_t f = 0; f < bt->n_fills; f++) {
+            const float *xf = bt->fill_xf + 6 * (size_t)f;
+            int raw = bt->fill_flags ? (bt->fill_flags[f] & 1) : 0;
+            for (uint64_t c = bt->fill_cmd_off[f]; c < bt->fill_cmd_off[f + 1]; c++) {
+                const float *fp = bt->pts + off[c];
+                for (int k = 0; k < npts_of(bt->verbs[c]); k++) {
+                    const double gx = dp[off[c] + 2 * k], gy = dp[off[c] + 2 * k + 1];
+                    const double vx = fp[2 * k], vy = fp[2 * k + 1];
+                    if (dpts) {
+                        if (raw) { dpts[off[c] + 2 * k] = gx; dpts[off[c] + 2 * k + 1] = gy; }
+                        else {
+                            dpts[off[c] + 2 * k] = xf[0] * gx + xf[2] * gy;
+                            dpts[off[c] + 2 * k + 1] = xf[1] * gx + xf[3] * gy;
+                        }
+                    }
+                    if (dxf && !raw) {
+                        dxf[6 * f + 0] += gx * vx; dxf[6 * f + 1] += gx * vy;
+                        dxf[6 * f + 2] += gy * vx; dxf[6 * f + 3] += gy * vy;
+                        dxf[6 * f + 4] += gx; dxf[6 * f + 5] += gy;
+                    }
+                }
+            }
+        }
+    }
+    *loss_out = 0.0;
+    if (!st) *loss_out = loss;
+done:
+    free(area); free(hgt); free(gimg); free(Gimg); free(left); free(gleft); free(dp); free(off);
+    return st;
+}
+
+int ochre_oracle_diff64(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, const double *target,
+                        double *loss_out, double *dpts, double *dxf) {
+    return diff64_impl(bt, counts, W, H, target, NULL, loss_out, dpts, dxf);
+}
+
+int ochre_oracle_backward64(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, const double *dl_ds,
+                            double *dpts, double *dxf) {
+    double loss;
+    return diff64_impl(bt, counts, W, H, NULL, dl_ds, &loss, dpts, dxf);
+}

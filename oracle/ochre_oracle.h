@@ -73,6 +73,17 @@ int ochre_oracle_cov64(const float *lines, const uint64_t *raster_line_off, uint
                        const int32_t *rect, double *out);
 void ochre_oracle_free(ochre_oracle_result *r);
 
+/* Differentiable model in double (see ochre_oracle.c): per-command line
+ * counts of the f32 flattening, then loss and gradients for a w x h canvas
+ * per raster against `target` (n_rasters * w * h).  dpts / dxf may be NULL. */
+int ochre_oracle_seg_counts(const ochre_oracle_batch *batch, uint32_t *counts);
+int ochre_oracle_diff64(const ochre_oracle_batch *batch, const uint32_t *counts, int w, int h, const double *target,
+                        double *loss, double *dpts, double *dxf);
+/* The same backward from a given dL/dS per pixel (S = accum + area before
+ * |.| and the clamp), n_rasters * w * h values. */
+int ochre_oracle_backward64(const ochre_oracle_batch *batch, const uint32_t *counts, int w, int h, const double *dl_ds,
+                            double *dpts, double *dxf);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,270 @@
+"""Differentiable fill: coverage render, L2 loss and the hand-written backward.
+
+The FP64 model in the oracle (``oracle.diff64``) is first checked against
+central finite differences (h = 1e-3 px on control points and translations;
+the same 1e-3 px displacement on the linear part of a transform), then the
+GPU's f32 gradient is checked against the FP64 gradient.  Tolerance for
+both: relative L2 error <= 1e-3 over the checked parameters.
+"""
+from __future__ import annotations
+
+import copy
+
+import numpy as np
+import pytest
+
+import oracle
+from ochre_gb300 import workloads as W
+
+REL_TOL = 1e-3
+FD_H = 1e-3
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64).ravel(), np.asarray(b, np.float64).ravel()
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _params(batch, n_pts, n_xf, seed):
+    """n_pts point coordinates and n_xf transform entries, picked at random
+    among those with a non-trivial gradient (non-raw fills)."""
+    rng = np.random.default_rng(seed)
+    pts = rng.choice(len(batch.pts), n_pts, replace=False)
+    xf = rng.choice(6 * batch.n_fills, n_xf, replace=False)
+    return pts, xf
+
+
+def _central_fd(batch, w, h, target, counts, pts_idx, xf_idx):
+    """Central differences of the FP64 loss; steps are taken on the f32
+    inputs and divided by the step actually represented."""
+    out = []
+    for i in pts_idx:
+        vals = []
+        for s in (1.0, -1.0):
+            b = copy.copy(batch)
+            b.pts = batch.pts.copy()
+            b.pts[i] = np.float32(float(batch.pts[i]) + s * FD_H)
+            vals.append((oracle.diff64(b, w, h, target, counts, grad=False)[0], float(b.pts[i])))
+        out.append((vals[0][0] - vals[1][0]) / (vals[0][1] - vals[1][1]))
+    for i in xf_idx:
+        f, k = divmod(int(i), 6)
+        if k < 4:
+            # the linear part scales coordinates: step so points move ~1e-3 px
+            c0, c1 = batch.fill_cmd_off[f], batch.fill_cmd_off[f + 1]
+            span = np.abs(batch.pts[_float_range(batch, c0, c1)]).max()
+            step = FD_H / max(float(span), 1.0)
+        else:
+            step = FD_H
+        vals = []
+        for s in (1.0, -1.0):
+            b = copy.copy(batch)
+            b.fill_xf = batch.fill_xf.copy()
+            b.fill_xf[f, k] = np.float32(float(batch.fill_xf[f, k]) + s * step)
+            vals.append((oracle.diff64(b, w, h, target, counts, grad=False)[0], float(b.fill_xf[f, k])))
+        out.append((vals[0][0] - vals[1][0]) / (vals[0][1] - vals[1][1]))
+    return np.array(out)
+
+
+def _float_range(batch, c0, c1):
+    from ochre_gb300.batch import FLOATS_PER_VERB
+    nf = FLOATS_PER_VERB[batch.verbs].astype(np.int64)
+    off = np.concatenate([[0], np.cumsum(nf)])
+    return slice(int(off[c0]), int(off[c1]))
+
+
+def _small_scenes():
+    return W.diff_scenes(n_scenes=3, seed=11, size=128.0, min_paths=2, max_paths=4, min_seg=4, max_seg=12)
+
+
+# ---------------------------------------------------------------- CPU: oracle
+
+
+@pytest.mark.parametrize("case", ["union", "scenes"])
+def test_fp64_gradient_matches_central_differences(case):
+    if case == "union":
+        b, w, h = W.diff_union(n_paths=6), 1024, 1024
+        tgt = oracle.coverage_image(W.diff_union(n_paths=6, perturb=2.0), w, h)
+    else:
+        b, w, h = _small_scenes(), 128, 128
+        pert = copy.copy(b)
+        pert.pts = (b.pts + np.random.default_rng(3).normal(0, 1.0, b.pts.shape)).astype(np.float32)
+        tgt = oracle.coverage_image(pert, w, h)
+    tgt = tgt.astype(np.float64)
+    counts = oracle.seg_counts(b)
+    loss, dp, dx = oracle.diff64(b, w, h, tgt, counts)
+    assert loss > 0.0
+    pi, xi = _params(b, 56, 8, seed=1)
+    fd = _central_fd(b, w, h, tgt, counts, pi, xi)
+    an = np.concatenate([dp[pi], dx.reshape(-1)[xi]])
+    assert np.linalg.norm(an) > 0.0
+    assert _rel(an, fd) <= REL_TOL, (_rel(an, fd), np.c_[an, fd])
+
+
+@pytest.mark.parametrize("on_grid", [False, True])
+def test_fp64_gradient_matches_central_differences_everywhere(on_grid):
+    """Every parameter of a small batch, including points on pixel corners
+    (the coverage is continuously differentiable there too)."""
+    b, w, h = _raw_and_multi_contour_batch(on_grid), 128, 128
+    pert = copy.copy(b)
+    pert.pts = (b.pts + np.random.default_rng(5).normal(0, 1.5, b.pts.shape)).astype(np.float32)
+    tgt = oracle.coverage_image(pert, w, h).astype(np.float64)
+    counts = oracle.seg_counts(b)
+    _, dp, dx = oracle.diff64(b, w, h, tgt, counts)
+    fd = _central_fd(b, w, h, tgt, counts, np.arange(len(b.pts)), np.arange(6 * b.n_fills))
+    an = np.concatenate([dp, dx.ravel()])
+    assert _rel(an, fd) <= REL_TOL, _rel(an, fd)
+
+
+def test_fp64_gradient_is_zero_at_the_target():
+    b = W.diff_union(n_paths=4)
+    tgt = oracle.coverage_image(b, 1024, 1024).astype(np.float64)
+    loss, dp, dx = oracle.diff64(b, 1024, 1024, tgt)
+    # the f32 image differs from the FP64 area only by rounding (~1e-4 per
+    # edge pixel), so loss and gradient nearly vanish; against a target
+    # perturbed by 2 px they are ~1e3 and ~1e1 (points) / ~1e4 (transforms)
+    assert loss < 1e-4
+    assert np.abs(dp).max() < 1e-2 and np.abs(dx).max() < 10.0
+
+
+def test_fp64_model_rejects_conics():
+    from ochre_gb300.batch import BatchBuilder
+    bb = BatchBuilder()
+    bb.begin_raster().fill([0, 4, 5], [0, 0, 10, 0, 10, 10, 0.5], [1, 0, 0, 1, 0, 0])
+    with pytest.raises(RuntimeError):
+        oracle.diff64(bb.build(), 16, 16, np.zeros((1, 16, 16)))
+
+
+# ---------------------------------------------------------------- GPU
+
+
+def _gpu_grad(batch, w, h, target):
+    import torch
+    from ochre_gb300 import DeviceBatch, GpuContext
+    ctx = GpuContext(0)
+    db = DeviceBatch(batch, 0)
+    cov = ctx.render_coverage(db, w, h)
+    t = torch.as_tensor(np.ascontiguousarray(target, np.float32), device="cuda:0")
+    dl = torch.empty_like(cov)
+    loss, _ = ctx.l2_loss(cov, t, dl)
+    dp, dx = ctx.fill_backward(db, w, h, dl)
+    torch.cuda.synchronize()
+    out = (float(loss.item()), dp.cpu().numpy()[:len(batch.pts)].astype(np.float64),
+           dx.cpu().numpy()[:batch.n_fills].astype(np.float64), cov.cpu().numpy())
+    ctx.close()
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["union", "scenes", "edge_cases"])
+def test_render_coverage_matches_oracle(name):
+    import torch
+    from ochre_gb300 import DeviceBatch, GpuContext
+    from tests.edge_cases import edge_batch
+    if name == "union":
+        b, w, h = W.diff_union(n_paths=32), 1024, 1024
+    elif name == "scenes":
+        b, w, h = W.diff_scenes(n_scenes=8, seed=12, size=256.0, min_paths=4, max_paths=32), 256, 256
+    else:
+        b, w, h = edge_batch()[0], 96, 80
+    ctx = GpuContext(0)
+    cov = ctx.render_coverage(DeviceBatch(b, 0), w, h)
+    torch.cuda.synchronize()
+    got = cov.cpu().numpy()
+    ctx.close()
+    ref = oracle.coverage_image(b, w, h)
+    assert got.shape == ref.shape
+    # same f32 accumulation up to summation order (pixels whose sum cancels
+    # to ~0 may differ in being exactly zero; the tile/span structure itself
+    # is checked exactly by the parity tests)
+    assert np.abs(got - ref).max() < 1e-3
+
+
+@pytest.mark.gpu
+def test_l2_loss_and_upstream_gradient():
+    import torch
+    from ochre_gb300 import GpuContext
+    g = torch.Generator(device="cuda:0").manual_seed(0)
+    cov = torch.rand((3, 70, 33), device="cuda:0", generator=g)
+    tgt = torch.rand((3, 70, 33), device="cuda:0", generator=g)
+    ctx = GpuContext(0)
+    dl = torch.empty_like(cov)
+    loss, _ = ctx.l2_loss(cov, tgt, dl)
+    torch.cuda.synchronize()
+    c, t = cov.cpu().double().numpy(), tgt.cpu().double().numpy()
+    assert abs(loss.item() - ((c - t) ** 2).sum()) < 1e-9 * max(1.0, ((c - t) ** 2).sum())
+    assert np.allclose(dl.cpu().numpy(), 2.0 * (cov - tgt).cpu().numpy(), atol=0, rtol=0)
+    ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["union", "scenes"])
+def test_gpu_gradient_matches_fp64(case):
+    """dL/d(control points) and dL/d(transform) against the FP64 reference
+    gradient of the same model (relative L2 error <= 1e-3)."""
+    if case == "union":
+        b, w, h = W.diff_union(n_paths=32), 1024, 1024
+        pert = W.diff_union(n_paths=32, perturb=2.0)
+    else:
+        b, w, h = W.diff_scenes(n_scenes=6, seed=13, size=256.0, min_paths=4, max_paths=24), 256, 256
+        pert = copy.copy(b)
+        pert.pts = (b.pts + np.random.default_rng(4).normal(0, 2.0, b.pts.shape)).astype(np.float32)
+    tgt = oracle.coverage_image(pert, w, h)
+    loss, dp, dx, cov = _gpu_grad(b, w, h, tgt)
+    rloss, rdp, rdx = oracle.diff64(b, w, h, tgt.astype(np.float64))
+    assert abs(loss - rloss) <= 1e-3 * rloss, (loss, rloss)
+    assert _rel(dp, rdp) <= REL_TOL, _rel(dp, rdp)
+    assert _rel(dx, rdx) <= REL_TOL, _rel(dx, rdx)
+
+
+@pytest.mark.gpu
+def test_gpu_gradient_matches_central_differences():
+    """The differentiable-fill workload's check: GPU gradient against FP64
+    central differences (h = 1e-3 px) on 64 random parameters."""
+    b, w, h = W.diff_union(n_paths=24), 1024, 1024
+    tgt = oracle.coverage_image(W.diff_union(n_paths=24, perturb=2.0), w, h)
+    _, dp, dx, _ = _gpu_grad(b, w, h, tgt)
+    counts = oracle.seg_counts(b)
+    pi, xi = _params(b, 56, 8, seed=2)
+    fd = _central_fd(b, w, h, tgt.astype(np.float64), counts, pi, xi)
+    an = np.concatenate([dp[pi], dx.reshape(-1)[xi]])
+    assert _rel(an, fd) <= REL_TOL, (_rel(an, fd), np.c_[an, fd])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("on_grid", [False, True])
+def test_gpu_gradient_raw_fills_and_multiple_contours(on_grid):
+    """Raw (untransformed) fills get point gradients and a zero transform
+    gradient; contours closed by Move, by Close and by finish all count.
+    With ``on_grid`` every point sits on a pixel corner, where the end points
+    and the lines through corners must take the walk's cells consistently."""
+    b = _raw_and_multi_contour_batch(on_grid)
+    w, h = 128, 128
+    pert = copy.copy(b)
+    pert.pts = (b.pts + np.random.default_rng(5).normal(0, 1.5, b.pts.shape)).astype(np.float32)
+    tgt = oracle.coverage_image(pert, w, h)
+    loss, dp, dx, _ = _gpu_grad(b, w, h, tgt)
+    rloss, rdp, rdx = oracle.diff64(b, w, h, tgt.astype(np.float64))
+    assert _rel(dp, rdp) <= REL_TOL, np.c_[dp, rdp]
+    assert _rel(dx, rdx) <= REL_TOL, np.c_[dx.ravel(), rdx.ravel()]
+    assert np.all(dx[1] == 0.0)
+
+
+def _raw_and_multi_contour_batch(on_grid=False):
+    """Two rasters: a transformed fill with two contours (the first closed by
+    the second Move) plus a raw fill, and a fill closed exactly at its start
+    under a general affine transform."""
+    from ochre_gb300.batch import BatchBuilder
+    bb = BatchBuilder()
+    bb.begin_raster()
+    # two contours, the first closed implicitly by the second Move
+    bb.fill([0, 3, 3, 0, 2, 2, 5],
+            [10, 10, 30, 5, 50, 20, 52, 40, 48, 60, 20, 55, 12, 30,
+             70, 70, 90, 72, 95, 90, 80, 100, 68, 88], [1, 0, 0, 1, 0, 0])
+    bb.fill([0, 1, 1, 1], [20, 80, 40, 82, 35, 100, 18, 96], [1, 0, 0, 1, 0, 0], raw=True)
+    bb.begin_raster()
+    bb.fill([0, 2, 2, 2], [5, 5, 40, 0, 60, 30, 70, 60, 30, 70, 8, 40, 5, 5], [0.9, 0.2, -0.1, 1.1, 4.5, 3.25])
+    b = bb.build()
+    if not on_grid:
+        off = np.tile(np.array([0.3719, 0.6133], np.float32), len(b.pts) // 2)
+        b.pts = (b.pts + off).astype(np.float32)
+    return b

@@ -185,15 +185,15 @@ def test_full_size_glyph_run_matches_oracle(gpu_ctx):
 @pytest.mark.parametrize("name,gen,kw,bound", [
     ("cubic_boxes", W.cubic_boxes, dict(n_paths=20), 2e-3),
     ("glyph_run", W.glyph_run, dict(n_paths=2000), 2e-3),
-    ("uneven_mix", W.uneven_mix, dict(n_paths=40), 0.1),
+    ("uneven_mix", W.uneven_mix, dict(n_paths=40), None),
     ("diff_union", W.diff_union, dict(n_paths=128), 2e-3),
     ("diff_scenes", W.diff_scenes, dict(n_scenes=2, max_paths=64), 2e-3),
 ])
 def test_coverage_error_vs_fp64(any_ctx, name, gen, kw, bound):
     """Pre-quantisation f32 coverage against the FP64 analytic area of the same
-    lines.  The bound for the uneven mix is loose on purpose: its long closing
-    lines (up to ~8000 px) drift in the reference's serial f32 DDA, which the
-    GPU reproduces bit for bit; the oracle shows the same error."""
+    lines.  The uneven mix has no absolute bound: its long lines (up to ~8000
+    px) drift in the reference's serial f32 walk, which the GPU reproduces,
+    so its error is bounded by the f32 restatement's own error instead."""
     b = gen(**kw)
     any_ctx.set_want_cov(True)
     try:
@@ -202,4 +202,8 @@ def test_coverage_error_vs_fp64(any_ctx, name, gen, kw, bound):
         any_ctx.set_want_cov(False)
     e = oracle.tile_cov_error_vs_fp64(b, got["tile_xy"], got["tile_cov"], got["raster_tile_off"])
     print(name, e)
-    assert e["max_abs"] < bound, e
+    if bound is None:
+        ref = oracle.run(b, want_cov=True)
+        e_ref = oracle.tile_cov_error_vs_fp64(b, ref["tile_xy"], ref["tile_cov"], ref["raster_tile_off"])
+        bound = e_ref["max_abs"] + 1e-3
+    assert e["max_abs"] < bound, (e, bound)
