@@ -219,6 +219,215 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def _event_ms(fn, stream, flush, reps):
+    """Median device time of fn() over reps calls, L2 flushed before each."""
+    import torch
+    out = []
+    for i in range(reps):
+        flush.fill_(i & 0xff)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return statistics.median(out)
+
+
+def _kernel_shares(ctx, fn):
+    import torch
+    ctx.set_profile(True)
+    fn()
+    torch.cuda.synchronize()
+    per = {}
+    for name, ms in ctx.timings():
+        d = per.setdefault(name, [0.0, 0])
+        d[0] += ms
+        d[1] += 1
+    ctx.set_profile(False)
+    total = sum(v[0] for v in per.values()) or 1.0
+    return sorted(({"kernel": k, "ms": v[0], "launches": v[1], "share": v[0] / total} for k, v in per.items()),
+                  key=lambda x: -x["ms"])
+
+
+def bench_uneven(ctx, stream, flush, steps, peak):
+    """Batched uneven-size mix (20,000 paths, lognormal segment counts) in one
+    call, against the plain chain run once per path (sampled)."""
+    import numpy as np
+    import torch
+    from ochre_gb300 import DeviceBatch, batch as B, workloads as W
+    bt = W.uneven_mix()
+    db = DeviceBatch(bt, ctx.device)
+    sp = stream.cuda_stream
+    for _ in range(2):
+        ctx.rasterize_device(db, sp)
+    st = ctx.stats()
+    ms = _event_ms(lambda: ctx.rasterize_device(db, sp), stream, flush, max(3, min(steps, 5)))
+    kernels = _kernel_shares(ctx, lambda: ctx.rasterize_device(db, sp))
+    dom = kernels[0]
+    dom_bytes = kernel_bytes(dom["kernel"], st, bt) / max(1, dom["launches"])
+    dom_ms = dom["ms"] / max(1, dom["launches"])
+    ach = dom_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    # the plain per-path chain: one chain (flatten -> DDA -> sort -> tiles) per path
+    rng = np.random.default_rng(0)
+    idx = np.sort(rng.choice(bt.n_rasters, 500, replace=False))
+    subs = [DeviceBatch(B.subset(bt, [int(i)]), ctx.device) for i in idx]
+    ctx.set_chain_only(True)
+    for d in subs[:10]:
+        ctx.rasterize_device(d, sp)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for d in subs:
+        ctx.rasterize_device(d, sp)
+    torch.cuda.synchronize()
+    per_path_s = (time.perf_counter() - t0) / len(subs)
+    chain_ms = _event_ms(lambda: ctx.rasterize_device(db, sp), stream, flush, 3)
+    ctx.set_chain_only(False)
+    comp = bt.input_bytes() + output_bytes(st["n_tiles"], st["n_spans"], bt.n_rasters)
+    return {
+        "workload": "uneven_mix: 20000 paths, lognormal(median 32) segments clipped to 4-20000, 8192x8192",
+        "paths_per_s": bt.n_rasters / (ms / 1e3), "tiles_per_s": st["n_tiles"] / (ms / 1e3), "ms_per_step": ms,
+        "tiles": st["n_tiles"], "spans": st["n_spans"], "lines": st["n_lines"], "sort_entries": st["n_entries"],
+        "path": "fused" if st.get("fused") else "chain", "launches_per_step": st["n_launches"],
+        "plain_per_path_chain": {"paths_per_s": 1.0 / per_path_s, "ms_per_path": 1e3 * per_path_s,
+                                 "sample_paths": len(subs), "timing": "host wall clock over the sample"},
+        "speedup_vs_per_path_chain": (bt.n_rasters / (ms / 1e3)) * per_path_s,
+        "one_call_chain_ms": chain_ms,
+        "roofline": {"kernel": dom["kernel"], "achieved_gbs": ach, "frac": ach / peak,
+                     "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+        "path_roofline": {"compulsory_bytes": comp, "achieved_gbs": comp / (ms / 1e3) / 1e9,
+                          "frac": comp / (ms / 1e3) / 1e9 / peak},
+        "kernels": kernels[:8],
+    }
+
+
+def bench_differentiable(ctx, stream, flush, steps, n_scenes):
+    """Forward (coverage render + L2 loss) and forward + backward scenes/s on
+    the single-raster union (256 paths x 32 cubics, 1024^2) and on batched
+    scenes (n_scenes x 512^2), with a gradient check against the FP64
+    reference on the union and on the first scenes of the batch."""
+    import copy
+
+    import numpy as np
+    import torch
+
+    import oracle
+    from ochre_gb300 import DeviceBatch, batch as B, workloads as W
+    out = {}
+    sp = stream.cuda_stream
+    cases = [("diff_union", W.diff_union(), W.diff_union(perturb=2.0), 1024, 1024)]
+    t0 = time.time()
+    sc = W.diff_scenes(n_scenes=n_scenes)
+    pert = copy.copy(sc)
+    pert.pts = (sc.pts + np.random.default_rng(4).normal(0, 2.0, sc.pts.shape)).astype(np.float32)
+    gen_s = time.time() - t0
+    cases.append(("diff_scenes", sc, pert, 512, 512))
+    for name, b, p, w, h in cases:
+        db, dp = DeviceBatch(b, ctx.device), DeviceBatch(p, ctx.device)
+        tgt = ctx.render_coverage(dp, w, h, stream=sp).clone()
+        del dp
+        cov = torch.empty((b.n_rasters, h, w), dtype=torch.float32, device=tgt.device)
+        dl = torch.empty_like(cov)
+        dpts = torch.empty(max(1, len(b.pts)), dtype=torch.float32, device=tgt.device)
+        dxf = torch.empty((max(1, b.n_fills), 6), dtype=torch.float32, device=tgt.device)
+
+        def fwd():
+            ctx.render_coverage(db, w, h, cov, stream=sp)
+            ctx.l2_loss(cov, tgt, dl, stream=sp)
+
+        def fwd_bwd():
+            fwd()
+            ctx.fill_backward(db, w, h, dl, dpts, dxf, stream=sp)
+
+        for _ in range(2):
+            fwd_bwd()
+        torch.cuda.synchronize()
+        reps = max(3, min(steps, 5))
+        f_ms = _event_ms(fwd, stream, flush, reps)
+        fb_ms = _event_ms(fwd_bwd, stream, flush, reps)
+        st = ctx.stats()
+        # gradient check against the FP64 reference (prefix of the batch)
+        k = b.n_rasters if name == "diff_union" else min(4, b.n_rasters)
+        sub = b if k == b.n_rasters else B.subset(b, list(range(k)))
+        g_dp = dpts.cpu().numpy()[:len(sub.pts)].astype(np.float64)
+        g_dx = dxf.cpu().numpy()[:sub.n_fills].astype(np.float64)
+        t_np = tgt[:k].cpu().numpy().astype(np.float64)
+        _, a_dp, a_dx = oracle.adjoint64(sub, w, h, t_np)
+        _, r_dp, r_dx = oracle.diff64(sub, w, h, t_np)
+        rel = lambda a, r: float(np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-300))
+        out[name] = {
+            "scenes": b.n_rasters, "canvas": [w, h], "fills": b.n_fills, "lines": st["n_lines"],
+            "fwd_ms": f_ms, "fwd_bwd_ms": fb_ms,
+            "fwd_scenes_per_s": b.n_rasters / (f_ms / 1e3), "fwd_bwd_scenes_per_s": b.n_rasters / (fb_ms / 1e3),
+            "fwd_bwd_over_fwd": f_ms / fb_ms,
+            "grad_rel_err": {
+                "scenes_checked": k,
+                "vs_fp64_reference": {"points": rel(g_dp, a_dp), "transforms": rel(g_dx, a_dx),
+                                      "note": "f32 forward (the reference's arithmetic), adjoint in double"},
+                "vs_fp64_forward": {"points": rel(g_dp, r_dp), "transforms": rel(g_dx, r_dx),
+                                    "note": "forward in double too: pixels whose |S| falls on the other "
+                                            "side of 1 in f32 change dL/dS there"}},
+            "kernels_backward": _kernel_shares(ctx, lambda: ctx.fill_backward(db, w, h, dl, dpts, dxf,
+                                                                              stream=sp))[:6],
+        }
+        del db, cov, dl, tgt, dpts, dxf
+        torch.cuda.empty_cache()
+    out["diff_scenes"]["generation_s"] = gen_s
+    out["fd_check"] = _fd_check(ctx, sp)
+    return out
+
+
+def _fd_check(ctx, sp, n_paths=16, n_params=64, h_px=1e-3):
+    """GPU gradient against central finite differences (h = 1e-3 px) of the
+    FP64 loss, on 64 random parameters of a union of 16 blobs x 32 cubics."""
+    import copy
+
+    import numpy as np
+    import torch
+
+    import oracle
+    from ochre_gb300 import DeviceBatch, workloads as W
+    b, w, h = W.diff_union(n_paths=n_paths), 1024, 1024
+    tgt = oracle.coverage_image(W.diff_union(n_paths=n_paths, perturb=2.0), w, h)
+    db = DeviceBatch(b, ctx.device)
+    cov = ctx.render_coverage(db, w, h, stream=sp)
+    t = torch.as_tensor(tgt, device=cov.device)
+    dl = torch.empty_like(cov)
+    ctx.l2_loss(cov, t, dl, stream=sp)
+    dp, dx = ctx.fill_backward(db, w, h, dl, stream=sp)
+    torch.cuda.synchronize()
+    dp, dx = dp.cpu().numpy().astype(np.float64), dx.cpu().numpy().astype(np.float64)
+    counts = oracle.seg_counts(b)
+    t64 = tgt.astype(np.float64)
+    rng = np.random.default_rng(2)
+    pi = rng.choice(len(b.pts), n_params - 8, replace=False)
+    xi = rng.choice(6 * b.n_fills, 8, replace=False)
+    fd, an = [], []
+    for i in pi:
+        v = []
+        for sgn in (1.0, -1.0):
+            bb = copy.copy(b)
+            bb.pts = b.pts.copy()
+            bb.pts[i] = np.float32(float(b.pts[i]) + sgn * h_px)
+            v.append((oracle.diff64(bb, w, h, t64, counts, grad=False)[0], float(bb.pts[i])))
+        fd.append((v[0][0] - v[1][0]) / (v[0][1] - v[1][1]))
+        an.append(dp[i])
+    for i in xi:
+        f, k = divmod(int(i), 6)
+        step = h_px if k >= 4 else h_px / 1024.0   # linear part: points move ~1e-3 px
+        v = []
+        for sgn in (1.0, -1.0):
+            bb = copy.copy(b)
+            bb.fill_xf = b.fill_xf.copy()
+            bb.fill_xf[f, k] = np.float32(float(b.fill_xf[f, k]) + sgn * step)
+            v.append((oracle.diff64(bb, w, h, t64, counts, grad=False)[0], float(bb.fill_xf[f, k])))
+        fd.append((v[0][0] - v[1][0]) / (v[0][1] - v[1][1]))
+        an.append(dx[f, k])
+    fd, an = np.array(fd), np.array(an)
+    return {"workload": f"diff_union {n_paths} paths x 32 cubics, 1024^2", "params": n_params, "h_px": h_px,
+            "rel_err": float(np.linalg.norm(an - fd) / np.linalg.norm(fd))}
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -355,6 +564,12 @@ def run_ours(args, ws, rank, local):
     if rank != 0:
         ctx.close()
         return
+    peaks, _ = load_peaks()
+    extensions = {}
+    if not args.no_extensions:
+        extensions["uneven_mix"] = bench_uneven(ctx, stream, flush, args.steps,
+                                                float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])))
+        extensions["differentiable"] = bench_differentiable(ctx, stream, flush, args.steps, args.diff_scenes)
     n_paths_all = batch.n_rasters * ws
     value = n_paths_all * args.steps / dev_s_max
     cpu = cpu_baseline(batch) if ws == 1 else None
@@ -386,6 +601,8 @@ def run_ours(args, ws, rank, local):
                         "ms_per_step": chain_step_ms, "launches_per_step": chain_st["n_launches"],
                         "note": "general flatten/DDA/sort/tile chain on the same batch"},
         "cpu_baseline": cpu,
+        "batched_uneven_mix": extensions.get("uneven_mix"),
+        "differentiable": extensions.get("differentiable"),
         "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s},
         "gpu_launches": launches,
@@ -404,6 +621,10 @@ def main():
     ap.add_argument("--workload", default="glyph_run")
     ap.add_argument("--n-paths", type=int, default=100_000)
     ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--diff-scenes", type=int, default=4096,
+                    help="scenes in the batched differentiable workload (512x512 each)")
+    ap.add_argument("--no-extensions", action="store_true",
+                    help="skip the uneven-mix and differentiable measurements")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

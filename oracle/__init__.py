@@ -125,7 +125,8 @@ def _as_batch(batch):
     return b, keep
 
 
-def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = False) -> dict:
+def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = False,
+        signed_cov: bool = False) -> dict:
     """Rasterize every raster of ``batch`` on the CPU.
 
     ``batch`` has the attributes of ``ochre_gb300.batch.Batch`` (numpy arrays
@@ -134,7 +135,7 @@ def run(batch, threads: int = 1, want_cov: bool = False, capture_lines: bool = F
     """
     lib = _load()
     b, keep = _as_batch(batch)
-    flags = (1 if want_cov else 0) | (2 if capture_lines else 0)
+    flags = (1 if want_cov else 0) | (2 if capture_lines else 0) | (4 if signed_cov else 0)
     res_p = ctypes.POINTER(_Result)()
     st = lib.ochre_oracle_run(ctypes.byref(b), int(threads), flags, ctypes.byref(res_p))
     if not res_p:
@@ -259,28 +260,52 @@ def backward64(batch, w: int, h: int, dl_ds: np.ndarray, counts=None):
     return dpts[:len(batch.pts)], dxf[:6 * (len(batch.fill_cmd_off) - 1)].reshape(-1, 6)
 
 
-def coverage_image(batch, w: int, h: int) -> np.ndarray:
-    """f32 model coverage min(|accum + area|, 1) of each raster on a w x h
-    canvas at the origin, from the f32 restatement (tiles) and its spans."""
-    ref = run(batch, want_cov=True)
+def _tile_images(batch, w: int, h: int):
+    """Signed pre-quantisation sums at boundary-tile pixels (f32 restatement),
+    the boundary-tile mask and the span mask, each [R, h, w] on a canvas at
+    the origin."""
+    ref = run(batch, want_cov=True, signed_cov=True)
     R = batch.n_rasters
-    img = np.zeros((R, h + 8, w + 8), np.float32)
+    S = np.zeros((R, h + 8, w + 8), np.float32)
+    T = np.zeros((R, h + 8, w + 8), bool)
+    P = np.zeros((R, h + 8, w + 8), bool)
     for r in range(R):
         t0, t1 = int(ref["raster_tile_off"][r]), int(ref["raster_tile_off"][r + 1])
         for t in range(t0, t1):
             x, y = int(ref["tile_xy"][t, 0]), int(ref["tile_xy"][t, 1])
             if x <= -8 or y <= -8 or x >= w or y >= h:
                 continue
-            blk = np.minimum(np.abs(ref["tile_cov"][t].reshape(8, 8)), 1.0)
+            blk = ref["tile_cov"][t].reshape(8, 8)
             xs, ys = max(x, 0), max(y, 0)
-            img[r, ys:y + 8, xs:x + 8] = blk[ys - y:, xs - x:]
+            S[r, ys:y + 8, xs:x + 8] = blk[ys - y:, xs - x:]
+            T[r, ys:y + 8, xs:x + 8] = True
         s0, s1 = int(ref["raster_span_off"][r]), int(ref["raster_span_off"][r + 1])
         for s in range(s0, s1):
             x, y, sw = int(ref["span_xy"][s, 0]), int(ref["span_xy"][s, 1]), int(ref["span_w"][s])
             if y <= -8 or y >= h or x + sw <= 0 or x >= w:
                 continue
-            img[r, max(y, 0):y + 8, max(x, 0):min(x + sw, w)] = 1.0
-    return img[:, :h, :w].copy()
+            P[r, max(y, 0):y + 8, max(x, 0):min(x + sw, w)] = True
+    return S[:, :h, :w], T[:, :h, :w], P[:, :h, :w]
+
+
+def coverage_image(batch, w: int, h: int) -> np.ndarray:
+    """f32 model coverage min(|accum + area|, 1) of each raster on a w x h
+    canvas at the origin, from the f32 restatement (tiles) and its spans."""
+    S, T, P = _tile_images(batch, w, h)
+    return np.where(T, np.minimum(np.abs(S), 1.0), np.where(P, 1.0, 0.0)).astype(np.float32)
+
+
+def adjoint64(batch, w: int, h: int, target: np.ndarray, counts=None):
+    """The FP64 reference gradient of the f32 model: the loss and dL/dS of
+    the f32 forward (the reference's arithmetic, as the GPU computes it),
+    then the adjoint through the lines, the flattening and the transforms in
+    double precision.  Returns (loss, dL/dpts, dL/dxf)."""
+    S, T, P = _tile_images(batch, w, h)
+    c = np.where(T, np.minimum(np.abs(S), 1.0), np.where(P, 1.0, 0.0)).astype(np.float64)
+    d = c - np.asarray(target, np.float64).reshape(c.shape)
+    g = np.where(T & (np.abs(S) < 1.0), np.sign(S) * 2.0 * d, 0.0)
+    dp, dx = backward64(batch, w, h, g, counts)
+    return float((d * d).sum()), dp, dx
 
 
 if __name__ == "__main__":  # pragma: no cover

@@ -450,8 +450,9 @@ static void finish(rasterizer *r, collector *out) {
             for (int y = 0; y < 8; y++) {
                 float accum = prev[y];
                 for (int x = 0; x < 8; x++) {
-                    float c = fabsf(accum + areas[y * 8 + x]);
-                    cov[y * 8 + x] = c;
+                    const float sum = accum + areas[y * 8 + x];
+                    float c = fabsf(sum);
+                    cov[y * 8 + x] = out->want_cov == 2 ? sum : c;
                     tile[y * 8 + x] = f2u8(rmin(c * 256.0f, 255.0f));
                     accum += heights[y * 8 + x];
                 }
@@ -581,7 +582,7 @@ int ochre_oracle_run(const ochre_oracle_batch *bt, int threads, int flags, ochre
     if (st) return st;
     raster_out *outs = (raster_out *)calloc(bt->n_rasters ? bt->n_rasters : 1, sizeof(raster_out));
     if (!outs) { free(off); return OCHRE_ORACLE_E_NOMEM; }
-    int want_cov = (flags & OCHRE_ORACLE_WANT_COV) != 0;
+    int want_cov = (flags & OCHRE_ORACLE_WANT_COV) ? ((flags & OCHRE_ORACLE_SIGNED_COV) ? 2 : 1) : 0;
     int capture = (flags & OCHRE_ORACLE_CAPTURE_LINES) != 0;
 
     if (threads <= 1) {

@@ -32,6 +32,7 @@ enum {
 enum {
     OCHRE_ORACLE_WANT_COV = 1,      /* also return |accum + area| per tile pixel */
     OCHRE_ORACLE_CAPTURE_LINES = 2, /* also return every line_to segment */
+    OCHRE_ORACLE_SIGNED_COV = 4,    /* with WANT_COV: accum + area before |.| */
 };
 
 /* Same layout as the product's ochre_batch (host pointers). */
