@@ -74,8 +74,10 @@ def kernel_bytes(name: str, st: dict, batch) -> int:
         return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 12 + C * 4
     if name == "flatten_emit":
         return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 16 + L * 20
-    if name == "dda_count_scan":
+    if name == "dda_count":
         return L * 20 + L * 4 + R * 16
+    if name == "dda_offset_scan":
+        return L * 8
     if name == "dda_emit":
         return L * 28 + R * 24 + E * (kb + 4) + B * 32
     if name == "sort_onesweep":
@@ -87,7 +89,8 @@ def kernel_bytes(name: str, st: dict, batch) -> int:
     if name == "tile_info_wind_scan":
         return T * 4 + T * (kb + 4 + 32) + T * 32 + R * 4
     if name == "tile_coverage":
-        return B * (4 + 32 + 16) + T * 32 + T * 68 + T * 12
+        # bins: value 4 + BinRec 32 + line 16; tiles: info 32 + 68 out + 12 span
+        return B * (4 + 32 + 16) + T * (32 + 68 + 12)
     if name == "span_scan":
         return T * 4 + T * 8 + N * 10 + R * 4
     if name == "raster_fused":

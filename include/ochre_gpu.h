@@ -191,7 +191,8 @@ int ochre_gpu_fill_backward(ochre_gpu_ctx *ctx, const ochre_batch *in, uint32_t 
  *     threads are serialised).  `stream` is a cudaStream_t (NULL: default). */
 #define OCHRE_NOALLOC_SCRATCH_BYTES (32u << 20)
 
-typedef struct ochre_output_buffers {
+typedef struct ochre_output_buffers {  /* device pointers; tile_alpha 8-byte aligned, tile_xy,
+                                          span_xy and span_tile 4-byte aligned (else OCHRE_E_INVALID) */
     int16_t *tile_xy;           /* 2 * tile_capacity */
     uint8_t *tile_alpha;        /* 64 * tile_capacity */
     uint32_t tile_capacity;

@@ -313,6 +313,16 @@ __device__ __forceinline__ T shfl_up_T(T v, int delta) {
     return r;
 }
 template <class T>
+__device__ __forceinline__ T shfl_down_T(T v, int delta) {
+    static_assert(sizeof(T) % 4 == 0, "T must be a multiple of 4 bytes");
+    T r;
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&v);
+    uint32_t* d = reinterpret_cast<uint32_t*>(&r);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) / 4); i++) d[i] = __shfl_down_sync(0xffffffffu, s[i], delta);
+    return r;
+}
+template <class T>
 __device__ __forceinline__ T shfl_idx_T(T v, int lane) {
     T r;
     const uint32_t* s = reinterpret_cast<const uint32_t*>(&v);

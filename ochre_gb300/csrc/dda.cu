@@ -54,37 +54,65 @@ __device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* ca
     return nb + nc;
 }
 
-// Entry counts folded into the entry-offset scan; the bbox is reduced per
-// raster across the warp (lines of a raster are contiguous) before the
-// atomics.
-struct LineCountIn {
-    const float4* lines;
-    const uint32_t* line_raster;
-    int4* bbox;
-    uint32_t* err;
-    uint64_t n;
-    __device__ __forceinline__ uint32_t operator()(uint64_t i) const {
+// Entry counts per line (written in place of the offsets, then scanned)
+// and the raster tile boxes.  Counting is a separate kernel, not folded into
+// the offset scan: a walk's length varies from one cell to thousands, and a
+// single-pass scan would hold every later block behind the slowest walk.
+// Boxes are reduced before any global atomic: lanes of one raster (lines of
+// a raster are contiguous) by warp reductions, then the block's first
+// BOX_SLOTS rasters in shared memory; the block then updates each global box
+// only where it grows.
+constexpr int BOX_SLOTS = 8;
+__device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1) {
+    const int4 cur = ld_words(d);
+    if (x0 < cur.x) atomicMin(&d->x, x0);
+    if (y0 < cur.y) atomicMin(&d->y, y0);
+    if (x1 > cur.z) atomicMax(&d->z, x1);
+    if (y1 > cur.w) atomicMax(&d->w, y1);
+}
+__global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ lines,
+                                                    const uint32_t* __restrict__ line_raster, uint32_t n_lines,
+                                                    int4* bbox, uint32_t* __restrict__ counts, uint32_t* err) {
+    __shared__ int4 s_box[BOX_SLOTS];
+    __shared__ uint32_t s_r0;
+    const uint32_t i0 = blockIdx.x * blockDim.x;
+    const uint32_t i = i0 + threadIdx.x;
+    if (threadIdx.x < BOX_SLOTS) s_box[threadIdx.x] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
+    if (threadIdx.x == 0) s_r0 = line_raster[i0];
+    __syncthreads();
+    const uint32_t r0 = s_r0;
+    BBoxAcc bb{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
+    uint32_t r = r0;
+    if (i < n_lines) {
         const float4 l = lines[i];
-        BBoxAcc bb{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
         bool capped = false;
-        const uint32_t c = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped);
+        counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped);
         if (capped) atomicOr(err, ERR_LIMIT);
-        // lanes of one raster (contiguous lines) reduce first; the group's
-        // leader updates the raster's box only where it grows
-        const uint32_t r = line_raster[i];
-        const unsigned grp = __match_any_sync(__activemask(), r);
-        const int x0 = __reduce_min_sync(grp, bb.x0), y0 = __reduce_min_sync(grp, bb.y0);
-        const int x1 = __reduce_max_sync(grp, bb.x1), y1 = __reduce_max_sync(grp, bb.y1);
-        if ((int)(threadIdx.x & 31) == __ffs(grp) - 1 && x0 <= x1) {
-            int4* d = bbox + r;
-            const int4 cur = ld_words(d);
-            if (x0 < cur.x) atomicMin(&d->x, x0);
-            if (y0 < cur.y) atomicMin(&d->y, y0);
-            if (x1 > cur.z) atomicMax(&d->z, x1);
-            if (y1 > cur.w) atomicMax(&d->w, y1);
-        }
-        return c;
+        r = line_raster[i];
     }
+    const unsigned grp = __match_any_sync(0xffffffffu, r);
+    const int x0 = __reduce_min_sync(grp, bb.x0), y0 = __reduce_min_sync(grp, bb.y0);
+    const int x1 = __reduce_max_sync(grp, bb.x1), y1 = __reduce_max_sync(grp, bb.y1);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1 && x0 <= x1) {
+        if (r - r0 < (uint32_t)BOX_SLOTS) {
+            int4* d = s_box + (r - r0);
+            atomicMin(&d->x, x0);
+            atomicMin(&d->y, y0);
+            atomicMax(&d->z, x1);
+            atomicMax(&d->w, y1);
+        } else {
+            box_grow(bbox + r, x0, y0, x1, y1);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < BOX_SLOTS) {
+        const int4 b = s_box[threadIdx.x];
+        if (b.x <= b.z) box_grow(bbox + r0 + threadIdx.x, b.x, b.y, b.z, b.w);
+    }
+}
+struct CountIn32 {
+    const uint32_t* counts;
+    __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return counts[i]; }
 };
 struct OffOut32 {
     uint32_t* off;
@@ -236,11 +264,14 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     if (n_lines) {
         OCHRE_CUDA_TRY(ctx->line_ent_off.ensure((size_t)n_lines * 4));
         OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<uint32_t>)));
-        OCHRE_LAUNCH(ctx, "dda_count_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
-            n_lines, LineCountIn{ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->raster_bbox.as<int4>(),
-                                 &ds->err, n_lines},
-            OffOut32{ctx->line_ent_off.as<uint32_t>()}, OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket,
-            &ds->n_line_ent, &ds->err, s)));
+        OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<(n_lines + 255) / 256, 256, 0, s>>>(
+            ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, ctx->raster_bbox.as<int4>(),
+            ctx->line_ent_off.as<uint32_t>(), &ds->err));
+        OCHRE_CUDA_TRY(cudaGetLastError());
+        // in place: every count is read by the thread that writes its offset
+        OCHRE_LAUNCH(ctx, "dda_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+            n_lines, CountIn32{ctx->line_ent_off.as<uint32_t>()}, OffOut32{ctx->line_ent_off.as<uint32_t>()},
+            OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_line_ent, &ds->err, s)));
     }
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(R) * sizeof(ScanStatus<RasterScan>)));
     OCHRE_LAUNCH(ctx, "raster_key_scan", s, OCHRE_CUDA_TRY(launch_scan<RasterScan>(

@@ -57,6 +57,12 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
         out->span_width == nullptr || out->span_tile == nullptr || out->raster_tile_off == nullptr ||
         out->raster_span_off == nullptr)
         return OCHRE_E_INVALID;
+    // the kernels store tile rows 8 bytes at a time and positions as 32-bit words
+    auto misaligned = [](const void* p, uintptr_t a) { return (reinterpret_cast<uintptr_t>(p) & (a - 1)) != 0; };
+    if (misaligned(out->tile_xy, 4) || misaligned(out->tile_alpha, 8) || misaligned(out->span_xy, 4) ||
+        misaligned(out->span_width, 2) || misaligned(out->span_tile, 4) || misaligned(out->raster_tile_off, 4) ||
+        misaligned(out->raster_span_off, 4))
+        return OCHRE_E_INVALID;
     out->n_tiles = 0;
     out->n_spans = 0;
     std::lock_guard<std::mutex> lock(g_mutex);

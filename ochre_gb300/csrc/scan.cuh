@@ -62,31 +62,55 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, In in, Out out, Op o
         const T ex = shfl_up_T(w, 1);
         const T tile_agg = shfl_idx_T(w, WARPS - 1);
         if (lane < WARPS) s_warp[lane] = lane == 0 ? identity : ex;
-        if (lane == 0) {
-            T prefix = identity;
-            ScanStatus<T>* me = status + tile;
-            if (tile == 0) {
+        // Decoupled look-back by the whole warp, 32 predecessors per round:
+        // lane k inspects tile top - k; the window up to the nearest inclusive
+        // value is combined in tile order (earlier tiles on the left).
+        T prefix = identity;
+        ScanStatus<T>* me = status + tile;
+        if (tile == 0) {
+            if (lane == 0) {
                 st_words(&me->inc, tile_agg);
                 st_release(&me->flag, 2u);
-            } else {
+            }
+        } else {
+            if (lane == 0) {
                 st_words(&me->agg, tile_agg);
                 st_release(&me->flag, 1u);
-                int64_t j = (int64_t)tile - 1;
-                long long spins = 0;
-                while (j >= 0) {
-                    const uint32_t f = ld_acquire(&status[j].flag);
-                    if (f == 0u) {
-                        if (++spins > SPIN_LIMIT) { atomicOr(err, ERR_TIMEOUT); break; }
-                        if (spins > 64) __nanosleep(64);
-                        continue;
+            }
+            int64_t top = (int64_t)tile - 1;
+            long long spins = 0;
+            while (top >= 0) {
+                const int64_t j = top - lane;
+                uint32_t f = 2u;   // before tile 0: an inclusive identity
+                if (j >= 0) f = ld_acquire(&status[j].flag);
+                const uint32_t m2 = __ballot_sync(0xffffffffu, f == 2u);
+                const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
+                const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
+                if (__ballot_sync(0xffffffffu, f == 0u) & need) {
+                    if (++spins > SPIN_LIMIT) {
+                        if (lane == 0) atomicOr(err, ERR_TIMEOUT);
+                        break;
                     }
-                    if (f == 2u) { prefix = op(ld_words(&status[j].inc), prefix); break; }
-                    prefix = op(ld_words(&status[j].agg), prefix);
-                    --j;
+                    if (spins > 64) __nanosleep(64);
+                    continue;
                 }
+                T v = identity;
+                if (lane <= limit && j >= 0) v = ld_words(f == 2u ? &status[j].inc : &status[j].agg);
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const T o = shfl_down_T(v, d);
+                    if (lane + d < 32) v = op(o, v);
+                }
+                prefix = op(shfl_idx_T(v, 0), prefix);
+                if (m2) break;
+                top -= 32;
+            }
+            if (lane == 0) {
                 st_words(&me->inc, op(prefix, tile_agg));
                 st_release(&me->flag, 2u);
             }
+        }
+        if (lane == 0) {
             s_prefix = prefix;
             const uint64_t tile_end = (uint64_t)(tile + 1) * (BLOCK * ITEMS);
             if (tile_end >= n && total != nullptr) *total = op(prefix, tile_agg);

@@ -119,6 +119,13 @@ struct InfoOut {
     }
 };
 
+// Shared-memory accumulators of one tile: 64 area cells, then 64 height
+// cells, row-major; pixel rows 4-7 sit 4 floats further on, so the 128-bit
+// row loads of eight lanes (rows 0-7 of one tile) hit distinct banks.
+constexpr int ACC_H = 68;          // offset of the height cells
+constexpr int ACC_STRIDE = 136;    // floats per tile
+__device__ __forceinline__ int acc_idx(int cell) { return cell + ((cell >> 5) << 2); }
+
 template <int CH>
 __global__ void __launch_bounds__(128) k_tile_cov(
     const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
@@ -126,7 +133,8 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     uint32_t* __restrict__ out_xy, uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov,
     uint32_t* __restrict__ span_flag, uint64_t* __restrict__ span_val, uint32_t* err, bool cov_signed) {
     constexpr int WARPS = 4;
-    __shared__ float s_acc[WARPS][CH][128];   // [tile][0..63 area, 64..127 height]
+    // [tile][area cells | height cells], ACC_STRIDE floats per tile; see acc_idx
+    __shared__ __align__(16) float s_acc[WARPS][CH][ACC_STRIDE];
     __shared__ uint32_t s_head[WARPS][CH];
     __shared__ TileInfo s_info[WARPS][CH + 1];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -136,19 +144,15 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     const uint32_t t0 = blk * CH;
     if (t0 >= n_tiles) return;
     const int nt = (int)min((uint32_t)CH, n_tiles - t0);
-    float (*acc)[128] = s_acc[wid];
+    float (*acc)[ACC_STRIDE] = s_acc[wid];
 
     // tile metadata (one extra for the span test of the last tile)
     for (int i = lane; i <= nt; i += 32) {
         if (t0 + i < n_tiles) s_info[wid][i] = info[t0 + i];
         else s_info[wid][i].raster = -1;
     }
-    for (int i = 0; i < nt; i++) {
-        acc[i][lane] = 0.0f;
-        acc[i][lane + 32] = 0.0f;
-        acc[i][lane + 64] = 0.0f;
-        acc[i][lane + 96] = 0.0f;
-    }
+    for (int k = lane; k < nt * (ACC_STRIDE / 4); k += 32)
+        reinterpret_cast<float4*>(acc[0])[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     __syncwarp();
     if (lane < nt) s_head[wid][lane] = s_info[wid][lane].head;
     __syncwarp();
@@ -181,17 +185,17 @@ __global__ void __launch_bounds__(128) k_tile_cov(
             float area, height;
             walk_increment(w, s, area, height);
             const int cell = ((s.y & 7) << 3) | (s.x & 7);
-            atomicAdd(a + cell, area);
-            atomicAdd(a + 64 + cell, height);
+            atomicAdd(a + acc_idx(cell), area);
+            atomicAdd(a + ACC_H + acc_idx(cell), height);
             if (k + 1 >= rec.n) break;
             walk_step(w, s);
         }
     }
     __syncwarp();
 
-    // lane -> cells 2*lane, 2*lane+1 of pixel row lane/4
-    const int row = lane >> 2;
-    const int c0 = 2 * lane;
+    // Each lane owns one pixel row of one tile: lane = 8 * g + y, four tiles
+    // (g) per pass.
+    const int y = lane & 7, g = lane >> 3;
 
     // Row sums of the block's last row segment -> publish (decoupled).
     int last_seg = 0;
@@ -200,99 +204,153 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     const bool starts_mid_row = !s_info[wid][0].row_head;
     const bool one_segment = last_seg == 0 && starts_mid_row;
     float part = 0.0f;
-    for (int i = last_seg; i < nt; i++) part += acc[i][64 + c0] + acc[i][64 + c0 + 1];
-    part += __shfl_xor_sync(0xffffffffu, part, 1);
-    part += __shfl_xor_sync(0xffffffffu, part, 2);   // all 4 lanes of a row hold its sum
+    for (int i = last_seg + g; i < nt; i += 4) {
+        const float4 h0 = *reinterpret_cast<const float4*>(&acc[i][ACC_H + acc_idx(8 * y)]);
+        const float4 h1 = *reinterpret_cast<const float4*>(&acc[i][ACC_H + acc_idx(8 * y + 4)]);
+        part += ((h0.x + h0.y) + (h0.z + h0.w)) + ((h1.x + h1.y) + (h1.z + h1.w));
+    }
+    part += __shfl_xor_sync(0xffffffffu, part, 8);
+    part += __shfl_xor_sync(0xffffffffu, part, 16);   // every lane of row y holds its sum
     float seg[8];
 #pragma unroll
-    for (int y = 0; y < 8; y++) seg[y] = __shfl_sync(0xffffffffu, part, 4 * y);
+    for (int r = 0; r < 8; r++) seg[r] = __shfl_sync(0xffffffffu, part, r);
     float carry_in = 0.0f;   // per lane: carry of this lane's pixel row
     if (lane == 0) {
         TileBlockState* me = state + blk;
         if (!one_segment) {
-            for (int y = 0; y < 8; y++) st_relaxed(reinterpret_cast<uint32_t*>(&me->inc[y]), __float_as_uint(seg[y]));
+            for (int r = 0; r < 8; r++) st_relaxed(reinterpret_cast<uint32_t*>(&me->inc[r]), __float_as_uint(seg[r]));
             st_release(&me->flag, 2u);
         } else {
-            for (int y = 0; y < 8; y++) st_relaxed(reinterpret_cast<uint32_t*>(&me->agg[y]), __float_as_uint(seg[y]));
+            for (int r = 0; r < 8; r++) st_relaxed(reinterpret_cast<uint32_t*>(&me->agg[r]), __float_as_uint(seg[r]));
             st_release(&me->flag, 1u);
         }
     }
     if (starts_mid_row) {
+        // Warp-cooperative decoupled look-back over the preceding blocks, 32
+        // per round (a long tile row spans many blocks): lane k inspects
+        // block top - k; the nearest inclusive value ends the walk.
         float c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (lane == 0) {
-            int64_t j = (int64_t)blk - 1;
-            long long spins = 0;
-            while (j >= 0) {
-                const uint32_t f = ld_acquire(&state[j].flag);
-                if (f == 0u) {
-                    if (++spins > SPIN_LIMIT) { atomicOr(err, ERR_TIMEOUT); break; }
-                    if (spins > 64) __nanosleep(64);
-                    continue;
+        int64_t top = (int64_t)blk - 1;
+        long long spins = 0;
+        while (top >= 0) {
+            const int64_t j = top - lane;
+            uint32_t f = 2u;   // before block 0: an inclusive zero
+            if (j >= 0) f = ld_acquire(&state[j].flag);
+            const uint32_t m2 = __ballot_sync(0xffffffffu, f == 2u);
+            const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
+            const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
+            if (__ballot_sync(0xffffffffu, f == 0u) & need) {
+                if (++spins > SPIN_LIMIT) {
+                    if (lane == 0) atomicOr(err, ERR_TIMEOUT);
+                    break;
                 }
+                if (spins > 16) __nanosleep(64);
+                continue;
+            }
+            float v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            if (lane <= limit && j >= 0) {
                 const float* src = f == 2u ? state[j].inc : state[j].agg;
-                for (int y = 0; y < 8; y++)
-                    c[y] = __uint_as_float(ld_relaxed(reinterpret_cast<const uint32_t*>(src + y))) + c[y];
-                if (f == 2u) break;
-                --j;
+#pragma unroll
+                for (int r = 0; r < 8; r++) v[r] = __uint_as_float(ld_relaxed(reinterpret_cast<const uint32_t*>(src + r)));
             }
-            if (one_segment) {
-                TileBlockState* me = state + blk;
-                for (int y = 0; y < 8; y++)
-                    st_relaxed(reinterpret_cast<uint32_t*>(&me->inc[y]), __float_as_uint(c[y] + seg[y]));
-                st_release(&me->flag, 2u);
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+#pragma unroll
+                for (int d = 16; d > 0; d >>= 1) v[r] += __shfl_xor_sync(0xffffffffu, v[r], d);
+                c[r] += v[r];
             }
+            if (m2) break;
+            top -= 32;
+        }
+        if (one_segment && lane == 0) {
+            TileBlockState* me = state + blk;
+            for (int r = 0; r < 8; r++)
+                st_relaxed(reinterpret_cast<uint32_t*>(&me->inc[r]), __float_as_uint(c[r] + seg[r]));
+            st_release(&me->flag, 2u);
         }
 #pragma unroll
-        for (int y = 0; y < 8; y++) {
-            const float v = __shfl_sync(0xffffffffu, c[y], 0);
-            if (row == y) carry_in = v;
-        }
+        for (int r = 0; r < 8; r++)
+            if (y == r) carry_in = c[r];
     }
 
-    // Tiles left to right, carry in registers (rasterizer.rs:232-250).
-    float carry = carry_in;
-    for (int i = 0; i < nt; i++) {
-        const TileInfo& ti = s_info[wid][i];
-        if (i > 0 && ti.row_head) carry = 0.0f;
-        const float a0 = acc[i][c0], a1 = acc[i][c0 + 1];
-        const float h0 = acc[i][64 + c0], h1 = acc[i][64 + c0 + 1];
-        const float hs = h0 + h1;
-        float incl = hs;
-        {
-            const float u1 = __shfl_up_sync(0xffffffffu, incl, 1, 4);
-            if ((lane & 3) >= 1) incl += u1;
-            const float u2 = __shfl_up_sync(0xffffffffu, incl, 2, 4);
-            if ((lane & 3) >= 2) incl += u2;
+    // Tiles left to right (rasterizer.rs:232-250): along its row a lane adds
+    // the cells in the reference's order; the carry into a tile is the carry
+    // into the previous tile of the row plus that tile's row sum (reset at
+    // each row start), a segmented scan over the four tiles of a pass.
+    float carry_row = carry_in;   // carry into the pass's first tile, row y
+    for (int i0 = 0; i0 < nt; i0 += 4) {
+        const int i = i0 + g;
+        const bool valid = i < nt;
+        float a[8], h[8];
+        if (valid) {
+            const float4 a0 = *reinterpret_cast<const float4*>(&acc[i][acc_idx(8 * y)]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&acc[i][acc_idx(8 * y + 4)]);
+            const float4 h0 = *reinterpret_cast<const float4*>(&acc[i][ACC_H + acc_idx(8 * y)]);
+            const float4 h1 = *reinterpret_cast<const float4*>(&acc[i][ACC_H + acc_idx(8 * y + 4)]);
+            a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w; a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+            h[0] = h0.x; h[1] = h0.y; h[2] = h0.z; h[3] = h0.w; h[4] = h1.x; h[5] = h1.y; h[6] = h1.z; h[7] = h1.w;
+        } else {
+#pragma unroll
+            for (int c = 0; c < 8; c++) a[c] = h[c] = 0.0f;
         }
-        float excl = __shfl_up_sync(0xffffffffu, incl, 1, 4);
-        if ((lane & 3) == 0) excl = 0.0f;
-        const float rowsum = __shfl_sync(0xffffffffu, incl, (lane & ~3) | 3);
-        const float acc0 = carry + excl;
-        const float sum0 = acc0 + a0;
-        const float cov0 = fabsf(sum0);
-        const float acc1 = acc0 + h0;
-        const float sum1 = acc1 + a1;
-        const float cov1 = fabsf(sum1);
-        const uint32_t t = t0 + i;
-        const uint32_t al0 = f2u8(rmin(cov0 * 256.0f, 255.0f));
-        const uint32_t al1 = f2u8(rmin(cov1 * 256.0f, 255.0f));
-        reinterpret_cast<uint16_t*>(out_alpha + (size_t)t * 64)[lane] = (uint16_t)(al0 | (al1 << 8));
-        if (out_cov)
-            reinterpret_cast<float2*>(out_cov + (size_t)t * 64)[lane] =
-                cov_signed ? make_float2(sum0, sum1) : make_float2(cov0, cov1);
-        carry = carry + rowsum;
-        if (lane == i) {
-            out_xy[t] = (uint32_t)(uint16_t)(int16_t)(ti.tx * 8) | ((uint32_t)(uint16_t)(int16_t)(ti.ty * 8) << 16);
-            const TileInfo& nx = s_info[wid][i + 1];
-            uint32_t has_span = 0;
-            if (nx.raster == ti.raster && nx.ty == ti.ty && nx.tx > ti.tx + 1 && ti.wind != 0) {
-                has_span = 1;
-                const uint32_t x = (uint16_t)(int16_t)((ti.tx + 1) * 8);
-                const uint32_t y = (uint16_t)(int16_t)(ti.ty * 8);
-                const uint32_t wd = (uint16_t)((uint16_t)(nx.tx - ti.tx - 1) * 8u);
-                span_val[t] = (uint64_t)x | ((uint64_t)y << 16) | ((uint64_t)wd << 32);
+        const float rs = ((h[0] + h[1]) + (h[2] + h[3])) + ((h[4] + h[5]) + (h[6] + h[7]));
+        const bool head = valid && i > 0 && s_info[wid][i].row_head;
+        // segmented inclusive scan of rs over g (lanes 8 apart), then shifted
+        // by one tile: ex = the sum of rs since the last row start before g
+        float v = rs;
+        bool f = head;
+#pragma unroll
+        for (int d = 8; d < 32; d <<= 1) {
+            const float vo = __shfl_up_sync(0xffffffffu, v, d);
+            const bool fo = __shfl_up_sync(0xffffffffu, f ? 1 : 0, d) != 0;
+            if (lane >= d) {
+                if (!f) v = vo + v;
+                f = f || fo;
             }
-            span_flag[t] = has_span;
+        }
+        float ex = __shfl_up_sync(0xffffffffu, v, 8);
+        bool exf = __shfl_up_sync(0xffffffffu, f ? 1 : 0, 8) != 0;
+        if (g == 0) {
+            ex = 0.0f;
+            exf = false;
+        }
+        const float carry = head ? 0.0f : (exf ? ex : carry_row + ex);
+        carry_row = __shfl_sync(0xffffffffu, carry + rs, 24 + y);
+        if (valid) {
+            const uint32_t t = t0 + i;
+            float accum = carry;
+            uint32_t lo = 0, hi = 0;
+            float cv[8];
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const float sum = accum + a[c];
+                const float cov = fabsf(sum);
+                cv[c] = cov_signed ? sum : cov;
+                const uint32_t al = f2u8(rmin(cov * 256.0f, 255.0f));
+                if (c < 4) lo |= al << (8 * c); else hi |= al << (8 * (c - 4));
+                accum = accum + h[c];
+            }
+            reinterpret_cast<uint2*>(out_alpha + (size_t)t * 64)[y] = make_uint2(lo, hi);
+            if (out_cov) {
+                float4* o = reinterpret_cast<float4*>(out_cov + (size_t)t * 64 + 8 * y);
+                o[0] = make_float4(cv[0], cv[1], cv[2], cv[3]);
+                o[1] = make_float4(cv[4], cv[5], cv[6], cv[7]);
+            }
+            if (y == 0) {
+                const TileInfo& ti = s_info[wid][i];
+                out_xy[t] = (uint32_t)(uint16_t)(int16_t)(ti.tx * 8) |
+                            ((uint32_t)(uint16_t)(int16_t)(ti.ty * 8) << 16);
+                const TileInfo& nx = s_info[wid][i + 1];
+                uint32_t has_span = 0;
+                if (nx.raster == ti.raster && nx.ty == ti.ty && nx.tx > ti.tx + 1 && ti.wind != 0) {
+                    has_span = 1;
+                    const uint32_t x = (uint16_t)(int16_t)((ti.tx + 1) * 8);
+                    const uint32_t yy = (uint16_t)(int16_t)(ti.ty * 8);
+                    const uint32_t wd = (uint16_t)((uint16_t)(nx.tx - ti.tx - 1) * 8u);
+                    span_val[t] = (uint64_t)x | ((uint64_t)yy << 16) | ((uint64_t)wd << 32);
+                }
+                span_flag[t] = has_span;
+            }
         }
     }
 }
