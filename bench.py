@@ -46,6 +46,10 @@ def load_peaks():
 
 def make_workload(name: str, n: int, seed: int):
     from ochre_gb300 import workloads as W
+    if name == "diff_union":
+        return W.diff_union(n_paths=n)
+    if name == "diff_scenes":
+        return W.diff_scenes(n_scenes=n)
     if name == "glyph_run":
         return W.glyph_run(n_paths=n, seed=seed)
     if name == "cubic_boxes":
@@ -431,6 +435,32 @@ def _fd_check(ctx, sp, n_paths=16, n_params=64, h_px=1e-3):
             "rel_err": float(np.linalg.norm(an - fd) / np.linalg.norm(fd))}
 
 
+def run_profile(args):
+    """Untimed runs of one workload for an external profiler (ncu): warmup +
+    steps calls of the rasterization (or of render + loss + backward)."""
+    import torch
+    from ochre_gb300 import DeviceBatch, GpuContext
+    batch = make_workload(args.workload, args.n_paths, args.seed)
+    ctx = GpuContext(0, chain_only=args.chain_only)
+    db = DeviceBatch(batch, 0)
+    sp = torch.cuda.current_stream().cuda_stream
+    if args.mode == "profile":
+        for _ in range(args.warmup + args.steps):
+            ctx.rasterize_device(db, sp)
+    else:
+        w = h = 1024 if args.workload == "diff_union" else 512
+        tgt = torch.zeros((batch.n_rasters, h, w), dtype=torch.float32, device="cuda:0")
+        cov = torch.empty_like(tgt)
+        dl = torch.empty_like(tgt)
+        for _ in range(args.warmup + args.steps):
+            ctx.render_coverage(db, w, h, cov, stream=sp)
+            ctx.l2_loss(cov, tgt, dl, stream=sp)
+            ctx.fill_backward(db, w, h, dl, stream=sp)
+    torch.cuda.synchronize()
+    print(json.dumps({"mode": args.mode, "workload": args.workload, "stats": ctx.stats()}), flush=True)
+    ctx.close()
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -628,7 +658,16 @@ def main():
                     help="scenes in the batched differentiable workload (512x512 each)")
     ap.add_argument("--no-extensions", action="store_true",
                     help="skip the uneven-mix and differentiable measurements")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "profile-diff"],
+                    help="profile: run warmup + steps rasterizations of the workload untimed, for ncu; "
+                         "profile-diff: the same for render + loss + backward of --workload diff_union|diff_scenes")
+    ap.add_argument("--chain-only", action="store_true", help="profile mode: force the general chain")
     args = ap.parse_args()
+    if args.mode != "bench":
+        from ochre_gb300 import build
+        build.build()
+        run_profile(args)
+        return
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -253,7 +253,8 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
     DevBuf* dev[] = {&ctx->in_verbs, &ctx->in_pts, &ctx->in_fill_off, &ctx->in_fill_xf, &ctx->in_fill_flags,
                      &ctx->in_raster_off, &ctx->cmd_foff, &ctx->cmd_mv, &ctx->cmd_ep, &ctx->cmd_line_off,
                      &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->raster_bbox, &ctx->raster_keybase,
-                     &ctx->raster_empty, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
+                     &ctx->raster_empty, &ctx->raster_wsum, &ctx->raster_wbase, &ctx->tile_head_bins,
+                     &ctx->tile_head_wind, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_state,
                      &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain,
                      &ctx->grad_g, &ctx->grad_gs, &ctx->grad_left, &ctx->grad_line, &ctx->grad_pts,

@@ -37,10 +37,13 @@ __device__ __forceinline__ void bbox_add(BBoxAcc& b, int x, int y) {
     b.y1 = max(b.y1, ty);
 }
 
-// Count bins and crossings of a line; extend its raster's tile bbox.
-__device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* capped) {
+// Count bins and crossings of a line; extend its raster's tile bbox; sum
+// the crossing signs.
+__device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* capped, int* wsum) {
+    *wsum = 0;
     if (veq(a, p)) return 0u;
     uint32_t nb = 0, nc = 0;
+    int ws = 0;
     int ptx = 0x7fffffff, pty = 0x7fffffff;
     const bool ok = walk_line(
         a, p,
@@ -48,9 +51,13 @@ __device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* ca
             const int tx = div8(s.x), ty = div8(s.y);
             if (tx != ptx || ty != pty) { nb++; ptx = tx; pty = ty; }
         },
-        [&](int, int, int) { nc++; },
+        [&](int, int, int sign) {
+            nc++;
+            ws += sign;
+        },
         [&](int x, int y) { bbox_add(bb, x, y); });
     if (!ok) *capped = true;
+    *wsum = ws;
     return nb + nc;
 }
 
@@ -58,10 +65,10 @@ __device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* ca
 // and the raster tile boxes.  Counting is a separate kernel, not folded into
 // the offset scan: a walk's length varies from one cell to thousands, and a
 // single-pass scan would hold every later block behind the slowest walk.
-// Boxes are reduced before any global atomic: lanes of one raster (lines of
-// a raster are contiguous) by warp reductions, then the block's first
-// BOX_SLOTS rasters in shared memory; the block then updates each global box
-// only where it grows.
+// Boxes (and the rasters' crossing-sign sums) are reduced before any global
+// atomic: lanes of one raster (lines of a raster are contiguous) by warp
+// reductions, then the block's first BOX_SLOTS rasters in shared memory; the
+// block then updates each global box only where it grows.
 constexpr int BOX_SLOTS = 8;
 __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1) {
     const int4 cur = ld_words(d);
@@ -72,42 +79,54 @@ __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1
 }
 __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ lines,
                                                     const uint32_t* __restrict__ line_raster, uint32_t n_lines,
-                                                    int4* bbox, uint32_t* __restrict__ counts, uint32_t* err) {
+                                                    int4* bbox, int* raster_wsum, uint32_t* __restrict__ counts,
+                                                    uint32_t* err) {
     __shared__ int4 s_box[BOX_SLOTS];
+    __shared__ int s_ws[BOX_SLOTS];
     __shared__ uint32_t s_r0;
     const uint32_t i0 = blockIdx.x * blockDim.x;
     const uint32_t i = i0 + threadIdx.x;
-    if (threadIdx.x < BOX_SLOTS) s_box[threadIdx.x] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
+    if (threadIdx.x < BOX_SLOTS) {
+        s_box[threadIdx.x] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
+        s_ws[threadIdx.x] = 0;
+    }
     if (threadIdx.x == 0) s_r0 = line_raster[i0];
     __syncthreads();
     const uint32_t r0 = s_r0;
     BBoxAcc bb{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
     uint32_t r = r0;
+    int ws = 0;
     if (i < n_lines) {
         const float4 l = lines[i];
         bool capped = false;
-        counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped);
+        counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped, &ws);
         if (capped) atomicOr(err, ERR_LIMIT);
         r = line_raster[i];
     }
     const unsigned grp = __match_any_sync(0xffffffffu, r);
     const int x0 = __reduce_min_sync(grp, bb.x0), y0 = __reduce_min_sync(grp, bb.y0);
     const int x1 = __reduce_max_sync(grp, bb.x1), y1 = __reduce_max_sync(grp, bb.y1);
-    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1 && x0 <= x1) {
+    const int wsg = __reduce_add_sync(grp, ws);
+    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) {
         if (r - r0 < (uint32_t)BOX_SLOTS) {
-            int4* d = s_box + (r - r0);
-            atomicMin(&d->x, x0);
-            atomicMin(&d->y, y0);
-            atomicMax(&d->z, x1);
-            atomicMax(&d->w, y1);
+            if (x0 <= x1) {
+                int4* d = s_box + (r - r0);
+                atomicMin(&d->x, x0);
+                atomicMin(&d->y, y0);
+                atomicMax(&d->z, x1);
+                atomicMax(&d->w, y1);
+            }
+            if (wsg) atomicAdd(s_ws + (r - r0), wsg);
         } else {
-            box_grow(bbox + r, x0, y0, x1, y1);
+            if (x0 <= x1) box_grow(bbox + r, x0, y0, x1, y1);
+            if (wsg) atomicAdd(raster_wsum + r, wsg);
         }
     }
     __syncthreads();
     if (threadIdx.x < BOX_SLOTS) {
         const int4 b = s_box[threadIdx.x];
         if (b.x <= b.z) box_grow(bbox + r0 + threadIdx.x, b.x, b.y, b.z, b.w);
+        if (s_ws[threadIdx.x]) atomicAdd(raster_wsum + r0 + threadIdx.x, s_ws[threadIdx.x]);
     }
 }
 struct CountIn32 {
@@ -119,9 +138,12 @@ struct OffOut32 {
     __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
 };
 
-__global__ void k_bbox_init(int4* bbox, uint32_t n) {
+__global__ void k_bbox_init(int4* bbox, int* wsum, uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) bbox[i] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
+    if (i < n) {
+        bbox[i] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
+        wsum[i] = 0;
+    }
 }
 
 // Per-raster key space: w * h * 2 keys; rasters without increments get a
@@ -130,28 +152,31 @@ __global__ void k_bbox_init(int4* bbox, uint32_t n) {
 struct RasterScan {
     uint64_t ks;
     uint32_t ne;
-    uint32_t pad;
+    int32_t w;   // crossing signs of the rasters so far
 };
 struct OpRaster {
     __device__ __forceinline__ RasterScan operator()(RasterScan a, RasterScan b) const {
-        return RasterScan{a.ks + b.ks, a.ne + b.ne, 0u};
+        return RasterScan{a.ks + b.ks, a.ne + b.ne, a.w + b.w};
     }
 };
 struct RasterIn {
     const int4* bbox;
+    const int* wsum;
     __device__ __forceinline__ RasterScan operator()(uint64_t r) const {
         const int4 b = bbox[r];
-        if (b.x > b.z) return RasterScan{2ull, 1u, 0u};
+        if (b.x > b.z) return RasterScan{2ull, 1u, wsum[r]};
         const uint64_t w = (uint64_t)(b.z - b.x + 1), h = (uint64_t)(b.w - b.y + 1);
-        return RasterScan{w * h * 2ull, 0u, 0u};
+        return RasterScan{w * h * 2ull, 0u, wsum[r]};
     }
 };
 struct RasterOut {
     int4* bbox;
     uint64_t* key_base;
     uint32_t* empty;   // 0: has increments; else 1 + rank among empty rasters
+    int* wbase;        // crossing signs of all earlier rasters
     __device__ __forceinline__ void operator()(uint64_t r, RasterScan ex, RasterScan v) const {
         key_base[r] = ex.ks;
+        wbase[r] = ex.w;
         if (v.ne) {
             bbox[r] = make_int4(0, 0, 0, 0);
             empty[r] = ex.ne + 1u;
@@ -258,7 +283,10 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_CUDA_TRY(ctx->raster_bbox.ensure((size_t)R * sizeof(int4)));
     OCHRE_CUDA_TRY(ctx->raster_keybase.ensure((size_t)R * 8));
     OCHRE_CUDA_TRY(ctx->raster_empty.ensure((size_t)R * 4));
-    OCHRE_LAUNCH(ctx, "bbox_init", s, k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(), R));
+    OCHRE_CUDA_TRY(ctx->raster_wsum.ensure((size_t)R * 4));
+    OCHRE_CUDA_TRY(ctx->raster_wbase.ensure((size_t)R * 4));
+    OCHRE_LAUNCH(ctx, "bbox_init", s, k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(),
+                                                                                 ctx->raster_wsum.as<int>(), R));
     OCHRE_CUDA_TRY(cudaGetLastError());
     OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_line_ent, 0, sizeof(uint32_t), s));
     if (n_lines) {
@@ -266,7 +294,7 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
         OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<uint32_t>)));
         OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<(n_lines + 255) / 256, 256, 0, s>>>(
             ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, ctx->raster_bbox.as<int4>(),
-            ctx->line_ent_off.as<uint32_t>(), &ds->err));
+            ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());
         // in place: every count is read by the thread that writes its offset
         OCHRE_LAUNCH(ctx, "dda_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
@@ -275,8 +303,9 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     }
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(R) * sizeof(ScanStatus<RasterScan>)));
     OCHRE_LAUNCH(ctx, "raster_key_scan", s, OCHRE_CUDA_TRY(launch_scan<RasterScan>(
-        R, RasterIn{ctx->raster_bbox.as<int4>()},
-        RasterOut{ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->raster_empty.as<uint32_t>()},
+        R, RasterIn{ctx->raster_bbox.as<int4>(), ctx->raster_wsum.as<int>()},
+        RasterOut{ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->raster_empty.as<uint32_t>(),
+                  ctx->raster_wbase.as<int>()},
         OpRaster{}, RasterScan{0, 0, 0}, ctx->scan_status.p, &ds->ticket,
         reinterpret_cast<RasterScan*>(&ds->keyspace), &ds->err, s)));
     int st = read_scalars(ctx, s);

@@ -54,8 +54,10 @@ struct DevScalars {
     uint64_t keyspace;     // total key space (raster scan .ks)
     uint32_t n_empty;      // rasters without increments (raster scan .ne)
     uint32_t pad1;
-    uint32_t n_tiles;      // tile-head scan total .heads
-    uint32_t n_bins;       // tile-head scan total .bins
+    uint32_t n_tiles;      // tile-head scan total .heads   }
+    uint32_t n_bins;       // tile-head scan total .bins    } (HeadScan layout)
+    int32_t head_wind;     // sum of all crossing signs     }
+    uint32_t pad2;         //                               }
     uint32_t n_spans;
     uint32_t sort_ticket;
     uint32_t fused_fallback;  // fused path: some raster did not fit
@@ -114,11 +116,15 @@ struct ochre_gpu_ctx {
     ochre::DevBuf lines, line_raster, line_ent_off;
     // per raster
     ochre::DevBuf raster_bbox, raster_keybase, raster_empty;
+    // per raster: sum of its tile-row crossing signs, and the sum over earlier rasters
+    ochre::DevBuf raster_wsum, raster_wbase;
     // sort entries
     ochre::DevBuf keys, vals, keys_alt, vals_alt, bins;
     ochre::DevBuf sort_hist, sort_lookback;
     // tiles
     ochre::DevBuf tile_head, tile_info, tile_state, span_flag, span_val;   // tile_state: TileBlockState
+    // per tile: bins and crossing-sign sum of all entries before its head
+    ochre::DevBuf tile_head_bins, tile_head_wind;
     // scan workspace
     ochre::DevBuf scan_status;
     ochre::DevBuf scalars;   // DevScalars

@@ -10,8 +10,8 @@
 //     prefix over the whole raster) is nonzero (:252-265).
 //
 // Tiles are numbered in sorted order, which is the reference's callback
-// order.  The winding is a segmented (per raster) scan fused with the pass
-// that gathers each tile's metadata.  Coverage runs one warp per aligned
+// order.  The tile-head scan also counts bins and sums crossing signs, so
+// each tile's metadata and winding follow without a per-tile search.  Coverage runs one warp per aligned
 // block of TILES_PER_WARP consecutive tiles: the warp replays the block's
 // bins into shared-memory accumulators, then walks its tiles left to right
 // keeping the row carry in registers (reset at each row start).  Only a
@@ -25,15 +25,18 @@
 
 namespace ochre {
 
-// Tile heads: the first bin entry of every run of equal keys.  The scan also
-// counts bin entries (statistics only).
+// Tile heads: the first bin entry of every run of equal keys.  The same
+// scan counts bin entries and sums the crossing signs, so that every tile
+// learns, at its head, how many bins and how much winding precede it.
 struct HeadScan {
     uint32_t heads;
     uint32_t bins;
+    int32_t w;
+    uint32_t pad;
 };
 struct OpHead {
     __device__ __forceinline__ HeadScan operator()(HeadScan a, HeadScan b) const {
-        return HeadScan{a.heads + b.heads, a.bins + b.bins};
+        return HeadScan{a.heads + b.heads, a.bins + b.bins, a.w + b.w, 0u};
     }
 };
 template <class K>
@@ -41,83 +44,58 @@ struct HeadIn {
     const K* keys;
     const uint32_t* vals;
     __device__ __forceinline__ HeadScan operator()(uint64_t i) const {
-        if (vals[i] & CROSS_TAG) return HeadScan{0u, 0u};
-        return HeadScan{(i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u, 1u};
+        const uint32_t v = vals[i];
+        if (v & CROSS_TAG) return HeadScan{0u, 0u, (int32_t)(int8_t)(v & 0xffu), 0u};
+        return HeadScan{(i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u, 1u, 0, 0u};
     }
 };
 struct HeadOut {
     uint32_t* head;
+    uint32_t* head_bins;
+    int32_t* head_wind;
     __device__ __forceinline__ void operator()(uint64_t i, HeadScan ex, HeadScan v) const {
-        if (v.heads) head[ex.heads] = (uint32_t)i;
+        if (v.heads) {
+            head[ex.heads] = (uint32_t)i;
+            head_bins[ex.heads] = ex.bins;
+            head_wind[ex.heads] = ex.w;
+        }
     }
 };
 
-// Tile metadata + winding.  The winding value of a tile is the sum of the
-// signs of all crossings of its raster whose key is <= the tile's key; each
-// tile contributes the crossings sorted between the previous tile and itself,
-// and the scan is segmented by raster: (w, head) o (w', head') =
-// head' ? (w', 1) : (w + w', head).
-struct WindScan {
-    int32_t w;
-    uint32_t head;
-};
-struct OpWind {
-    __device__ __forceinline__ WindScan operator()(WindScan a, WindScan b) const {
-        return b.head ? b : WindScan{a.w + b.w, a.head};
+// Tile metadata, one thread per tile.  The tile's bins are the bins between
+// its head and the next tile's head; its winding (rasterizer.rs:219, 253-258:
+// the signs of all crossings of its raster sorted before it, never reset)
+// is the crossing-sign sum before its head minus that of all earlier
+// rasters.
+__global__ void k_tile_info(const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins,
+                            const uint32_t* __restrict__ head, const uint32_t* __restrict__ head_bins,
+                            const int32_t* __restrict__ head_wind, const int32_t* __restrict__ raster_wbase,
+                            const uint32_t* __restrict__ total_bins, uint32_t n_tiles, uint32_t n_rasters,
+                            TileInfo* __restrict__ info, uint32_t* __restrict__ raster_tile_off) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_tiles) return;
+    const uint32_t h = head[t];
+    const BinRec* rec = bins + vals[h];
+    const int r = (int)rec->raster;
+    TileInfo ti;
+    ti.raster = r;
+    ti.tx = div8((int)rec->x);
+    ti.ty = div8((int)rec->y);
+    ti.head = h;
+    ti.nbins = (t + 1 < n_tiles ? head_bins[t + 1] : *total_bins) - head_bins[t];
+    ti.wind = head_wind[t] - raster_wbase[r];
+    bool ras_head = t == 0, row_head = t == 0;
+    if (t > 0) {
+        const BinRec* pr = bins + vals[head[t - 1]];
+        ras_head = (int)pr->raster != r;
+        row_head = ras_head || div8((int)pr->y) != ti.ty;
     }
-};
-template <class K>
-struct InfoIn {
-    const K* keys;
-    const uint32_t* vals;
-    const BinRec* bins;
-    const uint32_t* head;
-    uint32_t n_tiles;
-    uint64_t n_entries;
-    uint32_t n_rasters;
-    TileInfo* info;
-    uint32_t* raster_tile_off;
-    __device__ WindScan operator()(uint64_t t64) const {
-        const uint32_t t = (uint32_t)t64;
-        const uint32_t h = head[t];
-        const K key = keys[h];
-        const BinRec* rec = bins + vals[h];
-        const int r = (int)rec->raster;
-        TileInfo ti;
-        ti.raster = r;
-        ti.tx = div8((int)rec->x);
-        ti.ty = div8((int)rec->y);
-        ti.head = h;
-        uint32_t nb = 1;
-        while (h + nb < n_entries && keys[h + nb] == key) nb++;
-        ti.nbins = nb;
-        int w = 0;
-        for (int64_t j = (int64_t)h - 1; j >= 0; j--) {
-            const uint32_t v = vals[j];
-            if (!(v & CROSS_TAG) || (int)((v >> 8) & 0x7fffffu) != r) break;
-            w += (int)(int8_t)(v & 0xffu);
-        }
-        bool ras_head = t == 0, row_head = t == 0;
-        if (t > 0) {
-            const BinRec* pr = bins + vals[head[t - 1]];
-            ras_head = (int)pr->raster != r;
-            row_head = ras_head || div8((int)pr->y) != ti.ty;
-        }
-        ti.row_head = row_head ? 1u : 0u;
-        ti.wind = 0;
-        ti.pad = 0;
-        info[t] = ti;
-        if (ras_head) raster_tile_off[r] = t;
-        if (t + 1 == n_tiles) raster_tile_off[n_rasters] = n_tiles;
-        return WindScan{w, ras_head ? 1u : 0u};
-    }
-};
-struct InfoOut {
-    TileInfo* info;
-    __device__ __forceinline__ void operator()(uint64_t t, WindScan ex, WindScan v) const {
-        info[t].wind = OpWind{}(ex, v).w;
-    }
-};
+    ti.row_head = row_head ? 1u : 0u;
+    ti.pad = 0;
+    info[t] = ti;
+    if (ras_head) raster_tile_off[r] = t;
+    if (t + 1 == n_tiles) raster_tile_off[n_rasters] = n_tiles;
+}
 
 // Shared-memory accumulators of one tile: 64 area cells, then 64 height
 // cells, row-major; pixel rows 4-7 sit 4 floats further on, so the 128-bit
@@ -400,12 +378,16 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     DevScalars* ds = dev_scalars(ctx);
     const uint32_t R = in->n_rasters;
     OCHRE_CUDA_TRY(ctx->tile_head.ensure(E * 4));
+    OCHRE_CUDA_TRY(ctx->tile_head_bins.ensure(E * 4));
+    OCHRE_CUDA_TRY(ctx->tile_head_wind.ensure(E * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(E) * sizeof(ScanStatus<HeadScan>)));
     OCHRE_LAUNCH(ctx, "tile_head_scan", s,
-                 OCHRE_CUDA_TRY(launch_scan<HeadScan>(E, HeadIn<K>{ctx->keys.as<K>(), ctx->vals.as<uint32_t>()},
-                                                      HeadOut{ctx->tile_head.as<uint32_t>()}, OpHead{},
-                                                      HeadScan{0u, 0u}, ctx->scan_status.p, &ds->ticket,
-                                                      reinterpret_cast<HeadScan*>(&ds->n_tiles), &ds->err, s)));
+                 OCHRE_CUDA_TRY(launch_scan<HeadScan>(
+                     E, HeadIn<K>{ctx->keys.as<K>(), ctx->vals.as<uint32_t>()},
+                     HeadOut{ctx->tile_head.as<uint32_t>(), ctx->tile_head_bins.as<uint32_t>(),
+                             ctx->tile_head_wind.as<int32_t>()},
+                     OpHead{}, HeadScan{0u, 0u, 0, 0u}, ctx->scan_status.p, &ds->ticket,
+                     reinterpret_cast<HeadScan*>(&ds->n_tiles), &ds->err, s)));
     int st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
     const uint32_t T = host_scalars(ctx)->n_tiles;
@@ -421,15 +403,14 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     if (want_cov) OCHRE_CUDA_TRY(ctx->out_tile_cov.ensure((size_t)T * 64 * 4));
     OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
     OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
-    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(T) * sizeof(ScanStatus<WindScan>)));
-    OCHRE_LAUNCH(ctx, "tile_info_wind_scan", s,
-                 OCHRE_CUDA_TRY(launch_scan<WindScan>(
-                     T,
-                     InfoIn<K>{ctx->keys.as<K>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(),
-                               ctx->tile_head.as<uint32_t>(), T, E, R, ctx->tile_info.as<TileInfo>(),
-                               ctx->out_raster_tile_off.as<uint32_t>()},
-                     InfoOut{ctx->tile_info.as<TileInfo>()}, OpWind{}, WindScan{0, 0u}, ctx->scan_status.p,
-                     &ds->ticket, static_cast<WindScan*>(nullptr), &ds->err, s)));
+    if (T)
+        OCHRE_LAUNCH(ctx, "tile_info", s,
+                     k_tile_info<<<(T + 255) / 256, 256, 0, s>>>(
+                         ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->tile_head.as<uint32_t>(),
+                         ctx->tile_head_bins.as<uint32_t>(), ctx->tile_head_wind.as<int32_t>(),
+                         ctx->raster_wbase.as<int32_t>(), &ds->n_bins, T, R, ctx->tile_info.as<TileInfo>(),
+                         ctx->out_raster_tile_off.as<uint32_t>()));
+    OCHRE_CUDA_TRY(cudaGetLastError());
     switch (ctx->tune_chain_tiles_per_warp) {
     case 4: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<4>(ctx, T, want_cov, s)); break;
     case 8: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<8>(ctx, T, want_cov, s)); break;
