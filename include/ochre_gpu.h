@@ -213,6 +213,8 @@ int ochre_gpu_rasterize_noalloc(const ochre_batch *in, ochre_output_buffers *out
  *   "fused_threads"          threads per raster in the fused kernel: 64 | 128
  *   "fused_chunk"            tiles accumulated per pass in the fused kernel: 16 | 32
  *   "chain_tiles_per_warp"   tiles per warp in the chain's coverage kernel: 4 | 8 | 16
+ *   "chain_coverage_form"    coverage kernel form: 0 by tile-row count (default), 1 one warp
+ *                            per block of tiles with a look-back carry, 2 one warp per tile row
  * Results do not depend on them (beyond the 1 LSB alpha bound). */
 int ochre_gpu_set_tunable(ochre_gpu_ctx *ctx, const char *name, int value);
 int ochre_gpu_get_tunable(const ochre_gpu_ctx *ctx, const char *name, int *value);

@@ -255,7 +255,7 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
                      &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->raster_bbox, &ctx->raster_keybase,
                      &ctx->raster_empty, &ctx->raster_wsum, &ctx->raster_wbase, &ctx->tile_head_bins,
                      &ctx->tile_head_wind, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
-                     &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_state,
+                     &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_row_start, &ctx->tile_state,
                      &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain,
                      &ctx->grad_g, &ctx->grad_gs, &ctx->grad_left, &ctx->grad_line, &ctx->grad_pts,
                      &ctx->out_tile_xy,
@@ -384,6 +384,9 @@ int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     } else if (!std::strcmp(name, "chain_tiles_per_warp")) {
         if (value != 4 && value != 8 && value != 16) return OCHRE_E_INVALID;
         ctx->tune_chain_tiles_per_warp = value;
+    } else if (!std::strcmp(name, "chain_coverage_form")) {
+        if (value < 0 || value > 2) return OCHRE_E_INVALID;
+        ctx->tune_chain_coverage_form = value;
     } else {
         return OCHRE_E_INVALID;
     }
@@ -395,6 +398,7 @@ int ochre_gpu_get_tunable(const ochre_gpu_ctx* ctx, const char* name, int* value
     if (!std::strcmp(name, "fused_threads")) *value = ctx->tune_fused_threads;
     else if (!std::strcmp(name, "fused_chunk")) *value = ctx->tune_fused_chunk;
     else if (!std::strcmp(name, "chain_tiles_per_warp")) *value = ctx->tune_chain_tiles_per_warp;
+    else if (!std::strcmp(name, "chain_coverage_form")) *value = ctx->tune_chain_coverage_form;
     else return OCHRE_E_INVALID;
     return OCHRE_OK;
 }

@@ -63,7 +63,7 @@ struct DevScalars {
     uint32_t fused_fallback;  // fused path: some raster did not fit
     uint32_t fused_tiles;     // fused path totals
     uint32_t fused_spans;
-    uint32_t pad3;
+    uint32_t n_rows;          // tile rows (raster, tile_y) of the general chain
 };
 
 // Entry value tag for tile-row crossings: 1 | raster (23 bits) | sign byte.
@@ -82,6 +82,15 @@ struct alignas(16) BinRec {
 };
 static_assert(sizeof(BinRec) == 32, "BinRec must be 32 bytes");
 
+// Look-back state of one block of tiles (block-form coverage kernel): the row
+// sums (8 pixel rows) of the block's last row segment.
+struct TileBlockState {
+    uint32_t flag;       // 0: none, 1: aggregate (block continues one row), 2: inclusive
+    uint32_t pad;
+    float agg[8];
+    float inc[8];
+};
+
 struct TileInfo {
     int32_t raster;
     int32_t tx, ty;
@@ -92,14 +101,6 @@ struct TileInfo {
     uint32_t pad;
 };
 
-// Look-back state of one block of tiles for the row-carry chain: the row
-// sums (8 pixel rows) of the block's last row segment.
-struct TileBlockState {
-    uint32_t flag;       // 0: none, 1: aggregate (block continues one row), 2: inclusive
-    uint32_t pad;
-    float agg[8];
-    float inc[8];
-};
 
 }  // namespace ochre
 
@@ -122,7 +123,7 @@ struct ochre_gpu_ctx {
     ochre::DevBuf keys, vals, keys_alt, vals_alt, bins;
     ochre::DevBuf sort_hist, sort_lookback;
     // tiles
-    ochre::DevBuf tile_head, tile_info, tile_state, span_flag, span_val;   // tile_state: TileBlockState
+    ochre::DevBuf tile_head, tile_info, tile_row_start, tile_state, span_flag, span_val;   // tile_state: TileBlockState
     // per tile: bins and crossing-sign sum of all entries before its head
     ochre::DevBuf tile_head_bins, tile_head_wind;
     // scan workspace
@@ -149,6 +150,7 @@ struct ochre_gpu_ctx {
     int tune_fused_threads = 64;
     int tune_fused_chunk = 16;
     int tune_chain_tiles_per_warp = 8;
+    int tune_chain_coverage_form = 0;   // 0: by row count, 1: block form, 2: row form
 
     // Tracing: every kernel launch of a run is counted; with OCHRE_CTX_PROFILE
     // each one is also bracketed by a pair of CUDA events on its stream.

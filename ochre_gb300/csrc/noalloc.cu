@@ -95,7 +95,7 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
                                  &ctx.raster_bbox, &ctx.raster_keybase, &ctx.raster_empty,
                                  &ctx.raster_wsum, &ctx.raster_wbase, &ctx.tile_head_bins, &ctx.tile_head_wind, &ctx.keys, &ctx.vals,
                                  &ctx.keys_alt, &ctx.vals_alt, &ctx.bins, &ctx.sort_hist, &ctx.sort_lookback,
-                                 &ctx.tile_head, &ctx.tile_info, &ctx.tile_state, &ctx.span_flag, &ctx.span_val,
+                                 &ctx.tile_head, &ctx.tile_info, &ctx.tile_row_start, &ctx.tile_state, &ctx.span_flag, &ctx.span_val,
                                  &ctx.scan_status, &ctx.scalars, &ctx.fused_chain, &ctx.out_tile_cov,
                                  &ctx.grad_g, &ctx.grad_gs, &ctx.grad_left, &ctx.grad_line, &ctx.grad_pts};
     for (ochre::DevBuf* b : internal) use_arena(*b, &arena);

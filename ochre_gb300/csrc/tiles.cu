@@ -12,13 +12,12 @@
 // Tiles are numbered in sorted order, which is the reference's callback
 // order.  The tile-head scan also counts bins and sums crossing signs, so
 // each tile's metadata and winding follow without a per-tile search.  Coverage runs one warp per aligned
-// block of TILES_PER_WARP consecutive tiles: the warp replays the block's
-// bins into shared-memory accumulators, then walks its tiles left to right
-// keeping the row carry in registers (reset at each row start).  Only a
-// block whose first tile continues a row from the previous block needs a
-// carry from outside: blocks publish the row sums of their last row segment
-// and resolve the carry by decoupled look-back over earlier blocks (taken by
-// atomic ticket, bounded spins).
+// whole tile row (raster, tile_y) at a time, taken by ticket: chunk by chunk
+// of TILES_PER_WARP tiles it replays the chunk's bins into shared-memory
+// accumulators, then walks the tiles left to right keeping the row carry in
+// registers, so no carry ever crosses warps.
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 #include "scan.cuh"
@@ -104,8 +103,15 @@ constexpr int ACC_H = 68;          // offset of the height cells
 constexpr int ACC_STRIDE = 136;    // floats per tile
 __device__ __forceinline__ int acc_idx(int cell) { return cell + ((cell >> 5) << 2); }
 
+// Coverage, block form: one warp per aligned block of TILES_PER_WARP
+// consecutive tiles (blocks may cross rows).  A block that continues a row
+// from the previous block resolves its carry by decoupled look-back: blocks
+// publish the row sums of their last row segment (taken by atomic ticket,
+// bounded spins).  Used when there are too few tile rows to occupy the GPU
+// with one warp per row; with many long rows the look-back chains grow long,
+// and the row form below is used instead.
 template <int CH>
-__global__ void __launch_bounds__(128) k_tile_cov(
+__global__ void __launch_bounds__(128) k_tile_cov_blocks(
     const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
     const TileInfo* __restrict__ info, uint32_t n_tiles, TileBlockState* state, uint32_t* ticket,
     uint32_t* __restrict__ out_xy, uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov,
@@ -333,6 +339,168 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     }
 }
 
+// Coverage, row form: one warp per tile row (see the file comment).
+template <int CH>
+__global__ void __launch_bounds__(128) k_tile_cov(
+    const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
+    const TileInfo* __restrict__ info, uint32_t n_tiles, const uint32_t* __restrict__ row_start,
+    const uint32_t* __restrict__ n_rows_p, uint32_t* ticket, uint32_t* __restrict__ out_xy,
+    uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov, uint32_t* __restrict__ span_flag,
+    uint64_t* __restrict__ span_val, bool cov_signed) {
+    constexpr int WARPS = 4;
+    __shared__ __align__(16) float s_acc[WARPS][CH][ACC_STRIDE];
+    __shared__ uint32_t s_head[WARPS][CH];
+    __shared__ TileInfo s_info[WARPS][CH + 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // lane = 8 * g + y: pixel row y of the g-th tile of a pass of four
+    const int y = lane & 7, g = lane >> 3;
+    const uint32_t n_rows = *n_rows_p;
+    float (*acc)[ACC_STRIDE] = s_acc[wid];
+
+    for (;;) {
+        // one tile row (raster, tile_y) per warp at a time: the row carry
+        // (rasterizer.rs:243-250) never leaves the warp
+        uint32_t k = 0;
+        if (lane == 0) k = atomicAdd(ticket, 1u);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= n_rows) return;
+        const uint32_t tb = row_start[k];
+        const uint32_t te = k + 1 < n_rows ? row_start[k + 1] : n_tiles;
+        float carry_row = 0.0f;   // carry into the next tile, pixel row y
+        for (uint32_t t0 = tb; t0 < te; t0 += CH) {
+            const int nt = (int)min((uint32_t)CH, te - t0);
+            // tile metadata (one extra for the span test of the last tile)
+            for (int i = lane; i <= nt; i += 32) {
+                if (t0 + i < n_tiles) s_info[wid][i] = info[t0 + i];
+                else s_info[wid][i].raster = -1;
+            }
+            for (int q = lane; q < nt * (ACC_STRIDE / 4); q += 32)
+                reinterpret_cast<float4*>(acc[0])[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            __syncwarp();
+            if (lane < nt) s_head[wid][lane] = s_info[wid][lane].head;
+            __syncwarp();
+
+            // Replay every bin of the chunk (rasterizer.rs:97-106, 223-228).
+            // The chunk's entries are contiguous; crossing entries in between
+            // are skipped.
+            const uint32_t e0 = s_info[wid][0].head;
+            const uint32_t e1 = s_info[wid][nt - 1].head + s_info[wid][nt - 1].nbins;
+            for (uint32_t e = e0 + lane; e < e1; e += 32) {
+                const uint32_t v = vals[e];
+                if (v & CROSS_TAG) continue;
+                int slot = 0;
+#pragma unroll
+                for (int i = 1; i < CH; i++)
+                    if (i < nt && s_head[wid][i] <= e) slot = i;
+                const BinRec rec = bins[v];
+                if (rec.n == 0) continue;
+                const float4 l = lines[rec.line];
+                Walk w;
+                WalkState st;
+                walk_setup(v2(l.x, l.y), v2(l.z, l.w), w, st);
+                st.x = rec.x;
+                st.y = rec.y;
+                st.row_t0 = rec.row_t0;
+                st.row_t1 = rec.row_t1;
+                st.col_t0 = rec.col_t0;
+                st.col_t1 = rec.col_t1;
+                float* a = acc[slot];
+                for (uint32_t c = 0;; c++) {
+                    float area, height;
+                    walk_increment(w, st, area, height);
+                    const int cell = ((st.y & 7) << 3) | (st.x & 7);
+                    atomicAdd(a + acc_idx(cell), area);
+                    atomicAdd(a + ACC_H + acc_idx(cell), height);
+                    if (c + 1 >= rec.n) break;
+                    walk_step(w, st);
+                }
+            }
+            __syncwarp();
+
+            // Tiles left to right (rasterizer.rs:232-250): along its row a lane
+            // adds the cells in the reference's order; the carry into a tile is
+            // the carry into the previous tile plus that tile's row sum.
+            for (int i0 = 0; i0 < nt; i0 += 4) {
+                const int i = i0 + g;
+                const bool valid = i < nt;
+                float a[8], h[8];
+                if (valid) {
+                    const float4 a0 = *reinterpret_cast<const float4*>(&acc[i][acc_idx(8 * y)]);
+                    const float4 a1 = *reinterpret_cast<const float4*>(&acc[i][acc_idx(8 * y + 4)]);
+                    const float4 h0 = *reinterpret_cast<const float4*>(&acc[i][ACC_H + acc_idx(8 * y)]);
+                    const float4 h1 = *reinterpret_cast<const float4*>(&acc[i][ACC_H + acc_idx(8 * y + 4)]);
+                    a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w; a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+                    h[0] = h0.x; h[1] = h0.y; h[2] = h0.z; h[3] = h0.w; h[4] = h1.x; h[5] = h1.y; h[6] = h1.z; h[7] = h1.w;
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 8; c++) a[c] = h[c] = 0.0f;
+                }
+                const float rs = ((h[0] + h[1]) + (h[2] + h[3])) + ((h[4] + h[5]) + (h[6] + h[7]));
+                // exclusive sum of rs over the tiles of the pass before this one
+                float v = rs;
+#pragma unroll
+                for (int d = 8; d < 32; d <<= 1) {
+                    const float vo = __shfl_up_sync(0xffffffffu, v, d);
+                    if (lane >= d) v = vo + v;
+                }
+                float ex = __shfl_up_sync(0xffffffffu, v, 8);
+                if (g == 0) ex = 0.0f;
+                const float carry = carry_row + ex;
+                carry_row = __shfl_sync(0xffffffffu, carry + rs, 24 + y);
+                if (valid) {
+                    const uint32_t t = t0 + i;
+                    float accum = carry;
+                    uint32_t lo = 0, hi = 0;
+                    float cv[8];
+#pragma unroll
+                    for (int c = 0; c < 8; c++) {
+                        const float sum = accum + a[c];
+                        const float cov = fabsf(sum);
+                        cv[c] = cov_signed ? sum : cov;
+                        const uint32_t al = f2u8(rmin(cov * 256.0f, 255.0f));
+                        if (c < 4) lo |= al << (8 * c); else hi |= al << (8 * (c - 4));
+                        accum = accum + h[c];
+                    }
+                    reinterpret_cast<uint2*>(out_alpha + (size_t)t * 64)[y] = make_uint2(lo, hi);
+                    if (out_cov) {
+                        float4* o = reinterpret_cast<float4*>(out_cov + (size_t)t * 64 + 8 * y);
+                        o[0] = make_float4(cv[0], cv[1], cv[2], cv[3]);
+                        o[1] = make_float4(cv[4], cv[5], cv[6], cv[7]);
+                    }
+                    if (y == 0) {
+                        const TileInfo& ti = s_info[wid][i];
+                        out_xy[t] = (uint32_t)(uint16_t)(int16_t)(ti.tx * 8) |
+                                    ((uint32_t)(uint16_t)(int16_t)(ti.ty * 8) << 16);
+                        const TileInfo& nx = s_info[wid][i + 1];
+                        uint32_t has_span = 0;
+                        if (nx.raster == ti.raster && nx.ty == ti.ty && nx.tx > ti.tx + 1 && ti.wind != 0) {
+                            has_span = 1;
+                            const uint32_t x = (uint16_t)(int16_t)((ti.tx + 1) * 8);
+                            const uint32_t yy = (uint16_t)(int16_t)(ti.ty * 8);
+                            const uint32_t wd = (uint16_t)((uint16_t)(nx.tx - ti.tx - 1) * 8u);
+                            span_val[t] = (uint64_t)x | ((uint64_t)yy << 16) | ((uint64_t)wd << 32);
+                        }
+                        span_flag[t] = has_span;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Row starts: the tiles that begin a (raster, tile_y) row, compacted.
+struct RowIn {
+    const TileInfo* info;
+    __device__ __forceinline__ uint32_t operator()(uint64_t t) const { return info[t].row_head; }
+};
+struct RowOut {
+    uint32_t* row_start;
+    __device__ __forceinline__ void operator()(uint64_t t, uint32_t ex, uint32_t v) const {
+        if (v) row_start[ex] = (uint32_t)t;
+    }
+};
+
 struct SpanIn {
     const uint32_t* flag;
     __device__ __forceinline__ uint32_t operator()(uint64_t t) const { return flag[t]; }
@@ -359,17 +527,37 @@ struct SpanOut {
 };
 
 // One launch of the coverage kernel with TPW tiles per warp (4 warps per CTA).
+// Coverage launch.  With at least ROW_FORM_MIN_ROWS_PER_SM tile rows per SM
+// the row form runs (persistent warps taking rows by ticket); otherwise the
+// block form, whose look-back chains stay short when rows are few.
+constexpr uint32_t ROW_FORM_MIN_ROWS_PER_SM = 64;
+
 template <int TPW>
-static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, bool want_cov, cudaStream_t s) {
+static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, uint32_t n_rows, bool want_cov, cudaStream_t s) {
     DevScalars* ds = dev_scalars(ctx);
-    const uint32_t blocks = (T + TPW - 1) / TPW;
-    cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)blocks * sizeof(TileBlockState), s);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     cudaMemsetAsync(&ds->ticket, 0, 4, s);
-    k_tile_cov<TPW><<<(blocks + 3) / 4, 128, 0, s>>>(
-        ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(), T,
-        ctx->tile_state.as<TileBlockState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
-        ctx->out_tile_alpha.as<uint8_t>(), want_cov ? ctx->out_tile_cov.as<float>() : nullptr,
-        ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(), &ds->err, ctx->cov_signed);
+    float* cov = want_cov ? ctx->out_tile_cov.as<float>() : nullptr;
+    const bool row_form = ctx->tune_chain_coverage_form == 2 ||
+                          (ctx->tune_chain_coverage_form == 0 && n_rows >= ROW_FORM_MIN_ROWS_PER_SM * (uint32_t)sms);
+    if (row_form) {
+        // no more warps than rows, nor than the GPU keeps resident (16 CTAs of 4 warps per SM)
+        const uint32_t ctas = (uint32_t)std::min<uint64_t>(((uint64_t)n_rows + 3) / 4, (uint64_t)sms * 16);
+        k_tile_cov<TPW><<<ctas, 128, 0, s>>>(
+            ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(),
+            T, ctx->tile_row_start.as<uint32_t>(), &ds->n_rows, &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
+            ctx->out_tile_alpha.as<uint8_t>(), cov, ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(),
+            ctx->cov_signed);
+    } else {
+        const uint32_t blocks = (T + TPW - 1) / TPW;
+        cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)blocks * sizeof(TileBlockState), s);
+        k_tile_cov_blocks<TPW><<<(blocks + 3) / 4, 128, 0, s>>>(
+            ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(),
+            T, ctx->tile_state.as<TileBlockState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
+            ctx->out_tile_alpha.as<uint8_t>(), cov, ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(),
+            &ds->err, ctx->cov_signed);
+    }
 }
 
 template <class K>
@@ -392,9 +580,9 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     if (st != OCHRE_OK) return st;
     const uint32_t T = host_scalars(ctx)->n_tiles;
     *n_tiles_out = T;
-    const uint32_t blocks = (T + 3) / 4;   // >= blocks of the smallest tiles-per-warp shape
     OCHRE_CUDA_TRY(ctx->tile_info.ensure((size_t)T * sizeof(TileInfo)));
-    OCHRE_CUDA_TRY(ctx->tile_state.ensure((size_t)blocks * sizeof(TileBlockState)));
+    OCHRE_CUDA_TRY(ctx->tile_row_start.ensure((size_t)T * 4));
+    OCHRE_CUDA_TRY(ctx->tile_state.ensure((size_t)((T + 3) / 4) * sizeof(TileBlockState)));
     OCHRE_CUDA_TRY(ctx->span_flag.ensure((size_t)T * 4));
     OCHRE_CUDA_TRY(ctx->span_val.ensure((size_t)T * 8));
     OCHRE_CUDA_TRY(ctx->out_tile_xy.ensure((size_t)T * 4));
@@ -411,10 +599,20 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
                          ctx->raster_wbase.as<int32_t>(), &ds->n_bins, T, R, ctx->tile_info.as<TileInfo>(),
                          ctx->out_raster_tile_off.as<uint32_t>()));
     OCHRE_CUDA_TRY(cudaGetLastError());
+    if (T) {
+        OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(T) * sizeof(ScanStatus<uint32_t>)));
+        OCHRE_LAUNCH(ctx, "tile_row_scan", s,
+                     OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+                         T, RowIn{ctx->tile_info.as<TileInfo>()}, RowOut{ctx->tile_row_start.as<uint32_t>()},
+                         OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_rows, &ds->err, s)));
+    }
+    st = read_scalars(ctx, s);
+    if (st != OCHRE_OK) return st;
+    const uint32_t n_rows = host_scalars(ctx)->n_rows;
     switch (ctx->tune_chain_tiles_per_warp) {
-    case 4: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<4>(ctx, T, want_cov, s)); break;
-    case 8: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<8>(ctx, T, want_cov, s)); break;
-    case 16: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<16>(ctx, T, want_cov, s)); break;
+    case 4: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<4>(ctx, T, n_rows, want_cov, s)); break;
+    case 8: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<8>(ctx, T, n_rows, want_cov, s)); break;
+    case 16: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<16>(ctx, T, n_rows, want_cov, s)); break;
     default: return OCHRE_E_INVALID;
     }
     OCHRE_CUDA_TRY(cudaGetLastError());

@@ -32,9 +32,31 @@ def gpu_ctx_chain():
     ctx.close()
 
 
-@pytest.fixture(params=["fused", "chain"])
+@pytest.fixture(scope="session")
+def gpu_ctx_chain_rows():
+    """The general chain with the one-warp-per-tile-row coverage kernel forced
+    (the default picks it only when there are many tile rows)."""
+    from ochre_gb300 import GpuContext, autotune
+    ctx = GpuContext(0, chain_only=True)
+    autotune.apply(ctx, {"chain_coverage_form": 2})
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(scope="session")
+def gpu_ctx_chain_blocks():
+    """The general chain with the block-form coverage kernel forced."""
+    from ochre_gb300 import GpuContext, autotune
+    ctx = GpuContext(0, chain_only=True)
+    autotune.apply(ctx, {"chain_coverage_form": 1})
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(params=["fused", "chain", "chain_rows", "chain_blocks"])
 def any_ctx(request):
-    return request.getfixturevalue("gpu_ctx" if request.param == "fused" else "gpu_ctx_chain")
+    return request.getfixturevalue({"fused": "gpu_ctx", "chain": "gpu_ctx_chain", "chain_rows": "gpu_ctx_chain_rows",
+                                    "chain_blocks": "gpu_ctx_chain_blocks"}[request.param])
 
 
 @pytest.fixture(autouse=True)
