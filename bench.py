@@ -308,6 +308,33 @@ def bench_uneven(ctx, stream, flush, steps, peak):
     }
 
 
+def bench_stroke(ctx, stream, flush, steps):
+    """Stroked paths (Rasterizer::stroke): 20,000 rasters of 2-24 mixed
+    segments, widths 0.5-8 px; the device stroke stage plus the fill path,
+    with parity on a 1,000-path sample."""
+    import numpy as np
+
+    import oracle
+    from ochre_gb300 import DeviceBatch, batch as B, workloads as W
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from compare import compare
+    bt = W.stroke_run()
+    db = DeviceBatch(bt, ctx.device)
+    sp = stream.cuda_stream
+    for _ in range(2):
+        ctx.rasterize_device(db, sp)
+    st = ctx.stats()
+    ms = _event_ms(lambda: ctx.rasterize_device(db, sp), stream, flush, max(3, min(steps, 10)))
+    samp = B.subset(bt, list(range(0, bt.n_rasters, 20)))
+    with np.errstate(all="ignore"):
+        cst = compare(ctx.rasterize(samp), oracle.run(samp, threads=os.cpu_count() or 1), samp.n_rasters)
+    return {"workload": "stroke_run: 20000 stroked paths, 2-24 segments, width 0.5-8 px", "paths_per_s":
+            bt.n_rasters / (ms / 1e3), "ms_per_step": ms, "tiles": st["n_tiles"], "path": "fused" if st.get("fused")
+            else "chain", "parity_sample": {"paths": samp.n_rasters, "tiles_spans_exact": True,
+                                           "alpha_max_lsb": cst["max_lsb"], "alpha_diff_fraction": cst["diff_fraction"]},
+            "kernels": _kernel_shares(ctx, lambda: ctx.rasterize_device(db, sp))[:6]}
+
+
 def bench_differentiable(ctx, stream, flush, steps, n_scenes):
     """Forward (coverage render + L2 loss) and forward + backward scenes/s on
     the single-raster union (256 paths x 32 cubics, 1024^2) and on batched
@@ -603,6 +630,7 @@ def run_ours(args, ws, rank, local):
         extensions["uneven_mix"] = bench_uneven(ctx, stream, flush, args.steps,
                                                 float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])))
         extensions["differentiable"] = bench_differentiable(ctx, stream, flush, args.steps, args.diff_scenes)
+        extensions["stroke"] = bench_stroke(ctx, stream, flush, args.steps)
     n_paths_all = batch.n_rasters * ws
     value = n_paths_all * args.steps / dev_s_max
     cpu = cpu_baseline(batch) if ws == 1 else None
@@ -636,6 +664,7 @@ def run_ours(args, ws, rank, local):
         "cpu_baseline": cpu,
         "batched_uneven_mix": extensions.get("uneven_mix"),
         "differentiable": extensions.get("differentiable"),
+        "stroke": extensions.get("stroke"),
         "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s},
         "gpu_launches": launches,

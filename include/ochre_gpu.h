@@ -62,6 +62,11 @@ typedef enum ochre_verb {
 /* fill_flags bit: the fill's commands are already in device space and are
  * not transformed (Rasterizer::command/move_to/line_to, rasterizer.rs:61-157). */
 #define OCHRE_FILL_RAW 1u
+/* fill_flags bit: the fill is stroked (Rasterizer::stroke, rasterizer.rs:169-171)
+ * with width fill_width[f]: flattened in its own space, offset by width / 2 on
+ * both sides with miter joins and butt caps (path.rs:113-274), then filled
+ * with its transform. */
+#define OCHRE_FILL_STROKE 2u
 
 /* A batch of independent rasterizers.  Raster r owns fills
  * [raster_fill_off[r], raster_fill_off[r+1]) (one fill per raster when
@@ -81,6 +86,7 @@ typedef struct ochre_batch {
     uint32_t n_fills;
     const uint32_t *raster_fill_off; /* n_rasters + 1, or NULL */
     uint32_t n_rasters;
+    const float *fill_width;         /* n_fills stroke widths, or NULL (no stroked fills) */
 } ochre_batch;
 
 /* Output, in TileBuilder callback order per raster (rasterizer.rs:241, 263):
@@ -240,6 +246,11 @@ int ochre_rasterizer_command(ochre_rasterizer *r, uint8_t verb, const float *flo
 /* Rasterizer::fill (rasterizer.rs:161): a path under a transform (6 floats). */
 int ochre_rasterizer_fill(ochre_rasterizer *r, const uint8_t *verbs, size_t n_verbs,
                           const float *pts, size_t n_floats, const float xf[6]);
+
+/* Rasterizer::stroke (rasterizer.rs:169-171): the path is stroked with the
+ * given width in its own space, then filled with the transform. */
+int ochre_rasterizer_stroke(ochre_rasterizer *r, const uint8_t *verbs, size_t n_verbs, const float *pts,
+                            size_t n_floats, float width, const float xf[6]);
 /* Rasterizer::finish (rasterizer.rs:180): rasterizes on the GPU, then calls
  * tile/span in the reference's order.  Consumes (frees) the rasterizer, even
  * on error. */

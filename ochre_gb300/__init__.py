@@ -5,13 +5,15 @@ Mirrors glowcoil/ochre 0.2.0's public API (``Rasterizer::fill`` /
 hand-written CUDA kernels.  There is no CPU fallback: entry points raise if the
 CUDA library or a device is missing.
 """
-from .batch import (CLOSE, CONIC, CUBIC, FILL_RAW, IDENTITY, LINE, MOVE, QUADRATIC, Batch, BatchBuilder,
-                    concat, subset)
+from ._lib import OchreError
+from .batch import (CLOSE, CONIC, CUBIC, FILL_RAW, FILL_STROKE, IDENTITY, LINE, MOVE, QUADRATIC, Batch,
+                    BatchBuilder, concat, subset)
 from .rasterizer import (TILE_SIZE, DeviceBatch, GpuContext, Mat2x2, PathCmd, Rasterizer, TileBuilder,
                          Transform, Vec2, default_context, encode_path)
 
 __all__ = [
-    "MOVE", "LINE", "QUADRATIC", "CUBIC", "CONIC", "CLOSE", "FILL_RAW", "IDENTITY", "Batch", "BatchBuilder",
+    "MOVE", "LINE", "QUADRATIC", "CUBIC", "CONIC", "CLOSE", "FILL_RAW", "FILL_STROKE", "IDENTITY", "Batch",
+    "BatchBuilder", "OchreError",
     "concat", "subset", "TILE_SIZE", "DeviceBatch", "GpuContext", "Mat2x2", "PathCmd", "Rasterizer",
     "TileBuilder", "Transform", "Vec2", "default_context", "encode_path",
 ]

@@ -21,7 +21,8 @@ EXPORTS = [
     "ochre_gpu_create", "ochre_gpu_destroy", "ochre_gpu_set_flags", "ochre_gpu_rasterize_device",
     "ochre_gpu_rasterize", "ochre_gpu_last_stats", "ochre_gpu_last_timings", "ochre_gpu_status_string",
     "ochre_rasterizer_new", "ochre_rasterizer_move_to", "ochre_rasterizer_line_to",
-    "ochre_rasterizer_command", "ochre_rasterizer_fill", "ochre_rasterizer_finish", "ochre_rasterizer_free",
+    "ochre_rasterizer_command", "ochre_rasterizer_fill", "ochre_rasterizer_stroke", "ochre_rasterizer_finish",
+    "ochre_rasterizer_free",
     "ochre_gpu_rasterize_noalloc", "ochre_gpu_set_tunable", "ochre_gpu_get_tunable",
     "ochre_gpu_render_coverage", "ochre_gpu_l2_loss", "ochre_gpu_fill_backward",
 ]
@@ -41,6 +42,7 @@ class Batch(ctypes.Structure):
         ("fill_cmd_off", ctypes.c_void_p), ("fill_xf", ctypes.c_void_p),
         ("fill_flags", ctypes.c_void_p), ("n_fills", ctypes.c_uint32),
         ("raster_fill_off", ctypes.c_void_p), ("n_rasters", ctypes.c_uint32),
+        ("fill_width", ctypes.c_void_p),
     ]
 
 
@@ -115,6 +117,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_rasterizer_command.argtypes = [vp, u8, ctypes.POINTER(ctypes.c_float)]
         L.ochre_rasterizer_fill.argtypes = [vp, ctypes.POINTER(u8), ctypes.c_size_t, ctypes.POINTER(ctypes.c_float),
                                             ctypes.c_size_t, ctypes.POINTER(ctypes.c_float)]
+        L.ochre_rasterizer_stroke.argtypes = [vp, ctypes.POINTER(u8), ctypes.c_size_t, ctypes.POINTER(ctypes.c_float),
+                                              ctypes.c_size_t, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]
         L.ochre_rasterizer_finish.argtypes = [vp, TILE_FN, SPAN_FN, vp]
         L.ochre_rasterizer_free.argtypes = [vp]
         L.ochre_rasterizer_free.restype = None

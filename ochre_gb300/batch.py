@@ -34,6 +34,7 @@ import numpy as np
 MOVE, LINE, QUADRATIC, CUBIC, CONIC, CLOSE = 0, 1, 2, 3, 4, 5
 FLOATS_PER_VERB = np.array([2, 2, 4, 6, 5, 0], dtype=np.int64)
 FILL_RAW = 1
+FILL_STROKE = 2
 
 IDENTITY = np.array([1.0, 0.0, 0.0, 1.0, 0.0, 0.0], dtype=np.float32)
 
@@ -47,6 +48,7 @@ class Batch:
     fill_flags: Optional[np.ndarray]        # uint8 [n_fills] or None
     raster_fill_off: Optional[np.ndarray]   # uint32 [n_rasters + 1] or None (one fill per raster)
     n_rasters: int
+    fill_width: Optional[np.ndarray] = None # float32 [n_fills]: stroke width where flags & FILL_STROKE
 
     @property
     def n_cmds(self) -> int:
@@ -60,6 +62,10 @@ class Batch:
         """Compulsory input bytes: 1 per verb, 4 per float, 24 per transform."""
         return int(self.verbs.nbytes + self.pts.nbytes + 24 * self.n_fills)
 
+    @property
+    def has_strokes(self) -> bool:
+        return self.fill_flags is not None and bool(np.any(self.fill_flags & FILL_STROKE))
+
     def validate(self) -> None:
         v = self.verbs
         if v.dtype != np.uint8 or (len(v) and int(v.max()) > CLOSE):
@@ -72,6 +78,8 @@ class Batch:
             raise ValueError("fill_cmd_off must start at 0, end at n_cmds and be non-decreasing")
         if self.fill_xf.shape != (self.n_fills, 6):
             raise ValueError("fill_xf must be [n_fills, 6]")
+        if self.has_strokes and (self.fill_width is None or len(self.fill_width) != self.n_fills):
+            raise ValueError("stroked fills need fill_width [n_fills]")
         if self.raster_fill_off is None:
             if self.n_rasters != self.n_fills:
                 raise ValueError("without raster_fill_off there is one fill per raster")
@@ -90,6 +98,7 @@ class BatchBuilder:
         self._fill_ncmd: list[int] = []
         self._xf: list[np.ndarray] = []
         self._flags: list[int] = []
+        self._width: list[float] = []
         self._raster_nfill: list[int] = []
 
     def begin_raster(self) -> "BatchBuilder":
@@ -97,7 +106,9 @@ class BatchBuilder:
         return self
 
     def fill(self, verbs: Sequence[int] | np.ndarray, pts: Sequence[float] | np.ndarray,
-             transform: Optional[Iterable[float]] = None, raw: bool = False) -> "BatchBuilder":
+             transform: Optional[Iterable[float]] = None, raw: bool = False,
+             stroke_width: Optional[float] = None) -> "BatchBuilder":
+        """Rasterizer::fill (or Rasterizer::stroke when ``stroke_width`` is set)."""
         if not self._raster_nfill:
             self.begin_raster()
         v = np.asarray(verbs, dtype=np.uint8).reshape(-1)
@@ -107,7 +118,8 @@ class BatchBuilder:
         self._fill_ncmd.append(len(v))
         xf = IDENTITY if transform is None else np.asarray(list(transform), dtype=np.float32).reshape(6)
         self._xf.append(xf)
-        self._flags.append(FILL_RAW if raw else 0)
+        self._flags.append((FILL_RAW if raw else 0) | (FILL_STROKE if stroke_width is not None else 0))
+        self._width.append(0.0 if stroke_width is None else float(stroke_width))
         self._raster_nfill[-1] += 1
         return self
 
@@ -122,7 +134,8 @@ class BatchBuilder:
         roff = np.zeros(len(self._raster_nfill) + 1, dtype=np.uint32)
         if self._raster_nfill:
             roff[1:] = np.cumsum(self._raster_nfill)
-        b = Batch(verbs, pts, off, xf, flags if np.any(flags) else None, roff, len(self._raster_nfill))
+        width = np.asarray(self._width, dtype=np.float32) if np.any(flags & FILL_STROKE) else None
+        b = Batch(verbs, pts, off, xf, flags if np.any(flags) else None, roff, len(self._raster_nfill), width)
         b.validate()
         return b
 
@@ -144,8 +157,12 @@ def concat(batches: Sequence[Batch]) -> Batch:
     off = np.concatenate(offs + [np.array([cbase])]).astype(np.uint32)
     roff = np.concatenate(roffs + [np.array([fbase])]).astype(np.uint32)
     fl = np.concatenate(flags).astype(np.uint8)
+    width = None
+    if any(b.fill_width is not None for b in batches):
+        width = np.concatenate([b.fill_width if b.fill_width is not None else np.zeros(b.n_fills, np.float32)
+                                for b in batches]).astype(np.float32)
     out = Batch(verbs, pts, off, np.concatenate(xfs).astype(np.float32),
-                fl if np.any(fl) else None, roff, sum(b.n_rasters for b in batches))
+                fl if np.any(fl) else None, roff, sum(b.n_rasters for b in batches), width)
     out.validate()
     return out
 
@@ -160,5 +177,7 @@ def subset(b: Batch, rasters: Sequence[int]) -> Batch:
         for f in range(int(roff[r]), int(roff[r + 1])):
             c0, c1 = int(b.fill_cmd_off[f]), int(b.fill_cmd_off[f + 1])
             raw = b.fill_flags is not None and bool(b.fill_flags[f] & FILL_RAW)
-            bb.fill(b.verbs[c0:c1], b.pts[fpo[c0]:fpo[c1]], b.fill_xf[f], raw=raw)
+            stroke = b.fill_flags is not None and bool(b.fill_flags[f] & FILL_STROKE)
+            bb.fill(b.verbs[c0:c1], b.pts[fpo[c0]:fpo[c1]], b.fill_xf[f], raw=raw,
+                    stroke_width=float(b.fill_width[f]) if stroke else None)
     return bb.build()

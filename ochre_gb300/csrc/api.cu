@@ -145,12 +145,19 @@ static int validate_host(const ochre_batch* in) {
     return OCHRE_OK;
 }
 
-int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s) {
+int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out, cudaStream_t s) {
     std::memset(out, 0, sizeof *out);
     ctx->stats = ochre_stats{};
     ctx->prof_used = 0;
     ctx->launches = 0;
     ctx->timings.clear();
+    // stroked fills become plain fills first (Rasterizer::stroke, rasterizer.rs:169-171)
+    ochre_batch expanded;
+    {
+        const int sst = stage_stroke(ctx, in_orig, s, &expanded);
+        if (sst != OCHRE_OK) return sst;
+    }
+    const ochre_batch* in = &expanded;
     OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
     const uint32_t R = in->n_rasters;
     OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
@@ -258,6 +265,10 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_row_start, &ctx->tile_state,
                      &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain,
                      &ctx->grad_g, &ctx->grad_gs, &ctx->grad_left, &ctx->grad_line, &ctx->grad_pts,
+                     &ctx->sk_cmd_foff, &ctx->sk_cmd_mv, &ctx->sk_cmd_ep, &ctx->sk_poly_off, &ctx->sk_poly_foff,
+                     &ctx->sk_pverbs, &ctx->sk_ppts, &ctx->sk_pfoff, &ctx->sk_pfill_off, &ctx->sk_first_close,
+                     &ctx->sk_unit_start, &ctx->sk_out_off, &ctx->sk_out_foff, &ctx->sk_unit_fill, &ctx->sk_overbs,
+                     &ctx->sk_opts, &ctx->sk_ofill_off, &ctx->sk_oflags, &ctx->in_fill_width,
                      &ctx->out_tile_xy,
                      &ctx->out_tile_alpha, &ctx->out_tile_cov, &ctx->out_span_xy, &ctx->out_span_w,
                      &ctx->out_span_tile, &ctx->out_raster_tile_off, &ctx->out_raster_span_off};
@@ -317,6 +328,12 @@ int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result*
         OCHRE_CUDA_TRY(ctx->in_fill_flags.ensure(in->n_fills));
         OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_fill_flags.p, in->fill_flags, in->n_fills, cudaMemcpyHostToDevice, s));
         d.fill_flags = ctx->in_fill_flags.as<uint8_t>();
+    }
+    if (in->fill_width && in->n_fills) {
+        OCHRE_CUDA_TRY(ctx->in_fill_width.ensure((size_t)in->n_fills * 4));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_fill_width.p, in->fill_width, (size_t)in->n_fills * 4,
+                                       cudaMemcpyHostToDevice, s));
+        d.fill_width = ctx->in_fill_width.as<float>();
     }
     if (in->raster_fill_off) {
         OCHRE_CUDA_TRY(ctx->in_raster_off.ensure(((size_t)in->n_rasters + 1) * 4));
@@ -422,6 +439,7 @@ struct ochre_rasterizer {
     std::vector<uint32_t> fill_off{0};
     std::vector<float> xf;
     std::vector<uint8_t> flags;
+    std::vector<float> width;
     // A run of raw commands (move_to/line_to/command) is one untransformed fill.
     bool open_raw = false;
 };
@@ -432,6 +450,7 @@ static void raw_cmd(ochre_rasterizer* r, uint8_t verb, const float* f, int nf) {
     if (!r->open_raw) {
         r->xf.insert(r->xf.end(), kIdentity, kIdentity + 6);
         r->flags.push_back(OCHRE_FILL_RAW);
+        r->width.push_back(0.0f);
         r->fill_off.push_back((uint32_t)r->verbs.size());
         r->open_raw = true;
     }
@@ -486,7 +505,17 @@ int ochre_rasterizer_fill(ochre_rasterizer* r, const uint8_t* verbs, size_t n_ve
     r->pts.insert(r->pts.end(), pts, pts + need);
     r->xf.insert(r->xf.end(), xf, xf + 6);
     r->flags.push_back(0);
+    r->width.push_back(0.0f);
     r->fill_off.push_back((uint32_t)r->verbs.size());
+    return OCHRE_OK;
+}
+
+int ochre_rasterizer_stroke(ochre_rasterizer* r, const uint8_t* verbs, size_t n_verbs, const float* pts,
+                            size_t n_floats, float width, const float xf[6]) {
+    const int st = ochre_rasterizer_fill(r, verbs, n_verbs, pts, n_floats, xf);
+    if (st != OCHRE_OK) return st;
+    r->flags.back() = OCHRE_FILL_STROKE;
+    r->width.back() = width;
     return OCHRE_OK;
 }
 
@@ -502,6 +531,7 @@ int ochre_rasterizer_finish(ochre_rasterizer* r, ochre_tile_fn tile, ochre_span_
     b.fill_cmd_off = r->fill_off.data();
     b.fill_xf = r->xf.data();
     b.fill_flags = r->flags.data();
+    b.fill_width = r->width.data();
     b.n_fills = (uint32_t)(r->fill_off.size() - 1);
     const uint32_t raster_off[2] = {0, b.n_fills};
     b.raster_fill_off = raster_off;

@@ -24,36 +24,6 @@
 
 namespace ochre {
 
-struct CmdScan {
-    uint32_t foff;   // exclusive sum of floats consumed
-    uint32_t mv;     // 1 + index of the most recent Move (0: none)
-    uint32_t ep;     // 1 + index of the most recent non-Close command (0: none)
-};
-struct OpCmd {
-    __device__ __forceinline__ CmdScan operator()(CmdScan a, CmdScan b) const {
-        return CmdScan{a.foff + b.foff, max(a.mv, b.mv), max(a.ep, b.ep)};
-    }
-};
-struct CmdIn {
-    const uint8_t* verbs;
-    uint32_t* err;
-    __device__ __forceinline__ CmdScan operator()(uint64_t i) const {
-        const uint8_t v = verbs[i];
-        if (v > V_CLOSE) atomicOr(err, ERR_INVALID);
-        const uint32_t id = (uint32_t)i + 1u;
-        return CmdScan{floats_per_verb(v), v == V_MOVE ? id : 0u, v <= V_CONIC ? id : 0u};
-    }
-};
-struct CmdOut {
-    uint32_t* foff;
-    uint32_t* mv;
-    uint32_t* ep;
-    __device__ __forceinline__ void operator()(uint64_t i, CmdScan ex, CmdScan) const {
-        foff[i] = ex.foff;
-        mv[i] = ex.mv;
-        ep[i] = ex.ep;
-    }
-};
 
 // Runs the flattening of one command, calling line(a, b) for each line_to
 // in order.  Returns false when a cap was hit.

@@ -38,6 +38,39 @@ struct CmdCtx {
     uint32_t fill;
 };
 
+// Command scan: float offset, most recent Move, most recent non-Close
+// command, per command (exclusive), in one pass.
+struct CmdScan {
+    uint32_t foff;   // exclusive sum of floats consumed
+    uint32_t mv;     // 1 + index of the most recent Move (0: none)
+    uint32_t ep;     // 1 + index of the most recent non-Close command (0: none)
+};
+struct OpCmd {
+    __device__ __forceinline__ CmdScan operator()(CmdScan a, CmdScan b) const {
+        return CmdScan{a.foff + b.foff, max(a.mv, b.mv), max(a.ep, b.ep)};
+    }
+};
+struct CmdIn {
+    const uint8_t* verbs;
+    uint32_t* err;
+    __device__ __forceinline__ CmdScan operator()(uint64_t i) const {
+        const uint8_t v = verbs[i];
+        if (v > V_CLOSE) atomicOr(err, ERR_INVALID);
+        const uint32_t id = (uint32_t)i + 1u;
+        return CmdScan{floats_per_verb(v), v == V_MOVE ? id : 0u, v <= V_CONIC ? id : 0u};
+    }
+};
+struct CmdOut {
+    uint32_t* foff;
+    uint32_t* mv;
+    uint32_t* ep;
+    __device__ __forceinline__ void operator()(uint64_t i, CmdScan ex, CmdScan) const {
+        foff[i] = ex.foff;
+        mv[i] = ex.mv;
+        ep[i] = ex.ep;
+    }
+};
+
 __device__ __forceinline__ uint32_t fill_of(const BatchView& b, uint32_t c) {
     return upper_bound_u32(b.fill_off, b.n_fills + 1, c) - 1u;
 }

@@ -565,6 +565,7 @@ int ochre_gpu_fill_backward(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t 
     if (!ctx || !in || (in->n_rasters && w && h && !dl_dcov) || (in->n_floats && !dl_dpts) ||
         (in->n_fills && !dl_dxf) || w > MAX_CANVAS || h > MAX_CANVAS)
         return OCHRE_E_INVALID;
+    if (in->fill_width) return OCHRE_E_INVALID;   // stroked fills are not differentiated
     if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
     // recompute the forward structure (lines, cells, tiles) and signed coverage

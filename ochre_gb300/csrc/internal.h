@@ -145,6 +145,10 @@ struct ochre_gpu_ctx {
     bool cov_signed = false;   // tile_cov holds accum + area (signed) instead of |accum + area|
     // differentiable path scratch
     ochre::DevBuf grad_g, grad_gs, grad_left, grad_line, grad_pts;
+    // stroke stage: input command scan, polyline, units, output batch
+    ochre::DevBuf sk_cmd_foff, sk_cmd_mv, sk_cmd_ep, sk_poly_off, sk_poly_foff, sk_pverbs, sk_ppts, sk_pfoff,
+        sk_pfill_off, sk_first_close, sk_unit_start, sk_out_off, sk_out_foff, sk_unit_fill, sk_overbs, sk_opts,
+        sk_ofill_off, sk_oflags, in_fill_width;
 
     // Launch-shape tunables (ochre_gpu_set_tunable; chosen by the autotuner).
     int tune_fused_threads = 64;
@@ -173,6 +177,8 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
 int stage_sort(ochre_gpu_ctx* ctx, uint64_t n_entries, uint32_t key_bits, cudaStream_t s, uint32_t* passes);
 int stage_tiles(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t n_entries, cudaStream_t s, uint32_t* n_tiles,
                 uint32_t* n_spans);
+// Rewrites stroked fills into plain fills (stroke.cu); *out views device memory.
+int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochre_batch* out);
 int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
                 uint32_t* n_spans);
 

@@ -97,7 +97,12 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
                                  &ctx.keys_alt, &ctx.vals_alt, &ctx.bins, &ctx.sort_hist, &ctx.sort_lookback,
                                  &ctx.tile_head, &ctx.tile_info, &ctx.tile_row_start, &ctx.tile_state, &ctx.span_flag, &ctx.span_val,
                                  &ctx.scan_status, &ctx.scalars, &ctx.fused_chain, &ctx.out_tile_cov,
-                                 &ctx.grad_g, &ctx.grad_gs, &ctx.grad_left, &ctx.grad_line, &ctx.grad_pts};
+                                 &ctx.grad_g, &ctx.grad_gs, &ctx.grad_left, &ctx.grad_line, &ctx.grad_pts,
+                                 &ctx.sk_cmd_foff, &ctx.sk_cmd_mv, &ctx.sk_cmd_ep, &ctx.sk_poly_off,
+                                 &ctx.sk_poly_foff, &ctx.sk_pverbs, &ctx.sk_ppts, &ctx.sk_pfoff, &ctx.sk_pfill_off,
+                                 &ctx.sk_first_close, &ctx.sk_unit_start, &ctx.sk_out_off, &ctx.sk_out_foff,
+                                 &ctx.sk_unit_fill, &ctx.sk_overbs, &ctx.sk_opts, &ctx.sk_ofill_off, &ctx.sk_oflags,
+                                 &ctx.in_fill_width};
     for (ochre::DevBuf* b : internal) use_arena(*b, &arena);
     const size_t R1 = (size_t)in->n_rasters + 1;
     use_caller(ctx.out_tile_xy, out->tile_xy, (size_t)out->tile_capacity * 4, &arena);

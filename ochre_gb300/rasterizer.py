@@ -196,6 +196,16 @@ class Rasterizer:
             pts.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(pts),
             xf.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "fill")
 
+    def stroke(self, path: Sequence[PathCmd], width: float, transform: Transform) -> None:
+        """rasterizer.rs:169-171: the path stroked with ``width`` (in its own
+        space), then filled with ``transform``."""
+        verbs, pts = encode_path(path)
+        xf = transform.as_array()
+        _lib.check(_lib.load().ochre_rasterizer_stroke(
+            self._live(), verbs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), len(verbs),
+            pts.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), len(pts), float(width),
+            xf.ctypes.data_as(ctypes.POINTER(ctypes.c_float))), "stroke")
+
     def finish(self, builder: TileBuilder) -> None:
         h = self._live()
         self._h = None  # finish consumes the rasterizer
@@ -228,11 +238,13 @@ class Rasterizer:
 # ---------------------------------------------------------------------------
 # Batched entry points
 # ---------------------------------------------------------------------------
-def _c_batch(verbs_p, n_cmds, pts_p, n_floats, off_p, xf_p, flags_p, n_fills, roff_p, n_rasters) -> _lib.Batch:
+def _c_batch(verbs_p, n_cmds, pts_p, n_floats, off_p, xf_p, flags_p, n_fills, roff_p, n_rasters,
+             width_p=None) -> _lib.Batch:
     b = _lib.Batch()
     b.verbs, b.n_cmds, b.pts, b.n_floats = verbs_p, n_cmds, pts_p, n_floats
     b.fill_cmd_off, b.fill_xf, b.fill_flags, b.n_fills = off_p, xf_p, flags_p, n_fills
     b.raster_fill_off, b.n_rasters = roff_p, n_rasters
+    b.fill_width = width_p
     return b
 
 
@@ -251,11 +263,13 @@ class DeviceBatch:
         self.fill_flags = t(batch.fill_flags, np.uint8) if batch.fill_flags is not None else None
         self.raster_off = (t(batch.raster_fill_off.astype(np.int32), np.int32)
                            if batch.raster_fill_off is not None else None)
+        fw = getattr(batch, "fill_width", None)
+        self.fill_width = t(fw, np.float32) if fw is not None and batch.n_fills else None
         self.c = _c_batch(self.verbs.data_ptr(), batch.n_cmds, self.pts.data_ptr(), len(batch.pts),
                           self.fill_off.data_ptr(), self.fill_xf.data_ptr(),
                           self.fill_flags.data_ptr() if self.fill_flags is not None else None,
                           batch.n_fills, self.raster_off.data_ptr() if self.raster_off is not None else None,
-                          batch.n_rasters)
+                          batch.n_rasters, self.fill_width.data_ptr() if self.fill_width is not None else None)
 
     def input_bytes(self) -> int:
         return self.batch.input_bytes()
@@ -345,7 +359,8 @@ class GpuContext:
 
         c = _c_batch(p(batch.verbs, np.uint8), batch.n_cmds, p(batch.pts, np.float32), len(batch.pts),
                      p(batch.fill_cmd_off, np.uint32), p(batch.fill_xf, np.float32), p(batch.fill_flags, np.uint8),
-                     batch.n_fills, p(batch.raster_fill_off, np.uint32), batch.n_rasters)
+                     batch.n_fills, p(batch.raster_fill_off, np.uint32), batch.n_rasters,
+                     p(getattr(batch, "fill_width", None), np.float32))
         r = _lib.Result()
         _lib.check(_lib.load().ochre_gpu_rasterize(self.handle, ctypes.byref(c), ctypes.byref(r)), "rasterize")
         return r

@@ -297,6 +297,56 @@ def diff_scenes(n_scenes: int = 4096, seed: int = 5, size: float = 512.0, min_pa
     return _batch_from_streams(verbs, pts, n_seg + 2, np.arange(n_fills), xf, n_fills, roff, n_scenes)
 
 
+def stroke_run(n_paths: int = 20_000, seed: int = 6, canvas: float = 2048.0) -> Batch:
+    """Stroked paths (Rasterizer::stroke), one rasterizer each: open and
+    closed contours of 2-24 mixed line / quadratic / cubic segments (a random
+    walk with steps of 4-60 px), widths 0.5-8 px, random rotation and scale
+    0.5-2 per path, placed on a canvas.  About a quarter are closed."""
+    from .batch import FILL_STROKE, LINE
+    rng = np.random.default_rng(seed)
+    n_seg = rng.integers(2, 25, size=n_paths)
+    closed = rng.uniform(size=n_paths) < 0.25
+    tot = int(n_seg.sum())
+    kinds = rng.choice(np.array([LINE, QUADRATIC, CUBIC], np.uint8), size=tot, p=[0.4, 0.3, 0.3])
+    step = rng.uniform(4.0, 60.0, size=n_paths)
+    seg_path = np.repeat(np.arange(n_paths), n_seg)
+    # every segment gets 3 random-walk points; lines use the last, quadratics the last 2
+    walk = rng.normal(0.0, 1.0, size=(tot, 3, 2)) * step[seg_path, None, None]
+    ends = np.cumsum(walk.reshape(-1, 2), axis=0).reshape(tot, 3, 2)
+    first = np.concatenate([[0], np.cumsum(n_seg)[:-1]])
+    base = ends[first, 0] - walk[first, 0]          # path start: the walk's origin
+    ends = ends - np.repeat(base, n_seg, axis=0)[:, None, :]
+    ncmd = n_seg + 1 + closed.astype(np.int64)
+    verbs = np.empty(int(ncmd.sum()), np.uint8)
+    cstart = np.concatenate([[0], np.cumsum(ncmd)[:-1]])
+    verbs[cstart] = MOVE
+    seg_local = np.arange(tot) - first[seg_path]
+    seg_cmd = cstart[seg_path] + 1 + seg_local
+    verbs[seg_cmd] = kinds
+    verbs[(cstart + ncmd - 1)[closed]] = CLOSE
+    fpv = FLOATS_PER_VERB[verbs]
+    foff = np.concatenate([[0], np.cumsum(fpv)]).astype(np.int64)
+    pts = np.zeros(int(foff[-1]), np.float32)
+    o = foff[seg_cmd]
+    lin = kinds == LINE
+    pts[o[lin]], pts[o[lin] + 1] = ends[lin, 2, 0], ends[lin, 2, 1]
+    q = kinds == QUADRATIC
+    pts[o[q]], pts[o[q] + 1], pts[o[q] + 2], pts[o[q] + 3] = ends[q, 1, 0], ends[q, 1, 1], ends[q, 2, 0], ends[q, 2, 1]
+    c = kinds == CUBIC
+    for k in range(3):
+        pts[o[c] + 2 * k], pts[o[c] + 2 * k + 1] = ends[c, k, 0], ends[c, k, 1]
+    ang = rng.uniform(0.0, 2.0 * np.pi, size=n_paths)
+    sc = rng.uniform(0.5, 2.0, size=n_paths)
+    tx = rng.uniform(128.0, canvas - 128.0, size=(n_paths, 2))
+    xf = np.stack([sc * np.cos(ang), -sc * np.sin(ang), sc * np.sin(ang), sc * np.cos(ang), tx[:, 0], tx[:, 1]], axis=1)
+    off = np.concatenate([[0], np.cumsum(ncmd)]).astype(np.uint32)
+    flags = np.full(n_paths, FILL_STROKE, np.uint8)
+    width = rng.uniform(0.5, 8.0, size=n_paths).astype(np.float32)
+    b = Batch(verbs, pts, off, xf.astype(np.float32), flags, None, n_paths, width)
+    b.validate()
+    return b
+
+
 CONFIGS = {
     1: ("cubic_boxes", cubic_boxes),
     2: ("glyph_run", glyph_run),

@@ -49,6 +49,7 @@ class _Batch(ctypes.Structure):
         ("fill_cmd_off", ctypes.c_void_p), ("fill_xf", ctypes.c_void_p),
         ("fill_flags", ctypes.c_void_p), ("n_fills", ctypes.c_uint32),
         ("raster_fill_off", ctypes.c_void_p), ("n_rasters", ctypes.c_uint32),
+        ("fill_width", ctypes.c_void_p),
     ]
 
 
@@ -90,6 +91,12 @@ def _load():
         lib.ochre_oracle_backward64.argtypes = [ctypes.POINTER(_Batch), ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.ochre_oracle_backward64.restype = ctypes.c_int
+        lib.ochre_oracle_stroke.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_float,
+                                            ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64),
+                                            ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)]
+        lib.ochre_oracle_stroke.restype = ctypes.c_int
+        lib.free.argtypes = [ctypes.c_void_p]
+        lib.free.restype = None
         _lib = lib
     return _lib
 
@@ -122,6 +129,7 @@ def _as_batch(batch):
     b.n_fills = len(batch.fill_cmd_off) - 1
     b.raster_fill_off = p(batch.raster_fill_off, np.uint32)
     b.n_rasters = batch.n_rasters
+    b.fill_width = p(getattr(batch, "fill_width", None), np.float32)
     return b, keep
 
 
@@ -210,6 +218,27 @@ def tile_cov_error_vs_fp64(batch, gpu_tile_xy, gpu_tile_cov, gpu_raster_tile_off
             errs.append(np.abs(gpu_tile_cov[t].astype(np.float64) - block))
     e = np.concatenate(errs) if errs else np.zeros(1)
     return {"max_abs": float(e.max()), "mean_abs": float(e.mean()), "pixels": int(e.size)}
+
+
+def stroke(verbs, pts, width: float):
+    """Rasterizer::stroke's preprocessing of one path (path.rs:113-274):
+    returns (verbs, pts) of the Move / Line / Close path that is filled."""
+    lib = _load()
+    v = np.ascontiguousarray(verbs, np.uint8)
+    p = np.ascontiguousarray(pts, np.float32)
+    ov, op = ctypes.c_void_p(), ctypes.c_void_p()
+    n, nf = ctypes.c_uint64(), ctypes.c_uint64()
+    st = lib.ochre_oracle_stroke(v.ctypes.data if len(v) else None, len(v), p.ctypes.data if len(p) else None,
+                                 float(width), ctypes.byref(ov), ctypes.byref(n), ctypes.byref(op), ctypes.byref(nf))
+    if st:
+        raise RuntimeError(f"oracle stroke failed with status {st}")
+    try:
+        out_v = _copy(ov.value, np.uint8, n.value)
+        out_p = _copy(op.value, np.float32, nf.value)
+    finally:
+        lib.free(ov)
+        lib.free(op)
+    return out_v, out_p
 
 
 def seg_counts(batch) -> np.ndarray:

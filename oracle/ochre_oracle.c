@@ -83,6 +83,9 @@ static vec2 vsub(vec2 a, vec2 b) { return v2(a.x - b.x, a.y - b.y); }
 static vec2 vscale(float s, vec2 a) { return v2(s * a.x, s * a.y); }
 static int veq(vec2 a, vec2 b) { return a.x == b.x && a.y == b.y; }
 static float vlength(vec2 a) { return sqrtf(a.x * a.x + a.y * a.y); }
+static float vdot(vec2 a, vec2 b) { return a.x * b.x + a.y * b.y; }
+/* Vec2 * f32 (geom.rs:108-117) */
+static vec2 vmul(vec2 a, float s) { return v2(a.x * s, a.y * s); }
 /* lerp(t, a, b) = (1 - t) * a + t * b */
 static vec2 vlerp(float t, vec2 a, vec2 b) {
     return vadd(vscale(1.0f - t, a), vscale(t, b));
@@ -497,6 +500,215 @@ typedef struct {
     int error;
 } raster_out;
 
+/* ------------------------------------------------------------------ */
+/* path.rs:113-274: flatten() and stroke()                             */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    uint8_t *verbs;
+    float *pts;          /* 2 per command (Close: unused zeros) */
+    size_t n, cap;
+    int error;
+} pbuf;
+
+static void pb_push(pbuf *b, uint8_t verb, vec2 p) {
+    if (b->error) return;
+    if (b->n == b->cap) {
+        size_t c = b->cap ? b->cap * 2 : 64;
+        uint8_t *v = (uint8_t *)realloc(b->verbs, c);
+        float *q = (float *)realloc(b->pts, c * 2 * sizeof(float));
+        if (v) b->verbs = v;
+        if (q) b->pts = q;
+        if (!v || !q) { b->error = OCHRE_ORACLE_E_NOMEM; return; }
+        b->cap = c;
+    }
+    b->verbs[b->n] = verb;
+    b->pts[2 * b->n] = p.x;
+    b->pts[2 * b->n + 1] = p.y;
+    b->n++;
+}
+
+static vec2 pb_point(const pbuf *b, size_t i) { return v2(b->pts[2 * i], b->pts[2 * i + 1]); }
+
+/* path.rs:76-101, emitting Line commands */
+static void pb_flatten_conic(pbuf *b, vec2 last, vec2 control, vec2 point, float weight, float t0, float t1,
+                             vec2 p0, vec2 p1, int depth) {
+    float t = 0.5f * (t0 + t1);
+    vec2 wc = vscale(weight, control);
+    vec2 p01 = vlerp(t, last, wc);
+    vec2 p12 = vlerp(t, wc, point);
+    float denom = (1.0f - t) * (1.0f - t) + 2.0f * t * (1.0f - t) * weight + t * t;
+    vec2 midpoint = vscale(1.0f / denom, vlerp(t, p01, p12));
+    float err = vlength(vsub(midpoint, vscale(0.5f, vadd(p0, p1))));
+    if (err > TOLERANCE) {
+        if (depth >= CONIC_DEPTH_CAP) { b->error = OCHRE_ORACLE_E_LIMIT; return; }
+        pb_flatten_conic(b, last, control, point, weight, t0, t, p0, midpoint, depth + 1);
+        pb_flatten_conic(b, last, control, point, weight, t, t1, midpoint, p1, depth + 1);
+    } else {
+        pb_push(b, OCHRE_ORACLE_LINE, midpoint);
+        pb_push(b, OCHRE_ORACLE_LINE, p1);
+    }
+}
+
+/* path.rs:113-142: `last` starts at the origin and follows every command's
+ * end point (Close leaves it). */
+static void path_flatten(const uint8_t *verbs, uint64_t n, const float *pts, pbuf *out) {
+    vec2 last = v2(0.0f, 0.0f);
+    uint64_t fo = 0;
+    for (uint64_t c = 0; c < n && !out->error; c++) {
+        const float *fp = pts + fo;
+        fo += FLOATS_PER_VERB[verbs[c]];
+        switch (verbs[c]) {
+        case OCHRE_ORACLE_MOVE:
+            pb_push(out, OCHRE_ORACLE_MOVE, v2(fp[0], fp[1]));
+            last = v2(fp[0], fp[1]);
+            break;
+        case OCHRE_ORACLE_LINE:
+            pb_push(out, OCHRE_ORACLE_LINE, v2(fp[0], fp[1]));
+            last = v2(fp[0], fp[1]);
+            break;
+        case OCHRE_ORACLE_QUADRATIC: {
+            vec2 control = v2(fp[0], fp[1]), point = v2(fp[2], fp[3]);
+            float dt = sqrtf((4.0f * TOLERANCE) / vlength(vadd(vsub(last, vscale(2.0f, control)), point)));
+            float t = 0.0f;
+            uint32_t k = 0;
+            while (t < 1.0f) {
+                t = rmin(t + dt, 1.0f);
+                pb_push(out, OCHRE_ORACLE_LINE, vlerp(t, vlerp(t, last, control), vlerp(t, control, point)));
+                if (++k >= FLATTEN_CAP) { out->error = OCHRE_ORACLE_E_LIMIT; break; }
+            }
+            last = point;
+            break;
+        }
+        case OCHRE_ORACLE_CUBIC: {
+            vec2 c1 = v2(fp[0], fp[1]), c2 = v2(fp[2], fp[3]), point = v2(fp[4], fp[5]);
+            vec2 a = vadd(vsub(vadd(vscale(-1.0f, last), vscale(3.0f, c1)), vscale(3.0f, c2)), point);
+            vec2 bb = vscale(3.0f, vadd(vsub(last, vscale(2.0f, c1)), c2));
+            float conc = rmax(vlength(bb), vlength(vadd(a, bb)));
+            float dt = sqrtf((sqrtf(8.0f) * TOLERANCE) / conc);
+            float t = 0.0f;
+            uint32_t k = 0;
+            while (t < 1.0f) {
+                t = rmin(t + dt, 1.0f);
+                vec2 p01 = vlerp(t, last, c1), p12 = vlerp(t, c1, c2), p23 = vlerp(t, c2, point);
+                pb_push(out, OCHRE_ORACLE_LINE, vlerp(t, vlerp(t, p01, p12), vlerp(t, p12, p23)));
+                if (++k >= FLATTEN_CAP) { out->error = OCHRE_ORACLE_E_LIMIT; break; }
+            }
+            last = point;
+            break;
+        }
+        case OCHRE_ORACLE_CONIC: {
+            vec2 control = v2(fp[0], fp[1]), point = v2(fp[2], fp[3]);
+            pb_flatten_conic(out, last, control, point, fp[4], 0.0f, 1.0f, last, point, 0);
+            last = point;
+            break;
+        }
+        default:
+            pb_push(out, OCHRE_ORACLE_CLOSE, v2(0.0f, 0.0f));
+            break;
+        }
+    }
+}
+
+/* path.rs:160-168 */
+static void stroke_join(pbuf *out, float width, vec2 prev_normal, vec2 next_normal, vec2 point) {
+    const float offset = 1.0f / (1.0f + vdot(prev_normal, next_normal));
+    if (fabsf(offset) > 2.0f) {
+        pb_push(out, OCHRE_ORACLE_LINE, vadd(point, vscale(0.5f * width, prev_normal)));
+        pb_push(out, OCHRE_ORACLE_LINE, vadd(point, vscale(0.5f * width, next_normal)));
+    } else {
+        pb_push(out, OCHRE_ORACLE_LINE, vadd(point, vscale(0.5f * width * offset, vadd(prev_normal, next_normal))));
+    }
+}
+
+/* path.rs:170-212: one side of a contour (poly[c0, c1)) */
+static void stroke_offset(pbuf *out, float width, const pbuf *poly, size_t c0, size_t c1, int closed, int reverse) {
+    const size_t len = c1 - c0;
+    const vec2 first_point = closed == reverse ? pb_point(poly, c0) : pb_point(poly, c1 - 1);
+    vec2 prev_point = first_point;
+    vec2 prev_normal = v2(0.0f, 0.0f);
+    for (size_t i = 0;; i++) {
+        vec2 next_point;
+        if (i < len) next_point = reverse ? pb_point(poly, c0 + len - i - 1) : pb_point(poly, c0 + i);
+        else next_point = first_point;
+        if (!veq(next_point, prev_point) || i == len) {
+            const vec2 next_tangent = vsub(next_point, prev_point);
+            vec2 next_normal = v2(-next_tangent.y, next_tangent.x);
+            const float next_normal_len = vlength(next_normal);
+            next_normal = next_normal_len == 0.0f ? v2(0.0f, 0.0f) : vmul(next_normal, 1.0f / next_normal_len);
+            stroke_join(out, width, prev_normal, next_normal, prev_point);
+            prev_point = next_point;
+            prev_normal = next_normal;
+        }
+        if (i + 1 > len) break;
+    }
+}
+
+/* path.rs:214-274.  Contours run from a Move (or the command after a Close)
+ * to the next Move / Close / end; `closed` becomes true at the first Close
+ * and stays true for the rest of the path. */
+static void stroke_path(const pbuf *poly, float width, pbuf *out) {
+    size_t start = 0, end = 0;
+    int closed = 0;
+    for (size_t k = 0;; k++) {
+        const int have = k < poly->n;
+        const uint8_t verb = have ? poly->verbs[k] : 0xff;
+        if (have && verb == OCHRE_ORACLE_CLOSE) closed = 1;
+        if (!have || verb == OCHRE_ORACLE_MOVE || verb == OCHRE_ORACLE_CLOSE) {
+            if (start != end) {
+                size_t base = out->n;
+                stroke_offset(out, width, poly, start, end, closed, 0);
+                if (!out->error) out->verbs[base] = OCHRE_ORACLE_MOVE;
+                if (closed) pb_push(out, OCHRE_ORACLE_CLOSE, v2(0.0f, 0.0f));
+                base = out->n;
+                stroke_offset(out, width, poly, start, end, closed, 1);
+                if (closed && !out->error) out->verbs[base] = OCHRE_ORACLE_MOVE;
+                pb_push(out, OCHRE_ORACLE_CLOSE, v2(0.0f, 0.0f));
+            }
+        }
+        if (!have) break;
+        if (verb == OCHRE_ORACLE_MOVE) {
+            start = end;
+            end = start + 1;
+        } else if (verb == OCHRE_ORACLE_LINE) {
+            end += 1;
+        } else {   /* Close */
+            start = end + 1;
+            end = start;
+            closed = 1;
+        }
+    }
+}
+
+int ochre_oracle_stroke(const uint8_t *verbs, uint64_t n_cmds, const float *pts, float width,
+                        uint8_t **out_verbs, uint64_t *out_n_cmds, float **out_pts, uint64_t *out_n_floats) {
+    *out_verbs = NULL;
+    *out_pts = NULL;
+    *out_n_cmds = 0;
+    *out_n_floats = 0;
+    for (uint64_t c = 0; c < n_cmds; c++)
+        if (verbs[c] > 5) return OCHRE_ORACLE_E_INVALID;
+    pbuf poly = {0}, out = {0};
+    path_flatten(verbs, n_cmds, pts, &poly);
+    if (!poly.error) stroke_path(&poly, width, &out);
+    int st = poly.error ? poly.error : out.error;
+    free(poly.verbs);
+    free(poly.pts);
+    if (st) { free(out.verbs); free(out.pts); return st; }
+    /* compact the float stream: Move/Line keep 2 floats, Close none */
+    uint64_t nf = 0;
+    for (size_t i = 0; i < out.n; i++)
+        if (out.verbs[i] != OCHRE_ORACLE_CLOSE) {
+            out.pts[nf] = out.pts[2 * i];
+            out.pts[nf + 1] = out.pts[2 * i + 1];
+            nf += 2;
+        }
+    *out_verbs = out.verbs;
+    *out_pts = out.pts;
+    *out_n_cmds = out.n;
+    *out_n_floats = nf;
+    return 0;
+}
+
 static void run_raster(const ochre_oracle_batch *bt, const uint64_t *cmd_float_off, uint32_t ri,
                        int want_cov, int capture, raster_out *ro) {
     rasterizer r;
@@ -509,6 +721,29 @@ static void run_raster(const ochre_oracle_batch *bt, const uint64_t *cmd_float_o
     for (uint32_t f = f0; f < f1 && !r.error; f++) {
         const float *xf = bt->fill_xf + 6 * (size_t)f;
         int raw = bt->fill_flags ? (bt->fill_flags[f] & 1) : 0;
+        if (bt->fill_flags && (bt->fill_flags[f] & 2) && bt->fill_width) {
+            /* Rasterizer::stroke (rasterizer.rs:169-171): fill(stroke(flatten(path)), transform) */
+            const uint32_t c0 = bt->fill_cmd_off[f], c1 = bt->fill_cmd_off[f + 1];
+            uint8_t *sv;
+            float *sp;
+            uint64_t sn, snf;
+            int e = ochre_oracle_stroke(bt->verbs + c0, c1 - c0, bt->pts + cmd_float_off[c0], bt->fill_width[f],
+                                        &sv, &sn, &sp, &snf);
+            if (e) { r.error = e; break; }
+            uint64_t fo = 0;
+            for (uint64_t k = 0; k < sn && !r.error; k++) {
+                vec2 q[1] = {v2(0.0f, 0.0f)};
+                if (sv[k] != OCHRE_ORACLE_CLOSE) {
+                    q[0] = v2(sp[fo], sp[fo + 1]);
+                    fo += 2;
+                    if (!raw) q[0] = xf_apply(xf, q[0]);
+                }
+                command(&r, sv[k], q, 0.0f);
+            }
+            free(sv);
+            free(sp);
+            continue;
+        }
         for (uint32_t c = bt->fill_cmd_off[f]; c < bt->fill_cmd_off[f + 1] && !r.error; c++) {
             uint8_t verb = bt->verbs[c];
             const float *fp = bt->pts + cmd_float_off[c];

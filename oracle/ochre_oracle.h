@@ -47,6 +47,7 @@ typedef struct ochre_oracle_batch {
     uint32_t n_fills;
     const uint32_t *raster_fill_off; /* n_rasters + 1; NULL means one fill per raster */
     uint32_t n_rasters;
+    const float *fill_width;         /* n_fills, or NULL: stroke width of fills whose flags have bit1 */
 } ochre_oracle_batch;
 
 typedef struct ochre_oracle_result {
@@ -73,6 +74,14 @@ int ochre_oracle_run(const ochre_oracle_batch *batch, int threads, int flags, oc
 int ochre_oracle_cov64(const float *lines, const uint64_t *raster_line_off, uint32_t n_rasters,
                        const int32_t *rect, double *out);
 void ochre_oracle_free(ochre_oracle_result *r);
+
+/* Rasterizer::stroke's path preprocessing (path.rs:113-274): the path
+ * flattened at the reference tolerance in its own space, then offset by
+ * width / 2 on both sides with the reference's joins and caps.  Output:
+ * Move / Line / Close commands (2 floats for Move and Line); the caller
+ * frees *out_verbs and *out_pts with free(). */
+int ochre_oracle_stroke(const uint8_t *verbs, uint64_t n_cmds, const float *pts, float width,
+                        uint8_t **out_verbs, uint64_t *out_n_cmds, float **out_pts, uint64_t *out_n_floats);
 
 /* Differentiable model in double (see ochre_oracle.c): per-command line
  * counts of the f32 flattening, then loss and gradients for a w x h canvas

@@ -255,6 +255,89 @@ def rasterize(commands):
     return tiles, spans, len(incs)
 
 
+def path_polyline(verbs, flo):
+    """path.rs:113-142 (flatten) on raw float32 points: list of (verb, point)."""
+    from ochre_gb300.batch import FLOATS_PER_VERB
+    last = (ZERO, ZERO)
+    out = []
+    o = 0
+    for v in verbs:
+        v = int(v)
+        fl = [F(q) for q in flo[o:o + int(FLOATS_PER_VERB[v])]]
+        o += int(FLOATS_PER_VERB[v])
+        if v in (0, 1):
+            out.append((v, (fl[0], fl[1])))
+            last = (fl[0], fl[1])
+        elif v == 5:
+            out.append((5, None))
+        else:
+            npts = {2: 2, 3: 3, 4: 2}[v]
+            pts = [(fl[2 * k], fl[2 * k + 1]) for k in range(npts)]
+            for seg in lines_of_raster([(0, [last], ZERO), (v, pts, fl[4] if v == 4 else ZERO)]):
+                if seg[0] != "move":
+                    out.append((1, seg[1]))
+            # lines_of_raster closes the contour at its end; drop that closing line
+            if not (pts[-1][0] == last[0] and pts[-1][1] == last[1]):
+                out.pop()
+            last = pts[-1]
+    return out
+
+
+def stroke_polyline(poly, width):
+    """path.rs:150-274 restated: contours first, then both offset sides."""
+    width = F(width)
+    half = F(0.5) * width
+    contours = []          # (points, closed)
+    cur = []
+    closed = False
+    started = False
+    for v, p in poly + [(None, None)]:
+        if v == 5:
+            closed = True
+        if v in (None, 0, 5) and cur:
+            contours.append((cur, closed))
+        if v == 0:
+            cur = [p]
+        elif v == 1:
+            cur = cur + [p]
+        elif v == 5:
+            cur = []
+    out = []
+
+    def side(pts, closed, reverse):
+        seq = pts[::-1] if reverse else pts
+        first = pts[0] if closed == reverse else pts[-1]
+        res = []
+        prev, pn = first, (ZERO, ZERO)
+        for i in range(len(seq) + 1):
+            nxt = seq[i] if i < len(seq) else first
+            if i < len(seq) and nxt[0] == prev[0] and nxt[1] == prev[1]:
+                continue
+            tx, ty = nxt[0] - prev[0], nxt[1] - prev[1]
+            nn = (-ty, tx)
+            ln = np.sqrt(nn[0] * nn[0] + nn[1] * nn[1])
+            nn = (ZERO, ZERO) if ln == ZERO else (nn[0] * (ONE / ln), nn[1] * (ONE / ln))
+            off = ONE / (ONE + (pn[0] * nn[0] + pn[1] * nn[1]))
+            if abs(off) > F(2.0):
+                res.append((prev[0] + half * pn[0], prev[1] + half * pn[1]))
+                res.append((prev[0] + half * nn[0], prev[1] + half * nn[1]))
+            else:
+                k = half * off
+                res.append((prev[0] + k * (pn[0] + nn[0]), prev[1] + k * (pn[1] + nn[1])))
+            prev, pn = nxt, nn
+        return res
+
+    for pts, cl in contours:
+        fwd = side(pts, cl, False)
+        out += [(0 if j == 0 else 1, q) for j, q in enumerate(fwd)]
+        if cl:
+            out.append((5, None))
+        bwd = side(pts, cl, True)
+        out += [(0 if (j == 0 and cl) else 1, q) for j, q in enumerate(bwd)]
+        out.append((5, None))
+    return out
+
+
 def commands_of_batch(batch, raster):
     """Device-space command list of one raster of a Batch."""
     from ochre_gb300.batch import FLOATS_PER_VERB
@@ -264,6 +347,13 @@ def commands_of_batch(batch, raster):
     for f in range(int(roff[raster]), int(roff[raster + 1])):
         xf = [F(v) for v in batch.fill_xf[f]]
         raw = batch.fill_flags is not None and bool(batch.fill_flags[f] & 1)
+        if batch.fill_flags is not None and batch.fill_flags[f] & 2:
+            c0, c1 = int(batch.fill_cmd_off[f]), int(batch.fill_cmd_off[f + 1])
+            poly = path_polyline(batch.verbs[c0:c1], batch.pts[fpo[c0]:fpo[c1]])
+            for v, q in stroke_polyline(poly, batch.fill_width[f]):
+                pts = [] if q is None else [q if raw else apply(xf, q)]
+                out.append((v, pts, ZERO))
+            continue
         for c in range(int(batch.fill_cmd_off[f]), int(batch.fill_cmd_off[f + 1])):
             v = int(batch.verbs[c])
             fl = [F(q) for q in batch.pts[fpo[c]:fpo[c + 1]]]
