@@ -225,6 +225,16 @@ int ochre_gpu_rasterize_noalloc(const ochre_batch *in, ochre_output_buffers *out
 int ochre_gpu_set_tunable(ochre_gpu_ctx *ctx, const char *name, int value);
 int ochre_gpu_get_tunable(const ochre_gpu_ctx *ctx, const char *name, int *value);
 
+/* Headless compositing (the reference example's GL path, examples/svg.rs,
+ * restated): the rasters of a device result (ochre_gpu_rasterize_device),
+ * each coloured with colors[4r .. 4r+3] (RGBA8), drawn in raster order onto
+ * the RGBA8 canvas (w * h * 4 bytes, device, row-major, read and written):
+ * fragment = colour * (1, 1, 1, mask / 255), blended SRC_ALPHA,
+ * ONE_MINUS_SRC_ALPHA on all channels and quantised to 8 bits after every
+ * quad.  colors and canvas are 4-byte aligned device pointers. */
+int ochre_gpu_composite(ochre_gpu_ctx *ctx, const ochre_result *res, uint32_t n_rasters, const uint8_t *colors,
+                        uint32_t w, uint32_t h, uint8_t *canvas, void *stream);
+
 /* Status text for a code. */
 const char *ochre_gpu_status_string(int status);
 

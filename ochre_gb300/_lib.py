@@ -24,7 +24,7 @@ EXPORTS = [
     "ochre_rasterizer_command", "ochre_rasterizer_fill", "ochre_rasterizer_stroke", "ochre_rasterizer_finish",
     "ochre_rasterizer_free",
     "ochre_gpu_rasterize_noalloc", "ochre_gpu_set_tunable", "ochre_gpu_get_tunable",
-    "ochre_gpu_render_coverage", "ochre_gpu_l2_loss", "ochre_gpu_fill_backward",
+    "ochre_gpu_render_coverage", "ochre_gpu_l2_loss", "ochre_gpu_fill_backward", "ochre_gpu_composite",
 ]
 
 
@@ -128,6 +128,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_gpu_l2_loss.argtypes = [vp, vp, vp, ctypes.c_uint64, vp, vp, vp]
         L.ochre_gpu_fill_backward.argtypes = [vp, ctypes.POINTER(Batch), u32, u32, vp, vp, vp, vp]
         L.ochre_gpu_get_tunable.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+        L.ochre_gpu_composite.argtypes = [vp, ctypes.POINTER(Result), u32, vp, u32, u32, vp, vp]
         _lib = L
         return L
 

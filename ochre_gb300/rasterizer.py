@@ -454,6 +454,18 @@ class GpuContext:
                                                        stream), "fill_backward")
         return dl_dpts, dl_dxf
 
+    def composite(self, result: _lib.Result, n_rasters: int, colors, canvas, stream: Optional[int] = None):
+        """Draw the rasters of a device result (rasterize_device) onto an RGBA8
+        canvas (uint8 CUDA tensor [h, w, 4], updated in place) with one RGBA8
+        colour per raster (uint8 CUDA tensor [n_rasters, 4]), in raster order:
+        the reference example's tile/span quads, colour * mask, blended
+        SRC_ALPHA / ONE_MINUS_SRC_ALPHA, quantised after every quad."""
+        stream = self._torch_stream(stream)
+        h, w = int(canvas.shape[0]), int(canvas.shape[1])
+        _lib.check(_lib.load().ochre_gpu_composite(self.handle, ctypes.byref(result), n_rasters, colors.data_ptr(),
+                                                   w, h, canvas.data_ptr(), stream), "composite")
+        return canvas
+
     def stats(self) -> dict:
         s = _lib.Stats()
         _lib.check(_lib.load().ochre_gpu_last_stats(self.handle, ctypes.byref(s)))

@@ -95,6 +95,10 @@ def _load():
                                             ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64),
                                             ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)]
         lib.ochre_oracle_stroke.restype = ctypes.c_int
+        lib.ochre_oracle_composite.argtypes = [ctypes.c_uint32] + [ctypes.c_void_p] * 7 + [ctypes.c_uint32,
+                                                                                           ctypes.c_uint32,
+                                                                                           ctypes.c_void_p]
+        lib.ochre_oracle_composite.restype = None
         lib.free.argtypes = [ctypes.c_void_p]
         lib.free.restype = None
         _lib = lib
@@ -239,6 +243,20 @@ def stroke(verbs, pts, width: float):
         lib.free(ov)
         lib.free(op)
     return out_v, out_p
+
+
+def composite(result: dict, n_rasters: int, colors, w: int, h: int, canvas=None) -> np.ndarray:
+    """Headless compositing of a result (dict of run()'s layout) with one
+    RGBA8 colour per raster onto an RGBA8 [h, w, 4] canvas (white if None)."""
+    lib = _load()
+    cv = np.full((h, w, 4), 255, np.uint8) if canvas is None else np.ascontiguousarray(canvas, np.uint8).copy()
+    arr = lambda k, dt: np.ascontiguousarray(result[k], dt)
+    keep = [arr("tile_xy", np.int16), arr("tile_alpha", np.uint8), arr("raster_tile_off", np.uint64),
+            arr("span_xy", np.int16), arr("span_w", np.uint16), arr("raster_span_off", np.uint64),
+            np.ascontiguousarray(colors, np.uint8).reshape(-1)]
+    ptr = lambda a: a.ctypes.data if a.size else None
+    lib.ochre_oracle_composite(n_rasters, *[ptr(a) for a in keep], w, h, cv.ctypes.data)
+    return cv
 
 
 def seg_counts(batch) -> np.ndarray:

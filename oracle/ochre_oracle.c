@@ -1487,3 +1487,59 @@ int ochre_oracle_backward64(const ochre_oracle_batch *bt, const uint32_t *counts
     double loss;
     return diff64_impl(bt, counts, W, H, NULL, dl_ds, &loss, dpts, dxf);
 }
+
+/* ------------------------------------------------------------------ */
+/* Headless compositing (examples/svg.rs restated without GL)          */
+/* ------------------------------------------------------------------ */
+/* Every tile is an 8x8 quad textured with its alpha mask, every span an
+ * n x 8 quad with mask 1 (the atlas texel at (0,0) is 255,
+ * examples/svg.rs:33-38, 85-87), coloured with its raster's RGBA8 colour;
+ * the fragment is colour * (1, 1, 1, mask) (:341-353) and blends with
+ * SRC_ALPHA, ONE_MINUS_SRC_ALPHA on all four channels (:173-174) into an
+ * RGBA8 target, quantised after every quad (f -> floor(f * 255 + 0.5)).
+ * Rasters are drawn in order (:139-165); within a raster nothing overlaps. */
+static uint8_t unorm8(float f) {
+    float q = floorf(f * 255.0f + 0.5f);
+    if (!(q >= 0.0f)) q = 0.0f;
+    if (q > 255.0f) q = 255.0f;
+    return (uint8_t)q;
+}
+
+static void blend_px(uint8_t *dst, const uint8_t *col, uint8_t mask) {
+    const float a = ((float)col[3] / 255.0f) * ((float)mask / 255.0f);
+    const float ia = 1.0f - a;
+    for (int c = 0; c < 3; c++) {
+        const float s = (float)col[c] / 255.0f;
+        const float d = (float)dst[c] / 255.0f;
+        dst[c] = unorm8(s * a + d * ia);
+    }
+    const float d = (float)dst[3] / 255.0f;
+    dst[3] = unorm8(a * a + d * ia);
+}
+
+void ochre_oracle_composite(uint32_t n_rasters, const int16_t *tile_xy, const uint8_t *tile_alpha,
+                            const uint64_t *raster_tile_off, const int16_t *span_xy, const uint16_t *span_w,
+                            const uint64_t *raster_span_off, const uint8_t *colors, uint32_t w, uint32_t h,
+                            uint8_t *canvas) {
+    for (uint32_t r = 0; r < n_rasters; r++) {
+        const uint8_t *col = colors + 4 * (size_t)r;
+        for (uint64_t t = raster_tile_off[r]; t < raster_tile_off[r + 1]; t++) {
+            const int x0 = tile_xy[2 * t], y0 = tile_xy[2 * t + 1];
+            for (int py = 0; py < 8; py++)
+                for (int px = 0; px < 8; px++) {
+                    const int x = x0 + px, y = y0 + py;
+                    if (x < 0 || y < 0 || x >= (int)w || y >= (int)h) continue;
+                    blend_px(canvas + 4 * ((size_t)y * w + x), col, tile_alpha[64 * t + 8 * py + px]);
+                }
+        }
+        for (uint64_t s = raster_span_off[r]; s < raster_span_off[r + 1]; s++) {
+            const int x0 = span_xy[2 * s], y0 = span_xy[2 * s + 1];
+            for (int py = 0; py < 8; py++)
+                for (int px = 0; px < (int)span_w[s]; px++) {
+                    const int x = x0 + px, y = y0 + py;
+                    if (x < 0 || y < 0 || x >= (int)w || y >= (int)h) continue;
+                    blend_px(canvas + 4 * ((size_t)y * w + x), col, 255);
+                }
+        }
+    }
+}

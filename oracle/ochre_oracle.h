@@ -83,6 +83,13 @@ void ochre_oracle_free(ochre_oracle_result *r);
 int ochre_oracle_stroke(const uint8_t *verbs, uint64_t n_cmds, const float *pts, float width,
                         uint8_t **out_verbs, uint64_t *out_n_cmds, float **out_pts, uint64_t *out_n_floats);
 
+/* Headless compositing of results (see ochre_oracle.c): rasters drawn in
+ * order with their RGBA8 colours onto an RGBA8 w x h canvas (in place). */
+void ochre_oracle_composite(uint32_t n_rasters, const int16_t *tile_xy, const uint8_t *tile_alpha,
+                            const uint64_t *raster_tile_off, const int16_t *span_xy, const uint16_t *span_w,
+                            const uint64_t *raster_span_off, const uint8_t *colors, uint32_t w, uint32_t h,
+                            uint8_t *canvas);
+
 /* Differentiable model in double (see ochre_oracle.c): per-command line
  * counts of the f32 flattening, then loss and gradients for a w x h canvas
  * per raster against `target` (n_rasters * w * h).  dpts / dxf may be NULL. */
