@@ -4,11 +4,14 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <vector>
 
 #include "common.cuh"
+#include "flatten.cuh"
+#include "scan.cuh"
 #include "internal.h"
 
 namespace ochre {
@@ -62,17 +65,51 @@ cudaError_t HostBuf::ensure(size_t bytes) {
     if (e != cudaSuccess) return e;
     if (p) cudaFreeHost(p);
     p = q;
+    dev = nullptr;
+    cap = want;
+    return cudaSuccess;
+}
+cudaError_t HostBuf::ensure_mapped(size_t bytes) {
+    if (bytes <= cap && p != nullptr && dev != nullptr) return cudaSuccess;
+    if (bytes == 0) bytes = 16;
+    size_t want = cap ? cap : 256;
+    while (want < bytes) want *= 2;
+    void* q = nullptr;
+    void* d = nullptr;
+    cudaError_t e = cudaHostAlloc(&q, want, cudaHostAllocMapped);
+    if (e != cudaSuccess) return e;
+    e = cudaHostGetDevicePointer(&d, q, 0);
+    if (e != cudaSuccess) {
+        cudaFreeHost(q);
+        return e;
+    }
+    if (p) cudaFreeHost(p);
+    p = q;
+    dev = d;
     cap = want;
     return cudaSuccess;
 }
 void HostBuf::release() {
     if (p) cudaFreeHost(p);
     p = nullptr;
+    dev = nullptr;
     cap = 0;
 }
 
+__global__ void k_copy_words(const uint32_t* __restrict__ src, uint32_t n, uint32_t* dst) {
+    const uint32_t i = threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
 int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
-    OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_scalars.p, ctx->scalars.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    if (ctx->h_scalars_dev) {
+        k_copy_words<<<1, 64, 0, s>>>(ctx->scalars.as<uint32_t>(), (uint32_t)(sizeof(DevScalars) / 4),
+                                       static_cast<uint32_t*>(ctx->h_scalars_dev));
+        OCHRE_CUDA_TRY(cudaGetLastError());
+    } else {
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_scalars.p, ctx->scalars.p, sizeof(DevScalars), cudaMemcpyDeviceToHost,
+                                       s));
+    }
     OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
     return OCHRE_OK;
 }
@@ -244,10 +281,28 @@ int ochre_gpu_create(ochre_gpu_ctx** out, int device, uint32_t flags) {
     ctx->flags = flags;
     if (cudaSetDevice(device) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        ctx->scalars.ensure(sizeof(DevScalars)) != cudaSuccess ||
-        ctx->h_scalars.ensure(sizeof(DevScalars)) != cudaSuccess) {
+        ctx->scalars.ensure(sizeof(DevScalars)) != cudaSuccess) {
         ochre_gpu_destroy(ctx);
         return OCHRE_E_CUDA;
+    }
+    // scalars read back through mapped pinned host memory
+    {
+        void* hp = nullptr;
+        void* dp = nullptr;
+        if (cudaHostAlloc(&hp, sizeof(DevScalars), cudaHostAllocMapped) == cudaSuccess &&
+            cudaHostGetDevicePointer(&dp, hp, 0) == cudaSuccess) {
+            std::memset(hp, 0, sizeof(DevScalars));
+            ctx->h_scalars.p = hp;
+            ctx->h_scalars.cap = sizeof(DevScalars);
+            ctx->h_scalars_dev = dp;
+        } else {
+            cudaGetLastError();
+            if (hp) cudaFreeHost(hp);
+            if (ctx->h_scalars.ensure(sizeof(DevScalars)) != cudaSuccess) {
+                ochre_gpu_destroy(ctx);
+                return OCHRE_E_CUDA;
+            }
+        }
     }
     *out = ctx;
     return OCHRE_OK;
@@ -341,18 +396,65 @@ int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result*
                                        cudaMemcpyHostToDevice, s));
         d.raster_fill_off = ctx->in_raster_off.as<uint32_t>();
     }
+    // Outputs: when the previous call sized them, the kernels write straight
+    // into mapped pinned host memory (no device->host copy after the run);
+    // otherwise, or when this batch outgrows them, into device memory, then
+    // copied, and the host buffers are resized for the next call.
+    const size_t R = in->n_rasters;
+    const bool want_cov = (ctx->flags & OCHRE_CTX_WANT_COV) != 0;
+    HostBuf* hb[] = {&ctx->h_tile_xy, &ctx->h_tile_alpha, &ctx->h_span_xy, &ctx->h_span_w, &ctx->h_span_tile,
+                     &ctx->h_raster_tile_off, &ctx->h_raster_span_off, &ctx->h_tile_cov};
+    DevBuf* ob[] = {&ctx->out_tile_xy, &ctx->out_tile_alpha, &ctx->out_span_xy, &ctx->out_span_w, &ctx->out_span_tile,
+                    &ctx->out_raster_tile_off, &ctx->out_raster_span_off, &ctx->out_tile_cov};
+    const int nb = want_cov ? 8 : 7;
+    bool zero_copy = ctx->h_raster_tile_off.dev != nullptr && ctx->h_raster_tile_off.cap >= (R + 1) * 4 &&
+                     ctx->h_raster_span_off.cap >= (R + 1) * 4;
+    for (int i = 0; i < nb && zero_copy; i++) zero_copy = hb[i]->dev != nullptr;
     ochre_result dr;
+    if (zero_copy) {
+        Arena flag;   // records an overflow of the fixed outputs
+        DevBuf saved[8];
+        for (int i = 0; i < nb; i++) {
+            saved[i] = *ob[i];
+            DevBuf v;
+            v.p = hb[i]->dev;
+            v.cap = hb[i]->cap;
+            v.fixed = true;
+            v.arena = &flag;
+            *ob[i] = v;
+        }
+        st = run_device(ctx, &d, &dr, s);
+        for (int i = 0; i < nb; i++) *ob[i] = saved[i];
+        if (st == OCHRE_OK) {
+            OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
+            out->n_tiles = dr.n_tiles;
+            out->n_spans = dr.n_spans;
+            out->tile_xy = ctx->h_tile_xy.as<int16_t>();
+            out->tile_alpha = ctx->h_tile_alpha.as<uint8_t>();
+            out->tile_cov = (dr.tile_cov && dr.n_tiles) ? ctx->h_tile_cov.as<float>() : nullptr;
+            out->span_xy = ctx->h_span_xy.as<int16_t>();
+            out->span_width = ctx->h_span_w.as<uint16_t>();
+            out->span_tile = ctx->h_span_tile.as<uint32_t>();
+            out->raster_tile_off = ctx->h_raster_tile_off.as<uint32_t>();
+            out->raster_span_off = ctx->h_raster_span_off.as<uint32_t>();
+            return OCHRE_OK;
+        }
+        if (!flag.overflow && st != OCHRE_E_CAPACITY) return st;   // a real error, not a capacity one
+    }
     st = run_device(ctx, &d, &dr, s);
     if (st != OCHRE_OK) return st;
-    // device -> pinned host
-    const size_t T = dr.n_tiles, N = dr.n_spans, R = in->n_rasters;
-    OCHRE_CUDA_TRY(ctx->h_tile_xy.ensure(T * 4));
-    OCHRE_CUDA_TRY(ctx->h_tile_alpha.ensure(T * 64));
-    OCHRE_CUDA_TRY(ctx->h_span_xy.ensure(N * 4));
-    OCHRE_CUDA_TRY(ctx->h_span_w.ensure(N * 2));
-    OCHRE_CUDA_TRY(ctx->h_span_tile.ensure(N * 4));
-    OCHRE_CUDA_TRY(ctx->h_raster_tile_off.ensure((R + 1) * 4));
-    OCHRE_CUDA_TRY(ctx->h_raster_span_off.ensure((R + 1) * 4));
+    // device -> pinned host, and host buffers mapped and sized (x1.25) for the next call
+    const size_t T = dr.n_tiles, N = dr.n_spans;
+    // spans: the general chain reserves one span slot per tile
+    const size_t Tc = T + T / 4 + 64, Nc = Tc;
+    OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
+    OCHRE_CUDA_TRY(ctx->h_tile_xy.ensure_mapped(Tc * 4));
+    OCHRE_CUDA_TRY(ctx->h_tile_alpha.ensure_mapped(Tc * 64));
+    OCHRE_CUDA_TRY(ctx->h_span_xy.ensure_mapped(Nc * 4));
+    OCHRE_CUDA_TRY(ctx->h_span_w.ensure_mapped(Nc * 2));
+    OCHRE_CUDA_TRY(ctx->h_span_tile.ensure_mapped(Nc * 4));
+    OCHRE_CUDA_TRY(ctx->h_raster_tile_off.ensure_mapped((R + 1) * 4));
+    OCHRE_CUDA_TRY(ctx->h_raster_span_off.ensure_mapped((R + 1) * 4));
     if (T) {
         OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_tile_xy.p, dr.tile_xy, T * 4, cudaMemcpyDeviceToHost, s));
         OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_tile_alpha.p, dr.tile_alpha, T * 64, cudaMemcpyDeviceToHost, s));
@@ -364,10 +466,9 @@ int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result*
     }
     OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_raster_tile_off.p, dr.raster_tile_off, (R + 1) * 4, cudaMemcpyDeviceToHost, s));
     OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_raster_span_off.p, dr.raster_span_off, (R + 1) * 4, cudaMemcpyDeviceToHost, s));
-    if (dr.tile_cov && T) {
-        OCHRE_CUDA_TRY(ctx->h_tile_cov.ensure(T * 256));
+    if (want_cov) OCHRE_CUDA_TRY(ctx->h_tile_cov.ensure_mapped(Tc * 256));
+    if (dr.tile_cov && T)
         OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_tile_cov.p, dr.tile_cov, T * 256, cudaMemcpyDeviceToHost, s));
-    }
     OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
     out->n_tiles = dr.n_tiles;
     out->n_spans = dr.n_spans;

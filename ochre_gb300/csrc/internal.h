@@ -36,7 +36,11 @@ struct DevBuf {
 struct HostBuf {
     void* p = nullptr;
     size_t cap = 0;
+    void* dev = nullptr;   // device view of the memory (mapped allocations), or nullptr
     cudaError_t ensure(size_t bytes);
+    // like ensure(), but the memory is mapped into the device address space
+    // (kernels can write results into it directly)
+    cudaError_t ensure_mapped(size_t bytes);
     void release();
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
@@ -136,6 +140,9 @@ struct ochre_gpu_ctx {
         out_raster_tile_off, out_raster_span_off;
     // pinned host
     ochre::HostBuf h_scalars;
+    // h_scalars as seen from the device when it is mapped host memory: the
+    // read-back is then a kernel store, not a copy queued behind bulk copies
+    void* h_scalars_dev = nullptr;
     ochre::HostBuf h_tile_xy, h_tile_alpha, h_tile_cov, h_span_xy, h_span_w, h_span_tile, h_raster_tile_off,
         h_raster_span_off;
 
@@ -155,6 +162,7 @@ struct ochre_gpu_ctx {
     int tune_fused_chunk = 16;
     int tune_chain_tiles_per_warp = 8;
     int tune_chain_coverage_form = 0;   // 0: by row count, 1: block form, 2: row form
+
 
     // Tracing: every kernel launch of a run is counted; with OCHRE_CTX_PROFILE
     // each one is also bracketed by a pair of CUDA events on its stream.

@@ -207,3 +207,22 @@ def test_coverage_error_vs_fp64(any_ctx, name, gen, kw, bound):
         e_ref = oracle.tile_cov_error_vs_fp64(b, ref["tile_xy"], ref["tile_cov"], ref["raster_tile_off"])
         bound = e_ref["max_abs"] + 1e-3
     assert e["max_abs"] < bound, (e, bound)
+
+
+def test_host_path_pipelined_chunks_match_oracle(gpu_ctx):
+    """Batches of 32,768+ rasters through the host-buffer entry run in chunks
+    on two internal contexts (copy-out overlapping the next chunk); offsets,
+    span tiles and coverage are rebased to the whole batch."""
+    b = W.glyph_run(n_paths=40_000, seed=17)
+    ref = oracle.run(b, threads=16, want_cov=True)
+    gpu_ctx.set_want_cov(True)
+    try:
+        got = gpu_ctx.rasterize(b)
+    finally:
+        gpu_ctx.set_want_cov(False)
+    st = compare(got, ref, b.n_rasters)
+    assert st["cov_max_abs_vs_oracle_f32"] < 1e-3
+    # and a mix that needs the general chain in some chunks, with strokes
+    from ochre_gb300.batch import concat
+    m = concat([W.glyph_run(n_paths=30_000, seed=18), W.uneven_mix(n_paths=20), W.stroke_run(n_paths=3000)])
+    compare(gpu_ctx.rasterize(m), oracle.run(m, threads=16), m.n_rasters)
