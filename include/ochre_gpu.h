@@ -216,8 +216,9 @@ int ochre_gpu_rasterize_noalloc(const ochre_batch *in, ochre_output_buffers *out
 
 /* Launch-shape tunables, chosen per GPU by the project's autotuner
  * (ochre_gb300/autotune.py) and applied per context:
- *   "fused_threads"          threads per raster in the fused kernel: 64 | 128
- *   "fused_chunk"            tiles accumulated per pass in the fused kernel: 16 | 32
+ *   "fused_threads"          threads per raster in the fused kernel: 64 | 96 | 128
+ *   "fused_chunk"            tiles accumulated per pass in the fused kernel: 8 | 16 | 32
+ *                            (shapes built: 64x8, 64x16, 64x32, 96x8, 96x16, 128x16, 128x32)
  *   "chain_tiles_per_warp"   tiles per warp in the chain's coverage kernel: 4 | 8 | 16
  *   "chain_coverage_form"    coverage kernel form: 0 by tile-row count (default), 1 one warp
  *                            per block of tiles with a look-back carry, 2 one warp per tile row

@@ -17,7 +17,7 @@ from typing import Optional
 
 from . import _lib, build
 
-FUSED_SHAPES = [(64, 16), (64, 32), (128, 16), (128, 32)]
+FUSED_SHAPES = [(64, 8), (64, 16), (64, 32), (96, 8), (96, 16), (128, 16), (128, 32)]
 CHAIN_TILES_PER_WARP = [4, 8, 16]
 CACHE = os.path.join(build.BUILD, "tune.json")
 

@@ -494,10 +494,10 @@ int ochre_gpu_last_timings(const ochre_gpu_ctx* ctx, ochre_kernel_time* out, uin
 int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     if (!ctx || !name) return OCHRE_E_INVALID;
     if (!std::strcmp(name, "fused_threads")) {
-        if (value != 64 && value != 128) return OCHRE_E_INVALID;
+        if (value != 64 && value != 96 && value != 128) return OCHRE_E_INVALID;
         ctx->tune_fused_threads = value;
     } else if (!std::strcmp(name, "fused_chunk")) {
-        if (value != 16 && value != 32) return OCHRE_E_INVALID;
+        if (value != 8 && value != 16 && value != 32) return OCHRE_E_INVALID;
         ctx->tune_fused_chunk = value;
     } else if (!std::strcmp(name, "chain_tiles_per_warp")) {
         if (value != 4 && value != 8 && value != 16) return OCHRE_E_INVALID;

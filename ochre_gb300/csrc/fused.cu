@@ -734,7 +734,10 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         a.raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
         int st0 = OCHRE_OK;
         switch (ctx->tune_fused_threads * 1000 + ctx->tune_fused_chunk) {
+        case 64008: st0 = launch_fused<64, 8>(ctx, a, s); break;
         case 64016: st0 = launch_fused<64, 16>(ctx, a, s); break;
+        case 96008: st0 = launch_fused<96, 8>(ctx, a, s); break;
+        case 96016: st0 = launch_fused<96, 16>(ctx, a, s); break;
         case 64032: st0 = launch_fused<64, 32>(ctx, a, s); break;
         case 128016: st0 = launch_fused<128, 16>(ctx, a, s); break;
         case 128032: st0 = launch_fused<128, 32>(ctx, a, s); break;

@@ -226,3 +226,17 @@ def test_host_path_pipelined_chunks_match_oracle(gpu_ctx):
     from ochre_gb300.batch import concat
     m = concat([W.glyph_run(n_paths=30_000, seed=18), W.uneven_mix(n_paths=20), W.stroke_run(n_paths=3000)])
     compare(gpu_ctx.rasterize(m), oracle.run(m, threads=16), m.n_rasters)
+
+
+@pytest.mark.parametrize("shape", __import__("ochre_gb300.autotune", fromlist=["FUSED_SHAPES"]).FUSED_SHAPES)
+def test_every_fused_shape_matches_oracle(shape):
+    """Every launch shape the autotuner may pick gives the same results."""
+    from ochre_gb300 import GpuContext, autotune
+    b = W.glyph_run(n_paths=3000, seed=23)
+    ref = oracle.run(b, threads=16)
+    ctx = GpuContext(0)
+    autotune.apply(ctx, {"fused_threads": shape[0], "fused_chunk": shape[1]})
+    got = ctx.rasterize(b)
+    assert ctx.stats()["fused"] == 1
+    compare(got, ref, b.n_rasters)
+    ctx.close()
