@@ -175,17 +175,22 @@ def dist_setup():
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:   # host-only ranks (the reference arm, tests)
+            dist.init_process_group("gloo")
     return ws, rank, local
 
 
 def reduce_max(x: float, ws: int) -> float:
+    """Max over ranks (the timing rule: the slowest rank's time)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
