@@ -41,28 +41,11 @@ def readme_path() -> Batch:
     return bb.build()
 
 
-def _assemble(verbs_per_contour, floats_per_contour, contour_fill, n_fills, xf, raster_fill_off, n_rasters):
-    """Concatenate per-contour verb/float arrays (already in order)."""
-    verbs = np.concatenate(verbs_per_contour) if verbs_per_contour else np.zeros(0, np.uint8)
-    pts = np.concatenate(floats_per_contour) if floats_per_contour else np.zeros(0, np.float32)
-    ncmd = np.array([len(v) for v in verbs_per_contour], dtype=np.int64)
-    fill_ncmd = np.bincount(contour_fill, weights=ncmd, minlength=n_fills).astype(np.int64)
-    off = np.zeros(n_fills + 1, np.uint32)
-    off[1:] = np.cumsum(fill_ncmd)
-    b = Batch(verbs.astype(np.uint8), pts.astype(np.float32), off, xf.astype(np.float32), None,
-              raster_fill_off, n_rasters)
-    b.validate()
-    return b
-
-
-def _contour_stream(n_seg: np.ndarray, kind: np.ndarray, pts: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
-    """Vectorised verb/float streams for closed contours.
-
-    ``n_seg[c]`` segments per contour, ``kind`` per segment (QUADRATIC or
-    CUBIC), ``pts`` per segment = 6 floats (quadratics use the first 4).
-    Each contour is Move(start), segments, Close; returns (verbs, floats)
-    concatenated, plus the per-contour command counts.
-    """
+def _contour_stream(n_seg: np.ndarray, kind: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Verb stream of closed contours: ``n_seg[c]`` segments per contour,
+    ``kind`` per segment (QUADRATIC or CUBIC); each contour is Move(start),
+    segments, Close.  Returns the verbs and the command index of every
+    segment."""
     n_c = len(n_seg)
     seg_start = np.concatenate([[0], np.cumsum(n_seg)[:-1]]).astype(np.int64)
     ncmd_c = n_seg + 2
@@ -80,7 +63,7 @@ def _contour_stream(n_seg: np.ndarray, kind: np.ndarray, pts: np.ndarray) -> tup
 
 def _streams(n_seg, kind, start_xy, seg_floats):
     """Build verbs and the float stream for contours (start point + segments)."""
-    verbs, seg_cmd = _contour_stream(n_seg, kind, seg_floats)
+    verbs, seg_cmd = _contour_stream(n_seg, kind)
     nf = FLOATS_PER_VERB[verbs]
     foff = np.concatenate([[0], np.cumsum(nf)]).astype(np.int64)
     pts = np.zeros(int(foff[-1]), np.float32)
