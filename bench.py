@@ -161,11 +161,43 @@ def cpu_baseline(batch, reps: int = 3) -> dict:
         oracle.run(batch, threads=threads)  # warm
         t0 = time.perf_counter()
         for _ in range(reps):
-            oracle.run(batch, threads=threads)
+            r = oracle.run(batch, threads=threads)
         dt = (time.perf_counter() - t0) / reps
+    n_tiles = int(len(r["tile_xy"]))
+    # one core, on the first 10,000 paths (a few seconds)
+    from ochre_gb300.batch import subset
+    n1 = min(batch.n_rasters, 10000)
+    one = subset(batch, range(n1))
+    with np.errstate(all="ignore"):
+        t0 = time.perf_counter()
+        r1 = oracle.run(one, threads=1)
+        dt1 = time.perf_counter() - t0
     return {"value": batch.n_rasters / dt, "unit": "paths/s", "cores": threads, "kind": "port",
+            "tiles_per_s": n_tiles / dt, "cpu_model": _cpu_model(),
             "sample": f"the full workload ({batch.n_rasters} paths) x {reps} repetitions, "
-                      f"oracle/ochre_oracle.c on {threads} threads"}
+                      f"oracle/ochre_oracle.c on {threads} threads",
+            "one_core": {"value": n1 / dt1, "unit": "paths/s", "tiles_per_s": len(r1["tile_xy"]) / dt1,
+                         "sample": f"the first {n1} paths of the workload, one thread"}}
+
+
+def _cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 def dist_setup():

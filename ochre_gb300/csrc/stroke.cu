@@ -11,8 +11,8 @@
 //   1. command scan of the input (float offsets, most recent endpoint);
 //   2. polyline sizes per command (path-space flatten counts), scan, emit;
 //   3. units: one per stroked contour, one per copied command; compaction;
-//   4. output sizes per unit (the offset sides counted join by join), scan,
-//      emit; fill offsets of the output.
+//   4. output sizes per unit (the offset sides counted join by join, one
+//      thread per unit), scan in place, emit; fill offsets of the output.
 // A contour is walked by one thread (its joins depend on the previous
 // distinct point).  Contours start at a Move or after a Close; `closed` is
 // set by a Close ending the contour or by any earlier Close of the path
@@ -86,6 +86,24 @@ struct PairOut {
         foff[i] = ex.nf;
     }
 };
+// Counts already stored in the two offset arrays (scanned in place).
+struct PairIn {
+    const uint32_t* n;
+    const uint32_t* nf;
+    __device__ __forceinline__ Pair operator()(uint64_t i) const { return Pair{n[i], nf[i]}; }
+};
+
+// One thread per item: a count functor with a long serial walk per item runs
+// at full occupancy here, and the scan over the stored counts stays light.
+template <class Count>
+__global__ void __launch_bounds__(128) k_pair_count(uint64_t n, Count count, uint32_t* __restrict__ out_n,
+                                                    uint32_t* __restrict__ out_nf) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Pair p = count(i);
+    out_n[i] = p.n;
+    out_nf[i] = p.nf;
+}
 
 __global__ void k_poly_emit(const uint8_t* __restrict__ verbs, const float* __restrict__ pts,
                             const uint32_t* __restrict__ fill_off, uint32_t n_fills, const uint8_t* __restrict__ flags,
@@ -377,9 +395,13 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     OCHRE_CUDA_TRY(ctx->sk_poly_off.ensure((n + 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_poly_foff.ensure((n + 1) * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n) * sizeof(ScanStatus<Pair>)));
-    OCHRE_LAUNCH(ctx, "stroke_poly_scan", s, OCHRE_CUDA_TRY(launch_scan<Pair>(
+    OCHRE_LAUNCH(ctx, "stroke_poly_count", s, k_pair_count<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
         n, PolyCount{in->verbs, in->pts, in->fill_cmd_off, F, in->fill_flags, ctx->sk_cmd_foff.as<uint32_t>(),
                      ctx->sk_cmd_ep.as<uint32_t>(), &ds->err},
+        ctx->sk_poly_off.as<uint32_t>(), ctx->sk_poly_foff.as<uint32_t>()));
+    OCHRE_CUDA_TRY(cudaGetLastError());
+    OCHRE_LAUNCH(ctx, "stroke_poly_scan", s, OCHRE_CUDA_TRY(launch_scan<Pair>(
+        n, PairIn{ctx->sk_poly_off.as<uint32_t>(), ctx->sk_poly_foff.as<uint32_t>()},
         PairOut{ctx->sk_poly_off.as<uint32_t>(), ctx->sk_poly_foff.as<uint32_t>()}, OpPair{}, Pair{0u, 0u},
         ctx->scan_status.p, &ds->ticket, reinterpret_cast<Pair*>(&ds->n_lines), &ds->err, s)));
     // (n_lines, n_line_ent) hold the polyline totals here; the fill chain resets them
@@ -435,10 +457,14 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     OCHRE_CUDA_TRY(ctx->sk_unit_fill.ensure(((size_t)U + 1) * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(U ? U : 1) * sizeof(ScanStatus<Pair>)));
     if (U) {
-        OCHRE_LAUNCH(ctx, "stroke_out_scan", s, OCHRE_CUDA_TRY(launch_scan<Pair>(
+        OCHRE_LAUNCH(ctx, "stroke_out_count", s, k_pair_count<<<(U + 127) / 128, 128, 0, s>>>(
             U, OutCount{ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
                         ctx->sk_pfoff.as<uint32_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
                         ctx->sk_first_close.as<uint32_t>(), in->fill_width},
+            ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()));
+        OCHRE_CUDA_TRY(cudaGetLastError());
+        OCHRE_LAUNCH(ctx, "stroke_out_scan", s, OCHRE_CUDA_TRY(launch_scan<Pair>(
+            U, PairIn{ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()},
             PairOut{ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()}, OpPair{}, Pair{0u, 0u},
             ctx->scan_status.p, &ds->ticket, reinterpret_cast<Pair*>(&ds->n_lines), &ds->err, s)));
     } else {
