@@ -152,6 +152,35 @@ int ochre_gpu_last_stats(const ochre_gpu_ctx *ctx, ochre_stats *out);
  * up to `cap` entries and the total count to *n. */
 int ochre_gpu_last_timings(const ochre_gpu_ctx *ctx, ochre_kernel_time *out, uint32_t cap, uint32_t *n);
 
+/* ---- CUDA-graph execution -------------------------------------------------
+ * The whole fill -> finish launch chain of ochre_gpu_rasterize_device,
+ * captured once into a CUDA graph and replayed by one graph launch per call
+ * (no host read-backs between stages, one synchronisation per call).  For
+ * batches rasterized over and over with the same structure: animation
+ * frames (new transforms), optimisation loops (new points).  No counterpart
+ * in the reference, which rasterizes one path per call on the CPU.
+ *   - `in` holds device pointers; they and every count in `in` are fixed for
+ *     the graph's life.  The values behind them may change between launches
+ *     (points, transforms, verbs of the same float layout).  Stroked fills
+ *     (fill_width) are not supported (OCHRE_E_INVALID).
+ *   - Creation runs the batch once eagerly and plans every internal buffer at
+ *     `headroom` (1 to 16) times its count.  A launch whose counts outgrow the
+ *     plan (or, for a batch planned on the fused kernel, a raster that no
+ *     longer fits it) re-plans from an eager run and replays once.
+ *   - The graph owns its buffers (a private context created on ctx's device
+ *     with ctx's flags and tunables).  Results of a launch are device
+ *     pointers into them, valid until the next launch or destroy.
+ *   - `stream` is a cudaStream_t, or NULL for the graph's own stream; the
+ *     launch returns when the replay has finished. */
+typedef struct ochre_graph ochre_graph;
+int ochre_graph_create(ochre_gpu_ctx *ctx, const ochre_batch *in, float headroom, ochre_graph **out);
+int ochre_graph_launch(ochre_graph *g, ochre_result *out, void *stream);
+/* Counts of the last launch (n_launches = kernels in the graph). */
+int ochre_graph_last_stats(const ochre_graph *g, ochre_stats *out);
+/* Kernels captured, re-plans so far, and 1 when the plan is the fused kernel. */
+int ochre_graph_info(const ochre_graph *g, uint32_t *kernels, uint32_t *replans, uint32_t *fused);
+void ochre_graph_destroy(ochre_graph *g);
+
 /* ---- Differentiable fill -------------------------------------------------
  * Extends the reference's forward model (rasterizer.rs:180-268) with dense
  * coverage images and a hand-written backward pass.  Raster r renders into a

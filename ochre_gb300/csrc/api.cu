@@ -12,12 +12,17 @@
 #include "common.cuh"
 #include "flatten.cuh"
 #include "scan.cuh"
+#include <atomic>
+
 #include "internal.h"
 
 namespace ochre {
 
+std::atomic<uint64_t> g_dev_allocs{0};
+
 cudaError_t DevBuf::ensure(size_t bytes) {
     if (bytes <= cap && p != nullptr) return cudaSuccess;
+    g_dev_allocs.fetch_add(1, std::memory_order_relaxed);
     if (fixed) {
         if (arena != nullptr) arena->overflow = true;
         return cudaErrorMemoryAllocation;
@@ -101,7 +106,38 @@ __global__ void k_copy_words(const uint32_t* __restrict__ src, uint32_t n, uint3
     if (i < n) dst[i] = src[i];
 }
 
-int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
+__global__ void k_plan_cap(uint32_t* count, uint32_t cap, uint32_t* err) {
+    if (*count > cap) {
+        *count = 0u;
+        atomicOr(err, ERR_CAPACITY);
+    }
+}
+
+__global__ void k_plan_entries(DevScalars* ds, uint32_t cap, uint32_t key_bits) {
+    const uint64_t e = (uint64_t)ds->n_line_ent + ds->n_empty;
+    const uint64_t k = ds->keyspace;
+    const bool keys_fit = key_bits >= 64 || k == 0 || ((k - 1) >> key_bits) == 0;
+    if (e > cap || !keys_fit) {
+        ds->n_entries = 0u;
+        ds->n_lines = 0u;   // no line emits an entry
+        atomicOr(&ds->err, ERR_CAPACITY);
+    } else {
+        ds->n_entries = (uint32_t)e;
+    }
+}
+
+cudaError_t launch_plan_cap(ochre_gpu_ctx* ctx, uint32_t* count, uint32_t cap, cudaStream_t s) {
+    k_plan_cap<<<1, 1, 0, s>>>(count, cap, &dev_scalars(ctx)->err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_bits, cudaStream_t s) {
+    k_plan_entries<<<1, 1, 0, s>>>(dev_scalars(ctx), cap, key_bits);
+    return cudaGetLastError();
+}
+
+int copy_scalars_async(ochre_gpu_ctx* ctx, cudaStream_t s) {
+    static_assert(sizeof(DevScalars) / 4 <= 64, "one word per thread of k_copy_words");
     if (ctx->h_scalars_dev) {
         k_copy_words<<<1, 64, 0, s>>>(ctx->scalars.as<uint32_t>(), (uint32_t)(sizeof(DevScalars) / 4),
                                        static_cast<uint32_t*>(ctx->h_scalars_dev));
@@ -110,6 +146,12 @@ int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
         OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->h_scalars.p, ctx->scalars.p, sizeof(DevScalars), cudaMemcpyDeviceToHost,
                                        s));
     }
+    return OCHRE_OK;
+}
+
+int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
+    const int st = copy_scalars_async(ctx, s);
+    if (st != OCHRE_OK) return st;
     OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
     return OCHRE_OK;
 }

@@ -41,6 +41,13 @@ constexpr uint32_t WALK_CAP = 1u << 20;      // pixel cells per line
 constexpr int CONIC_DEPTH_CAP = 40;          // conic subdivision depth
 constexpr long long SPIN_LIMIT = 1ll << 23;  // polls of a look-back flag (~1 s with backoff)
 
+// The count a kernel works on: its launch-time value, or, when the count is
+// held on the device (launch chains replayed from a CUDA graph), the device
+// value, never more than the launch-time capacity.
+__device__ __forceinline__ uint64_t dev_count(uint64_t cap, const uint32_t* n_dev) {
+    return n_dev != nullptr ? min(cap, (uint64_t)*n_dev) : cap;
+}
+
 // ---------------------------------------------------------------------
 // Rust scalar semantics
 // ---------------------------------------------------------------------

@@ -78,13 +78,15 @@ __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1
     if (y1 > cur.w) atomicMax(&d->w, y1);
 }
 __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ lines,
-                                                    const uint32_t* __restrict__ line_raster, uint32_t n_lines,
-                                                    int4* bbox, int* raster_wsum, uint32_t* __restrict__ counts,
-                                                    uint32_t* err) {
+                                                    const uint32_t* __restrict__ line_raster, uint32_t n_cap,
+                                                    const uint32_t* n_dev, int4* bbox, int* raster_wsum,
+                                                    uint32_t* __restrict__ counts, uint32_t* err) {
     __shared__ int4 s_box[BOX_SLOTS];
     __shared__ int s_ws[BOX_SLOTS];
     __shared__ uint32_t s_r0;
+    const uint32_t n_lines = (uint32_t)dev_count(n_cap, n_dev);
     const uint32_t i0 = blockIdx.x * blockDim.x;
+    if (i0 >= n_lines) return;
     const uint32_t i = i0 + threadIdx.x;
     if (threadIdx.x < BOX_SLOTS) {
         s_box[threadIdx.x] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
@@ -194,11 +196,11 @@ __device__ __forceinline__ K make_key(uint64_t base, const int4& bb, int tx, int
 
 template <class K>
 __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster,
-                            const uint32_t* __restrict__ ent_off, uint64_t n_lines,
+                            const uint32_t* __restrict__ ent_off, uint64_t n_cap, const uint32_t* n_dev,
                             const int4* __restrict__ bbox, const uint64_t* __restrict__ key_base,
                             K* __restrict__ keys, uint32_t* __restrict__ vals, BinRec* __restrict__ bins) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n_lines) return;
+    if (i >= dev_count(n_cap, n_dev)) return;
     const float4 l = lines[i];
     const V2 a = v2(l.x, l.y), p = v2(l.z, l.w);
     if (veq(a, p)) return;
@@ -253,13 +255,18 @@ __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __
 
 template <class K>
 __global__ void k_empty_emit(const uint32_t* __restrict__ empty, uint32_t n_rasters, uint32_t first_entry,
+                             const uint32_t* first_dev, const uint32_t* n_ent_dev,
                              const uint64_t* __restrict__ key_base, K* __restrict__ keys,
                              uint32_t* __restrict__ vals, BinRec* __restrict__ bins) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n_rasters) return;
     const uint32_t rank = empty[r];
     if (!rank) return;
+    // device-held counts (graph replays): entries after the lines' entries,
+    // none when the entry count was over capacity (zeroed)
+    if (first_dev != nullptr) first_entry = *first_dev;
     const uint32_t e = first_entry + rank - 1u;
+    if (n_ent_dev != nullptr && e >= *n_ent_dev) return;
     BinRec rec;
     rec.line = 0xffffffffu;
     rec.raster = r;
@@ -289,17 +296,20 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
                                                                                  ctx->raster_wsum.as<int>(), R));
     OCHRE_CUDA_TRY(cudaGetLastError());
     OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_line_ent, 0, sizeof(uint32_t), s));
+    // graph replays: n_lines is the capacity, the count is on the device
+    const GraphPlan* plan = ctx->plan;
+    const uint32_t* lines_dev = plan ? &ds->n_lines : nullptr;
     if (n_lines) {
         OCHRE_CUDA_TRY(ctx->line_ent_off.ensure((size_t)n_lines * 4));
         OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<uint32_t>)));
         OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<(n_lines + 255) / 256, 256, 0, s>>>(
-            ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, ctx->raster_bbox.as<int4>(),
+            ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
             ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());
         // in place: every count is read by the thread that writes its offset
         OCHRE_LAUNCH(ctx, "dda_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
             n_lines, CountIn32{ctx->line_ent_off.as<uint32_t>()}, OffOut32{ctx->line_ent_off.as<uint32_t>()},
-            OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_line_ent, &ds->err, s)));
+            OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_line_ent, &ds->err, s, lines_dev)));
     }
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(R) * sizeof(ScanStatus<RasterScan>)));
     OCHRE_LAUNCH(ctx, "raster_key_scan", s, OCHRE_CUDA_TRY(launch_scan<RasterScan>(
@@ -308,16 +318,29 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
                   ctx->raster_wbase.as<int>()},
         OpRaster{}, RasterScan{0, 0, 0}, ctx->scan_status.p, &ds->ticket,
         reinterpret_cast<RasterScan*>(&ds->keyspace), &ds->err, s)));
-    int st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    st = check_device_error(ctx);
-    if (st != OCHRE_OK) return st;
-    const DevScalars* hs = host_scalars(ctx);
-    const uint64_t E = (uint64_t)hs->n_line_ent + hs->n_empty;
-    if (E > MAX_COUNT) return OCHRE_E_CAPACITY;
-    uint64_t K = hs->keyspace;
-    uint32_t bits = 1;
-    while (bits < 64 && (K - 1) >> bits) bits++;
+    uint64_t E;
+    uint32_t bits;
+    uint32_t first_entry = 0;
+    bool any_empty = true;
+    if (plan) {
+        // entry total and key space checked against the plan on the device
+        OCHRE_LAUNCH(ctx, "plan_entries", s, OCHRE_CUDA_TRY(launch_plan_entries(ctx, plan->entries, plan->key_bits, s)));
+        E = plan->entries;
+        bits = plan->key_bits;
+    } else {
+        int st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
+        const DevScalars* hs = host_scalars(ctx);
+        E = (uint64_t)hs->n_line_ent + hs->n_empty;
+        if (E > MAX_COUNT) return OCHRE_E_CAPACITY;
+        const uint64_t K = hs->keyspace;
+        bits = 1;
+        while (bits < 64 && (K - 1) >> bits) bits++;
+        first_entry = hs->n_line_ent;
+        any_empty = hs->n_empty != 0;
+    }
     *key_bits = bits;
     *n_entries = E;
     ctx->keys64 = bits > 32;
@@ -332,24 +355,28 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
         if (ctx->keys64)
             OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<blocks, 128, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
-                ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(),
+                lines_dev, ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(),
                 ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
         else
             OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<blocks, 128, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
-                ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(),
+                lines_dev, ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(),
                 ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
         OCHRE_CUDA_TRY(cudaGetLastError());
     }
-    if (hs->n_empty) {
+    if (any_empty) {
+        const uint32_t* first_dev = plan ? &ds->n_line_ent : nullptr;
+        const uint32_t* ent_dev = plan ? &ds->n_entries : nullptr;
         if (ctx->keys64)
             OCHRE_LAUNCH(ctx, "empty_emit", s, k_empty_emit<uint64_t><<<(R + 255) / 256, 256, 0, s>>>(
-                ctx->raster_empty.as<uint32_t>(), R, hs->n_line_ent, ctx->raster_keybase.as<uint64_t>(),
-                ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
+                ctx->raster_empty.as<uint32_t>(), R, first_entry, first_dev, ent_dev,
+                ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(),
+                ctx->bins.as<BinRec>()));
         else
             OCHRE_LAUNCH(ctx, "empty_emit", s, k_empty_emit<uint32_t><<<(R + 255) / 256, 256, 0, s>>>(
-                ctx->raster_empty.as<uint32_t>(), R, hs->n_line_ent, ctx->raster_keybase.as<uint64_t>(),
-                ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
+                ctx->raster_empty.as<uint32_t>(), R, first_entry, first_dev, ent_dev,
+                ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(),
+                ctx->bins.as<BinRec>()));
         OCHRE_CUDA_TRY(cudaGetLastError());
     }
     return OCHRE_OK;

@@ -153,13 +153,18 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
                                         reinterpret_cast<CmdScan*>(&ds->n_floats), &ds->err, s)));
 
     // The verbs must not consume more floats than the point stream holds:
-    // check before any kernel reads a point.
-    int st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
+    // check before any kernel reads a point.  (A graph replay keeps the verbs
+    // of its planning run, which checked them.)
+    const GraphPlan* plan = ctx->plan;
+    int st = OCHRE_OK;
     const DevScalars* hs = host_scalars(ctx);
-    if (hs->n_floats > in->n_floats) return OCHRE_E_INVALID;
-    st = check_device_error(ctx);
-    if (st != OCHRE_OK) return st;
+    if (!plan) {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        if (hs->n_floats > in->n_floats) return OCHRE_E_INVALID;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
+    }
 
     BatchView b{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                 in->n_fills, in->n_rasters, n, ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
@@ -167,11 +172,18 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
     OCHRE_LAUNCH(ctx, "flatten_count_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(n, CountIn{b, &ds->err}, OffOut{ctx->cmd_line_off.as<uint32_t>()},
                                          OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_lines,
                                          &ds->err, s)));
-    st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    st = check_device_error(ctx);
-    if (st != OCHRE_OK) return st;
-    const uint32_t L = hs->n_lines;
+    uint32_t L;
+    if (plan) {
+        // the line count stays on the device; above the plan it is zeroed
+        OCHRE_LAUNCH(ctx, "plan_lines", s, OCHRE_CUDA_TRY(launch_plan_cap(ctx, &ds->n_lines, plan->lines, s)));
+        L = plan->lines;
+    } else {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
+        L = hs->n_lines;
+    }
     *n_lines = L;
     if (L == 0) return OCHRE_OK;
     if (L > MAX_COUNT) return OCHRE_E_CAPACITY;

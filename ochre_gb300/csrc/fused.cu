@@ -688,6 +688,8 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
     if (cap_guess > MAX_COUNT) cap_guess = MAX_COUNT;
     uint32_t tile_cap = (uint32_t)cap_guess;
     uint32_t span_cap_fixed = 0;
+    const GraphPlan* plan = ctx->plan;
+    if (plan) tile_cap = plan->tiles;   // graph replays: the planned capacity, no retry
     if (fixed_out) {
         tile_cap = (uint32_t)std::min(ctx->out_tile_xy.cap / 4, ctx->out_tile_alpha.cap / 64);
         span_cap_fixed = (uint32_t)std::min(std::min(ctx->out_span_xy.cap / 4, ctx->out_span_w.cap / 2),
@@ -744,6 +746,11 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         default: return OCHRE_E_INVALID;
         }
         if (st0 != OCHRE_OK) return st0;
+        if (plan) {
+            // totals, fallback and errors are read after the replay
+            *handled = true;
+            return OCHRE_OK;
+        }
         int st = read_scalars(ctx, s);
         if (st != OCHRE_OK) return st;
         const DevScalars* hs = host_scalars(ctx);

@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <atomic>
 #include <vector>
 
 #include "../../include/ochre_gpu.h"
@@ -54,7 +55,7 @@ struct DevScalars {
     uint32_t cmd_ep_tot;
     uint32_t n_lines;      // total lines
     uint32_t n_line_ent;   // entries produced by lines
-    uint32_t pad0;
+    uint32_t n_entries;    // all sort entries: n_line_ent + n_empty
     uint64_t keyspace;     // total key space (raster scan .ks)
     uint32_t n_empty;      // rasters without increments (raster scan .ne)
     uint32_t pad1;
@@ -68,6 +69,20 @@ struct DevScalars {
     uint32_t fused_tiles;     // fused path totals
     uint32_t fused_spans;
     uint32_t n_rows;          // tile rows (raster, tile_y) of the general chain
+};
+
+// Capacities of a launch chain captured into a CUDA graph.  Every buffer is
+// sized from them once; the counts stay on the device, each kernel reads its
+// count there and its grid covers the capacity.  A check kernel at every
+// sizing point flags a count above its capacity (ERR_CAPACITY) and zeroes it,
+// so that no later kernel works past a buffer.
+struct GraphPlan {
+    bool fused;          // the batch is one fused launch (else the general chain)
+    uint32_t lines;      // general chain: lines, sort entries, tiles
+    uint32_t entries;
+    uint32_t tiles;      // (fused: output tiles and spans)
+    uint32_t key_bits;   // sort key bits; keys are 64-bit above 32
+    uint32_t rows;       // tile rows of the planning run (coverage form and grid)
 };
 
 // Entry value tag for tile-row crossings: 1 | raster (23 bits) | sign byte.
@@ -163,6 +178,10 @@ struct ochre_gpu_ctx {
     int tune_chain_tiles_per_warp = 8;
     int tune_chain_coverage_form = 0;   // 0: by row count, 1: block form, 2: row form
 
+    // Set while the chain is planned for (and captured into) a CUDA graph:
+    // stages size buffers from it and never read counts back to the host.
+    const ochre::GraphPlan* plan = nullptr;
+
 
     // Tracing: every kernel launch of a run is counted; with OCHRE_CTX_PROFILE
     // each one is also bracketed by a pair of CUDA events on its stream.
@@ -193,8 +212,20 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
 // The whole chain for one batch (device pointers), results in ctx buffers.
 int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s);
 
+// Graph replays: device checks of counts against the plan (api.cu).  The
+// entry check sets n_entries = n_line_ent + n_empty and zeroes it, and the
+// line count, when it or the key space exceeds the plan; the other zeroes
+// *count above cap.  Both flag ERR_CAPACITY.
+cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_bits, cudaStream_t s);
+cudaError_t launch_plan_cap(ochre_gpu_ctx* ctx, uint32_t* count, uint32_t cap, cudaStream_t s);
+
 // Read the device scalars into ctx->h_scalars (synchronises the stream).
 int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);
+// The same copy, enqueued only.
+int copy_scalars_async(ochre_gpu_ctx* ctx, cudaStream_t s);
+// Device allocations made by DevBuf::ensure so far (a graph capture must
+// make none: its nodes keep the pointers they saw).
+extern std::atomic<uint64_t> g_dev_allocs;
 inline DevScalars* dev_scalars(ochre_gpu_ctx* ctx) { return ctx->scalars.as<DevScalars>(); }
 inline DevScalars* host_scalars(ochre_gpu_ctx* ctx) { return ctx->h_scalars.as<DevScalars>(); }
 int check_device_error(ochre_gpu_ctx* ctx);

@@ -21,16 +21,21 @@ struct ScanStatus {
 };
 
 template <int BLOCK, int ITEMS, class T, class Op, class In, class Out>
-__global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, In in, Out out, Op op, T identity,
-                                                 ScanStatus<T>* status, uint32_t* ticket, T* total,
+__global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_dev, In in, Out out, Op op,
+                                                 T identity, ScanStatus<T>* status, uint32_t* ticket, T* total,
                                                  uint32_t* err) {
     constexpr int WARPS = BLOCK / 32;
     __shared__ uint32_t s_tile;
     __shared__ T s_warp[WARPS];
     __shared__ T s_prefix;
+    // A count held on the device (graph replays): the grid covers the
+    // capacity n, the scan covers min(*n_dev, n).  Tiles past the count end
+    // before publishing anything; no tile that scans waits on them.
+    n = dev_count(n, n_dev);
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
+    if ((uint64_t)tile * (BLOCK * ITEMS) >= n) return;
     const uint64_t base = (uint64_t)tile * (BLOCK * ITEMS) + (uint64_t)threadIdx.x * ITEMS;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
@@ -139,9 +144,10 @@ constexpr int SCAN_BLOCK = 256;
 constexpr int SCAN_ITEMS = 8;
 inline uint64_t scan_tiles(uint64_t n) { return (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS); }
 
+// `n_dev` (optional): the count lives on the device and `n` is its capacity.
 template <class T, class Op, class In, class Out>
 cudaError_t launch_scan(uint64_t n, In in, Out out, Op op, T identity, void* status, uint32_t* ticket, T* total,
-                        uint32_t* err, cudaStream_t stream) {
+                        uint32_t* err, cudaStream_t stream, const uint32_t* n_dev = nullptr) {
     const uint64_t tiles = scan_tiles(n);
     if (tiles == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(status, 0, tiles * sizeof(ScanStatus<T>), stream);
@@ -149,7 +155,7 @@ cudaError_t launch_scan(uint64_t n, In in, Out out, Op op, T identity, void* sta
     e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
     k_scan<SCAN_BLOCK, SCAN_ITEMS, T, Op, In, Out><<<(unsigned)tiles, SCAN_BLOCK, 0, stream>>>(
-        n, in, out, op, identity, reinterpret_cast<ScanStatus<T>*>(status), ticket, total, err);
+        n, n_dev, in, out, op, identity, reinterpret_cast<ScanStatus<T>*>(status), ticket, total, err);
     return cudaGetLastError();
 }
 

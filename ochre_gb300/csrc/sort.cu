@@ -25,9 +25,10 @@ constexpr int SORT_TILE = SORT_BLOCK * SORT_ITEMS;
 constexpr uint32_t LB_AGG = 1u << 30, LB_INC = 2u << 30, LB_MASK = (1u << 30) - 1u;
 
 template <class K>
-__global__ void __launch_bounds__(256) k_sort_hist(const K* __restrict__ keys, uint64_t n, int passes,
-                                                   uint32_t* __restrict__ hist) {
+__global__ void __launch_bounds__(256) k_sort_hist(const K* __restrict__ keys, uint64_t n, const uint32_t* n_dev,
+                                                   int passes, uint32_t* __restrict__ hist) {
     __shared__ uint32_t sh[8][256];
+    n = dev_count(n, n_dev);
     for (int i = threadIdx.x; i < 8 * 256; i += blockDim.x) (&sh[0][0])[i] = 0u;
     __syncthreads();
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -59,7 +60,8 @@ __global__ void k_sort_offsets(const uint32_t* __restrict__ hist, uint32_t* __re
 template <class K>
 __global__ void __launch_bounds__(SORT_BLOCK) k_onesweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                                                          K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
-                                                         uint64_t n, int shift, const uint32_t* __restrict__ digit_off,
+                                                         uint64_t n, const uint32_t* n_dev, int shift,
+                                                         const uint32_t* __restrict__ digit_off,
                                                          uint32_t* lookback, uint32_t* ticket, uint32_t* err) {
     extern __shared__ __align__(16) unsigned char smem[];
     K* s_keys = reinterpret_cast<K*>(smem);
@@ -75,6 +77,10 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_onesweep(const K* __restrict__ k
     __syncthreads();
     const uint32_t tile = s_misc[0];
     const uint64_t tile_base = (uint64_t)tile * SORT_TILE;
+    // device-held count (graph replays): tiles past it end before publishing;
+    // every tile that sorts precedes them
+    n = dev_count(n, n_dev);
+    if (tile_base >= n) return;
     const uint64_t warp_base = tile_base + (uint64_t)warp * 32 * SORT_ITEMS;
     const uint32_t lt_mask = (1u << lane) - 1u;
 
@@ -180,6 +186,9 @@ __global__ void __launch_bounds__(SORT_BLOCK) k_onesweep(const K* __restrict__ k
 template <class K>
 static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStream_t s, uint32_t* passes_done) {
     DevScalars* ds = dev_scalars(ctx);
+    // graph replays: n is the capacity, the count is on the device, and every
+    // pass runs (no read-back to skip passes whose digit is constant)
+    const uint32_t* n_dev = ctx->plan ? &ds->n_entries : nullptr;
     const int passes = (int)((key_bits + 7) / 8);
     const uint64_t tiles = (n + SORT_TILE - 1) / SORT_TILE;
     OCHRE_CUDA_TRY(ctx->sort_hist.ensure((size_t)passes * 256 * 4 * 2));
@@ -194,7 +203,7 @@ static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStre
     {
         int blocks = (int)((n + 255) / 256);
         if (blocks > 152 * 8) blocks = 152 * 8;
-        OCHRE_LAUNCH(ctx, "sort_hist", s, k_sort_hist<K><<<blocks, 256, 0, s>>>(kin, n, passes, hist));
+        OCHRE_LAUNCH(ctx, "sort_hist", s, k_sort_hist<K><<<blocks, 256, 0, s>>>(kin, n, n_dev, passes, hist));
         OCHRE_CUDA_TRY(cudaGetLastError());
         OCHRE_LAUNCH(ctx, "sort_offsets", s, k_sort_offsets<<<passes, 256, 0, s>>>(hist, off));
         OCHRE_CUDA_TRY(cudaGetLastError());
@@ -203,17 +212,19 @@ static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStre
     OCHRE_CUDA_TRY(cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // Skip passes whose digit is constant over all keys (one bucket holds n).
     uint32_t h_hist[8 * 256];
-    OCHRE_CUDA_TRY(cudaMemcpyAsync(h_hist, hist, (size_t)passes * 256 * 4, cudaMemcpyDeviceToHost, s));
-    OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
+    if (!n_dev) {
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(h_hist, hist, (size_t)passes * 256 * 4, cudaMemcpyDeviceToHost, s));
+        OCHRE_CUDA_TRY(cudaStreamSynchronize(s));
+    }
     uint32_t done = 0;
     for (int p = 0; p < passes; p++) {
         bool trivial = false;
-        for (int d = 0; d < 256; d++)
+        for (int d = 0; d < 256 && !n_dev; d++)
             if (h_hist[(size_t)p * 256 + d] == n) trivial = true;
         if (trivial) continue;
         OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->sort_lookback.p, 0, (size_t)tiles * 256 * 4, s));
         OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->sort_ticket, 0, 4, s));
-        OCHRE_LAUNCH(ctx, "sort_onesweep", s, k_onesweep<K><<<(unsigned)tiles, SORT_BLOCK, smem, s>>>(kin, vin, kout, vout, n, 8 * p, off + p * 256,
+        OCHRE_LAUNCH(ctx, "sort_onesweep", s, k_onesweep<K><<<(unsigned)tiles, SORT_BLOCK, smem, s>>>(kin, vin, kout, vout, n, n_dev, 8 * p, off + p * 256,
                                                                 ctx->sort_lookback.as<uint32_t>(), &ds->sort_ticket,
                                                                 &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());

@@ -69,9 +69,10 @@ struct HeadOut {
 __global__ void k_tile_info(const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins,
                             const uint32_t* __restrict__ head, const uint32_t* __restrict__ head_bins,
                             const int32_t* __restrict__ head_wind, const int32_t* __restrict__ raster_wbase,
-                            const uint32_t* __restrict__ total_bins, uint32_t n_tiles, uint32_t n_rasters,
-                            TileInfo* __restrict__ info, uint32_t* __restrict__ raster_tile_off) {
+                            const uint32_t* __restrict__ total_bins, uint32_t n_tiles, const uint32_t* n_dev,
+                            uint32_t n_rasters, TileInfo* __restrict__ info, uint32_t* __restrict__ raster_tile_off) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    n_tiles = (uint32_t)dev_count(n_tiles, n_dev);
     if (t >= n_tiles) return;
     const uint32_t h = head[t];
     const BinRec* rec = bins + vals[h];
@@ -113,10 +114,12 @@ __device__ __forceinline__ int acc_idx(int cell) { return cell + ((cell >> 5) <<
 template <int CH>
 __global__ void __launch_bounds__(128) k_tile_cov_blocks(
     const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
-    const TileInfo* __restrict__ info, uint32_t n_tiles, TileBlockState* state, uint32_t* ticket,
-    uint32_t* __restrict__ out_xy, uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov,
+    const TileInfo* __restrict__ info, uint32_t n_tiles, const uint32_t* n_dev, TileBlockState* state,
+    uint32_t* ticket, uint32_t* __restrict__ out_xy, uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov,
     uint32_t* __restrict__ span_flag, uint64_t* __restrict__ span_val, uint32_t* err, bool cov_signed) {
     constexpr int WARPS = 4;
+    // device-held count (graph replays): blocks past it end before publishing
+    n_tiles = (uint32_t)dev_count(n_tiles, n_dev);
     // [tile][area cells | height cells], ACC_STRIDE floats per tile; see acc_idx
     __shared__ __align__(16) float s_acc[WARPS][CH][ACC_STRIDE];
     __shared__ uint32_t s_head[WARPS][CH];
@@ -343,7 +346,7 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
 template <int CH>
 __global__ void __launch_bounds__(128) k_tile_cov(
     const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
-    const TileInfo* __restrict__ info, uint32_t n_tiles, const uint32_t* __restrict__ row_start,
+    const TileInfo* __restrict__ info, uint32_t n_tiles, const uint32_t* n_dev, const uint32_t* __restrict__ row_start,
     const uint32_t* __restrict__ n_rows_p, uint32_t* ticket, uint32_t* __restrict__ out_xy,
     uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov, uint32_t* __restrict__ span_flag,
     uint64_t* __restrict__ span_val, bool cov_signed) {
@@ -355,6 +358,7 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     // lane = 8 * g + y: pixel row y of the g-th tile of a pass of four
     const int y = lane & 7, g = lane >> 3;
     const uint32_t n_rows = *n_rows_p;
+    n_tiles = (uint32_t)dev_count(n_tiles, n_dev);
     float (*acc)[ACC_STRIDE] = s_acc[wid];
 
     for (;;) {
@@ -509,6 +513,7 @@ struct SpanOut {
     const uint64_t* val;
     const TileInfo* info;
     uint32_t n_tiles, n_rasters;
+    const uint32_t* n_dev;   // device-held tile count (graph replays), else null
     uint32_t* xy;
     uint16_t* w;
     uint32_t* tile;
@@ -522,7 +527,7 @@ struct SpanOut {
         }
         const int r = info[t].raster;
         if (t == 0 || info[t - 1].raster != r) raster_span_off[r] = ex;
-        if (t + 1 == n_tiles) raster_span_off[n_rasters] = ex + v;
+        if (t + 1 == dev_count(n_tiles, n_dev)) raster_span_off[n_rasters] = ex + v;
     }
 };
 
@@ -539,6 +544,9 @@ static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, uint32_t n_rows, boo
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     cudaMemsetAsync(&ds->ticket, 0, 4, s);
     float* cov = want_cov ? ctx->out_tile_cov.as<float>() : nullptr;
+    // graph replays: T is the capacity and n_rows the planned row count; the
+    // kernels read both counts on the device
+    const uint32_t* t_dev = ctx->plan ? &ds->n_tiles : nullptr;
     const bool row_form = ctx->tune_chain_coverage_form == 2 ||
                           (ctx->tune_chain_coverage_form == 0 && n_rows >= ROW_FORM_MIN_ROWS_PER_SM * (uint32_t)sms);
     if (row_form) {
@@ -546,7 +554,7 @@ static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, uint32_t n_rows, boo
         const uint32_t ctas = (uint32_t)std::min<uint64_t>(((uint64_t)n_rows + 3) / 4, (uint64_t)sms * 16);
         k_tile_cov<TPW><<<ctas, 128, 0, s>>>(
             ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(),
-            T, ctx->tile_row_start.as<uint32_t>(), &ds->n_rows, &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
+            T, t_dev, ctx->tile_row_start.as<uint32_t>(), &ds->n_rows, &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
             ctx->out_tile_alpha.as<uint8_t>(), cov, ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(),
             ctx->cov_signed);
     } else {
@@ -554,7 +562,7 @@ static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, uint32_t n_rows, boo
         cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)blocks * sizeof(TileBlockState), s);
         k_tile_cov_blocks<TPW><<<(blocks + 3) / 4, 128, 0, s>>>(
             ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(),
-            T, ctx->tile_state.as<TileBlockState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
+            T, t_dev, ctx->tile_state.as<TileBlockState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
             ctx->out_tile_alpha.as<uint8_t>(), cov, ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(),
             &ds->err, ctx->cov_signed);
     }
@@ -569,16 +577,26 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     OCHRE_CUDA_TRY(ctx->tile_head_bins.ensure(E * 4));
     OCHRE_CUDA_TRY(ctx->tile_head_wind.ensure(E * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(E) * sizeof(ScanStatus<HeadScan>)));
+    // graph replays: E and T are capacities, the counts stay on the device
+    const GraphPlan* plan = ctx->plan;
+    const uint32_t* t_dev = plan ? &ds->n_tiles : nullptr;
     OCHRE_LAUNCH(ctx, "tile_head_scan", s,
                  OCHRE_CUDA_TRY(launch_scan<HeadScan>(
                      E, HeadIn<K>{ctx->keys.as<K>(), ctx->vals.as<uint32_t>()},
                      HeadOut{ctx->tile_head.as<uint32_t>(), ctx->tile_head_bins.as<uint32_t>(),
                              ctx->tile_head_wind.as<int32_t>()},
                      OpHead{}, HeadScan{0u, 0u, 0, 0u}, ctx->scan_status.p, &ds->ticket,
-                     reinterpret_cast<HeadScan*>(&ds->n_tiles), &ds->err, s)));
-    int st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    const uint32_t T = host_scalars(ctx)->n_tiles;
+                     reinterpret_cast<HeadScan*>(&ds->n_tiles), &ds->err, s, plan ? &ds->n_entries : nullptr)));
+    int st = OCHRE_OK;
+    uint32_t T;
+    if (plan) {
+        OCHRE_LAUNCH(ctx, "plan_tiles", s, OCHRE_CUDA_TRY(launch_plan_cap(ctx, &ds->n_tiles, plan->tiles, s)));
+        T = plan->tiles;
+    } else {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        T = host_scalars(ctx)->n_tiles;
+    }
     *n_tiles_out = T;
     OCHRE_CUDA_TRY(ctx->tile_info.ensure((size_t)T * sizeof(TileInfo)));
     OCHRE_CUDA_TRY(ctx->tile_row_start.ensure((size_t)T * 4));
@@ -596,7 +614,7 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
                      k_tile_info<<<(T + 255) / 256, 256, 0, s>>>(
                          ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->tile_head.as<uint32_t>(),
                          ctx->tile_head_bins.as<uint32_t>(), ctx->tile_head_wind.as<int32_t>(),
-                         ctx->raster_wbase.as<int32_t>(), &ds->n_bins, T, R, ctx->tile_info.as<TileInfo>(),
+                         ctx->raster_wbase.as<int32_t>(), &ds->n_bins, T, t_dev, R, ctx->tile_info.as<TileInfo>(),
                          ctx->out_raster_tile_off.as<uint32_t>()));
     OCHRE_CUDA_TRY(cudaGetLastError());
     if (T) {
@@ -604,11 +622,16 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
         OCHRE_LAUNCH(ctx, "tile_row_scan", s,
                      OCHRE_CUDA_TRY(launch_scan<uint32_t>(
                          T, RowIn{ctx->tile_info.as<TileInfo>()}, RowOut{ctx->tile_row_start.as<uint32_t>()},
-                         OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_rows, &ds->err, s)));
+                         OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_rows, &ds->err, s, t_dev)));
     }
-    st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    const uint32_t n_rows = host_scalars(ctx)->n_rows;
+    uint32_t n_rows;
+    if (plan) {
+        n_rows = plan->rows;
+    } else {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        n_rows = host_scalars(ctx)->n_rows;
+    }
     switch (ctx->tune_chain_tiles_per_warp) {
     case 4: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<4>(ctx, T, n_rows, want_cov, s)); break;
     case 8: OCHRE_LAUNCH(ctx, "tile_coverage", s, launch_tile_cov<8>(ctx, T, n_rows, want_cov, s)); break;
@@ -624,10 +647,14 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     OCHRE_LAUNCH(ctx, "span_scan", s,
                  OCHRE_CUDA_TRY(launch_scan<uint32_t>(
                      T, SpanIn{ctx->span_flag.as<uint32_t>()},
-                     SpanOut{ctx->span_val.as<uint64_t>(), ctx->tile_info.as<TileInfo>(), T, R,
+                     SpanOut{ctx->span_val.as<uint64_t>(), ctx->tile_info.as<TileInfo>(), T, R, t_dev,
                              ctx->out_span_xy.as<uint32_t>(), ctx->out_span_w.as<uint16_t>(),
                              ctx->out_span_tile.as<uint32_t>(), ctx->out_raster_span_off.as<uint32_t>()},
-                     OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_spans, &ds->err, s)));
+                     OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_spans, &ds->err, s, t_dev)));
+    if (plan) {
+        *n_spans_out = 0;   // on the device; read after the replay
+        return OCHRE_OK;
+    }
     st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
     *n_spans_out = host_scalars(ctx)->n_spans;

@@ -238,6 +238,52 @@ class Rasterizer:
 # ---------------------------------------------------------------------------
 # Batched entry points
 # ---------------------------------------------------------------------------
+class Graph:
+    """A captured fill -> finish launch chain for one DeviceBatch (its device
+    pointers and counts fixed; the values behind them may change between
+    launches).  Owns its buffers; results are device pointers valid until the
+    next launch."""
+
+    def __init__(self, ctx: "GpuContext", dbatch: "DeviceBatch", headroom: float = 1.25):
+        L = _lib.load()
+        h = ctypes.c_void_p()
+        self.dbatch = dbatch   # keeps the device storage alive
+        self.n_rasters = dbatch.batch.n_rasters
+        self._ctx = ctx
+        _lib.check(L.ochre_graph_create(ctx.handle, ctypes.byref(dbatch.c), ctypes.c_float(headroom),
+                                        ctypes.byref(h)), "ochre_graph_create")
+        self.handle = h
+
+    def launch(self, stream: Optional[int] = None) -> _lib.Result:
+        r = _lib.Result()
+        _lib.check(_lib.load().ochre_graph_launch(self.handle, ctypes.byref(r), stream), "ochre_graph_launch")
+        return r
+
+    def rasterize(self, stream: Optional[int] = None) -> dict:
+        """launch() with the result copied to numpy arrays."""
+        return self._ctx.device_result_to_numpy(self.launch(stream), self.n_rasters)
+
+    def stats(self) -> _lib.Stats:
+        st = _lib.Stats()
+        _lib.check(_lib.load().ochre_graph_last_stats(self.handle, ctypes.byref(st)))
+        return st
+
+    def info(self) -> dict:
+        k, r, f = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _lib.check(_lib.load().ochre_graph_info(self.handle, ctypes.byref(k), ctypes.byref(r), ctypes.byref(f)))
+        return {"kernels": k.value, "replans": r.value, "fused": bool(f.value)}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) is not None:
+            _lib.load().ochre_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 def _c_batch(verbs_p, n_cmds, pts_p, n_floats, off_p, xf_p, flags_p, n_fills, roff_p, n_rasters,
              width_p=None) -> _lib.Batch:
     b = _lib.Batch()
@@ -371,6 +417,11 @@ class GpuContext:
         _lib.check(_lib.load().ochre_gpu_rasterize_device(self.handle, ctypes.byref(dbatch.c), ctypes.byref(r),
                                                           stream), "rasterize_device")
         return r
+
+    def graph(self, dbatch: DeviceBatch, headroom: float = 1.25) -> "Graph":
+        """The launch chain of rasterize_device for this batch, captured into a
+        CUDA graph (ochre_graph_create)."""
+        return Graph(self, dbatch, headroom)
 
     def device_result_to_numpy(self, r: _lib.Result, n_rasters: int) -> dict:
         out = {}

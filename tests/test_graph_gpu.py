@@ -1,0 +1,130 @@
+"""CUDA-graph execution (ochre_graph_*): replays match the oracle and the
+eager chain, values may change between launches, and a batch that outgrows
+its plan is re-planned.  Runs through the C ABI on the GPU."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import oracle
+from compare import compare
+from golden.make_golden import NAMES, load
+from ochre_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _scaled(b, k):
+    """The batch with every fill's matrix (not its offset) scaled by k."""
+    xf = b.fill_xf.copy()
+    xf[:, :4] *= np.float32(k)
+    return dataclasses.replace(b, fill_xf=xf)
+
+
+def _check(ctx, g, b):
+    got = g.rasterize()
+    compare(got, oracle.run(b, threads=8), b.n_rasters)
+    return got
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_golden_graph_matches_eager(any_ctx, name):
+    from ochre_gb300 import DeviceBatch
+    b, exp = load(name)
+    db = DeviceBatch(b)
+    eager = any_ctx.device_result_to_numpy(any_ctx.rasterize_device(db), b.n_rasters)
+    g = any_ctx.graph(db)
+    try:
+        for _ in range(3):   # replays are repeatable
+            got = g.rasterize()
+            compare(got, exp, b.n_rasters)
+            for k in ("tile_xy", "tile_alpha", "span_xy", "span_w", "raster_tile_off", "raster_span_off"):
+                assert np.array_equal(got[k], eager[k]), k
+        assert g.info()["replans"] == 0
+    finally:
+        g.close()
+
+
+@pytest.mark.parametrize("gen,kw", [
+    (W.glyph_run, dict(n_paths=2000)),
+    (W.uneven_mix, dict(n_paths=120)),
+    (W.cubic_boxes, dict(n_paths=40)),
+    (W.diff_union, dict()),
+])
+def test_workload_graph_parity(any_ctx, gen, kw):
+    from ochre_gb300 import DeviceBatch
+    b = gen(**kw)
+    db = DeviceBatch(b)
+    g = any_ctx.graph(db)
+    try:
+        _check(any_ctx, g, b)
+        st = g.stats()
+        assert st.n_tiles > 0 and st.n_launches == g.info()["kernels"]
+    finally:
+        g.close()
+
+
+def test_new_values_between_launches(gpu_ctx_chain):
+    """Transforms rewritten in place on the device: the same graph
+    rasterizes the new geometry (counts within the plan's headroom)."""
+    from ochre_gb300 import DeviceBatch
+    b = W.uneven_mix(n_paths=100, seed=5)
+    db = DeviceBatch(b)
+    g = gpu_ctx_chain.graph(db, headroom=2.0)
+    try:
+        _check(gpu_ctx_chain, g, b)
+        for k in (1.1, 0.7, 1.3):
+            b2 = _scaled(b, k)
+            db.fill_xf.copy_(db.fill_xf.new_tensor(b2.fill_xf.reshape(-1)))
+            _check(gpu_ctx_chain, g, b2)
+        assert g.info()["replans"] == 0
+    finally:
+        g.close()
+
+
+def test_outgrown_plan_replans(gpu_ctx_chain):
+    """Counts above the plan's capacities: flagged on the device, re-planned
+    from an eager run, replayed; results exact."""
+    from ochre_gb300 import DeviceBatch
+    b = W.uneven_mix(n_paths=100, seed=7)
+    db = DeviceBatch(b)
+    g = gpu_ctx_chain.graph(db, headroom=1.0)
+    try:
+        _check(gpu_ctx_chain, g, b)
+        b2 = _scaled(b, 2.5)
+        db.fill_xf.copy_(db.fill_xf.new_tensor(b2.fill_xf.reshape(-1)))
+        _check(gpu_ctx_chain, g, b2)
+        assert g.info()["replans"] == 1
+        # the new plan holds the grown batch: no further re-plan
+        _check(gpu_ctx_chain, g, b2)
+        assert g.info()["replans"] == 1
+    finally:
+        g.close()
+
+
+def test_fused_plan_falls_back_to_chain(gpu_ctx):
+    """A batch planned on the fused kernel whose raster grows past the fused
+    limits is re-planned onto the general chain."""
+    from ochre_gb300 import DeviceBatch
+    b = W.glyph_run(n_paths=500, seed=3)
+    db = DeviceBatch(b)
+    g = gpu_ctx.graph(db)
+    try:
+        assert g.info()["fused"]
+        _check(gpu_ctx, g, b)
+        xf = b.fill_xf.copy()
+        xf[17, :4] *= np.float32(12.0)   # one glyph ~12x larger: past the fused grid
+        b2 = dataclasses.replace(b, fill_xf=xf)
+        db.fill_xf.copy_(db.fill_xf.new_tensor(b2.fill_xf.reshape(-1)))
+        _check(gpu_ctx, g, b2)
+        info = g.info()
+        assert info["replans"] == 1 and not info["fused"]
+    finally:
+        g.close()
+
+
+def test_graph_rejects_strokes(gpu_ctx):
+    from ochre_gb300 import DeviceBatch, OchreError
+    b = W.stroke_run(n_paths=10)
+    with pytest.raises(OchreError):
+        gpu_ctx.graph(DeviceBatch(b))
