@@ -372,6 +372,58 @@ def bench_stroke(ctx, stream, flush, steps):
             "kernels": _kernel_shares(ctx, lambda: ctx.rasterize_device(db, sp))[:6]}
 
 
+def bench_graph(ctx, stream, steps):
+    """CUDA-graph replay (ochre_graph_launch) against the eager chain
+    (ochre_gpu_rasterize_device) on batches rasterized again and again with
+    the same structure: host wall clock per call, each call ending with its
+    results on the device and the host synchronised."""
+    import numpy as np
+    import torch
+    from ochre_gb300 import DeviceBatch, batch as B, workloads as W
+    sp = stream.cuda_stream
+    um = W.uneven_mix(n_paths=64, seed=3)
+    sizes = np.diff(um.fill_cmd_off)
+    mid = int(np.argsort(sizes)[len(sizes) // 2])
+    cases = [
+        ("one glyph", B.subset(W.glyph_run(n_paths=8, seed=2), [0])),
+        ("one uneven-mix path (median size)", B.subset(um, [mid])),
+        ("glyph run, 1,000 paths", W.glyph_run(n_paths=1000, seed=2)),
+        ("union of 256 cubic fills on 1024x1024", W.diff_union()),
+        ("uneven mix, 1,000 paths", W.uneven_mix(n_paths=1000, seed=4)),
+    ]
+    reps = max(30, 5 * steps)
+    out = []
+    for name, b in cases:
+        db = DeviceBatch(b, ctx.device)
+        eager_r = ctx.rasterize_device(db, sp)
+        n_tiles = eager_r.n_tiles
+        g = ctx.graph(db)
+        try:
+            r = g.launch(sp)
+            assert r.n_tiles == n_tiles and g.info()["replans"] == 0, (name, r.n_tiles, n_tiles)
+
+            def per_call(fn):
+                for _ in range(3):
+                    fn()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    fn()
+                return (time.perf_counter() - t0) / reps * 1e3
+
+            eager_ms = per_call(lambda: ctx.rasterize_device(db, sp))
+            eager_launches = ctx.stats()["n_launches"]
+            graph_ms = per_call(lambda: g.launch(sp))
+            info = g.info()
+            out.append({"batch": name, "rasters": b.n_rasters, "tiles": int(n_tiles),
+                        "form": "fused" if info["fused"] else "chain", "eager_ms_per_call": eager_ms,
+                        "graph_ms_per_call": graph_ms, "speedup": eager_ms / graph_ms,
+                        "eager_launches": eager_launches, "graph_kernels": info["kernels"]})
+        finally:
+            g.close()
+    return {"timing": f"host wall clock, mean of {reps} calls after 3 warm-up calls", "cases": out}
+
+
 def bench_differentiable(ctx, stream, flush, steps, n_scenes):
     """Forward (coverage render + L2 loss) and forward + backward scenes/s on
     the single-raster union (256 paths x 32 cubics, 1024^2) and on batched
@@ -668,6 +720,7 @@ def run_ours(args, ws, rank, local):
                                                 float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])))
         extensions["differentiable"] = bench_differentiable(ctx, stream, flush, args.steps, args.diff_scenes)
         extensions["stroke"] = bench_stroke(ctx, stream, flush, args.steps)
+        extensions["graph"] = bench_graph(ctx, stream, args.steps)
     n_paths_all = batch.n_rasters * ws
     value = n_paths_all * args.steps / dev_s_max
     cpu = cpu_baseline(batch) if ws == 1 else None
@@ -702,6 +755,7 @@ def run_ours(args, ws, rank, local):
         "batched_uneven_mix": extensions.get("uneven_mix"),
         "differentiable": extensions.get("differentiable"),
         "stroke": extensions.get("stroke"),
+        "graph": extensions.get("graph"),
         "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s},
         "gpu_launches": launches,
