@@ -29,6 +29,7 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "scan.cuh"
 
 namespace ochre {
 
@@ -57,7 +58,6 @@ struct FusedSmem {
     uint32_t raster;
     uint32_t flag;                 // per-raster fallback
     uint32_t n_cross;
-    uint32_t float_base;
     uint32_t tile_base, span_base;
     int32_t gx0, gy0, gw, gh;
 };
@@ -120,25 +120,28 @@ __device__ __forceinline__ int block_excl_max(int v, int& incl_last, int32_t (*t
     return max(base, ex);
 }
 
-// Publish raster r's aggregate, resolve its exclusive prefix with a
-// warp-cooperative decoupled look-back (32 predecessors per round), publish
-// its inclusive value.  Called by one full warp; returns the prefix in every
-// lane.  Every wait is bounded.
-__device__ __forceinline__ void chain_resolve(Chain* slots, uint32_t r, uint32_t a0, uint32_t a1, uint32_t* err,
-                                              uint32_t& p0, uint32_t& p1) {
-    const int lane = threadIdx.x & 31;
+// Publish raster r's counts: its aggregate, or, for raster 0, its inclusive
+// value.  One thread.
+__device__ __forceinline__ void chain_publish(Chain* slots, uint32_t r, uint32_t a0, uint32_t a1) {
     Chain* me = slots + r;
-    if (lane == 0) {
-        if (r == 0) {
-            st_relaxed(&me->inc[0], a0);
-            st_relaxed(&me->inc[1], a1);
-            st_release(&me->flag, 2u);
-        } else {
-            st_relaxed(&me->agg[0], a0);
-            st_relaxed(&me->agg[1], a1);
-            st_release(&me->flag, 1u);
-        }
+    if (r == 0) {
+        st_relaxed(&me->inc[0], a0);
+        st_relaxed(&me->inc[1], a1);
+        st_release(&me->flag, 2u);
+    } else {
+        st_relaxed(&me->agg[0], a0);
+        st_relaxed(&me->agg[1], a1);
+        st_release(&me->flag, 1u);
     }
+}
+
+// Resolve raster r's exclusive prefix (its aggregate a0, a1 already
+// published) by a warp-cooperative decoupled look-back, 32 predecessors per
+// round, and publish its inclusive value.  Called by one full warp; returns
+// the prefix in every lane.  Every wait is bounded.
+__device__ __forceinline__ void chain_lookback(Chain* slots, uint32_t r, uint32_t a0, uint32_t a1, uint32_t* err,
+                                               uint32_t& p0, uint32_t& p1) {
+    const int lane = threadIdx.x & 31;
     p0 = 0;
     p1 = 0;
     if (r == 0) return;
@@ -177,6 +180,7 @@ __device__ __forceinline__ void chain_resolve(Chain* slots, uint32_t r, uint32_t
         top -= 32;
     }
     if (lane == 0) {
+        Chain* me = slots + r;
         st_relaxed(&me->inc[0], p0 + a0);
         st_relaxed(&me->inc[1], p1 + a1);
         st_release(&me->flag, 2u);
@@ -186,13 +190,13 @@ __device__ __forceinline__ void chain_resolve(Chain* slots, uint32_t r, uint32_t
 struct FusedArgs {
     const uint8_t* verbs;
     const float* pts;
+    const uint32_t* cmd_foff;   // float offset of every command (exclusive scan of floats per verb)
     const uint32_t* fill_off;
     const float* fill_xf;
     const uint8_t* fill_flags;
     const uint32_t* raster_off;
     uint32_t n_fills, n_rasters;
     uint64_t n_floats;
-    Chain* cf;               // float offsets
     Chain* co;               // output tiles / spans
     uint32_t* ticket;
     uint32_t* fallback;      // any raster did not fit
@@ -207,6 +211,8 @@ struct FusedArgs {
     uint32_t* span_tile;
     uint32_t* raster_tile_off;
     uint32_t* raster_span_off;
+    uint8_t* stage_alpha;    // per CTA: F_TMAX tiles of alpha (and of coverage when out_cov)
+    float* stage_cov;
 };
 
 __device__ __forceinline__ V2 load_pt(const float* p) { return v2(__ldg(p), __ldg(p + 1)); }
@@ -221,13 +227,13 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
     for (;;) {
         if (tid == 0) {
             S.raster = atomicAdd(A.ticket, 1u);
-            S.flag = 0;
+            // batch already falls back: skip the work, keep the output chain moving
+            S.flag = ld_relaxed(A.fallback) != 0u ? 1u : 0u;
             S.n_cross = 0;
         }
         __syncthreads();
         const uint32_t r = S.raster;
         if (r >= A.n_rasters) return;
-        const bool give_up = ld_relaxed(A.fallback) != 0u;   // batch already falls back: only keep chains moving
 
         // ---------------- A. commands -> lines ----------------
         uint32_t f0, f1;
@@ -235,26 +241,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
         else { f0 = r; f1 = r + 1; }
         const uint32_t c0 = __ldg(A.fill_off + f0), c1 = __ldg(A.fill_off + f1);
         const int n_cmd = (int)(c1 - c0);
-        // float count of the whole raster (loop so that the float chain is
-        // always published, whatever the raster's size)
-        int nf_total = 0;
-        for (int base = 0; base < n_cmd; base += FUSED_THREADS) {
-            const int i = base + tid;
-            const uint8_t v = i < n_cmd ? __ldg(A.verbs + c0 + i) : V_CLOSE;
-            int t;
-            block_excl_sum<F_WARPS>((int)floats_per_verb(v), t, S.warp_tmp);
-            nf_total += t;
-        }
-        if (wid == 0) {
-            uint32_t p0, p1;
-            chain_resolve(A.cf, r, (uint32_t)nf_total, 0u, A.err, p0, p1);
-            if (lane == 0) {
-                S.float_base = p0;
-                if (n_cmd > F_CMAX || give_up) S.flag = 1;
-            }
-        }
-        __syncthreads();
-        bool bail = S.flag != 0;
+        bool bail = S.flag != 0 || n_cmd > F_CMAX;
 
         uint8_t verb = V_CLOSE;
         V2 pt0 = v2(0, 0), pt1 = v2(0, 0), pt2 = v2(0, 0);
@@ -266,18 +253,17 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
         if (!bail) {
             const bool active = tid < n_cmd;
             verb = active ? __ldg(A.verbs + c0 + tid) : V_CLOSE;
-            int tot;
-            const int foff = block_excl_sum<F_WARPS>((int)floats_per_verb(verb), tot, S.warp_tmp);
+            const uint32_t foff = active ? __ldg(A.cmd_foff + c0 + tid) : 0u;
             bool ok = true;
             if (active) {
                 uint32_t f = f0;
                 if (f1 - f0 > 1) f = upper_bound_u32(A.fill_off, A.n_fills + 1, c0 + tid) - 1u;
                 const bool raw = A.fill_flags != nullptr && (__ldg(A.fill_flags + f) & OCHRE_FILL_RAW);
                 const float* xf = A.fill_xf + 6 * (size_t)f;
-                const float* fp = A.pts + S.float_base + foff;
+                const float* fp = A.pts + foff;
                 const int np = verb == V_MOVE || verb == V_LINE ? 1 : verb == V_QUAD || verb == V_CONIC ? 2
                              : verb == V_CUBIC ? 3 : 0;
-                if ((uint64_t)S.float_base + foff + floats_per_verb(verb) > A.n_floats || verb > V_CLOSE) ok = false;
+                if ((uint64_t)foff + floats_per_verb(verb) > A.n_floats || verb > V_CLOSE) ok = false;
                 if (ok && np >= 1) pt0 = load_pt(fp);
                 if (ok && np >= 2) pt1 = load_pt(fp + 2);
                 if (ok && np >= 3) pt2 = load_pt(fp + 4);
@@ -486,14 +472,15 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
         __syncthreads();
         bail = bail || S.flag != 0;
         int n_real = 0, n_tiles = 0, n_spans = 0;
+        int per = 0, t_lo = 0, srank = 0;
+        uint32_t span_bits = 0;
         if (!bail) {
             n_real = S.row_base[GDIM];
             n_tiles = n_real == 0 ? 1 : n_real;   // rasterizer.rs:194-208
             // spans (rasterizer.rs:252-265): thread tid owns a contiguous run
             // of tiles so that span ranks follow tile order
-            const int per = (n_real + FUSED_THREADS - 1) / FUSED_THREADS;   // <= 2
-            const int t_lo = tid * per;
-            uint32_t span_bits = 0;
+            per = (n_real + FUSED_THREADS - 1) / FUSED_THREADS;   // <= 2
+            t_lo = tid * per;
             int my = 0;
             const int nc = min((int)S.n_cross, F_XMAX);
             for (int k = 0; k < per; k++) {
@@ -514,64 +501,22 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                     }
                 }
             }
-            const int srank = block_excl_sum<F_WARPS>(my, n_spans, S.warp_tmp);
-            if (wid == 0) {
-                uint32_t p0, p1;
-                chain_resolve(A.co, r, (uint32_t)n_tiles, (uint32_t)n_spans, A.err, p0, p1);
-                if (lane == 0) {
-                    S.tile_base = p0;
-                    S.span_base = p1;
-                    A.raster_tile_off[r] = p0;
-                    A.raster_span_off[r] = p1;
-                    if (r + 1 == A.n_rasters) {
-                        A.raster_tile_off[r + 1] = p0 + n_tiles;
-                        A.raster_span_off[r + 1] = p1 + n_spans;
-                        A.totals[0] = p0 + n_tiles;
-                        A.totals[1] = p1 + n_spans;
-                    }
-                }
-            }
-            __syncthreads();
-            const uint32_t tb = S.tile_base, sb = S.span_base;
-            if ((uint64_t)tb + n_tiles > A.tile_cap || (uint64_t)sb + n_spans > A.span_cap) {
-                if (tid == 0) atomicOr(A.err, ERR_CAPACITY);
-                bail = true;
-            } else if (n_real == 0) {
-                // no increments: one all-zero tile at (0, 0)
-                if (tid < 16) reinterpret_cast<uint32_t*>(A.out_alpha + (size_t)tb * 64)[tid] = 0u;
-                if (A.out_cov) A.out_cov[(size_t)tb * 64 + tid] = 0.0f;
-                if (tid == 0) A.out_xy[tb] = 0u;
-            } else {
-                int sr = srank;
-                for (int k = 0; k < per; k++) {
-                    const int t = t_lo + k;
-                    if (t >= n_real) break;
-                    const int g = S.tile_g[t];
-                    const int tx = S.gx0 + (g & 31), ty = S.gy0 + (g >> 5);
-                    A.out_xy[tb + t] = (uint32_t)(uint16_t)(int16_t)(tx * 8) |
-                                       ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
-                    if (span_bits >> k & 1u) {
-                        const uint32_t right = S.touched[g >> 5] >> ((g & 31) + 1);
-                        const int gap = __ffs(right) - 1;
-                        A.span_xy[sb + sr] = (uint32_t)(uint16_t)(int16_t)((tx + 1) * 8) |
-                                             ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
-                        A.span_w[sb + sr] = (uint16_t)((uint16_t)gap * 8u);
-                        A.span_tile[sb + sr] = tb + t;
-                        sr++;
-                    }
-                }
-            }
-        } else if (wid == 0) {
-            // keep the output chain moving (the batch falls back; results are discarded)
-            uint32_t p0, p1;
-            chain_resolve(A.co, r, 0u, 0u, A.err, p0, p1);
-            if (lane == 0) atomicOr(A.fallback, 1u);
+            srank = block_excl_sum<F_WARPS>(my, n_spans, S.warp_tmp);
         }
-        __syncthreads();
+        // The raster's output counts go out now; its offsets are resolved
+        // after the coverage below, when its predecessors have long published
+        // theirs.  A raster that does not fit publishes zeros and turns the
+        // batch over to the general chain.
+        if (tid == 0) {
+            chain_publish(A.co, r, bail ? 0u : (uint32_t)n_tiles, bail ? 0u : (uint32_t)n_spans);
+            if (bail) atomicOr(A.fallback, 1u);
+        }
 
         // ---------------- C. accumulate and shade, CHUNK tiles at a time ----------------
+        // Alpha (and coverage) go to this CTA's staging slots: tile i of the
+        // raster at stage + (blockIdx.x * F_TMAX + i) * 64.
         if (!bail && n_real > 0) {
-            const uint32_t tb = S.tile_base;
+            const size_t stage0 = (size_t)blockIdx.x * F_TMAX;
             const int gx0 = S.gx0, gy0 = S.gy0;
             for (int lo = 0; lo < n_real; lo += CHUNK) {
                 const int nch = min(CHUNK, n_real - lo);
@@ -641,22 +586,84 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                     const float acc0 = S.carry[i][row] + excl;
                     const float cov0 = fabsf(acc0 + a0);
                     const float cov1 = fabsf((acc0 + h0) + a1);
-                    const uint32_t t = tb + lo + i;
+                    const size_t t = stage0 + lo + i;
                     const uint32_t al0 = f2u8(rmin(cov0 * 256.0f, 255.0f));
                     const uint32_t al1 = f2u8(rmin(cov1 * 256.0f, 255.0f));
-                    reinterpret_cast<uint16_t*>(A.out_alpha + (size_t)t * 64)[lane] = (uint16_t)(al0 | (al1 << 8));
-                    if (A.out_cov) reinterpret_cast<float2*>(A.out_cov + (size_t)t * 64)[lane] = make_float2(cov0, cov1);
+                    reinterpret_cast<uint16_t*>(A.stage_alpha + t * 64)[lane] = (uint16_t)(al0 | (al1 << 8));
+                    if (A.out_cov) reinterpret_cast<float2*>(A.stage_cov + t * 64)[lane] = make_float2(cov0, cov1);
                 }
                 __syncthreads();
+            }
+        }
+
+        // ---------------- offsets, then every output of the raster ----------------
+        if (wid == 0) {
+            uint32_t p0, p1;
+            const uint32_t a0 = bail ? 0u : (uint32_t)n_tiles, a1 = bail ? 0u : (uint32_t)n_spans;
+            chain_lookback(A.co, r, a0, a1, A.err, p0, p1);
+            if (lane == 0) {
+                S.tile_base = p0;
+                S.span_base = p1;
+                if (!bail) {
+                    A.raster_tile_off[r] = p0;
+                    A.raster_span_off[r] = p1;
+                    if (r + 1 == A.n_rasters) {
+                        A.raster_tile_off[r + 1] = p0 + n_tiles;
+                        A.raster_span_off[r + 1] = p1 + n_spans;
+                        A.totals[0] = p0 + n_tiles;
+                        A.totals[1] = p1 + n_spans;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (!bail) {
+            const uint32_t tb = S.tile_base, sb = S.span_base;
+            if ((uint64_t)tb + n_tiles > A.tile_cap || (uint64_t)sb + n_spans > A.span_cap) {
+                if (tid == 0) atomicOr(A.err, ERR_CAPACITY);
+            } else if (n_real == 0) {
+                // no increments: one all-zero tile at (0, 0)
+                if (tid < 16) reinterpret_cast<uint32_t*>(A.out_alpha + (size_t)tb * 64)[tid] = 0u;
+                if (A.out_cov && tid < 64) A.out_cov[(size_t)tb * 64 + tid] = 0.0f;
+                if (tid == 0) A.out_xy[tb] = 0u;
+            } else {
+                // staged alpha / coverage -> their final place (8-byte pieces)
+                const size_t stage0 = (size_t)blockIdx.x * F_TMAX;
+                const uint2* sa = reinterpret_cast<const uint2*>(A.stage_alpha + stage0 * 64);
+                uint2* da = reinterpret_cast<uint2*>(A.out_alpha + (size_t)tb * 64);
+                for (int q = tid; q < n_real * 8; q += FUSED_THREADS) da[q] = sa[q];
+                if (A.out_cov) {
+                    const float2* sc = reinterpret_cast<const float2*>(A.stage_cov + stage0 * 64);
+                    float2* dc = reinterpret_cast<float2*>(A.out_cov + (size_t)tb * 64);
+                    for (int q = tid; q < n_real * 32; q += FUSED_THREADS) dc[q] = sc[q];
+                }
+                int sr = srank;
+                for (int k = 0; k < per; k++) {
+                    const int t = t_lo + k;
+                    if (t >= n_real) break;
+                    const int g = S.tile_g[t];
+                    const int tx = S.gx0 + (g & 31), ty = S.gy0 + (g >> 5);
+                    A.out_xy[tb + t] = (uint32_t)(uint16_t)(int16_t)(tx * 8) |
+                                       ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
+                    if (span_bits >> k & 1u) {
+                        const uint32_t right = S.touched[g >> 5] >> ((g & 31) + 1);
+                        const int gap = __ffs(right) - 1;
+                        A.span_xy[sb + sr] = (uint32_t)(uint16_t)(int16_t)((tx + 1) * 8) |
+                                             ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
+                        A.span_w[sb + sr] = (uint16_t)((uint16_t)gap * 8u);
+                        A.span_tile[sb + sr] = tb + t;
+                        sr++;
+                    }
+                }
             }
         }
         __syncthreads();
     }
 }
 
-// One launch of a kernel shape: a persistent grid of (SMs x resident CTAs).
+// Persistent grid of a kernel shape: SMs x resident CTAs.
 template <int T, int C>
-static int launch_fused(ochre_gpu_ctx* ctx, const FusedArgs& a, cudaStream_t s) {
+static int fused_full_grid() {
     static int grid = 0;
     if (grid == 0) {
         int dev = 0, sms = 0, per = 0;
@@ -665,10 +672,42 @@ static int launch_fused(ochre_gpu_ctx* ctx, const FusedArgs& a, cudaStream_t s) 
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_raster_fused<T, C>, T, 0);
         grid = sms * (per > 0 ? per : 1);
     }
-    OCHRE_LAUNCH(ctx, "raster_fused", s, k_raster_fused<T, C><<<grid, T, 0, s>>>(a));
-    OCHRE_CUDA_TRY(cudaGetLastError());
-    return OCHRE_OK;
+    return grid;
 }
+
+// The tuned shape: with a == nullptr, its full grid into *grid; else one
+// launch over *grid CTAs.
+static int fused_shape(ochre_gpu_ctx* ctx, const FusedArgs* a, int* grid, cudaStream_t s) {
+#define OCHRE_FUSED_CASE(T, C)                                                        \
+    case T * 1000 + C:                                                                \
+        if (!a) {                                                                     \
+            *grid = fused_full_grid<T, C>();                                          \
+            return OCHRE_OK;                                                          \
+        }                                                                             \
+        OCHRE_LAUNCH(ctx, "raster_fused", s, k_raster_fused<T, C><<<*grid, T, 0, s>>>(*a)); \
+        OCHRE_CUDA_TRY(cudaGetLastError());                                           \
+        return OCHRE_OK;
+    switch (ctx->tune_fused_threads * 1000 + ctx->tune_fused_chunk) {
+        OCHRE_FUSED_CASE(64, 8)
+        OCHRE_FUSED_CASE(64, 16)
+        OCHRE_FUSED_CASE(64, 32)
+        OCHRE_FUSED_CASE(96, 8)
+        OCHRE_FUSED_CASE(96, 16)
+        OCHRE_FUSED_CASE(128, 16)
+        OCHRE_FUSED_CASE(128, 32)
+    default: return OCHRE_E_INVALID;
+    }
+#undef OCHRE_FUSED_CASE
+}
+
+struct VerbFloats {
+    const uint8_t* verbs;
+    __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return floats_per_verb(__ldg(verbs + i)); }
+};
+struct FloatOff {
+    uint32_t* off;
+    __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
+};
 
 // Runs the fused kernel over the whole batch.  *handled is false when some
 // raster does not fit (the caller then runs the general chain).
@@ -678,9 +717,22 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
     DevScalars* ds = dev_scalars(ctx);
     const uint32_t R = in->n_rasters;
     if (R == 0) return OCHRE_OK;
-    OCHRE_CUDA_TRY(ctx->fused_chain.ensure((size_t)R * 2 * sizeof(Chain)));
-    Chain* cf = ctx->fused_chain.as<Chain>();
-    Chain* co = cf + R;
+    OCHRE_CUDA_TRY(ctx->fused_chain.ensure((size_t)R * sizeof(Chain)));
+    Chain* co = ctx->fused_chain.as<Chain>();
+    // no more CTAs than rasters; each CTA stages the coverage of its raster
+    int grid = 0;
+    {
+        const int st = fused_shape(ctx, nullptr, &grid, s);
+        if (st != OCHRE_OK) return st;
+    }
+    grid = (int)std::min<uint32_t>((uint32_t)grid, R);
+    const bool want_cov = (ctx->flags & OCHRE_CTX_WANT_COV) != 0;
+    const size_t stage_tiles = (size_t)grid * F_TMAX;
+    OCHRE_CUDA_TRY(ctx->fused_stage.ensure(stage_tiles * 64 * (want_cov ? 5 : 1)));
+    // float offset of every command (the kernel reads its points there)
+    const uint64_t n_cmds = in->n_cmds;
+    OCHRE_CUDA_TRY(ctx->cmd_foff.ensure((size_t)std::max<uint64_t>(n_cmds, 1) * 4));
+    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_cmds) * sizeof(ScanStatus<uint32_t>)));
     // capacity guess: the last run's totals, else 48 tiles per raster; with
     // caller-provided (fixed) outputs, their capacity
     const bool fixed_out = ctx->out_tile_xy.fixed;
@@ -699,18 +751,24 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         const uint32_t span_cap = fixed_out ? span_cap_fixed : tile_cap;
         OCHRE_CUDA_TRY(ctx->out_tile_xy.ensure((size_t)tile_cap * 4));
         OCHRE_CUDA_TRY(ctx->out_tile_alpha.ensure((size_t)tile_cap * 64));
-        const bool want_cov = (ctx->flags & OCHRE_CTX_WANT_COV) != 0;
         if (want_cov) OCHRE_CUDA_TRY(ctx->out_tile_cov.ensure((size_t)tile_cap * 256));
         OCHRE_CUDA_TRY(ctx->out_span_xy.ensure((size_t)span_cap * 4));
         OCHRE_CUDA_TRY(ctx->out_span_w.ensure((size_t)span_cap * 2));
         OCHRE_CUDA_TRY(ctx->out_span_tile.ensure((size_t)span_cap * 4));
         OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
         OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
-        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->fused_chain.p, 0, (size_t)R * 2 * sizeof(Chain), s));
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->fused_chain.p, 0, (size_t)R * sizeof(Chain), s));
         OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+        if (n_cmds)
+            OCHRE_LAUNCH(ctx, "fused_float_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+                n_cmds, VerbFloats{in->verbs}, FloatOff{ctx->cmd_foff.as<uint32_t>()}, OpSumU32{}, 0u,
+                ctx->scan_status.p, &ds->sort_ticket, &ds->n_floats, &ds->err, s)));
         FusedArgs a;
         a.verbs = in->verbs;
         a.pts = in->pts;
+        a.cmd_foff = ctx->cmd_foff.as<uint32_t>();
+        a.stage_alpha = ctx->fused_stage.as<uint8_t>();
+        a.stage_cov = want_cov ? reinterpret_cast<float*>(ctx->fused_stage.as<uint8_t>() + stage_tiles * 64) : nullptr;
         a.fill_off = in->fill_cmd_off;
         a.fill_xf = in->fill_xf;
         a.fill_flags = in->fill_flags;
@@ -718,7 +776,6 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         a.n_fills = in->n_fills;
         a.n_rasters = R;
         a.n_floats = in->n_floats;
-        a.cf = cf;
         a.co = co;
         a.ticket = &ds->ticket;
         a.fallback = &ds->fused_fallback;
@@ -734,17 +791,7 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         a.span_tile = ctx->out_span_tile.as<uint32_t>();
         a.raster_tile_off = ctx->out_raster_tile_off.as<uint32_t>();
         a.raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
-        int st0 = OCHRE_OK;
-        switch (ctx->tune_fused_threads * 1000 + ctx->tune_fused_chunk) {
-        case 64008: st0 = launch_fused<64, 8>(ctx, a, s); break;
-        case 64016: st0 = launch_fused<64, 16>(ctx, a, s); break;
-        case 96008: st0 = launch_fused<96, 8>(ctx, a, s); break;
-        case 96016: st0 = launch_fused<96, 16>(ctx, a, s); break;
-        case 64032: st0 = launch_fused<64, 32>(ctx, a, s); break;
-        case 128016: st0 = launch_fused<128, 16>(ctx, a, s); break;
-        case 128032: st0 = launch_fused<128, 32>(ctx, a, s); break;
-        default: return OCHRE_E_INVALID;
-        }
+        const int st0 = fused_shape(ctx, &a, &grid, s);
         if (st0 != OCHRE_OK) return st0;
         if (plan) {
             // totals, fallback and errors are read after the replay

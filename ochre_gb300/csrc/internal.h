@@ -149,6 +149,7 @@ struct ochre_gpu_ctx {
     ochre::DevBuf scan_status;
     ochre::DevBuf scalars;   // DevScalars
     ochre::DevBuf fused_chain;   // fused path: per-raster look-back slots
+    ochre::DevBuf fused_stage;   // fused path: per-CTA staged alpha (and coverage) of its raster
     uint32_t fused_tile_cap = 0; // fused path: output capacity guess (tiles)
     // device outputs
     ochre::DevBuf out_tile_xy, out_tile_alpha, out_tile_cov, out_span_xy, out_span_w, out_span_tile,
