@@ -286,6 +286,14 @@ __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
 __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t* p) {
+    uint64_t v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed64(uint64_t* p, uint64_t v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
 // Look-back slots publish data with relaxed stores followed by a release
 // store of the flag; readers acquire the flag, then read the data relaxed.
 // The release/acquire pair orders the data, so no separate fence is needed.

@@ -62,14 +62,17 @@ struct FusedSmem {
     int32_t gx0, gy0, gw, gh;
 };
 
-// Per-raster look-back slots: flag (0 none, 1 aggregate, 2 inclusive) and two
-// counters in each of agg / inc.
-struct Chain {
-    uint32_t flag;
-    uint32_t agg[2];
-    uint32_t inc[2];
-    uint32_t pad[3];
-};
+// Per-raster look-back slot: one 64-bit word holding a flag (bits 62-63: 0
+// none, 1 aggregate, 2 inclusive) and two 30-bit counts (tiles in bits 0-29,
+// spans in bits 30-59).  One naturally aligned 64-bit access reads or writes
+// flag and counts together, so readers need no acquire/release pairing.
+// Counts saturate at 2^30 - 1, above every output capacity.
+constexpr uint64_t CH_AGG = 1ull << 62, CH_INC = 2ull << 62;
+constexpr uint32_t CH_MAX = (1u << 30) - 1u;
+__device__ __forceinline__ uint64_t ch_pack(uint64_t flag, uint32_t a0, uint32_t a1) {
+    return flag | ((uint64_t)min(a1, CH_MAX) << 30) | min(a0, CH_MAX);
+}
+constexpr int CH_PER_LANE = 4;   // predecessors one lane reads per look-back round
 
 // ---- block-wide scans over WARPS * 32 threads (one value each) ----
 template <int WARPS>
@@ -122,24 +125,17 @@ __device__ __forceinline__ int block_excl_max(int v, int& incl_last, int32_t (*t
 
 // Publish raster r's counts: its aggregate, or, for raster 0, its inclusive
 // value.  One thread.
-__device__ __forceinline__ void chain_publish(Chain* slots, uint32_t r, uint32_t a0, uint32_t a1) {
-    Chain* me = slots + r;
-    if (r == 0) {
-        st_relaxed(&me->inc[0], a0);
-        st_relaxed(&me->inc[1], a1);
-        st_release(&me->flag, 2u);
-    } else {
-        st_relaxed(&me->agg[0], a0);
-        st_relaxed(&me->agg[1], a1);
-        st_release(&me->flag, 1u);
-    }
+__device__ __forceinline__ void chain_publish(uint64_t* slots, uint32_t r, uint32_t a0, uint32_t a1) {
+    st_relaxed64(slots + r, ch_pack(r == 0 ? CH_INC : CH_AGG, a0, a1));
 }
 
 // Resolve raster r's exclusive prefix (its aggregate a0, a1 already
-// published) by a warp-cooperative decoupled look-back, 32 predecessors per
-// round, and publish its inclusive value.  Called by one full warp; returns
-// the prefix in every lane.  Every wait is bounded.
-__device__ __forceinline__ void chain_lookback(Chain* slots, uint32_t r, uint32_t a0, uint32_t a1, uint32_t* err,
+// published) by a warp-cooperative decoupled look-back over 32 x CH_PER_LANE
+// predecessors per round (independent loads, one latency per round), and
+// publish its inclusive value.  Predecessor q of a round (q = k * 32 + lane,
+// nearest first) is raster top - q.  Called by one full warp; returns the
+// prefix in every lane.  Every wait is bounded.
+__device__ __forceinline__ void chain_lookback(uint64_t* slots, uint32_t r, uint32_t a0, uint32_t a1, uint32_t* err,
                                                uint32_t& p0, uint32_t& p1) {
     const int lane = threadIdx.x & 31;
     p0 = 0;
@@ -148,14 +144,27 @@ __device__ __forceinline__ void chain_lookback(Chain* slots, uint32_t r, uint32_
     int64_t top = (int64_t)r - 1;   // nearest predecessor not yet summed
     long long spins = 0;
     while (top >= 0) {
-        const int64_t j = top - lane;
-        uint32_t f = 2u;   // before raster 0: an inclusive zero
-        if (j >= 0) f = ld_acquire(&slots[j].flag);
-        const uint32_t m2 = __ballot_sync(0xffffffffu, f == 2u);
-        const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
-        const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
-        const uint32_t m0 = __ballot_sync(0xffffffffu, f == 0u);
-        if (m0 & need) {
+        uint64_t w[CH_PER_LANE];
+#pragma unroll
+        for (int k = 0; k < CH_PER_LANE; k++) {
+            const int64_t j = top - (k * 32 + lane);
+            w[k] = j >= 0 ? ld_relaxed64(slots + j) : CH_INC;   // before raster 0: an inclusive zero
+        }
+        // nearest inclusive predecessor of the round: q_inc (32 * CH_PER_LANE if none)
+        int q_inc = 32 * CH_PER_LANE;
+#pragma unroll
+        for (int k = CH_PER_LANE - 1; k >= 0; k--) {
+            const uint32_t m2 = __ballot_sync(0xffffffffu, (w[k] >> 62) == 2u);
+            if (m2) q_inc = k * 32 + __ffs(m2) - 1;
+        }
+        // every predecessor up to it must have published
+        bool missing = false;
+#pragma unroll
+        for (int k = 0; k < CH_PER_LANE; k++) {
+            const bool need = k * 32 + lane <= q_inc;
+            if (__ballot_sync(0xffffffffu, need && (w[k] >> 62) == 0u)) missing = true;
+        }
+        if (missing) {
             if (++spins > SPIN_LIMIT) {
                 if (lane == 0) atomicOr(err, ERR_TIMEOUT);
                 break;
@@ -164,10 +173,12 @@ __device__ __forceinline__ void chain_lookback(Chain* slots, uint32_t r, uint32_
             continue;
         }
         uint32_t v0 = 0, v1 = 0;
-        if (lane <= limit && j >= 0) {
-            const uint32_t* src = f == 2u ? slots[j].inc : slots[j].agg;
-            v0 = ld_relaxed(src);
-            v1 = ld_relaxed(src + 1);
+#pragma unroll
+        for (int k = 0; k < CH_PER_LANE; k++) {
+            if (k * 32 + lane <= q_inc) {
+                v0 += (uint32_t)(w[k] & CH_MAX);
+                v1 += (uint32_t)((w[k] >> 30) & CH_MAX);
+            }
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) {
@@ -176,15 +187,12 @@ __device__ __forceinline__ void chain_lookback(Chain* slots, uint32_t r, uint32_
         }
         p0 += v0;
         p1 += v1;
-        if (m2) break;
-        top -= 32;
+        if (q_inc < 32 * CH_PER_LANE) break;
+        top -= 32 * CH_PER_LANE;
     }
-    if (lane == 0) {
-        Chain* me = slots + r;
-        st_relaxed(&me->inc[0], p0 + a0);
-        st_relaxed(&me->inc[1], p1 + a1);
-        st_release(&me->flag, 2u);
-    }
+    p0 = min(p0, CH_MAX);
+    p1 = min(p1, CH_MAX);
+    if (lane == 0) st_relaxed64(slots + r, ch_pack(CH_INC, p0 + a0, p1 + a1));
 }
 
 struct FusedArgs {
@@ -197,7 +205,7 @@ struct FusedArgs {
     const uint32_t* raster_off;
     uint32_t n_fills, n_rasters;
     uint64_t n_floats;
-    Chain* co;               // output tiles / spans
+    uint64_t* co;            // look-back slots of the output tiles / spans
     uint32_t* ticket;
     uint32_t* fallback;      // any raster did not fit
     uint32_t* err;
@@ -717,8 +725,8 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
     DevScalars* ds = dev_scalars(ctx);
     const uint32_t R = in->n_rasters;
     if (R == 0) return OCHRE_OK;
-    OCHRE_CUDA_TRY(ctx->fused_chain.ensure((size_t)R * sizeof(Chain)));
-    Chain* co = ctx->fused_chain.as<Chain>();
+    OCHRE_CUDA_TRY(ctx->fused_chain.ensure((size_t)R * sizeof(uint64_t)));
+    uint64_t* co = ctx->fused_chain.as<uint64_t>();
     // no more CTAs than rasters; each CTA stages the coverage of its raster
     int grid = 0;
     {
@@ -757,7 +765,7 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         OCHRE_CUDA_TRY(ctx->out_span_tile.ensure((size_t)span_cap * 4));
         OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
         OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
-        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->fused_chain.p, 0, (size_t)R * sizeof(Chain), s));
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->fused_chain.p, 0, (size_t)R * sizeof(uint64_t), s));
         OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
         if (n_cmds)
             OCHRE_LAUNCH(ctx, "fused_float_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
