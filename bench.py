@@ -98,8 +98,11 @@ def kernel_bytes(name: str, st: dict, batch) -> int:
     if name == "span_scan":
         return T * 4 + T * 8 + N * 10 + R * 4
     if name == "raster_fused":
-        # the whole path in one kernel: compulsory input + output bytes
-        return batch.input_bytes() + 4 * (batch.n_fills + 1) + 68 * T + 10 * N + 8 * (R + 1)
+        # the whole path in one kernel: compulsory input + output bytes, and
+        # the float offset of every command (from the command scan)
+        return batch.input_bytes() + 4 * (batch.n_fills + 1) + 4 * C + 68 * T + 10 * N + 8 * (R + 1)
+    if name == "fused_float_scan":
+        return C * 1 + C * 4
     return 0
 
 
