@@ -101,3 +101,71 @@ def test_render_svg_matches_oracle():
     assert np.array_equal(img, ref)
     # the scene actually drew something in each part of the canvas
     assert (img[:, :, :3] != 255).any(axis=2).mean() > 0.5
+
+
+# The reference's own example documents (examples/res/*.svg), read where the
+# reference tree is present; nothing of them is stored in this repository.
+REF_SVG_DIR = "/root/reference/examples/res"
+REF_SVGS = ["Ghostscript_Tiger.svg", "calabi-yau.svg", "lorem-ipsum.svg"]
+
+
+@pytest.mark.parametrize("name", REF_SVGS)
+def test_reference_example_documents(name):
+    import os
+
+    import oracle
+    import oracle_py
+    path = os.path.join(REF_SVG_DIR, name)
+    if not os.path.exists(path):
+        pytest.skip("reference example documents not present")
+    with open(path) as f:
+        text = f.read()
+    paints, _ = svg.load_svg(text)
+    # every <path> element becomes at least one paint (fill and/or stroke)
+    assert len(paints) >= text.count("<path")
+    assert all(p.path for p in paints)
+    batch, colors = svg.paints_to_batch(paints)
+    batch.validate()
+    r = oracle.run(batch, threads=8)
+    assert r["status"] == 0 and len(r["tile_xy"]) > 0
+    # the independent numpy restatement agrees bit for bit on a sample
+    step = max(1, batch.n_rasters // 24)
+    for i in range(0, batch.n_rasters, step):
+        tiles, spans, _ = oracle_py.rasterize(oracle_py.commands_of_batch(batch, i))
+        a, b = int(r["raster_tile_off"][i]), int(r["raster_tile_off"][i + 1])
+        assert [tuple(t) for t in r["tile_xy"][a:b].tolist()] == [t[:2] for t in tiles], (name, i)
+        alpha = np.array([np.frombuffer(t[2], np.uint8) for t in tiles]).reshape(-1, 64)
+        assert np.array_equal(r["tile_alpha"][a:b], alpha), (name, i)
+        c, d = int(r["raster_span_off"][i]), int(r["raster_span_off"][i + 1])
+        assert d - c == len(spans), (name, i)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", REF_SVGS)
+def test_reference_example_documents_gpu(name):
+    """GPU rasterization and compositing of the reference's example documents
+    against the oracle.  The documents are read from the directory named by
+    OCHRE_SVG_DIR (skipped when unset)."""
+    import os
+
+    import oracle
+    from compare import compare
+    from ochre_gb300 import DeviceBatch, default_context
+    d = os.environ.get("OCHRE_SVG_DIR")
+    if not d or not os.path.exists(os.path.join(d, name)):
+        pytest.skip("OCHRE_SVG_DIR does not hold the document")
+    with open(os.path.join(d, name)) as f:
+        text = f.read()
+    paints, (w, h) = svg.load_svg(text)
+    batch, colors = svg.paints_to_batch(paints)
+    ref = oracle.run(batch, threads=8)
+    ctx = default_context()
+    got = ctx.device_result_to_numpy(ctx.rasterize_device(DeviceBatch(batch)), batch.n_rasters)
+    compare(got, ref, batch.n_rasters)
+    W, H = int(w or 1024), int(h or 1024)
+    img = svg.render_svg(text, W, H)
+    want = oracle.composite(ref, batch.n_rasters, colors, W, H)
+    # alpha may differ by 1 LSB (summation order), which can move a blended
+    # channel by a step per layer drawn over it
+    diff = np.abs(img.astype(np.int16) - want.astype(np.int16))
+    assert diff.max() <= 2 and (diff > 0).mean() < 0.01, (int(diff.max()), float((diff > 0).mean()))
