@@ -74,6 +74,8 @@ def kernel_bytes(name: str, st: dict, batch) -> int:
     kb = 8 if st["key_bits"] > 32 else 4
     if name == "cmd_scan":
         return C * 1 + C * 12
+    if name == "flatten_count":
+        return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 12 + C * 4
     if name == "flatten_count_scan":
         return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 12 + C * 4
     if name == "flatten_emit":

@@ -115,6 +115,20 @@ struct OffOut {
     uint32_t* off;
     __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
 };
+struct Load32 {
+    const uint32_t* v;
+    __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return v[i]; }
+};
+
+// One thread per command: the line counts of a batch with few commands
+// (a scan would give each of a handful of threads eight serial t loops).
+template <class In>
+__global__ void __launch_bounds__(128) k_count_each(uint64_t n, In in, uint32_t* __restrict__ out) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in(i);
+}
+// Below this many scan tiles the counts get their own kernel.
+constexpr uint64_t SPLIT_COUNT_TILES = 256;
 
 __global__ void k_cmd_emit(BatchView b, const uint32_t* __restrict__ line_off, uint32_t n_lines_cap,
                            float4* __restrict__ lines, uint32_t* __restrict__ line_raster, uint32_t* err) {
@@ -169,9 +183,19 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
     BatchView b{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                 in->n_fills, in->n_rasters, n, ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
                 ctx->cmd_ep.as<uint32_t>()};
-    OCHRE_LAUNCH(ctx, "flatten_count_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(n, CountIn{b, &ds->err}, OffOut{ctx->cmd_line_off.as<uint32_t>()},
-                                         OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_lines,
-                                         &ds->err, s)));
+    if (scan_tiles(n) < SPLIT_COUNT_TILES) {
+        // counts first (one thread per command), then the offsets in place
+        OCHRE_LAUNCH(ctx, "flatten_count", s, k_count_each<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
+            n, CountIn{b, &ds->err}, ctx->cmd_line_off.as<uint32_t>()));
+        OCHRE_CUDA_TRY(cudaGetLastError());
+        OCHRE_LAUNCH(ctx, "flatten_count_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+            n, Load32{ctx->cmd_line_off.as<uint32_t>()}, OffOut{ctx->cmd_line_off.as<uint32_t>()}, OpSumU32{}, 0u,
+            ctx->scan_status.p, &ds->ticket, &ds->n_lines, &ds->err, s)));
+    } else {
+        OCHRE_LAUNCH(ctx, "flatten_count_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
+            n, CountIn{b, &ds->err}, OffOut{ctx->cmd_line_off.as<uint32_t>()}, OpSumU32{}, 0u, ctx->scan_status.p,
+            &ds->ticket, &ds->n_lines, &ds->err, s)));
+    }
     uint32_t L;
     if (plan) {
         // the line count stays on the device; above the plan it is zeroed
