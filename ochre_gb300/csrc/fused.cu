@@ -44,9 +44,16 @@ constexpr int F_XMAX = 256;             // tile-row crossings per raster
 template <int THREADS, int CHUNK>
 struct FusedSmem {
     float4 lines[F_LMAX];
-    float acc[CHUNK][128];         // [tile][64 area | 64 height]
-    uint32_t cross[F_XMAX];        // grid tile << 16 | sign (i16)
-    V2 ep[THREADS];                // transformed end point (or Move point) per command
+    // The coverage accumulators and the data of the earlier phases are
+    // never live together: they share storage (more CTAs per SM).
+    struct Early {
+        V2 ep[THREADS];            // transformed end point (or Move point) per command
+        uint32_t cross[F_XMAX];    // grid tile << 16 | sign (i16)
+    };
+    union {
+        float acc[CHUNK][128];     // [tile][64 area | 64 height]
+        Early early;
+    } u;
     uint16_t line_g0[F_LMAX], line_g1[F_LMAX];   // grid-tile range of each line's cells
     uint16_t tile_g[F_TMAX];       // tile slot -> grid tile (row-major order)
     uint32_t touched[GDIM];        // one word per grid row
@@ -285,7 +292,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                     wgt = __ldg(fp + 4);
                     if (!isfinite(wgt)) ok = false;
                 }
-                S.ep[tid] = verb == V_CUBIC ? pt2 : (verb == V_QUAD || verb == V_CONIC) ? pt1 : pt0;
+                S.u.early.ep[tid] = verb == V_CUBIC ? pt2 : (verb == V_QUAD || verb == V_CONIC) ? pt1 : pt0;
             }
             if (!ok) atomicOr(A.err, ERR_INVALID);
             // last: endpoint of the most recent earlier non-Close command;
@@ -294,12 +301,12 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
             const int ep_ex = block_excl_max<F_WARPS>(active && verb != V_CLOSE ? tid : -1, ep_last, S.warp_tmp);
             const int mv_ex = block_excl_max<F_WARPS>(active && verb == V_MOVE ? tid : -1, mv_last, S.warp_tmp);
             if (active) {
-                last = ep_ex >= 0 ? S.ep[ep_ex] : v2(0, 0);
-                first = mv_ex >= 0 ? S.ep[mv_ex] : v2(0, 0);
+                last = ep_ex >= 0 ? S.u.early.ep[ep_ex] : v2(0, 0);
+                first = mv_ex >= 0 ? S.u.early.ep[mv_ex] : v2(0, 0);
                 is_last_cmd = tid == n_cmd - 1;
                 if (is_last_cmd) {
-                    last_end = ep_last >= 0 ? S.ep[ep_last] : v2(0, 0);
-                    first_end = mv_last >= 0 ? S.ep[mv_last] : v2(0, 0);
+                    last_end = ep_last >= 0 ? S.u.early.ep[ep_last] : v2(0, 0);
+                    first_end = mv_last >= 0 ? S.u.early.ep[mv_last] : v2(0, 0);
                 }
                 bool capped = false;
                 switch (verb) {
@@ -437,7 +444,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                             if ((unsigned)gx >= (unsigned)gw || (unsigned)gy >= (unsigned)gh) { out = true; return; }
                             const uint32_t c = atomicAdd(&S.n_cross, 1u);
                             if (c < (uint32_t)F_XMAX)
-                                S.cross[c] = ((uint32_t)(gy * GDIM + gx) << 16) | ((uint32_t)sign & 0xffffu);
+                                S.u.early.cross[c] = ((uint32_t)(gy * GDIM + gx) << 16) | ((uint32_t)sign & 0xffffu);
                             else
                                 out = true;
                         },
@@ -500,7 +507,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                 if (right != 0u && !(right & 1u)) {
                     int w = 0;
                     for (int c = 0; c < nc; c++) {
-                        const uint32_t e = S.cross[c];
+                        const uint32_t e = S.u.early.cross[c];
                         if ((int)(e >> 16) <= g) w += (int)(int16_t)(e & 0xffffu);
                     }
                     if (w != 0) {
@@ -529,7 +536,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
             for (int lo = 0; lo < n_real; lo += CHUNK) {
                 const int nch = min(CHUNK, n_real - lo);
                 const int g_lo = S.tile_g[lo], g_hi = S.tile_g[lo + nch - 1];
-                for (int q = tid; q < nch * 128; q += FUSED_THREADS) (&S.acc[0][0])[q] = 0.0f;
+                for (int q = tid; q < nch * 128; q += FUSED_THREADS) (&S.u.acc[0][0])[q] = 0.0f;
                 __syncthreads();
                 // walk the lines touching the chunk again, scatter-adding the
                 // increments of its tiles (rasterizer.rs:97-106, 223-228)
@@ -546,8 +553,8 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                             float area, height;
                             walk_increment(w, s, area, height);
                             const int cell = ((s.y & 7) << 3) | (s.x & 7);
-                            atomicAdd(&S.acc[i][cell], area);
-                            atomicAdd(&S.acc[i][64 + cell], height);
+                            atomicAdd(&S.u.acc[i][cell], area);
+                            atomicAdd(&S.u.acc[i][64 + cell], height);
                         },
                         [&](int, int, int) {}, [&](int, int) {});
                 }
@@ -555,7 +562,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                 // row sums, then carries along grid rows (rasterizer.rs:232-250)
                 for (int q = tid; q < nch * 8; q += FUSED_THREADS) {
                     const int i = q >> 3, y = q & 7;
-                    const float* h = S.acc[i] + 64 + y * 8;
+                    const float* h = S.u.acc[i] + 64 + y * 8;
                     float rs = 0.0f;
 #pragma unroll
                     for (int x = 0; x < 8; x++) rs += h[x];
@@ -581,7 +588,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                 __syncthreads();
                 const int row = lane >> 2, c0 = 2 * lane;
                 for (int i = wid; i < nch; i += F_WARPS) {
-                    const float* acc = S.acc[i];
+                    const float* acc = S.u.acc[i];
                     const float a0 = acc[c0], a1 = acc[c0 + 1];
                     const float h0 = acc[64 + c0];
                     float incl = h0 + acc[64 + c0 + 1];
