@@ -597,7 +597,9 @@ def run_ours(args, ws, rank, local):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 126 MB L2
     # launch shapes: the project's autotuner on a sample of this workload
     from ochre_gb300 import autotune
-    sample = make_workload(args.workload, min(args.n_paths, 20_000), args.seed + 7)
+    # (large enough that each persistent CTA takes tens of rasters, as in the
+    # full step, so that tail effects rank the shapes as the step does)
+    sample = make_workload(args.workload, min(args.n_paths, 50_000), args.seed + 7)
     tuned = autotune.tune(ctx, fused_sample=sample)
 
     for _ in range(max(3, args.warmup)):

@@ -128,3 +128,24 @@ def test_graph_rejects_strokes(gpu_ctx):
     b = W.stroke_run(n_paths=10)
     with pytest.raises(OchreError):
         gpu_ctx.graph(DeviceBatch(b))
+
+
+def test_graph_with_coverage_output():
+    """A graph of a context that also writes pre-quantisation coverage
+    (fused and chain plans): coverage identical to the eager call."""
+    from ochre_gb300 import DeviceBatch, GpuContext
+    for chain_only, b in ((False, W.glyph_run(n_paths=300, seed=4)), (True, W.diff_union())):
+        ctx = GpuContext(0, want_cov=True, chain_only=chain_only)
+        try:
+            db = DeviceBatch(b)
+            eager = ctx.device_result_to_numpy(ctx.rasterize_device(db), b.n_rasters)
+            g = ctx.graph(db)
+            try:
+                got = g.rasterize()
+                assert g.info()["fused"] == (not chain_only)
+                for k in ("tile_xy", "tile_alpha", "tile_cov", "span_xy", "raster_tile_off"):
+                    assert np.array_equal(got[k], eager[k]), (chain_only, k)
+            finally:
+                g.close()
+        finally:
+            ctx.close()
