@@ -11,10 +11,13 @@ pytestmark = pytest.mark.gpu
 
 
 def _run(batch, colors, w, h, canvas=None, ctx_kw=None):
+    """GPU rasterization + GPU compositing; returns the image and the
+    rasterization result (numpy)."""
     import torch
     from ochre_gb300 import DeviceBatch, GpuContext
     ctx = GpuContext(0, **(ctx_kw or {}))
     r = ctx.rasterize_device(DeviceBatch(batch, 0))
+    res = ctx.device_result_to_numpy(r, batch.n_rasters)
     cv = torch.full((h, w, 4), 255, dtype=torch.uint8, device="cuda:0") if canvas is None else \
         torch.as_tensor(canvas, device="cuda:0").contiguous()
     col = torch.as_tensor(np.ascontiguousarray(colors, np.uint8), device="cuda:0")
@@ -22,7 +25,21 @@ def _run(batch, colors, w, h, canvas=None, ctx_kw=None):
     torch.cuda.synchronize()
     out = cv.cpu().numpy()
     ctx.close()
-    return out
+    return out, res
+
+
+def _check(batch, colors, w, h, canvas=None):
+    """The rasterization against the oracle (structure exact, alpha within
+    1 LSB), and the compositing bit-exact against the oracle's compositing of
+    the same rasterization (so a 1-LSB alpha difference cannot show up as a
+    compositing difference)."""
+    from compare import compare
+    got, res = _run(batch, colors, w, h, canvas)
+    compare(res, oracle.run(batch, threads=8), batch.n_rasters)
+    ref = oracle.composite(res, batch.n_rasters, colors, w, h, canvas)
+    assert got.shape == ref.shape
+    assert np.array_equal(got, ref), int((got != ref).any(axis=2).sum())
+    return got
 
 
 @pytest.mark.parametrize("name,gen,kw,w,h", [
@@ -35,10 +52,7 @@ def test_composite_matches_oracle(name, gen, kw, w, h):
     b = gen(**kw)
     rng = np.random.default_rng(1)
     colors = rng.integers(0, 256, size=(b.n_rasters, 4), dtype=np.uint8)
-    got = _run(b, colors, w, h)
-    ref = oracle.composite(oracle.run(b, threads=8), b.n_rasters, colors, w, h)
-    assert got.shape == ref.shape
-    assert np.array_equal(got, ref), int((got != ref).any(axis=2).sum())
+    _check(b, colors, w, h)
 
 
 def test_composite_overlaps_in_raster_order():
@@ -51,6 +65,4 @@ def test_composite_overlaps_in_raster_order():
     b = bb.build()
     colors = np.array([[(37 * k) % 256, (91 * k) % 256, (53 * k + 7) % 256, 40 + 15 * k] for k in range(12)], np.uint8)
     canvas = np.random.default_rng(2).integers(0, 256, size=(70, 70, 4), dtype=np.uint8)
-    got = _run(b, colors, 70, 70, canvas)
-    ref = oracle.composite(oracle.run(b), b.n_rasters, colors, 70, 70, canvas)
-    assert np.array_equal(got, ref)
+    _check(b, colors, 70, 70, canvas)

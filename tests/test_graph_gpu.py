@@ -21,6 +21,17 @@ def _scaled(b, k):
     return dataclasses.replace(b, fill_xf=xf)
 
 
+def _same_as_eager(got, eager):
+    """Tile/span structure identical; alpha within 1 LSB and coverage within
+    1e-5 (shared-memory atomics add a tile's increments in no fixed order)."""
+    for k in ("tile_xy", "span_xy", "span_w", "span_tile", "raster_tile_off", "raster_span_off"):
+        assert np.array_equal(got[k], eager[k]), k
+    d = np.abs(got["tile_alpha"].astype(np.int16) - eager["tile_alpha"].astype(np.int16))
+    assert d.size == 0 or d.max() <= 1
+    if "tile_cov" in eager:
+        assert np.abs(got["tile_cov"] - eager["tile_cov"]).max(initial=0.0) <= 1e-5
+
+
 def _check(ctx, g, b):
     got = g.rasterize()
     compare(got, oracle.run(b, threads=8), b.n_rasters)
@@ -38,8 +49,7 @@ def test_golden_graph_matches_eager(any_ctx, name):
         for _ in range(3):   # replays are repeatable
             got = g.rasterize()
             compare(got, exp, b.n_rasters)
-            for k in ("tile_xy", "tile_alpha", "span_xy", "span_w", "raster_tile_off", "raster_span_off"):
-                assert np.array_equal(got[k], eager[k]), k
+            _same_as_eager(got, eager)
         assert g.info()["replans"] == 0
     finally:
         g.close()
@@ -143,8 +153,7 @@ def test_graph_with_coverage_output():
             try:
                 got = g.rasterize()
                 assert g.info()["fused"] == (not chain_only)
-                for k in ("tile_xy", "tile_alpha", "tile_cov", "span_xy", "raster_tile_off"):
-                    assert np.array_equal(got[k], eager[k]), (chain_only, k)
+                _same_as_eager(got, eager)
             finally:
                 g.close()
         finally:
