@@ -77,7 +77,8 @@ def tune(ctx, fused_sample=None, chain_sample=None, reps: int = 3, save: bool = 
     from . import workloads as W
     fused_sample = fused_sample if fused_sample is not None else W.glyph_run(n_paths=20_000, seed=99)
     # the chain's heavy case: paths too large for the fused kernel, many tile rows
-    chain_sample = chain_sample if chain_sample is not None else W.uneven_mix(n_paths=1000, seed=99)
+    # (4,000 paths: on 1,000 the tiles-per-warp ranking flips from run to run)
+    chain_sample = chain_sample if chain_sample is not None else W.uneven_mix(n_paths=4000, seed=99)
     t0 = time.time()
     report = {"fused": {}, "chain": {}}
     old_chain = ctx.chain_only
