@@ -12,17 +12,12 @@
 #include "common.cuh"
 #include "flatten.cuh"
 #include "scan.cuh"
-#include <atomic>
-
 #include "internal.h"
 
 namespace ochre {
 
-std::atomic<uint64_t> g_dev_allocs{0};
-
 cudaError_t DevBuf::ensure(size_t bytes) {
     if (bytes <= cap && p != nullptr) return cudaSuccess;
-    g_dev_allocs.fetch_add(1, std::memory_order_relaxed);
     if (fixed) {
         if (arena != nullptr) arena->overflow = true;
         return cudaErrorMemoryAllocation;
@@ -354,7 +349,24 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
-    DevBuf* dev[] = {&ctx->in_verbs, &ctx->in_pts, &ctx->in_fill_off, &ctx->in_fill_xf, &ctx->in_fill_flags,
+    for (DevBuf* b : device_buffers(ctx)) b->release();
+    HostBuf* host[] = {&ctx->h_scalars, &ctx->h_tile_xy, &ctx->h_tile_alpha, &ctx->h_tile_cov, &ctx->h_span_xy,
+                       &ctx->h_span_w, &ctx->h_span_tile, &ctx->h_raster_tile_off, &ctx->h_raster_span_off};
+    for (HostBuf* b : host) b->release();
+    for (auto& p : ctx->prof) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+}  // extern "C"
+
+namespace ochre {
+
+std::vector<DevBuf*> device_buffers(ochre_gpu_ctx* ctx) {
+    return {&ctx->in_verbs, &ctx->in_pts, &ctx->in_fill_off, &ctx->in_fill_xf, &ctx->in_fill_flags,
                      &ctx->in_raster_off, &ctx->cmd_foff, &ctx->cmd_mv, &ctx->cmd_ep, &ctx->cmd_line_off,
                      &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->raster_bbox, &ctx->raster_keybase,
                      &ctx->raster_empty, &ctx->raster_wsum, &ctx->raster_wbase, &ctx->tile_head_bins,
@@ -369,17 +381,11 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
                      &ctx->out_tile_xy,
                      &ctx->out_tile_alpha, &ctx->out_tile_cov, &ctx->out_span_xy, &ctx->out_span_w,
                      &ctx->out_span_tile, &ctx->out_raster_tile_off, &ctx->out_raster_span_off};
-    for (DevBuf* b : dev) b->release();
-    HostBuf* host[] = {&ctx->h_scalars, &ctx->h_tile_xy, &ctx->h_tile_alpha, &ctx->h_tile_cov, &ctx->h_span_xy,
-                       &ctx->h_span_w, &ctx->h_span_tile, &ctx->h_raster_tile_off, &ctx->h_raster_span_off};
-    for (HostBuf* b : host) b->release();
-    for (auto& p : ctx->prof) {
-        cudaEventDestroy(p.a);
-        cudaEventDestroy(p.b);
-    }
-    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
-    delete ctx;
 }
+
+}  // namespace ochre
+
+extern "C" {
 
 int ochre_gpu_set_flags(ochre_gpu_ctx* ctx, uint32_t flags) {
     if (!ctx) return OCHRE_E_INVALID;

@@ -28,6 +28,7 @@
 #include <cmath>
 #include <cstring>
 #include <new>
+#include <vector>
 
 struct ochre_graph {
     ochre_gpu_ctx* ctx = nullptr;   // private context (buffers, stream, scalars)
@@ -83,6 +84,15 @@ int planned_body(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s) {
     return copy_scalars_async(ctx, s);
 }
 
+// The context's device buffer addresses, sorted (the sort swaps its key and
+// value buffers between passes, which keeps this set).
+std::vector<void*> buffer_set(ochre_gpu_ctx* ctx) {
+    std::vector<void*> v;
+    for (const DevBuf* b : device_buffers(ctx)) v.push_back(b->p);
+    std::sort(v.begin(), v.end());
+    return v;
+}
+
 void drop_graph(ochre_graph* g) {
     if (g->exec) cudaGraphExecDestroy(g->exec);
     if (g->graph) cudaGraphDestroy(g->graph);
@@ -131,14 +141,14 @@ int build(ochre_graph* g) {
         ctx->plan = nullptr;
         return OCHRE_E_CUDA;
     }
-    const uint64_t allocs = g_dev_allocs.load();
+    const std::vector<void*> before = buffer_set(ctx);
     st = planned_body(ctx, &g->batch, s);
     cudaGraph_t graph = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(s, &graph);
     ctx->plan = nullptr;
     // a buffer that grew during the capture would leave earlier nodes on its
     // freed memory: the sizing run must have made every allocation
-    if (st == OCHRE_OK && g_dev_allocs.load() != allocs) st = OCHRE_E_CUDA;
+    if (st == OCHRE_OK && buffer_set(ctx) != before) st = OCHRE_E_CUDA;
     if (st != OCHRE_OK || ce != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         cudaGetLastError();

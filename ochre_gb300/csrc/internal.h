@@ -5,7 +5,6 @@
 
 #include <cstddef>
 #include <cstdint>
-#include <atomic>
 #include <vector>
 
 #include "../../include/ochre_gpu.h"
@@ -224,9 +223,9 @@ cudaError_t launch_plan_cap(ochre_gpu_ctx* ctx, uint32_t* count, uint32_t cap, c
 int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);
 // The same copy, enqueued only.
 int copy_scalars_async(ochre_gpu_ctx* ctx, cudaStream_t s);
-// Device allocations made by DevBuf::ensure so far (a graph capture must
-// make none: its nodes keep the pointers they saw).
-extern std::atomic<uint64_t> g_dev_allocs;
+// Every device buffer of a context (release on destroy; a graph capture
+// checks that none of them moved).
+std::vector<DevBuf*> device_buffers(ochre_gpu_ctx* ctx);
 inline DevScalars* dev_scalars(ochre_gpu_ctx* ctx) { return ctx->scalars.as<DevScalars>(); }
 inline DevScalars* host_scalars(ochre_gpu_ctx* ctx) { return ctx->h_scalars.as<DevScalars>(); }
 int check_device_error(ochre_gpu_ctx* ctx);
