@@ -764,7 +764,9 @@ def run_ours(args, ws, rank, local):
         "stroke": extensions.get("stroke"),
         "graph": extensions.get("graph"),
         "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s,
+                "note": "pinned host inputs: points read by the kernels in place over the host link, the "
+                        "other arrays copied; outputs written by the kernels into mapped host memory"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

@@ -131,6 +131,12 @@ cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_b
     return cudaGetLastError();
 }
 
+void wait_inputs(ochre_gpu_ctx* ctx, cudaStream_t s) {
+    if (!ctx->pts_pending) return;
+    cudaStreamWaitEvent(s, ctx->ev_pts, 0);
+    ctx->pts_pending = false;
+}
+
 int copy_scalars_async(ochre_gpu_ctx* ctx, cudaStream_t s) {
     static_assert(sizeof(DevScalars) / 4 <= 64, "one word per thread of k_copy_words");
     if (ctx->h_scalars_dev) {
@@ -357,6 +363,12 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
         cudaEventDestroy(p.a);
         cudaEventDestroy(p.b);
     }
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    if (ctx->ev_prior) cudaEventDestroy(ctx->ev_prior);
+    if (ctx->ev_pts) cudaEventDestroy(ctx->ev_pts);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -414,8 +426,52 @@ int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result*
     OCHRE_CUDA_TRY(ctx->in_pts.ensure(in->n_floats * 4));
     OCHRE_CUDA_TRY(ctx->in_fill_off.ensure(((size_t)in->n_fills + 1) * 4));
     OCHRE_CUDA_TRY(ctx->in_fill_xf.ensure((size_t)in->n_fills * 24));
+    // Whatever leaves this call, the point copy has finished and the run's
+    // stream is past it (the caller may free or reuse its arrays).
+    struct JoinInputs {
+        ochre_gpu_ctx* ctx;
+        cudaStream_t s;
+        ~JoinInputs() {
+            if (ctx->pts_pending) {
+                wait_inputs(ctx, s);
+                cudaStreamSynchronize(s);
+            }
+        }
+    } join{ctx, s};
+    // A large point array already in pinned host memory is read by the
+    // kernels in place (over the C2C link, overlapped with their work);
+    // otherwise it goes on a copy stream, so that the other copies and the
+    // stages before the first read of points (command and float-offset scans,
+    // clears) overlap it.
+    const size_t pts_bytes = (size_t)in->n_floats * 4;
+    const float* pts_in_place = nullptr;
+    if (pts_bytes >= ((size_t)4 << 20)) {
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, in->pts) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+            pa.devicePointer != nullptr)
+            pts_in_place = static_cast<const float*>(pa.devicePointer);
+        cudaGetLastError();
+    }
+    bool pts_async = pts_in_place == nullptr && pts_bytes >= ((size_t)4 << 20);
+    if (pts_async && !ctx->copy_stream) {
+        if (cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_prior, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_pts, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            pts_async = false;
+        }
+    }
+    if (pts_async) {
+        // after everything already queued on the run's stream (earlier runs read in_pts)
+        OCHRE_CUDA_TRY(cudaEventRecord(ctx->ev_prior, s));
+        OCHRE_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_prior, 0));
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_pts.p, in->pts, pts_bytes, cudaMemcpyHostToDevice, ctx->copy_stream));
+        OCHRE_CUDA_TRY(cudaEventRecord(ctx->ev_pts, ctx->copy_stream));
+        ctx->pts_pending = true;
+    } else if (in->n_floats && !pts_in_place) {
+        OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_pts.p, in->pts, pts_bytes, cudaMemcpyHostToDevice, s));
+    }
     if (in->n_cmds) OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_verbs.p, in->verbs, in->n_cmds, cudaMemcpyHostToDevice, s));
-    if (in->n_floats) OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_pts.p, in->pts, in->n_floats * 4, cudaMemcpyHostToDevice, s));
     if (in->fill_cmd_off)
         OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_fill_off.p, in->fill_cmd_off, ((size_t)in->n_fills + 1) * 4,
                                        cudaMemcpyHostToDevice, s));
@@ -424,7 +480,7 @@ int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result*
     if (in->n_fills)
         OCHRE_CUDA_TRY(cudaMemcpyAsync(ctx->in_fill_xf.p, in->fill_xf, (size_t)in->n_fills * 24, cudaMemcpyHostToDevice, s));
     d.verbs = ctx->in_verbs.as<uint8_t>();
-    d.pts = ctx->in_pts.as<float>();
+    d.pts = pts_in_place ? pts_in_place : ctx->in_pts.as<float>();
     d.fill_cmd_off = ctx->in_fill_off.as<uint32_t>();
     d.fill_xf = ctx->in_fill_xf.as<float>();
     if (in->fill_flags) {

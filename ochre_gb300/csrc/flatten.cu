@@ -180,6 +180,7 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
         if (st != OCHRE_OK) return st;
     }
 
+    wait_inputs(ctx, s);   // the counts read points
     BatchView b{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                 in->n_fills, in->n_rasters, n, ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
                 ctx->cmd_ep.as<uint32_t>()};

@@ -806,6 +806,7 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         a.span_tile = ctx->out_span_tile.as<uint32_t>();
         a.raster_tile_off = ctx->out_raster_tile_off.as<uint32_t>();
         a.raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
+        wait_inputs(ctx, s);   // the kernel reads points
         const int st0 = fused_shape(ctx, &a, &grid, s);
         if (st0 != OCHRE_OK) return st0;
         if (plan) {

@@ -178,6 +178,13 @@ struct ochre_gpu_ctx {
     int tune_chain_tiles_per_warp = 8;
     int tune_chain_coverage_form = 0;   // 0: by row count, 1: block form, 2: row form
 
+    // Host-batch entry: a large point array is copied on copy_stream while
+    // the first stages run; pts_pending until a stage that reads points has
+    // made the run's stream wait for ev_pts (wait_inputs).
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_prior = nullptr, ev_pts = nullptr;
+    bool pts_pending = false;
+
     // Set while the chain is planned for (and captured into) a CUDA graph:
     // stages size buffers from it and never read counts back to the host.
     const ochre::GraphPlan* plan = nullptr;
@@ -218,6 +225,10 @@ int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cud
 // *count above cap.  Both flag ERR_CAPACITY.
 cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_bits, cudaStream_t s);
 cudaError_t launch_plan_cap(ochre_gpu_ctx* ctx, uint32_t* count, uint32_t cap, cudaStream_t s);
+
+// Makes stream s wait for the batch's points if they are still being copied
+// (host-batch entry); every stage calls it before its first read of points.
+void wait_inputs(ochre_gpu_ctx* ctx, cudaStream_t s);
 
 // Read the device scalars into ctx->h_scalars (synchronises the stream).
 int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);

@@ -392,6 +392,7 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     st = check_device_error(ctx);
     if (st != OCHRE_OK) return st;
     // 2. polyline
+    wait_inputs(ctx, s);   // path-space flatten counts read points
     OCHRE_CUDA_TRY(ctx->sk_poly_off.ensure((n + 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_poly_foff.ensure((n + 1) * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n) * sizeof(ScanStatus<Pair>)));

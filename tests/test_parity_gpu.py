@@ -209,10 +209,11 @@ def test_coverage_error_vs_fp64(any_ctx, name, gen, kw, bound):
     assert e["max_abs"] < bound, (e, bound)
 
 
-def test_host_path_pipelined_chunks_match_oracle(gpu_ctx):
-    """Batches of 32,768+ rasters through the host-buffer entry run in chunks
-    on two internal contexts (copy-out overlapping the next chunk); offsets,
-    span tiles and coverage are rebased to the whole batch."""
+def test_host_path_large_batches_match_oracle(gpu_ctx):
+    """Large batches through the host-buffer entry: points copied on a side
+    stream while the first stages run, outputs written into mapped host
+    memory (zero-copy) once a call has sized it, coverage included; then a
+    mix that falls back to the general chain, with strokes."""
     b = W.glyph_run(n_paths=40_000, seed=17)
     ref = oracle.run(b, threads=16, want_cov=True)
     gpu_ctx.set_want_cov(True)
@@ -222,10 +223,26 @@ def test_host_path_pipelined_chunks_match_oracle(gpu_ctx):
         gpu_ctx.set_want_cov(False)
     st = compare(got, ref, b.n_rasters)
     assert st["cov_max_abs_vs_oracle_f32"] < 1e-3
-    # and a mix that needs the general chain in some chunks, with strokes
+    # a second call of the same size goes through the mapped outputs
+    gpu_ctx.set_want_cov(True)
+    try:
+        got = gpu_ctx.rasterize(b)
+    finally:
+        gpu_ctx.set_want_cov(False)
+    compare(got, ref, b.n_rasters)
+    # points in pinned host memory: read by the kernels in place
+    import dataclasses
+
+    import torch
+    pinned = dataclasses.replace(b, pts=torch.from_numpy(b.pts.copy()).pin_memory().numpy())
+    compare(gpu_ctx.rasterize(pinned), ref, b.n_rasters)
+    # and a mix that needs the general chain, with strokes
     from ochre_gb300.batch import concat
     m = concat([W.glyph_run(n_paths=30_000, seed=18), W.uneven_mix(n_paths=20), W.stroke_run(n_paths=3000)])
-    compare(gpu_ctx.rasterize(m), oracle.run(m, threads=16), m.n_rasters)
+    ref_m = oracle.run(m, threads=16)
+    compare(gpu_ctx.rasterize(m), ref_m, m.n_rasters)
+    m_pinned = dataclasses.replace(m, pts=torch.from_numpy(m.pts.copy()).pin_memory().numpy())
+    compare(gpu_ctx.rasterize(m_pinned), ref_m, m.n_rasters)
 
 
 @pytest.mark.parametrize("shape", __import__("ochre_gb300.autotune", fromlist=["FUSED_SHAPES"]).FUSED_SHAPES)
