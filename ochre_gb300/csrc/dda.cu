@@ -61,6 +61,42 @@ __device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* ca
     return nb + nc;
 }
 
+// Pixel cells a line's walk visits, about: its start cell and one per row
+// or column step (the reference's walk may add a cell at a corner tie).
+__device__ __forceinline__ uint32_t walk_cells(const float4& l) {
+    const float dx = fabsf(floorf(l.z) - floorf(l.x)), dy = fabsf(floorf(l.w) - floorf(l.y));
+    const float c = 1.0f + dx + dy;
+    return c < 65535.0f ? (uint32_t)c : 65535u;   // also NaN -> 65535 (bucketed last)
+}
+
+// Block-local work order by walk length: the BLOCK items of a block are
+// grouped by log2 of their cell count (unstable within a group), so each
+// warp walks lines of about the same length and a warp of short lines does
+// not run as long as the longest line of a random 32.  Returns the item
+// (0..BLOCK-1 within the block) this thread walks.  Every thread of the
+// block calls it.
+template <int BLOCK>
+__device__ __forceinline__ uint32_t order_by_length(uint32_t cells, uint32_t* s_cnt, uint16_t* s_item) {
+    constexpr int GROUPS = 17;
+    const uint32_t g = min(31u - (uint32_t)__clz(max(cells, 1u)), (uint32_t)GROUPS - 1u);
+    if (threadIdx.x < GROUPS) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
+    const uint32_t k = atomicAdd(&s_cnt[g], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int q = 0; q < GROUPS; q++) {
+            const uint32_t c = s_cnt[q];
+            s_cnt[q] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    s_item[s_cnt[g] + k] = (uint16_t)threadIdx.x;
+    __syncthreads();
+    return s_item[threadIdx.x];
+}
+
 // Entry counts per line (written in place of the offsets, then scanned)
 // and the raster tile boxes.  Counting is a separate kernel, not folded into
 // the offset scan: a walk's length varies from one cell to thousands, and a
@@ -84,10 +120,13 @@ __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ l
     __shared__ int4 s_box[BOX_SLOTS];
     __shared__ int s_ws[BOX_SLOTS];
     __shared__ uint32_t s_r0;
+    __shared__ uint32_t s_cnt[17];
+    __shared__ uint16_t s_item[256];
     const uint32_t n_lines = (uint32_t)dev_count(n_cap, n_dev);
     const uint32_t i0 = blockIdx.x * blockDim.x;
     if (i0 >= n_lines) return;
-    const uint32_t i = i0 + threadIdx.x;
+    const uint32_t cells = i0 + threadIdx.x < n_lines ? walk_cells(lines[i0 + threadIdx.x]) : 0u;
+    const uint32_t i = i0 + order_by_length<256>(cells, s_cnt, s_item);
     if (threadIdx.x < BOX_SLOTS) {
         s_box[threadIdx.x] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
         s_ws[threadIdx.x] = 0;
@@ -194,6 +233,7 @@ __device__ __forceinline__ K make_key(uint64_t base, const int4& bb, int tx, int
     return (K)(base + (((uint64_t)(ty - bb.y) * w + (uint64_t)(tx - bb.x)) << 1) + kind);
 }
 
+// (In line order: neighbouring lanes write neighbouring entry ranges.)
 template <class K>
 __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster,
                             const uint32_t* __restrict__ ent_off, uint64_t n_cap, const uint32_t* n_dev,

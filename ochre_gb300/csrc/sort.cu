@@ -57,8 +57,10 @@ __global__ void k_sort_offsets(const uint32_t* __restrict__ hist, uint32_t* __re
     off[p * 256 + d] = s[d] - hist[p * 256 + d];
 }
 
+// Three blocks per SM (register-bound otherwise: the 32-bit-key form would
+// take more than 85 registers and drop to two).
 template <class K>
-__global__ void __launch_bounds__(SORT_BLOCK) k_onesweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+__global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                                                          K* __restrict__ keys_out, uint32_t* __restrict__ vals_out,
                                                          uint64_t n, const uint32_t* n_dev, int shift,
                                                          const uint32_t* __restrict__ digit_off,
