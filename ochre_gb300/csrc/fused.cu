@@ -4,12 +4,13 @@
 // Reference: Rasterizer::fill/command/move_to/line_to/finish
 // (rasterizer.rs:61-268), PathCmd::transform/flatten (path.rs:16-109).
 //
+// Before the launch a command scan gives every command's float offset.
 // Per raster (CTA of FUSED_THREADS threads, rasters taken in index order by
 // atomic ticket):
-//   A. commands -> lines in shared memory: float offsets by a block scan
-//      seeded from a decoupled look-back chain over earlier rasters; `last`
-//      / `first` of every command by block max-scans; flatten counts (the
-//      serial t recurrence per curve) -> line offsets -> line emission.
+//   A. commands -> lines in shared memory: points at the scanned float
+//      offsets; `last` / `first` of every command by block max-scans; flatten
+//      counts (the serial t recurrence per curve) -> line offsets -> line
+//      emission.
 //   B. a GDIM x GDIM tile grid around the lines' end points (one tile of
 //      margin); a count walk per line (the reference's exact DDA) marks
 //      touched tiles in a bitmap, appends tile-row crossings to a list and
@@ -17,11 +18,15 @@
 //      row-major (the reference's (tile_y, tile_x) order).  A tile is
 //      followed by a span when the next tile on its row leaves a gap and the
 //      crossings with keys <= its own sum to a nonzero winding (the
-//      reference's running winding over its sorted TileIncrements).  Output
-//      offsets come from a second look-back chain.
+//      reference's running winding over its sorted TileIncrements).  The
+//      raster's tile and span counts are published (look-back aggregate).
 //   C. tiles in chunks of CHUNK: the lines touching a chunk are walked again
 //      and their increments scatter-added into shared per-tile accumulators;
-//      row sums give the carries along grid rows; alpha is written.
+//      row sums give the carries along grid rows; alpha goes to the CTA's
+//      staging slot.
+//   D. the raster's output offsets are resolved by decoupled look-back (the
+//      predecessors published their counts while this raster ran C), and
+//      the staged alpha, the tile positions and the spans are written out.
 // Any limit exceeded (commands, lines, grid size, tiles, increment slots,
 // crossings, a cell outside the grid) raises the fallback flag: the host then
 // runs the general chain for the whole batch.  Every wait is bounded.
@@ -34,7 +39,7 @@
 namespace ochre {
 
 // Kernel shape (template parameters, chosen by the autotuner):
-//   THREADS  threads per raster (= max commands per raster), 64 or 128;
+//   THREADS  threads per raster (= max commands per raster), 64, 96 or 128;
 //   CHUNK    tiles accumulated per pass (shared accumulators of CHUNK x 512 B).
 constexpr int F_LMAX = 256;             // lines per raster
 constexpr int GDIM = 32;                // grid side in tiles (one bitmap word per row)
