@@ -135,6 +135,47 @@ __device__ __forceinline__ int block_excl_max(int v, int& incl_last, int32_t (*t
     return max(base, ex);
 }
 
+// Two exclusive max-scans at once (values >= -1, identity -1): one pair of
+// barriers for both.
+template <int WARPS>
+__device__ __forceinline__ void block_excl_max2(int a, int b, int& a_ex, int& b_ex, int& a_last, int& b_last,
+                                                int32_t (*tmp)[4]) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int ia = a, ib = b;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int oa = __shfl_up_sync(0xffffffffu, ia, d);
+        const int ob = __shfl_up_sync(0xffffffffu, ib, d);
+        if (lane >= d) {
+            ia = max(ia, oa);
+            ib = max(ib, ob);
+        }
+    }
+    __syncthreads();
+    if (lane == 31) {
+        tmp[w][1] = ia;
+        tmp[w][2] = ib;
+    }
+    __syncthreads();
+    int base_a = -1, base_b = -1, tot_a = -1, tot_b = -1;
+#pragma unroll
+    for (int k = 0; k < WARPS; k++) {
+        const int ta = tmp[k][1], tb = tmp[k][2];
+        if (k < w) {
+            base_a = max(base_a, ta);
+            base_b = max(base_b, tb);
+        }
+        tot_a = max(tot_a, ta);
+        tot_b = max(tot_b, tb);
+    }
+    a_last = tot_a;
+    b_last = tot_b;
+    int ea = __shfl_up_sync(0xffffffffu, ia, 1), eb = __shfl_up_sync(0xffffffffu, ib, 1);
+    if (lane == 0) ea = eb = -1;
+    a_ex = max(base_a, ea);
+    b_ex = max(base_b, eb);
+}
+
 // Publish raster r's counts: its aggregate, or, for raster 0, its inclusive
 // value.  One thread.
 __device__ __forceinline__ void chain_publish(uint64_t* slots, uint32_t r, uint32_t a0, uint32_t a1) {
@@ -302,9 +343,9 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
             if (!ok) atomicOr(A.err, ERR_INVALID);
             // last: endpoint of the most recent earlier non-Close command;
             // first: point of the most recent earlier Move.
-            int ep_last, mv_last;
-            const int ep_ex = block_excl_max<F_WARPS>(active && verb != V_CLOSE ? tid : -1, ep_last, S.warp_tmp);
-            const int mv_ex = block_excl_max<F_WARPS>(active && verb == V_MOVE ? tid : -1, mv_last, S.warp_tmp);
+            int ep_last, mv_last, ep_ex, mv_ex;
+            block_excl_max2<F_WARPS>(active && verb != V_CLOSE ? tid : -1, active && verb == V_MOVE ? tid : -1, ep_ex,
+                                     mv_ex, ep_last, mv_last, S.warp_tmp);
             if (active) {
                 last = ep_ex >= 0 ? S.u.early.ep[ep_ex] : v2(0, 0);
                 first = mv_ex >= 0 ? S.u.early.ep[mv_ex] : v2(0, 0);
@@ -332,7 +373,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                 if (n_lines_cmd > F_LMAX) n_lines_cmd = F_LMAX + 1;
             }
         }
-        __syncthreads();
+        // (block_excl_sum's own barriers order the end-point reads above)
         int n_lines = 0;
         int loff = 0;
         if (!bail) {
@@ -410,8 +451,11 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
         }
         if (tid < GDIM) S.touched[tid] = 0u;
         __syncthreads();
-        if (tid == 0) {
+        // every thread derives the grid from the warps' boxes (no second barrier)
+        int gx0, gy0, gw, gh;
+        {
             int x0 = 0x7fffffff, y0 = 0x7fffffff, x1 = (int)0x80000000, y1 = (int)0x80000000;
+#pragma unroll
             for (int k = 0; k < F_WARPS; k++) {
                 x0 = min(x0, S.warp_tmp[k][0]);
                 y0 = min(y0, S.warp_tmp[k][1]);
@@ -419,16 +463,19 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                 y1 = max(y1, S.warp_tmp[k][3]);
             }
             if (x0 > x1) { x0 = 0; y0 = 0; x1 = 0; y1 = 0; }   // no lines: the (0,0) tile
-            S.gx0 = x0 - 1;
-            S.gy0 = y0 - 1;
-            S.gw = x1 - x0 + 3;
-            S.gh = y1 - y0 + 3;
-            if (S.gw > GDIM || S.gh > GDIM) S.flag = 1;
+            gx0 = x0 - 1;
+            gy0 = y0 - 1;
+            gw = x1 - x0 + 3;
+            gh = y1 - y0 + 3;
         }
-        __syncthreads();
-        bail = bail || S.flag != 0;
+        if (tid == 0) {
+            S.gx0 = gx0;
+            S.gy0 = gy0;
+            S.gw = gw;
+            S.gh = gh;
+        }
+        bail = bail || gw > GDIM || gh > GDIM;
         if (!bail) {
-            const int gx0 = S.gx0, gy0 = S.gy0, gw = S.gw, gh = S.gh;
             for (int l = tid; l < n_lines; l += FUSED_THREADS) {
                 const float4 L = S.lines[l];
                 int gmin = 0xffff, gmax = -1;
