@@ -62,6 +62,7 @@ struct FusedSmem {
     uint16_t line_g0[F_LMAX], line_g1[F_LMAX];   // grid-tile range of each line's cells
     uint16_t tile_g[F_TMAX];       // tile slot -> grid tile (row-major order)
     uint32_t touched[GDIM];        // one word per grid row
+    uint32_t span_mask[F_TMAX / 32];   // tile slot t is followed by a span
     uint16_t row_base[GDIM + 1];   // first tile slot of each grid row
     float rs[CHUNK][8];
     float carry[CHUNK][8];
@@ -511,7 +512,7 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
         __syncthreads();
         bail = bail || S.flag != 0;
 
-        // ---------------- compaction (row-major), spans, output offsets ----------------
+        // ---------------- compaction (row-major) and spans, by warp 0 ----------------
         if (!bail && wid == 0) {
             const uint32_t bits = S.touched[lane];
             const int cnt = __popc(bits);
@@ -534,41 +535,40 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                     b &= b - 1;
                     S.tile_g[slot++] = (uint16_t)(lane * GDIM + gx);
                 }
+                __syncwarp();
+                // spans (rasterizer.rs:252-265): a tile is followed by one when
+                // the next tile of its row leaves a gap and the crossings with
+                // keys <= its own sum to a nonzero winding; one bit per tile
+                const int nc = min((int)S.n_cross, F_XMAX);
+                for (int base = 0; base < F_TMAX; base += 32) {
+                    const int t = base + lane;
+                    bool has = false;
+                    if (t < total) {
+                        const int g = S.tile_g[t];
+                        const int gy = g >> 5, gx = g & 31;
+                        const uint32_t right = gx == 31 ? 0u : S.touched[gy] >> (gx + 1);
+                        if (right != 0u && !(right & 1u)) {
+                            int w = 0;
+                            for (int c = 0; c < nc; c++) {
+                                const uint32_t e = S.u.early.cross[c];
+                                if ((int)(e >> 16) <= g) w += (int)(int16_t)(e & 0xffffu);
+                            }
+                            has = w != 0;
+                        }
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, has);
+                    if (lane == 0) S.span_mask[base >> 5] = m;
+                }
             }
         }
         __syncthreads();
         bail = bail || S.flag != 0;
         int n_real = 0, n_tiles = 0, n_spans = 0;
-        int per = 0, t_lo = 0, srank = 0;
-        uint32_t span_bits = 0;
         if (!bail) {
             n_real = S.row_base[GDIM];
             n_tiles = n_real == 0 ? 1 : n_real;   // rasterizer.rs:194-208
-            // spans (rasterizer.rs:252-265): thread tid owns a contiguous run
-            // of tiles so that span ranks follow tile order
-            per = (n_real + FUSED_THREADS - 1) / FUSED_THREADS;   // <= 2
-            t_lo = tid * per;
-            int my = 0;
-            const int nc = min((int)S.n_cross, F_XMAX);
-            for (int k = 0; k < per; k++) {
-                const int t = t_lo + k;
-                if (t >= n_real) break;
-                const int g = S.tile_g[t];
-                const int gy = g >> 5, gx = g & 31;
-                const uint32_t right = gx == 31 ? 0u : S.touched[gy] >> (gx + 1);
-                if (right != 0u && !(right & 1u)) {
-                    int w = 0;
-                    for (int c = 0; c < nc; c++) {
-                        const uint32_t e = S.u.early.cross[c];
-                        if ((int)(e >> 16) <= g) w += (int)(int16_t)(e & 0xffffu);
-                    }
-                    if (w != 0) {
-                        span_bits |= 1u << k;
-                        my++;
-                    }
-                }
-            }
-            srank = block_excl_sum<F_WARPS>(my, n_spans, S.warp_tmp);
+#pragma unroll
+            for (int k = 0; k < F_TMAX / 32; k++) n_spans += __popc(S.span_mask[k]);
         }
         // The raster's output counts go out now; its offsets are resolved
         // after the coverage below, when its predecessors have long published
@@ -704,22 +704,22 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
                     float2* dc = reinterpret_cast<float2*>(A.out_cov + (size_t)tb * 64);
                     for (int q = tid; q < n_real * 32; q += FUSED_THREADS) dc[q] = sc[q];
                 }
-                int sr = srank;
-                for (int k = 0; k < per; k++) {
-                    const int t = t_lo + k;
-                    if (t >= n_real) break;
+                for (int t = tid; t < n_real; t += FUSED_THREADS) {
                     const int g = S.tile_g[t];
                     const int tx = S.gx0 + (g & 31), ty = S.gy0 + (g >> 5);
                     A.out_xy[tb + t] = (uint32_t)(uint16_t)(int16_t)(tx * 8) |
                                        ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
-                    if (span_bits >> k & 1u) {
+                    const uint32_t m = S.span_mask[t >> 5];
+                    if (m >> (t & 31) & 1u) {
+                        // span rank: the span tiles before t (tile order = callback order)
+                        int sr = __popc(m & ((1u << (t & 31)) - 1u));
+                        for (int k = 0; k < (t >> 5); k++) sr += __popc(S.span_mask[k]);
                         const uint32_t right = S.touched[g >> 5] >> ((g & 31) + 1);
                         const int gap = __ffs(right) - 1;
                         A.span_xy[sb + sr] = (uint32_t)(uint16_t)(int16_t)((tx + 1) * 8) |
                                              ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
                         A.span_w[sb + sr] = (uint16_t)((uint16_t)gap * 8u);
                         A.span_tile[sb + sr] = tb + t;
-                        sr++;
                     }
                 }
             }
