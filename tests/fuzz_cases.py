@@ -71,9 +71,10 @@ def _transform(rng, center):
     return [m[0, 0], m[0, 1], m[1, 0], m[1, 1], t[0], t[1]]
 
 
-def fuzz_batch(n_rasters: int, seed: int, span: float = 60.0, big_share: float = 0.1):
+def fuzz_batch(n_rasters: int, seed: int, span: float = 60.0, big_share: float = 0.1, stroke_share: float = 0.0):
     """``big_share`` of the rasters are eight times larger (most of those do
-    not fit the fused kernel, so the batch runs on the general chain)."""
+    not fit the fused kernel, so the batch runs on the general chain);
+    ``stroke_share`` of the transformed fills are strokes (width 0.25-12)."""
     rng = np.random.default_rng(seed)
     bb = BatchBuilder()
     for _ in range(n_rasters):
@@ -84,6 +85,8 @@ def fuzz_batch(n_rasters: int, seed: int, span: float = 60.0, big_share: float =
             verbs, pts = _fill(rng, span * (8.0 if big else 1.0), lead_move=not big)
             if rng.random() < 0.15:
                 bb.fill(verbs, _shift(verbs, pts, center), [1.0, 0.0, 0.0, 1.0, 0.0, 0.0], raw=True)
+            elif rng.random() < stroke_share:
+                bb.fill(verbs, pts, _transform(rng, center), stroke_width=float(rng.uniform(0.25, 12.0)))
             else:
                 bb.fill(verbs, pts, _transform(rng, center))
     return bb.build()

@@ -27,6 +27,14 @@ def test_fuzz_fused_form_is_used(gpu_ctx):
         assert gpu_ctx.stats()["fused"] == 1, seed
 
 
+@pytest.mark.parametrize("seed", [21, 22])
+def test_fuzz_strokes_match_oracle(any_ctx, seed):
+    b = fuzz_batch(1200, seed=seed, big_share=0.05, stroke_share=0.5)
+    assert b.has_strokes
+    st = compare(any_ctx.rasterize(b), oracle.run(b, threads=16), b.n_rasters)
+    assert st["diff_fraction"] < 0.01, st
+
+
 @pytest.mark.parametrize("big_share", [0.0, 0.2])
 def test_fuzz_graph_replay(gpu_ctx, big_share):
     from ochre_gb300 import DeviceBatch

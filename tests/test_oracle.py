@@ -171,13 +171,13 @@ def test_stroke_rasters_match_python_restatement():
         assert [(int(a), int(c), int(w), int(t)) for (a, c), w, t in zip(sxy.tolist(), sw, st)] == spans, name
 
 
-@pytest.mark.parametrize("seed", [11, 12])
-def test_fuzz_oracle_matches_python_restatement(seed):
+@pytest.mark.parametrize("seed,stroke_share", [(11, 0.0), (12, 0.0), (13, 0.5)])
+def test_fuzz_oracle_matches_python_restatement(seed, stroke_share):
     """Random command sequences (every verb, any order, degenerate curves,
     repeated points, shears, raw commands): both CPU restatements agree bit
     for bit, alpha included."""
     from fuzz_cases import fuzz_batch
-    b = fuzz_batch(90, seed=seed)
+    b = fuzz_batch(90, seed=seed, stroke_share=stroke_share)
     r = oracle.run(b)
     for i in range(b.n_rasters):
         tiles, spans, ninc = oracle_py.rasterize(oracle_py.commands_of_batch(b, i))
