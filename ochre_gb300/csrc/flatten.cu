@@ -166,24 +166,16 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
                                         OpCmd{}, total_id, ctx->scan_status.p, &ds->ticket,
                                         reinterpret_cast<CmdScan*>(&ds->n_floats), &ds->err, s)));
 
-    // The verbs must not consume more floats than the point stream holds:
-    // check before any kernel reads a point.  (A graph replay keeps the verbs
-    // of its planning run, which checked them.)
+    // A command whose points lie beyond the point array is flagged invalid
+    // by the kernels that read it (load_cmd), reported at the next read-back.
     const GraphPlan* plan = ctx->plan;
     int st = OCHRE_OK;
     const DevScalars* hs = host_scalars(ctx);
-    if (!plan) {
-        st = read_scalars(ctx, s);
-        if (st != OCHRE_OK) return st;
-        if (hs->n_floats > in->n_floats) return OCHRE_E_INVALID;
-        st = check_device_error(ctx);
-        if (st != OCHRE_OK) return st;
-    }
 
     wait_inputs(ctx, s);   // the counts read points
     BatchView b{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                 in->n_fills, in->n_rasters, n, ctx->cmd_foff.as<uint32_t>(), ctx->cmd_mv.as<uint32_t>(),
-                ctx->cmd_ep.as<uint32_t>()};
+                ctx->cmd_ep.as<uint32_t>(), in->n_floats};
     if (scan_tiles(n) < SPLIT_COUNT_TILES) {
         // counts first (one thread per command), then the offsets in place
         OCHRE_LAUNCH(ctx, "flatten_count", s, k_count_each<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(

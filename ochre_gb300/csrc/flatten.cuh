@@ -22,7 +22,13 @@ struct BatchView {
     const uint32_t* cmd_foff;
     const uint32_t* cmd_mv;
     const uint32_t* cmd_ep;
+    uint64_t n_floats;   // floats in pts: a command whose points lie beyond is invalid
 };
+
+// Command j's floats lie inside the point array.
+__device__ __forceinline__ bool cmd_in_bounds(const BatchView& b, uint32_t j) {
+    return (uint64_t)__ldg(b.cmd_foff + j) + floats_per_verb(__ldg(b.verbs + j)) <= b.n_floats;
+}
 
 // Everything a command's flattening depends on.
 struct CmdCtx {
@@ -108,6 +114,13 @@ __device__ inline CmdCtx load_cmd(const BatchView& b, uint32_t c) {
     k.fill = f;
     k.last_ref = ep > rc0 ? (int64_t)(ep - 1u) : -1;
     k.first_ref = mv > rc0 ? (int64_t)(mv - 1u) : -1;
+    // every command read below must lie inside the point array
+    if (!cmd_in_bounds(b, c) || (ep > rc0 && !cmd_in_bounds(b, ep - 1u)) || (mv > rc0 && !cmd_in_bounds(b, mv - 1u))) {
+        k.ok = false;
+        k.last = k.first = k.pt[0] = k.pt[1] = k.pt[2] = v2(0.0f, 0.0f);
+        k.w = 0.0f;
+        return k;
+    }
     k.last = ep > rc0 ? endpoint_of(b, ep - 1u, f) : v2(0.0f, 0.0f);
     if (mv > rc0) {
         const uint32_t m = mv - 1u;

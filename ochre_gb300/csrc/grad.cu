@@ -505,7 +505,7 @@ static int run_signed_chain(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStrea
 static BatchView view_of(ochre_gpu_ctx* ctx, const ochre_batch* in) {
     return BatchView{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                      in->n_fills, in->n_rasters, in->n_cmds, ctx->cmd_foff.as<uint32_t>(),
-                     ctx->cmd_mv.as<uint32_t>(), ctx->cmd_ep.as<uint32_t>()};
+                     ctx->cmd_mv.as<uint32_t>(), ctx->cmd_ep.as<uint32_t>(), in->n_floats};
 }
 
 }  // namespace ochre

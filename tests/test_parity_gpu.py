@@ -152,6 +152,21 @@ def test_invalid_inputs_are_reported(any_ctx):
     compare(got, oracle.run(b), 1)
 
 
+def test_verbs_beyond_the_points_are_reported(any_ctx):
+    """Verbs that consume more floats than the point array holds: flagged by
+    the kernels that would read them (host and device entries alike)."""
+    from ochre_gb300 import DeviceBatch, _lib
+    b = W.glyph_run(n_paths=50, seed=3)
+    short = type(b)(b.verbs, b.pts[:-5].copy(), b.fill_cmd_off, b.fill_xf, None, None, b.n_rasters)
+    with pytest.raises(_lib.OchreError) as e:
+        any_ctx.rasterize(short)
+    assert e.value.status == _lib.E_INVALID
+    with pytest.raises(_lib.OchreError) as e:
+        any_ctx.rasterize_device(DeviceBatch(short))
+    assert e.value.status == _lib.E_INVALID
+    compare(any_ctx.rasterize(b), oracle.run(b), b.n_rasters)
+
+
 def test_repeatable(any_ctx):
     """Two runs: identical structure; alpha may differ by the f32 summation
     order of shared-memory atomics (<= 1 LSB, the parity bound)."""
