@@ -110,32 +110,6 @@ __device__ __forceinline__ int block_excl_sum(int v, int& total, int32_t (*tmp)[
     total = tot;
     return base + inc - v;
 }
-// exclusive max-scan (values >= -1), identity -1
-template <int WARPS>
-__device__ __forceinline__ int block_excl_max(int v, int& incl_last, int32_t (*tmp)[4]) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int inc = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int o = __shfl_up_sync(0xffffffffu, inc, d);
-        if (lane >= d) inc = max(inc, o);
-    }
-    __syncthreads();
-    if (lane == 31) tmp[w][1] = inc;
-    __syncthreads();
-    int base = -1, tot = -1;
-#pragma unroll
-    for (int k = 0; k < WARPS; k++) {
-        const int t = tmp[k][1];
-        if (k < w) base = max(base, t);
-        tot = max(tot, t);
-    }
-    incl_last = tot;
-    int ex = __shfl_up_sync(0xffffffffu, inc, 1);
-    if (lane == 0) ex = -1;
-    return max(base, ex);
-}
-
 // Two exclusive max-scans at once (values >= -1, identity -1): one pair of
 // barriers for both.
 template <int WARPS>
