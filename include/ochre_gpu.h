@@ -198,7 +198,7 @@ int ochre_gpu_l2_loss(ochre_gpu_ctx *ctx, const float *cov, const float *target,
 
 /* Backward of ochre_gpu_render_coverage: from dL/d(coverage) (same layout),
  * writes dL/d(pts) (one value per input float, in the input (pre-transform)
- * space; conic weights get 0) and dL/d(transform) (6 per fill: m0 m1 m2 m3
+ * space; a conic weight gets its own derivative) and dL/d(transform) (6 per fill: m0 m1 m2 m3
  * ox oy).  The tile and line lists are recomputed, not stored.  Segment
  * counts, visited cells and tiles are held fixed (they are piecewise
  * constant in the inputs). */

@@ -167,6 +167,36 @@ __device__ void conic_flatten(V2 last, V2 control, V2 point, float w, bool* capp
     }
 }
 
+// The same subdivision, reporting with every emitted point its parameter t
+// on the conic (the midpoint of a leaf, then the leaf's end): the adjoint
+// needs t to differentiate the emitted points.
+template <class Emit>
+__device__ void conic_flatten_t(V2 last, V2 control, V2 point, float w, bool* capped, Emit emit) {
+    ConicFrame stack[CONIC_DEPTH_CAP + 2];
+    int sp = 0;
+    stack[sp++] = ConicFrame{0.0f, 1.0f, last, point, 0};
+    const V2 wc = vscale(w, control);
+    while (sp > 0) {
+        const ConicFrame f = stack[--sp];
+        const float t = __fmul_rn(0.5f, __fadd_rn(f.t0, f.t1));
+        const V2 p01 = vlerp(t, last, wc);
+        const V2 p12 = vlerp(t, wc, point);
+        const float u = __fsub_rn(1.0f, t);
+        const float denom = __fadd_rn(__fadd_rn(__fmul_rn(u, u), __fmul_rn(__fmul_rn(__fmul_rn(2.0f, t), u), w)),
+                                      __fmul_rn(t, t));
+        const V2 mid = vscale(__fdiv_rn(1.0f, denom), vlerp(t, p01, p12));
+        const float err = vlength(vsub(mid, vscale(0.5f, vadd(f.p0, f.p1))));
+        if (err > TOLERANCE) {
+            if (f.depth >= CONIC_DEPTH_CAP) { *capped = true; return; }
+            stack[sp++] = ConicFrame{t, f.t1, mid, f.p1, f.depth + 1};
+            stack[sp++] = ConicFrame{f.t0, t, f.p0, mid, f.depth + 1};
+        } else {
+            emit(mid, t);
+            emit(f.p1, f.t1);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------
 // The pixel DDA of rasterizer.rs:72-136.
 // ---------------------------------------------------------------------

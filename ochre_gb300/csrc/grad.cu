@@ -22,8 +22,9 @@
 //   * j * d(dt)/dtheta for unclamped t_j;
 //   device-space points p = M v + o, so dv = M^T dp, dM = dp v^T, do = dp.
 // Closing lines whose ends coincide are kept as zero-length edges (see
-// degenerate_dy).  Conic segments are not differentiated (their gradient is
-// zero).
+// degenerate_dy).  Conic points are the conic at the subdivision's
+// parameters t (held fixed, like the curves' line counts): linear in the
+// control points, with a weight derivative (path.rs:75-104).
 #include <algorithm>
 
 #include "common.cuh"
@@ -414,6 +415,42 @@ __global__ void k_cmd_grad(BatchView b, const uint32_t* __restrict__ line_off, u
         if (cubic) add_point(gp, b, self, 2, g3);
         break;
     }
+    case V_CONIC: {
+        // path.rs:75-104: every emitted point is the conic at a subdivision
+        // parameter t, q = ((1-t)^2 P0 + 2t(1-t) w P1 + t^2 P2) / D, D =
+        // (1-t)^2 + 2t(1-t) w + t^2; the subdivision (which t) is held fixed,
+        // so q is linear in the control points, and dq/dw = 2t(1-t)(P1 - q)/D.
+        const V2 P0 = k.last, P1 = k.pt[0], P2 = k.pt[1];
+        const float w = k.w;
+        const LineGrad first_line = lg[o0];
+        V2 g0 = v2(first_line.ax, first_line.ay), g1 = v2(0, 0), g2 = v2(0, 0);
+        float gw = 0.0f;
+        int j = 0;
+        bool capped = false;
+        conic_flatten_t(P0, P1, P2, w, &capped, [&](V2 q, float t) {
+            j++;
+            if (j > n_own) return;
+            const LineGrad gj = lg[o0 + j - 1];
+            V2 dq = v2(gj.bx, gj.by);
+            if (j < n_own) {
+                const LineGrad gn = lg[o0 + j];
+                dq = add2(dq, v2(gn.ax, gn.ay));
+            }
+            const float u = 1.0f - t;
+            const float D = u * u + 2.0f * t * u * w + t * t;
+            const float A = u * u / D, B = 2.0f * t * u * w / D, C = t * t / D;
+            g0 = add2(g0, mul2(A, dq));
+            g1 = add2(g1, mul2(B, dq));
+            g2 = add2(g2, mul2(C, dq));
+            const float dw = 2.0f * t * u / D;
+            gw += dw * ((P1.x - q.x) * dq.x + (P1.y - q.y) * dq.y);
+        });
+        add_last(g0);
+        add_point(gp, b, self, 0, g1);
+        add_point(gp, b, self, 1, g2);
+        atomicAdd(gp + __ldg(b.cmd_foff + c) + 4, gw);   // the weight (not transformed)
+        break;
+    }
     default:
         break;
     }
@@ -468,7 +505,7 @@ __global__ void k_fill_grad(BatchView b, const float* __restrict__ gp, float* __
                 acc[5] += gy;
             }
         }
-        if (v == V_CONIC) dl_dpts[fo + 4] = 0.0f;
+        if (v == V_CONIC) dl_dpts[fo + 4] = gp[fo + 4];   // the weight's gradient, as accumulated
     }
     // commands of a fill are contiguous: segmented reduction over the warp
     const uint32_t fprev = __shfl_up_sync(0xffffffffu, f, 1);

@@ -1192,25 +1192,61 @@ static void bwd_piece(void *u, long cx, long cy, dv2 p0, dv2 p1, int k0, double 
 typedef struct {
     dedge *e; size_t n, cap;
     pref *ra, *rb;          /* per edge: point refs of A and B when they are plain points (closing lines, lines) */
+    double *tb;             /* per edge: conic parameter of B (conic edges), else -1 */
 } edges_t;
 
-static int push_edge(edges_t *E, dv2 a, dv2 b, pref ra, pref rb) {
+/* Parameters t of the points a conic's subdivision emits, in order (path.rs:75-104
+ * in f32 as the forward runs it: the midpoint of every leaf, then its end). */
+typedef struct { double *t; size_t n, cap; int error; } tlist;
+static void tl_push(tlist *l, double t) {
+    if (l->n == l->cap) {
+        size_t c = l->cap ? 2 * l->cap : 64;
+        double *p = (double *)realloc(l->t, c * sizeof(double));
+        if (!p) { l->error = OCHRE_ORACLE_E_NOMEM; return; }
+        l->t = p; l->cap = c;
+    }
+    l->t[l->n++] = t;
+}
+static void conic_params(tlist *l, vec2 last, vec2 control, vec2 point, float weight, float t0, float t1, vec2 p0,
+                         vec2 p1, int depth) {
+    float t = 0.5f * (t0 + t1);
+    vec2 wc = vscale(weight, control);
+    vec2 p01 = vlerp(t, last, wc);
+    vec2 p12 = vlerp(t, wc, point);
+    float denom = (1.0f - t) * (1.0f - t) + 2.0f * t * (1.0f - t) * weight + t * t;
+    vec2 midpoint = vscale(1.0f / denom, vlerp(t, p01, p12));
+    float err = vlength(vsub(midpoint, vscale(0.5f, vadd(p0, p1))));
+    if (err > TOLERANCE) {
+        if (depth >= CONIC_DEPTH_CAP) { l->error = OCHRE_ORACLE_E_LIMIT; return; }
+        conic_params(l, last, control, point, weight, t0, t, p0, midpoint, depth + 1);
+        conic_params(l, last, control, point, weight, t, t1, midpoint, p1, depth + 1);
+    } else {
+        tl_push(l, t);
+        tl_push(l, t1);
+    }
+}
+
+static int push_edge_t(edges_t *E, dv2 a, dv2 b, pref ra, pref rb, double tb) {
     if (E->n == E->cap) {
         size_t c = E->cap ? E->cap * 2 : 256;
         dedge *p = (dedge *)realloc(E->e, c * sizeof(dedge));
         pref *qa = (pref *)realloc(E->ra, c * sizeof(pref));
         pref *qb = (pref *)realloc(E->rb, c * sizeof(pref));
+        double *qt = (double *)realloc(E->tb, c * sizeof(double));
         if (p) E->e = p;
         if (qa) E->ra = qa;
         if (qb) E->rb = qb;
-        if (!p || !qa || !qb) return OCHRE_ORACLE_E_NOMEM;
+        if (qt) E->tb = qt;
+        if (!p || !qa || !qb || !qt) return OCHRE_ORACLE_E_NOMEM;
         E->cap = c;
     }
     E->e[E->n].a = a; E->e[E->n].b = b;
     E->ra[E->n] = ra; E->rb[E->n] = rb;
+    E->tb[E->n] = tb;
     E->n++;
     return 0;
 }
+static int push_edge(edges_t *E, dv2 a, dv2 b, pref ra, pref rb) { return push_edge_t(E, a, b, ra, rb, -1.0); }
 
 static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, const double *target,
                        const double *dl_ds, double *loss_out, double *dpts, double *dxf) {
@@ -1240,6 +1276,7 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
         dv2 *cpts = (dv2 *)malloc((ncmd ? ncmd : 1) * 3 * sizeof(dv2));
         if (!e_first || !cpts) { free(e_first); free(cpts); st = OCHRE_ORACLE_E_NOMEM; break; }
         dv2 last = {0.0, 0.0}, first = {0.0, 0.0};
+        vec2 last32 = v2(0.0f, 0.0f);   /* the f32 forward's last point (conic subdivision) */
         pref last_ref = {-1, 0}, first_ref = {-1, 0};
         /* ---- edges ---- */
         for (uint32_t f = f0; f < f1 && !st; f++) {
@@ -1250,9 +1287,11 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
                 uint8_t verb = bt->verbs[c];
                 const float *fp = bt->pts + off[c];
                 dv2 *p = cpts + 3 * li;
+                vec2 p32[3];
                 for (int k = 0; k < npts_of(verb); k++) {
                     dv2 v = {fp[2 * k], fp[2 * k + 1]};
                     p[k] = raw ? v : dxf_apply(xf, v);
+                    p32[k] = raw ? v2(fp[2 * k], fp[2 * k + 1]) : xf_apply(xf, v2(fp[2 * k], fp[2 * k + 1]));
                 }
                 e_first[li] = E.n;
                 pref self0 = {(int64_t)c, 0}, none = {-1, 0};
@@ -1260,9 +1299,11 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
                     st = push_edge(&E, last, first, last_ref, first_ref);
                     first = p[0]; last = p[0];
                     first_ref = self0; last_ref = self0;
+                    last32 = p32[0];
                 } else if (verb == 1) {
                     st = push_edge(&E, last, p[0], last_ref, self0);
                     last = p[0]; last_ref = self0;
+                    last32 = p32[0];
                 } else if (verb == 2 || verb == 3) {
                     const uint32_t n = counts[c];
                     double dt;
@@ -1291,8 +1332,26 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
                     }
                     last = p[verb == 2 ? 1 : 2];
                     last_ref.cmd = (int64_t)c; last_ref.pt = verb == 2 ? 1 : 2;
+                    last32 = p32[verb == 2 ? 1 : 2];
                 } else if (verb == 4) {
-                    st = OCHRE_ORACLE_E_INVALID;   /* conics are outside the differentiable model */
+                    /* the conic at the f32 subdivision's parameters, in double */
+                    const double w = fp[4];
+                    tlist tl = {0};
+                    conic_params(&tl, last32, p32[0], p32[1], fp[4], 0.0f, 1.0f, last32, p32[1], 0);
+                    if (tl.error) st = tl.error;
+                    dv2 prev = last;
+                    for (size_t j = 0; j < tl.n && !st; j++) {
+                        const double t = tl.t[j], u = 1.0 - t;
+                        const double D = u * u + 2.0 * t * u * w + t * t;
+                        dv2 q = {(u * u * last.x + 2.0 * t * u * w * p[0].x + t * t * p[1].x) / D,
+                                 (u * u * last.y + 2.0 * t * u * w * p[0].y + t * t * p[1].y) / D};
+                        st = push_edge_t(&E, prev, q, none, none, t);
+                        prev = q;
+                    }
+                    free(tl.t);
+                    last = p[1];
+                    last_ref.cmd = (int64_t)c; last_ref.pt = 1;
+                    last32 = p32[1];
                 }
             }
         }
@@ -1432,6 +1491,33 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
                     ADDP(r2, g[2].x, g[2].y);
                     if (cubic) ADDP(r3, g[3].x, g[3].y);
                     last_ref.cmd = (int64_t)c; last_ref.pt = cubic ? 2 : 1; lastp = cubic ? p[2] : p[1];
+                } else if (verb == 4) {
+                    /* q_j = (u^2 P0 + 2tu w P1 + t^2 P2) / D at fixed t_j: linear in the
+                     * points; dq/dw = 2tu (P1 - q) / D */
+                    const size_t n = e1 - e0;
+                    const dv2 P0 = lastp, P1 = p[0];
+                    const double w = bt->pts[off[c] + 4];
+                    dv2 g0 = gA[e0], g1 = {0, 0}, g2 = {0, 0};
+                    double gw = 0.0;
+                    for (size_t j = 1; j <= n; j++) {
+                        const double t = E.tb[e0 + j - 1], u = 1.0 - t;
+                        const double D = u * u + 2.0 * t * u * w + t * t;
+                        const double A = u * u / D, B = 2.0 * t * u * w / D, C = t * t / D;
+                        dv2 dq = gB[e0 + j - 1];
+                        if (j < n) { dq.x += gA[e0 + j].x; dq.y += gA[e0 + j].y; }
+                        g0.x += A * dq.x; g0.y += A * dq.y;
+                        g1.x += B * dq.x; g1.y += B * dq.y;
+                        g2.x += C * dq.x; g2.y += C * dq.y;
+                        const dv2 q = E.e[e0 + j - 1].b;
+                        gw += 2.0 * t * u / D * ((P1.x - q.x) * dq.x + (P1.y - q.y) * dq.y);
+                    }
+                    (void)P0;
+                    ADDP(last_ref, g0.x, g0.y);
+                    pref r1 = {(int64_t)c, 0}, r2 = {(int64_t)c, 1};
+                    ADDP(r1, g1.x, g1.y);
+                    ADDP(r2, g2.x, g2.y);
+                    dp[off[c] + 4] += gw;   /* the weight, not transformed */
+                    last_ref.cmd = (int64_t)c; last_ref.pt = 1; lastp = p[1];
                 }
             }
             {
@@ -1442,7 +1528,7 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
 #undef ADDP
             free(gA); free(gB);
         }
-        free(E.e); free(E.ra); free(E.rb); free(e_first); free(cpts);
+        free(E.e); free(E.ra); free(E.rb); free(E.tb); free(e_first); free(cpts);
     }
     /* transform adjoint */
     if (!st && (dpts || dxf)) {
@@ -1467,6 +1553,7 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
                         dxf[6 * f + 4] += gx; dxf[6 * f + 5] += gy;
                     }
                 }
+                if (dpts && bt->verbs[c] == 4) dpts[off[c] + 4] = dp[off[c] + 4];
             }
         }
     }

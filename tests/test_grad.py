@@ -1,6 +1,6 @@
 """Differentiable fill: coverage render, L2 loss and the hand-written backward.
 
-The FP64 model in the oracle (``oracle.diff64``) is first checked against
+The FP64 model in the oracle (``oracle.diff64``, conics included) is first checked against
 central finite differences (h = 1e-3 px on control points and translations;
 the same 1e-3 px displacement on the linear part of a transform).  The GPU's
 gradient is then checked against the FP64 reference gradient of the f32
@@ -128,12 +128,50 @@ def test_fp64_gradient_is_zero_at_the_target():
     assert np.abs(dp).max() < 1e-2 and np.abs(dx).max() < 10.0
 
 
-def test_fp64_model_rejects_conics():
+def _conic_batch(seed=0):
+    """Three rasters: a circle of four conics (w = cos 45 deg) under a
+    shear, and a blob bounded by two conics of random weights."""
     from ochre_gb300.batch import BatchBuilder
+    rng = np.random.default_rng(seed)
     bb = BatchBuilder()
-    bb.begin_raster().fill([0, 4, 5], [0, 0, 10, 0, 10, 10, 0.5], [1, 0, 0, 1, 0, 0])
-    with pytest.raises(RuntimeError):
-        oracle.diff64(bb.build(), 16, 16, np.zeros((1, 16, 16)))
+    for r in range(3):
+        bb.begin_raster()
+        cx, cy = rng.uniform(40, 90, 2)
+        R = rng.uniform(15, 30)
+        w = 0.70710677
+        bb.fill([0, 4, 4, 4, 4, 5],
+                [cx + R, cy, cx + R, cy + R, cx, cy + R, w, cx - R, cy + R, cx - R, cy, w,
+                 cx - R, cy - R, cx, cy - R, w, cx + R, cy - R, cx + R, cy, w],
+                [1.0, 0.1 * r, -0.05, 1.1, 3.0 * r, 2.0])
+        bb.fill([0, 4, 1, 4, 5],
+                [cx - 10, cy - 5, cx, cy - 35, cx + 12, cy - 4, rng.uniform(0.3, 2.5), cx + 8, cy + 10,
+                 cx - 4, cy + 30, cx - 10, cy - 5, rng.uniform(0.3, 2.5)],
+                [0.9, 0.0, 0.0, 0.9, 5.0, 4.0])
+    return bb.build()
+
+
+def _conic_target(b, w, h):
+    pert = copy.copy(b)
+    pert.pts = (b.pts + np.random.default_rng(5).normal(0, 1.5, b.pts.shape)).astype(np.float32)
+    return oracle.coverage_image(pert, w, h).astype(np.float64)
+
+
+def test_fp64_conic_gradient_matches_central_differences():
+    """Conics (path.rs:75-104): the emitted points are the conic at the f32
+    subdivision's parameters (held fixed), differentiated in the control
+    points, the weight and the transform."""
+    b, w, h = _conic_batch(), 128, 128
+    tgt = _conic_target(b, w, h)
+    counts = oracle.seg_counts(b)
+    loss, dp, dx = oracle.diff64(b, w, h, tgt, counts)
+    assert loss > 0.0
+    fd = _central_fd(b, w, h, tgt, counts, np.arange(len(b.pts)), np.arange(6 * b.n_fills))
+    an = np.concatenate([dp, dx.ravel()])
+    assert _rel(an, fd) <= REL_TOL, _rel(an, fd)
+    from ochre_gb300.batch import FLOATS_PER_VERB
+    off = np.concatenate([[0], np.cumsum(FLOATS_PER_VERB[b.verbs])])
+    weights = [int(off[c]) + 4 for c in range(b.n_cmds) if b.verbs[c] == 4]
+    assert np.abs(dp[weights]).max() > 1.0   # the weights are differentiated too
 
 
 # ---------------------------------------------------------------- GPU
@@ -221,6 +259,19 @@ def test_gpu_gradient_matches_fp64(case):
     assert abs(loss - rloss) <= 1e-3 * rloss, (loss, rloss)
     assert _rel(dp, rdp) <= REL_TOL, _rel(dp, rdp)
     assert _rel(dx, rdx) <= REL_TOL, _rel(dx, rdx)
+
+
+@pytest.mark.gpu
+def test_gpu_conic_gradient_matches_fp64():
+    """Conic control points, weights and transforms against the FP64
+    reference gradient of the f32 model."""
+    b, w, h = _conic_batch(), 128, 128
+    tgt = _conic_target(b, w, h).astype(np.float32)
+    loss, dp, dx, cov = _gpu_grad(b, w, h, tgt)
+    aloss, adp, adx = oracle.adjoint64(b, w, h, tgt)
+    assert abs(loss - aloss) <= 1e-5 * aloss, (loss, aloss)
+    assert _rel(dp, adp) <= REL_TOL, _rel(dp, adp)
+    assert _rel(dx, adx) <= REL_TOL, _rel(dx, adx)
 
 
 @pytest.mark.gpu
