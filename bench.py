@@ -33,6 +33,7 @@ if ROOT not in sys.path:
 
 METRIC = "tiles/s & paths/s batched vs plain GPU at ≤1 LSB alpha; fwd+bwd scenes/s"
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+NOMINAL_HBM_GBS = 7900.0   # GB300 HBM3e, nominal
 
 
 def load_peaks():
@@ -749,6 +750,7 @@ def run_ours(args, ws, rank, local):
         "wall_s_timed_region": wall,
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,
                      "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak,
+                     "frac_of_nominal": achieved / NOMINAL_HBM_GBS,
                      "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "path_roofline": {"compulsory_bytes_per_step": comp_in + comp_out, "achieved_gbs": path_gbs,
                           "frac": path_gbs / peak, "note": "input verbs+points+transforms and 68 B/tile + 6 B/span"},
