@@ -344,6 +344,7 @@ def bench_uneven(ctx, stream, flush, steps, peak):
         "speedup_vs_per_path_chain": (bt.n_rasters / (ms / 1e3)) * per_path_s,
         "one_call_chain_ms": chain_ms,
         "roofline": {"kernel": dom["kernel"], "achieved_gbs": ach, "frac": ach / peak,
+                     "frac_of_nominal": ach / NOMINAL_HBM_GBS,
                      "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
         "path_roofline": {"compulsory_bytes": comp, "achieved_gbs": comp / (ms / 1e3) / 1e9,
                           "frac": comp / (ms / 1e3) / 1e9 / peak},
