@@ -71,14 +71,45 @@ __global__ void k_composite_spans(const uint32_t* __restrict__ span_xy, const ui
 }
 
 // ---- L2 loss ----
+// Per thread a compensated (Kahan) float sum of (cov - target)^2 (its error
+// does not grow with the count: FP64 arithmetic per pixel would bound this
+// kernel by the GPU's FP64 rate instead of HBM), one double per thread into
+// the block reduction.  16-byte accesses when all three arrays allow.
 __global__ void k_l2(const float* __restrict__ cov, const float* __restrict__ target, uint64_t n,
                      double* __restrict__ loss, float* __restrict__ dl) {
-    double acc = 0.0;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    float sum = 0.0f, comp = 0.0f;
+    auto add = [&](float d) {
+        const float y = d * d - comp;
+        const float t = sum + y;
+        comp = (t - sum) - y;
+        sum = t;
+    };
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    const bool vec = ((reinterpret_cast<uintptr_t>(cov) | reinterpret_cast<uintptr_t>(target) |
+                       reinterpret_cast<uintptr_t>(dl)) & 15u) == 0;
+    uint64_t done = 0;
+    if (vec) {
+        const uint64_t n4 = n / 4;
+        const float4* c4 = reinterpret_cast<const float4*>(cov);
+        const float4* t4 = reinterpret_cast<const float4*>(target);
+        float4* d4 = reinterpret_cast<float4*>(dl);
+        for (uint64_t i = tid; i < n4; i += stride) {
+            const float4 c = c4[i], g = t4[i];
+            const float4 d = make_float4(c.x - g.x, c.y - g.y, c.z - g.z, c.w - g.w);
+            add(d.x);
+            add(d.y);
+            add(d.z);
+            add(d.w);
+            if (dl) d4[i] = make_float4(2.0f * d.x, 2.0f * d.y, 2.0f * d.z, 2.0f * d.w);
+        }
+        done = n4 * 4;
+    }
+    for (uint64_t i = done + tid; i < n; i += stride) {
         const float d = cov[i] - target[i];
-        acc += (double)d * (double)d;
+        add(d);
         if (dl) dl[i] = 2.0f * d;
     }
+    double acc = (double)sum - (double)comp;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     __shared__ double s[32];

@@ -238,6 +238,20 @@ class Rasterizer:
 # ---------------------------------------------------------------------------
 # Batched entry points
 # ---------------------------------------------------------------------------
+CUDA_STREAM_LEGACY = 1   # cudaStreamLegacy: the legacy default stream
+
+
+def stream_arg(stream: Optional[int]) -> Optional[int]:
+    """A cudaStream_t for the C ABI.  None: the context's own stream (NULL).
+    A stream handle of 0 (torch's default stream is the legacy default
+    stream) becomes cudaStreamLegacy, so that the work is ordered with what
+    torch runs there; NULL would mean the context's own (non-blocking)
+    stream instead."""
+    if stream is None:
+        return None
+    return int(stream) if int(stream) != 0 else CUDA_STREAM_LEGACY
+
+
 class Graph:
     """A captured fill -> finish launch chain for one DeviceBatch (its device
     pointers and counts fixed; the values behind them may change between
@@ -256,7 +270,8 @@ class Graph:
 
     def launch(self, stream: Optional[int] = None) -> _lib.Result:
         r = _lib.Result()
-        _lib.check(_lib.load().ochre_graph_launch(self.handle, ctypes.byref(r), stream), "ochre_graph_launch")
+        _lib.check(_lib.load().ochre_graph_launch(self.handle, ctypes.byref(r), stream_arg(stream)),
+                   "ochre_graph_launch")
         return r
 
     def rasterize(self, stream: Optional[int] = None) -> dict:
@@ -415,7 +430,7 @@ class GpuContext:
         """Device buffers in, device result (pointers owned by the context)."""
         r = _lib.Result()
         _lib.check(_lib.load().ochre_gpu_rasterize_device(self.handle, ctypes.byref(dbatch.c), ctypes.byref(r),
-                                                          stream), "rasterize_device")
+                                                          stream_arg(stream)), "rasterize_device")
         return r
 
     def graph(self, dbatch: DeviceBatch, headroom: float = 1.25) -> "Graph":
@@ -464,7 +479,8 @@ class GpuContext:
     # ---- differentiable fill (device tensors as storage) ----
     def _torch_stream(self, stream: Optional[int]) -> int:
         import torch
-        return stream if stream is not None else torch.cuda.current_stream(self.device).cuda_stream
+        h = stream if stream is not None else torch.cuda.current_stream(self.device).cuda_stream
+        return stream_arg(h)
 
     def render_coverage(self, dbatch: DeviceBatch, w: int, h: int, out=None, stream: Optional[int] = None):
         """Dense coverage images [n_rasters, h, w] (float32 CUDA tensor),

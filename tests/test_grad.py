@@ -231,7 +231,9 @@ def test_l2_loss_and_upstream_gradient():
     loss, _ = ctx.l2_loss(cov, tgt, dl)
     torch.cuda.synchronize()
     c, t = cov.cpu().double().numpy(), tgt.cpu().double().numpy()
-    assert abs(loss.item() - ((c - t) ** 2).sum()) < 1e-9 * max(1.0, ((c - t) ** 2).sum())
+    # per thread a compensated float sum, thread sums in double: relative
+    # error of order the float epsilon
+    assert abs(loss.item() - ((c - t) ** 2).sum()) < 3e-7 * max(1.0, ((c - t) ** 2).sum())
     assert np.allclose(dl.cpu().numpy(), 2.0 * (cov - tgt).cpu().numpy(), atol=0, rtol=0)
     ctx.close()
 
