@@ -199,9 +199,13 @@ int ochre_gpu_l2_loss(ochre_gpu_ctx *ctx, const float *cov, const float *target,
 /* Backward of ochre_gpu_render_coverage: from dL/d(coverage) (same layout),
  * writes dL/d(pts) (one value per input float, in the input (pre-transform)
  * space; a conic weight gets its own derivative) and dL/d(transform) (6 per fill: m0 m1 m2 m3
- * ox oy).  The tile and line lists are recomputed, not stored.  Segment
- * counts, visited cells and tiles are held fixed (they are piecewise
- * constant in the inputs). */
+ * ox oy).  When the context's last call that ran the chain was
+ * ochre_gpu_render_coverage of the same batch (the same arrays and counts),
+ * the tile and line lists that call left are reused; the arrays must then
+ * still hold the values they had in that call.  Otherwise (any rasterization
+ * or compositing on the context in between, or another batch) they are
+ * recomputed.  Segment counts, visited cells and tiles are held fixed (they
+ * are piecewise constant in the inputs). */
 int ochre_gpu_fill_backward(ochre_gpu_ctx *ctx, const ochre_batch *in, uint32_t w, uint32_t h,
                             const float *dl_dcov, float *dl_dpts, float *dl_dxf, void *stream);
 

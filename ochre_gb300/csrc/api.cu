@@ -227,6 +227,7 @@ static int validate_host(const ochre_batch* in) {
 
 int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out, cudaStream_t s) {
     std::memset(out, 0, sizeof *out);
+    ctx->epoch++;
     ctx->stats = ochre_stats{};
     ctx->prof_used = 0;
     ctx->launches = 0;

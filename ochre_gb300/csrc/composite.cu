@@ -154,6 +154,7 @@ extern "C" int ochre_gpu_composite(ochre_gpu_ctx* ctx, const ochre_result* res, 
     if ((reinterpret_cast<uintptr_t>(canvas) & 3) || (reinterpret_cast<uintptr_t>(colors) & 3)) return OCHRE_E_INVALID;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    ctx->epoch++;   // the sort below reuses the chain's buffers
     ctx->prof_used = 0;
     ctx->launches = 0;
     const uint32_t T = res->n_tiles, N = res->n_spans;

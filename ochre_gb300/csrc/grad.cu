@@ -570,6 +570,13 @@ static int run_signed_chain(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStrea
     return st;
 }
 
+static bool same_batch(const ochre_batch& a, const ochre_batch& b) {
+    return a.verbs == b.verbs && a.n_cmds == b.n_cmds && a.pts == b.pts && a.n_floats == b.n_floats &&
+           a.fill_cmd_off == b.fill_cmd_off && a.fill_xf == b.fill_xf && a.fill_flags == b.fill_flags &&
+           a.n_fills == b.n_fills && a.raster_fill_off == b.raster_fill_off && a.n_rasters == b.n_rasters &&
+           a.fill_width == b.fill_width;
+}
+
 static BatchView view_of(ochre_gpu_ctx* ctx, const ochre_batch* in) {
     return BatchView{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                      in->n_fills, in->n_rasters, in->n_cmds, ctx->cmd_foff.as<uint32_t>(),
@@ -587,9 +594,12 @@ int ochre_gpu_render_coverage(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_
     if (!ctx || !in || (!cov && in->n_rasters && w && h) || w > MAX_CANVAS || h > MAX_CANVAS) return OCHRE_E_INVALID;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    ctx->saved.valid = false;
     ochre_result res;
     int st = run_signed_chain(ctx, in, s, &res);
     if (st != OCHRE_OK) return st;
+    if (!in->fill_width)
+        ctx->saved = ochre_gpu_ctx::SavedForward{true, ctx->epoch, *in, res, (uint32_t)ctx->stats.n_lines};
     const size_t npx = (size_t)in->n_rasters * w * h;
     if (npx) OCHRE_CUDA_TRY(cudaMemsetAsync(cov, 0, npx * sizeof(float), s));
     if (res.n_tiles) {
@@ -636,12 +646,21 @@ int ochre_gpu_fill_backward(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t 
     if (in->fill_width) return OCHRE_E_INVALID;   // stroked fills are not differentiated
     if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
-    // recompute the forward structure (lines, cells, tiles) and signed coverage
+    // the forward structure (lines, cells, tiles) and signed coverage: the
+    // one the last render_coverage of this batch left, else recomputed
     ochre_result res;
-    int st = run_signed_chain(ctx, in, s, &res);
-    if (st != OCHRE_OK) return st;
+    uint32_t L;
+    if (ctx->saved.valid && ctx->saved.epoch == ctx->epoch && same_batch(ctx->saved.in, *in)) {
+        res = ctx->saved.res;
+        L = ctx->saved.n_lines;
+        ctx->prof_used = 0;
+        ctx->launches = 0;
+    } else {
+        const int st = run_signed_chain(ctx, in, s, &res);
+        if (st != OCHRE_OK) return st;
+        L = (uint32_t)ctx->stats.n_lines;
+    }
     const uint32_t R = in->n_rasters;
-    const uint32_t L = (uint32_t)ctx->stats.n_lines;
     const size_t npx = (size_t)R * w * h;
     if (in->n_floats) OCHRE_CUDA_TRY(cudaMemsetAsync(dl_dpts, 0, in->n_floats * sizeof(float), s));
     if (in->n_fills) OCHRE_CUDA_TRY(cudaMemsetAsync(dl_dxf, 0, (size_t)in->n_fills * 6 * sizeof(float), s));

@@ -167,6 +167,18 @@ struct ochre_gpu_ctx {
     bool cov_signed = false;   // tile_cov holds accum + area (signed) instead of |accum + area|
     // differentiable path scratch
     ochre::DevBuf grad_g, grad_gs, grad_left, grad_line, grad_pts;
+    // Bumped by every call that rewrites the chain's buffers (run_device,
+    // compositing).  The chain structure left by ochre_gpu_render_coverage
+    // (lines, per-command line offsets, tiles with signed coverage) stays
+    // valid while it is unchanged, and the backward of the same batch reuses it.
+    uint64_t epoch = 0;
+    struct SavedForward {
+        bool valid;
+        uint64_t epoch;
+        ochre_batch in;
+        ochre_result res;
+        uint32_t n_lines;
+    } saved{};
     // stroke stage: input command scan, polyline, units, output batch
     ochre::DevBuf sk_cmd_foff, sk_cmd_mv, sk_cmd_ep, sk_poly_off, sk_poly_foff, sk_pverbs, sk_ppts, sk_pfoff,
         sk_pfill_off, sk_first_close, sk_unit_start, sk_out_off, sk_out_foff, sk_unit_fill, sk_overbs, sk_opts,

@@ -312,6 +312,37 @@ def test_gpu_gradient_matches_central_differences():
 
 
 @pytest.mark.gpu
+def test_backward_reuses_the_forward_structure():
+    """The backward right after render_coverage of the same batch reuses its
+    lines and tiles (fewer launches); after another rasterization on the
+    context, or on a fresh context, it recomputes them.  Same gradients."""
+    import torch
+    from ochre_gb300 import DeviceBatch, GpuContext
+    b, w, h = W.diff_union(n_paths=32), 1024, 1024
+    tgt = oracle.coverage_image(W.diff_union(n_paths=32, perturb=2.0), w, h)
+    ctx, fresh = GpuContext(0), GpuContext(0)
+    try:
+        db = DeviceBatch(b, 0)
+        cov = ctx.render_coverage(db, w, h)
+        dl = torch.empty_like(cov)
+        ctx.l2_loss(cov, torch.as_tensor(np.ascontiguousarray(tgt, np.float32), device="cuda:0"), dl)
+        runs = []
+        runs.append([t.cpu().numpy() for t in ctx.fill_backward(db, w, h, dl)] + [ctx.stats()["n_launches"]])
+        ctx.rasterize_device(DeviceBatch(W.glyph_run(n_paths=50), 0))
+        runs.append([t.cpu().numpy() for t in ctx.fill_backward(db, w, h, dl)] + [ctx.stats()["n_launches"]])
+        runs.append([t.cpu().numpy() for t in fresh.fill_backward(db, w, h, dl)] + [fresh.stats()["n_launches"]])
+        torch.cuda.synchronize()
+    finally:
+        ctx.close()
+        fresh.close()
+    (dp0, dx0, n0), (dp1, dx1, n1), (dp2, dx2, n2) = runs
+    assert n0 < n1 and n1 == n2
+    for dp, dx in ((dp1, dx1), (dp2, dx2)):
+        # float atomics add the per-line terms in no fixed order
+        assert _rel(dp0, dp) <= 1e-5 and _rel(dx0, dx) <= 1e-5
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("on_grid", [False, True])
 def test_gpu_gradient_raw_fills_and_multiple_contours(on_grid):
     """Raw (untransformed) fills get point gradients and a zero transform
