@@ -649,8 +649,8 @@ def run_ours(args, ws, rank, local):
 
     # ---- timed: device-resident inputs ----
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    clocks_path = os.path.join(ROOT, "gpurun_out", f"bench_clocks_r{rank}.csv") if os.path.isdir(
-        os.path.join(ROOT, "gpurun_out")) else f"/tmp/bench_clocks_r{rank}.csv"
+    # raw clock samples of the timed region (the JSON line carries their summary)
+    clocks_path = os.path.join(os.environ.get("OCHRE_BENCH_CLOCKS_DIR", "/tmp"), f"bench_clocks_r{rank}.csv")
     barrier(ws)
     torch.cuda.synchronize()
     wall0 = time.perf_counter()

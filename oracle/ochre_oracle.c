@@ -489,7 +489,7 @@ static void finish(rasterizer *r, collector *out) {
 }
 
 /* ------------------------------------------------------------------ */
-/* Batch driver: each raster is Rasterizer::new -> fill* -> finish      */
+/* Batch entry: each raster is Rasterizer::new -> fill* -> finish       */
 /* ------------------------------------------------------------------ */
 static const int FLOATS_PER_VERB[6] = {2, 2, 4, 6, 5, 0};
 
