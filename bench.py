@@ -528,6 +528,7 @@ def bench_differentiable(ctx, stream, flush, steps, n_scenes):
             "fwd_ms": f_ms, "fwd_bwd_ms": fb_ms,
             "fwd_scenes_per_s": b.n_rasters / (f_ms / 1e3), "fwd_bwd_scenes_per_s": b.n_rasters / (fb_ms / 1e3),
             "fwd_bwd_over_fwd": f_ms / fb_ms,
+            "roofline": _diff_roofline(b, w, h, f_ms, fb_ms),
             "grad_rel_err": {
                 "scenes_checked": k,
                 "vs_fp64_reference": {"points": rel(g_dp, a_dp), "transforms": rel(g_dx, a_dx),
@@ -542,6 +543,24 @@ def bench_differentiable(ctx, stream, flush, steps, n_scenes):
         torch.cuda.empty_cache()
     out["diff_scenes"]["generation_s"] = gen_s
     out["fd_check"] = _fd_check(ctx, sp)
+    return out
+
+
+def _diff_roofline(b, w, h, f_ms, fb_ms):
+    """Compulsory bytes of the differentiable step against the measured HBM
+    bandwidth.  Forward: the input read and 4 B of coverage written per
+    pixel; forward + backward adds 4 B of dL/dcov read per pixel, the input
+    read again and the gradients written (4 B per input float, 24 B per
+    transform)."""
+    peaks, kind = load_peaks()
+    peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+    px = b.n_rasters * w * h
+    fwd = b.input_bytes() + 4 * px
+    fb = fwd + 4 * px + b.input_bytes() + 4 * len(b.pts) + 24 * b.n_fills
+    out = {"unit": "GB/s", "peak": peak, "peak_kind": f"{kind} hbm_gbs", "bound": "hbm"}
+    for k, by, ms in (("fwd", fwd, f_ms), ("fwd_bwd", fb, fb_ms)):
+        gbs = by / (ms * 1e6)
+        out[k] = {"bytes": by, "achieved": gbs, "frac": gbs / peak}
     return out
 
 
