@@ -312,6 +312,28 @@ def test_gpu_gradient_matches_central_differences():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_gpu_gradient_fuzz(seed):
+    """Seeded random rasters (every verb in any order, conics, degenerate
+    curves, repeated points, pixel corners, shears, device-space fills;
+    some outlines cross the canvas edges): the GPU gradient against the FP64
+    reference gradient of the f32 model, the target the same rasters with
+    every transformed fill moved by N(0, 1.5) px."""
+    from fuzz_cases import fuzz_batch
+    b, w, h = fuzz_batch(12, seed, big_share=0.0), 768, 768
+    pert = copy.copy(b)
+    xf = b.fill_xf.copy()
+    xf[:, 4:] += np.random.default_rng(seed).normal(0, 1.5, (b.n_fills, 2)).astype(np.float32)
+    pert.fill_xf = xf
+    tgt = oracle.coverage_image(pert, w, h)
+    loss, dp, dx, _ = _gpu_grad(b, w, h, tgt)
+    rloss, rdp, rdx = oracle.adjoint64(b, w, h, tgt)
+    assert abs(loss - rloss) <= 1e-5 * rloss
+    assert _rel(dp, rdp) <= REL_TOL, _rel(dp, rdp)
+    assert _rel(dx, rdx) <= REL_TOL, _rel(dx, rdx)
+
+
+@pytest.mark.gpu
 def test_backward_reuses_the_forward_structure():
     """The backward right after render_coverage of the same batch reuses its
     lines and tiles (fewer launches); after another rasterization on the
