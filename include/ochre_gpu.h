@@ -143,8 +143,16 @@ int ochre_gpu_set_flags(ochre_gpu_ctx *ctx, uint32_t flags);
 int ochre_gpu_rasterize_device(ochre_gpu_ctx *ctx, const ochre_batch *in, ochre_result *out, void *stream);
 
 /* Same with host buffers: copies the batch to the device, rasterizes and
- * copies the result back into pinned host buffers owned by ctx. */
+ * copies the result back into pinned host buffers owned by ctx.  Checks the
+ * batch with ochre_validate_batch first. */
 int ochre_gpu_rasterize(ochre_gpu_ctx *ctx, const ochre_batch *in, ochre_result *out);
+
+/* Structural check of a batch in host memory, without a GPU: pointers present
+ * for nonzero counts, counts within the limits (OCHRE_E_CAPACITY), and
+ * fill_cmd_off / raster_fill_off starting at 0, non-decreasing and ending at
+ * n_cmds / n_fills (else OCHRE_E_INVALID).  Point values and verb codes are
+ * checked by the kernels that read them. */
+int ochre_validate_batch(const ochre_batch *in);
 
 int ochre_gpu_last_stats(const ochre_gpu_ctx *ctx, ochre_stats *out);
 

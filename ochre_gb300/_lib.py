@@ -26,6 +26,7 @@ EXPORTS = [
     "ochre_gpu_rasterize_noalloc", "ochre_gpu_set_tunable", "ochre_gpu_get_tunable",
     "ochre_gpu_render_coverage", "ochre_gpu_l2_loss", "ochre_gpu_fill_backward", "ochre_gpu_composite",
     "ochre_graph_create", "ochre_graph_launch", "ochre_graph_last_stats", "ochre_graph_info", "ochre_graph_destroy",
+    "ochre_validate_batch",
 ]
 
 
@@ -108,6 +109,7 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_gpu_set_flags.argtypes = [vp, u32]
         L.ochre_gpu_rasterize_device.argtypes = [vp, ctypes.POINTER(Batch), ctypes.POINTER(Result), vp]
         L.ochre_gpu_rasterize.argtypes = [vp, ctypes.POINTER(Batch), ctypes.POINTER(Result)]
+        L.ochre_validate_batch.argtypes = [ctypes.POINTER(Batch)]
         L.ochre_gpu_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
         L.ochre_gpu_last_timings.argtypes = [vp, ctypes.POINTER(KernelTime), u32, ctypes.POINTER(u32)]
         L.ochre_gpu_status_string.argtypes = [ctypes.c_int]

@@ -203,26 +203,12 @@ int check_device_error(ochre_gpu_ctx* ctx) {
     return OCHRE_OK;
 }
 
-// Host-side validation of the structural arrays of a host batch.
-static int validate_host(const ochre_batch* in) {
-    if (in->n_fills > 0 && (in->fill_cmd_off == nullptr || in->fill_xf == nullptr)) return OCHRE_E_INVALID;
-    if (in->n_cmds > 0 && (in->verbs == nullptr)) return OCHRE_E_INVALID;
-    if (in->n_floats > 0 && in->pts == nullptr) return OCHRE_E_INVALID;
-    if (in->n_cmds > MAX_COUNT || in->n_floats > 0xffffffffull) return OCHRE_E_CAPACITY;
-    if (in->n_rasters > MAX_RASTERS) return OCHRE_E_CAPACITY;
-    if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
-    if (in->n_fills == 0 && in->n_cmds != 0) return OCHRE_E_INVALID;
-    if (in->fill_cmd_off) {
-        if (in->fill_cmd_off[0] != 0 || in->fill_cmd_off[in->n_fills] != in->n_cmds) return OCHRE_E_INVALID;
-        for (uint32_t f = 0; f < in->n_fills; f++)
-            if (in->fill_cmd_off[f + 1] < in->fill_cmd_off[f]) return OCHRE_E_INVALID;
-    }
-    if (in->raster_fill_off) {
-        if (in->raster_fill_off[0] != 0 || in->raster_fill_off[in->n_rasters] != in->n_fills) return OCHRE_E_INVALID;
-        for (uint32_t r = 0; r < in->n_rasters; r++)
-            if (in->raster_fill_off[r + 1] < in->raster_fill_off[r]) return OCHRE_E_INVALID;
-    }
-    return OCHRE_OK;
+// 1 when a[0..n] is non-decreasing.  No early exit: the loop vectorises,
+// and reading the array (host memory) is what it costs.
+static bool non_decreasing(const uint32_t* a, uint64_t n) {
+    uint32_t bad = 0;
+    for (uint64_t i = 0; i < n; i++) bad |= (uint32_t)(a[i + 1] < a[i]);
+    return bad == 0;
 }
 
 int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out, cudaStream_t s) {
@@ -415,9 +401,27 @@ int ochre_gpu_rasterize_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_
     return run_device(ctx, in, out, s);
 }
 
+int ochre_validate_batch(const ochre_batch* in) {
+    if (!in) return OCHRE_E_INVALID;
+    if (in->n_fills > 0 && (in->fill_cmd_off == nullptr || in->fill_xf == nullptr)) return OCHRE_E_INVALID;
+    if (in->n_cmds > 0 && (in->verbs == nullptr)) return OCHRE_E_INVALID;
+    if (in->n_floats > 0 && in->pts == nullptr) return OCHRE_E_INVALID;
+    if (in->n_cmds > MAX_COUNT || in->n_floats > 0xffffffffull) return OCHRE_E_CAPACITY;
+    if (in->n_rasters > MAX_RASTERS) return OCHRE_E_CAPACITY;
+    if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
+    if (in->n_fills == 0 && in->n_cmds != 0) return OCHRE_E_INVALID;
+    if (in->fill_cmd_off && (in->fill_cmd_off[0] != 0 || in->fill_cmd_off[in->n_fills] != in->n_cmds ||
+                             !non_decreasing(in->fill_cmd_off, in->n_fills)))
+        return OCHRE_E_INVALID;
+    if (in->raster_fill_off && (in->raster_fill_off[0] != 0 || in->raster_fill_off[in->n_rasters] != in->n_fills ||
+                                !non_decreasing(in->raster_fill_off, in->n_rasters)))
+        return OCHRE_E_INVALID;
+    return OCHRE_OK;
+}
+
 int ochre_gpu_rasterize(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out) {
     if (!ctx || !in || !out) return OCHRE_E_INVALID;
-    int st = validate_host(in);
+    int st = ochre_validate_batch(in);
     if (st != OCHRE_OK) return st;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
     cudaStream_t s = ctx->own_stream;

@@ -309,6 +309,31 @@ def _c_batch(verbs_p, n_cmds, pts_p, n_floats, off_p, xf_p, flags_p, n_fills, ro
     return b
 
 
+def _host_c_batch(batch: Batch):
+    """(the C struct over the batch's host arrays, the arrays it points into)."""
+    keep = []
+
+    def p(a, dt):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a.ctypes.data
+
+    c = _c_batch(p(batch.verbs, np.uint8), batch.n_cmds, p(batch.pts, np.float32), len(batch.pts),
+                 p(batch.fill_cmd_off, np.uint32), p(batch.fill_xf, np.float32), p(batch.fill_flags, np.uint8),
+                 batch.n_fills, p(batch.raster_fill_off, np.uint32), batch.n_rasters,
+                 p(getattr(batch, "fill_width", None), np.float32))
+    return c, keep
+
+
+def validate_batch(batch: Batch) -> None:
+    """ochre_validate_batch: the structural check ochre_gpu_rasterize makes
+    before its first copy (no GPU needed); raises OchreError."""
+    c, keep = _host_c_batch(batch)
+    _lib.check(_lib.load().ochre_validate_batch(ctypes.byref(c)), "validate_batch")
+
+
 class DeviceBatch:
     """A Batch resident in device memory (torch CUDA tensors as storage)."""
 
@@ -409,19 +434,7 @@ class GpuContext:
     def rasterize_raw(self, batch: Batch) -> _lib.Result:
         """ochre_gpu_rasterize itself: results stay in the context's pinned
         host buffers (valid until the next call)."""
-        keep = []
-
-        def p(a, dt):
-            if a is None:
-                return None
-            a = np.ascontiguousarray(a, dtype=dt)
-            keep.append(a)
-            return a.ctypes.data
-
-        c = _c_batch(p(batch.verbs, np.uint8), batch.n_cmds, p(batch.pts, np.float32), len(batch.pts),
-                     p(batch.fill_cmd_off, np.uint32), p(batch.fill_xf, np.float32), p(batch.fill_flags, np.uint8),
-                     batch.n_fills, p(batch.raster_fill_off, np.uint32), batch.n_rasters,
-                     p(getattr(batch, "fill_width", None), np.float32))
+        c, keep = _host_c_batch(batch)
         r = _lib.Result()
         _lib.check(_lib.load().ochre_gpu_rasterize(self.handle, ctypes.byref(c), ctypes.byref(r)), "rasterize")
         return r

@@ -55,3 +55,38 @@ def test_create_without_gpu_fails_loudly():
     from ochre_gb300 import GpuContext
     with pytest.raises(_lib.OchreError):
         GpuContext(0)
+
+
+def test_validate_batch_checks_the_structure():
+    """ochre_validate_batch (host only): offset arrays must start at 0, not
+    decrease and end at the counts; the check ochre_gpu_rasterize makes."""
+    import dataclasses
+
+    import numpy as np
+
+    from ochre_gb300 import OchreError, validate_batch
+    from ochre_gb300 import workloads as W
+    b = W.glyph_run(n_paths=300, seed=4)
+    validate_batch(b)
+    bad_cases = []
+    off = b.fill_cmd_off.copy()
+    off[10], off[11] = off[11], off[10]            # decreasing
+    bad_cases.append(dataclasses.replace(b, fill_cmd_off=off))
+    off = b.fill_cmd_off.copy()
+    off[-1] -= 1                                    # does not end at n_cmds
+    bad_cases.append(dataclasses.replace(b, fill_cmd_off=off))
+    off = b.fill_cmd_off.copy()
+    off[0] = 1                                      # does not start at 0
+    bad_cases.append(dataclasses.replace(b, fill_cmd_off=off))
+    roff = np.arange(b.n_rasters + 1, dtype=np.uint32)
+    roff[5], roff[6] = roff[6], roff[5]
+    bad_cases.append(dataclasses.replace(b, raster_fill_off=roff))
+    bad_cases.append(dataclasses.replace(b, raster_fill_off=None, n_rasters=b.n_rasters - 1))
+    for bad in bad_cases:
+        with pytest.raises(OchreError) as e:
+            validate_batch(bad)
+        assert e.value.status == _lib.E_INVALID
+    # a raster holding several fills, and an empty batch
+    validate_batch(dataclasses.replace(b, raster_fill_off=np.array([0, 100, b.n_fills], np.uint32), n_rasters=2))
+    from ochre_gb300 import BatchBuilder
+    validate_batch(BatchBuilder().build())
