@@ -90,3 +90,34 @@ def test_validate_batch_checks_the_structure():
     validate_batch(dataclasses.replace(b, raster_fill_off=np.array([0, 100, b.n_fills], np.uint32), n_rasters=2))
     from ochre_gb300 import BatchBuilder
     validate_batch(BatchBuilder().build())
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes structures (sizes and field offsets) are the header's C
+    structures, compiled here with the host C compiler."""
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = [("ochre_batch", _lib.Batch), ("ochre_result", _lib.Result), ("ochre_stats", _lib.Stats),
+             ("ochre_kernel_time", _lib.KernelTime), ("ochre_output_buffers", _lib.OutputBuffers)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ochre_gpu.h"', "int main(void) {"]
+    for cname, cls in pairs:
+        lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'    printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    subprocess.run([cc, "-std=c11", "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                              text=True).stdout.splitlines())
+    for cname, cls in pairs:
+        assert int(got[cname]) == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, (cname, fname)
