@@ -185,3 +185,31 @@ def test_fuzz_oracle_matches_python_restatement(seed, stroke_share):
         assert [tuple(t) for t in xy.tolist()] == [t[:2] for t in tiles], i
         assert np.array_equal(alpha, np.array([np.frombuffer(t[2], np.uint8) for t in tiles]).reshape(-1, 64)), i
         assert [(int(a), int(c), int(w), int(t)) for (a, c), w, t in zip(sxy.tolist(), sw, st)] == spans, i
+
+
+def test_oracle_struct_layouts_match_its_header(tmp_path):
+    """The oracle wrapper's ctypes structures are oracle/ochre_oracle.h's."""
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    pairs = [("ochre_oracle_batch", oracle._Batch), ("ochre_oracle_result", oracle._Result)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "ochre_oracle.h"', "int main(void) {"]
+    for cname, cls in pairs:
+        lines.append(f'    printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'    printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.dirname(oracle.__file__), str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                              text=True).stdout.splitlines())
+    for cname, cls in pairs:
+        assert int(got[cname]) == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, (cname, fname)
