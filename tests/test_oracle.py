@@ -213,3 +213,21 @@ def test_oracle_struct_layouts_match_its_header(tmp_path):
         assert int(got[cname]) == ctypes.sizeof(cls), cname
         for fname, _ in cls._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, (cname, fname)
+
+
+@pytest.mark.parametrize("name,expect", [
+    ("readme_path", (70, 858, 50, 100, 23)),
+    ("cubic_boxes", (1_104_367, 10_086_440, 561_524, 873_599, 170_315)),
+    ("glyph_run", (7_825_524, 27_586_310, 1_235_618, 2_116_864, 253_952)),
+    ("diff_union", (130_435, 290_234, 10_026, 8_635, 992)),
+    ("stroke_run", (6_092_392, 76_028_159, 4_366_022, 5_825_432, 81_363)),
+])
+def test_configuration_counts(name, expect):
+    """Exact lines, increments, crossings, tiles and spans of the seeded
+    benchmark configurations (tests/golden/config_counts.py prints all of
+    them): pins the workload generators and the oracle together."""
+    import os
+    from ochre_gb300 import workloads as W
+    from golden.config_counts import counts
+    c = counts(getattr(W, name)(), threads=os.cpu_count() or 1)
+    assert (c["lines"], c["increments"], c["crossings"], c["tiles"], c["spans"]) == expect
