@@ -272,3 +272,21 @@ def test_every_fused_shape_matches_oracle(shape):
     assert ctx.stats()["fused"] == 1
     compare(got, ref, b.n_rasters)
     ctx.close()
+
+
+@pytest.mark.parametrize("name,tiles,spans", [
+    ("readme_path", 100, 23),
+    ("cubic_boxes", 873_599, 170_315),
+    ("glyph_run", 2_116_864, 253_952),
+    ("uneven_mix", 70_365_373, 17_974_124),
+    ("diff_union", 8_635, 992),
+    ("stroke_run", 5_825_432, 81_363),
+])
+def test_configuration_counts_match_oracle(gpu_ctx, name, tiles, spans):
+    """Full-size seeded configurations: the GPU's tile and span counts equal
+    the oracle's (pinned in tests/test_oracle.py)."""
+    from ochre_gb300 import DeviceBatch
+    b = getattr(W, name)()
+    gpu_ctx.rasterize_device(DeviceBatch(b))
+    st = gpu_ctx.stats()
+    assert (st["n_tiles"], st["n_spans"]) == (tiles, spans)
