@@ -15,6 +15,13 @@ tile coverage -> spans, producing the tiles and spans of every path.
   --impl reference : the reference's CPU algorithm (the oracle restatement,
            all host threads) on the same workload.
 
+The same JSON line also carries the extension workloads (uneven-size mix
+against one call per path, strokes, compositing, the differentiable render +
+loss + backward with its gradient checks and compulsory-byte roofline, and
+CUDA-graph replay against the eager call), the SM clocks sampled during the
+timed region (raw samples in $OCHRE_BENCH_CLOCKS_DIR, default /tmp) and the
+kernel launch count.
+
 Multi-GPU: paths are independent, so each rank rasterizes its own batch
 (weak scaling, no collective on the data path); value = all paths / max time.
 """
