@@ -141,6 +141,10 @@ def parse_path(d: str) -> List[PathCmd]:
     last_ctrl: Optional[Tuple[float, float]] = None   # for S (cubic) / T (quadratic)
     last_kind = None
     cmd = None
+    # After a closepath the next drawing command starts a new subpath at the
+    # same initial point (SVG 1.1 §8.3.3); ochre's Close moves nothing
+    # (rasterizer.rs:154), so that subpath gets an explicit Move.
+    after_close = False
     while not sc.done():
         c = sc.command()
         if c is not None:
@@ -153,9 +157,13 @@ def parse_path(d: str) -> List[PathCmd]:
             out.append(PathCmd.Close())
             cur = start
             last_ctrl, last_kind = None, None
+            after_close = True
             continue
         up = cmd.upper()
         rel = cmd.islower()
+        if after_close and up != "M":
+            out.append(PathCmd.Move(Vec2(*start)))
+        after_close = False
         if up == "A":
             a = [sc.number(), sc.number(), sc.number(), sc.flag(), sc.flag(), sc.number(), sc.number()]
         else:

@@ -38,6 +38,16 @@ def test_path_data_commands():
     assert got[11:] == [(0, [11, 21]), (1, [13, 23])]
 
 
+def test_drawing_after_closepath_starts_at_the_subpath_start():
+    """After z the next drawing command starts a new subpath at the initial
+    point (SVG 1.1 8.3.3): an explicit Move, since ochre's Close is a no-op."""
+    assert _flat(svg.parse_path("M0 0 L10 0 L10 10 z L5 5")) == [
+        (0, [0, 0]), (1, [10, 0]), (1, [10, 10]), (5, []), (0, [0, 0]), (1, [5, 5])]
+    assert _flat(svg.parse_path("M0 0 L10 0 z l5 5 z m1 1"))[3:] == [
+        (0, [0, 0]), (1, [5, 5]), (5, []), (0, [1, 1])]
+    assert _flat(svg.parse_path("M0 0 L10 0 z M3 3 L4 4"))[3:] == [(0, [3, 3]), (1, [4, 4])]
+
+
 def test_number_forms():
     p = svg.parse_path("M.5-1.5e1L1e-1.2 2,3-4.5.5")
     assert _flat(p) == [(0, [0.5, -15.0]), (1, [0.1, 0.2]), (1, [2, 3]), (1, [-4.5, 0.5])]
