@@ -717,10 +717,13 @@ def run_ours(args, ws, rank, local):
     dom_ms = dom["ms"] / max(1, dom["launches"])
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9 if dom_ms > 0 else 0.0
     traffic = None
+    inst_per_unit = None   # warp instructions per raster of the dominant kernel (ncu capture)
     tfile = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
     if os.path.exists(tfile):
         with open(tfile) as f:
-            traffic = json.load(f).get(dom["kernel"])
+            tj = json.load(f)
+        traffic = tj.get(dom["kernel"])
+        inst_per_unit = tj.get("warp_instructions_per_raster", {}).get(dom["kernel"])
 
     # ---- e2e: host C-ABI entry, pinned host inputs, H2D + D2H in the timed region ----
     def pinned(a):
@@ -797,6 +800,23 @@ def run_ours(args, ws, rank, local):
         extensions["composite"] = bench_composite(ctx, stream, flush, args.steps)
     n_paths_all = batch.n_rasters * ws
     value = n_paths_all * args.steps / dev_s_max
+    # The dominant kernel is issue-bound: its warp instructions per second
+    # against 4 per SM per cycle at the SM clock sampled in the timed region.
+    issue = None
+    clocks = clk.summary()
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    try:
+        if inst_per_unit and mhz and dom_ms:
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            peak_inst = sms * 4 * mhz * 1e6
+            ach_inst = inst_per_unit * batch.n_rasters / (dom_ms / 1e3)
+            issue = {"bound": "issue", "kernel": dom["kernel"], "unit": "warp instructions/s",
+                     "achieved": ach_inst, "peak": peak_inst, "frac": ach_inst / peak_inst,
+                     "warp_instructions_per_raster": inst_per_unit,
+                     "note": f"peak = {sms} SMs x 4 schedulers x {mhz:.0f} MHz; instructions per raster from "
+                             "the committed ncu capture, time from this run"}
+    except (RuntimeError, TypeError, ValueError, ZeroDivisionError) as e:
+        issue = {"error": str(e)}
     cpu = cpu_baseline(batch) if ws == 1 else None
     comp_in = batch.input_bytes()
     comp_out = output_bytes(st["n_tiles"], st["n_spans"], batch.n_rasters)
@@ -818,6 +838,7 @@ def run_ours(args, ws, rank, local):
                      "peak_kind": f"{peak_kind} hbm_gbs", "unit": "GB/s", "frac": achieved / peak,
                      "frac_of_nominal": achieved / NOMINAL_HBM_GBS,
                      "traffic": traffic, "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
+        "issue_roofline": issue,
         "path_roofline": {"compulsory_bytes_per_step": comp_in + comp_out, "achieved_gbs": path_gbs,
                           "frac": path_gbs / peak, "note": "input verbs+points+transforms and 68 B/tile + 6 B/span"},
         "kernels": kernels,
@@ -837,7 +858,7 @@ def run_ours(args, ws, rank, local):
                 "note": "pinned host inputs: points read by the kernels in place over the host link, the "
                         "other arrays copied; outputs written by the kernels into mapped host memory"},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
     ctx.close()
