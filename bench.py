@@ -267,7 +267,7 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "n_paths": batch.n_rasters, "seed": args.seed},
+        "config": bench_config(args, batch.n_rasters, ws),
         "tiles_per_s": n_tiles * args.steps / dt,
         "cpu_baseline": {"value": value, "unit": "paths/s", "cores": threads, "kind": "port",
                          "sample": f"the full workload ({batch.n_rasters} paths) per step, "
@@ -275,6 +275,15 @@ def run_reference(args, ws, rank):
         "e2e": {"value": value, "unit": "paths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+L2_RULE = "flushed (256 MiB write) between timed GPU steps, outside the events"
+
+
+def bench_config(args, n_paths: int, ws: int) -> dict:
+    """The workload of a bench line; both arms print the same dict."""
+    return {"workload": args.workload, "n_paths_per_gpu": n_paths, "seed": args.seed,
+            "parallelism": f"replicas{ws}" if ws > 1 else "single", "l2": L2_RULE}
 
 
 def _event_ms(fn, stream, flush, reps):
@@ -341,6 +350,19 @@ def bench_uneven(ctx, stream, flush, steps, peak):
     per_path_s = (time.perf_counter() - t0) / len(subs)
     chain_ms = _event_ms(lambda: ctx.rasterize_device(db, sp), stream, flush, 3)
     ctx.set_chain_only(False)
+    # parity (the metric's bar): the same 500 sampled paths, rasterized in one
+    # batched call, against the oracle
+    import oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from compare import compare
+    samp = B.subset(bt, [int(i) for i in idx])
+    got = ctx.rasterize(samp)
+    with np.errstate(all="ignore"):
+        cst = compare(got, oracle.run(samp, threads=os.cpu_count() or 1), samp.n_rasters)
+    parity = {"sample_paths": samp.n_rasters, "tiles": cst["tiles"], "spans": cst["spans"],
+              "tiles_spans_exact": True, "alpha_max_lsb": cst["max_lsb"],
+              "alpha_diff_fraction": cst["diff_fraction"],
+              "note": "500 paths sampled from the mix, one batched call; full size in tests/test_parity_gpu.py"}
     comp = bt.input_bytes() + output_bytes(st["n_tiles"], st["n_spans"], bt.n_rasters)
     return {
         "workload": "uneven_mix: 20000 paths, lognormal(median 32) segments clipped to 4-20000, 8192x8192",
@@ -351,6 +373,7 @@ def bench_uneven(ctx, stream, flush, steps, peak):
                                  "sample_paths": len(subs), "timing": "host wall clock over the sample"},
         "speedup_vs_per_path_chain": (bt.n_rasters / (ms / 1e3)) * per_path_s,
         "one_call_chain_ms": chain_ms,
+        "parity": parity,
         "roofline": {"kernel": dom["kernel"], "achieved_gbs": ach, "frac": ach / peak,
                      "frac_of_nominal": ach / NOMINAL_HBM_GBS,
                      "algorithmic_bytes_per_launch": dom_bytes, "ms_per_launch": dom_ms},
@@ -825,13 +848,11 @@ def run_ours(args, ws, rank, local):
         "metric": METRIC, "value": value, "unit": "paths/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "n_paths_per_gpu": batch.n_rasters, "seed": args.seed,
-                   "parallelism": f"replicas{ws}" if ws > 1 else "single",
-                   "l2": "flushed (256 MiB write) between timed steps, outside the events",
-                   "tiles_per_step": st["n_tiles"], "spans_per_step": st["n_spans"], "lines_per_step": st["n_lines"],
-                   "sort_entries_per_step": st["n_entries"], "key_bits": st["key_bits"],
-                   "sort_passes": st["sort_passes"], "launch_shape": tuned["choice"],
-                   "autotune_ms": tuned["ms"]},
+        "config": bench_config(args, batch.n_rasters, ws),
+        "workload_counts": {"tiles_per_step": st["n_tiles"], "spans_per_step": st["n_spans"],
+                            "lines_per_step": st["n_lines"], "sort_entries_per_step": st["n_entries"],
+                            "key_bits": st["key_bits"], "sort_passes": st["sort_passes"]},
+        "tuning": {"launch_shape": tuned["choice"], "autotune_ms": tuned["ms"]},
         "tiles_per_s": st["n_tiles"] * ws * args.steps / dev_s_max,
         "wall_s_timed_region": wall,
         "roofline": {"bound": "hbm", "kernel": dom["kernel"], "achieved": achieved, "peak": peak,

@@ -231,11 +231,13 @@ int ochre_gpu_fill_backward(ochre_gpu_ctx *ctx, const ochre_batch *in, uint32_t 
  *     array (roughly up to ~100k lines / ~150k tiles) or a caller buffer is
  *     too small; span_capacity must be >= the tile count (a span follows at
  *     most one tile), raster offsets need n_rasters + 1 entries.
- *   - The first call on each device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture.
+ *   - Every call looks up the array's device address (cudaGetSymbolAddress)
+ *     with the calling device current; the first call on a device also loads
+ *     the library's device code there, which places the array.  Make that
+ *     first call before any stream capture.
  *   - All calls share the array: calls that overlap on the GPU race (host
- *     threads are serialised).  `stream` is a cudaStream_t (NULL: default). */
+ *     threads are serialised; a call that fails waits for the work it queued
+ *     before returning).  `stream` is a cudaStream_t (NULL: default). */
 #define OCHRE_NOALLOC_SCRATCH_BYTES (32u << 20)
 
 typedef struct ochre_output_buffers {  /* device pointers; tile_alpha 8-byte aligned, tile_xy,

@@ -150,6 +150,14 @@ int copy_scalars_async(ochre_gpu_ctx* ctx, cudaStream_t s) {
     return OCHRE_OK;
 }
 
+cudaError_t reset_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s);
+    if (e == cudaSuccess && ctx->test_spin_log2 != 0u)
+        e = cudaMemcpyAsync(&dev_scalars(ctx)->spin_log2, &ctx->test_spin_log2, sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, s);
+    return e;
+}
+
 int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s) {
     const int st = copy_scalars_async(ctx, s);
     if (st != OCHRE_OK) return st;
@@ -212,6 +220,14 @@ static bool non_decreasing(const uint32_t* a, uint64_t n) {
 }
 
 int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out, cudaStream_t s) {
+    // the test hooks apply to this run only
+    struct HookReset {
+        ochre_gpu_ctx* c;
+        ~HookReset() {
+            c->test_spin_log2 = 0;
+            c->test_skip_first_raster = 0;
+        }
+    } hook_reset{ctx};
     std::memset(out, 0, sizeof *out);
     ctx->epoch++;
     ctx->stats = ochre_stats{};
@@ -225,7 +241,7 @@ int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out
         if (sst != OCHRE_OK) return sst;
     }
     const ochre_batch* in = &expanded;
-    OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+    OCHRE_CUDA_TRY(reset_scalars(ctx, s));
     const uint32_t R = in->n_rasters;
     OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
     OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
@@ -246,7 +262,7 @@ int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out
     if (handled) {
         ctx->stats.fused = 1;
     } else {
-        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+        OCHRE_CUDA_TRY(reset_scalars(ctx, s));
         uint32_t L = 0;
         st = stage_flatten(ctx, in, s, &L);
         if (st != OCHRE_OK) return st;
@@ -614,6 +630,12 @@ int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     } else if (!std::strcmp(name, "chain_coverage_form")) {
         if (value < 0 || value > 2) return OCHRE_E_INVALID;
         ctx->tune_chain_coverage_form = value;
+    } else if (!std::strcmp(name, "test_spin_log2")) {
+        if (value < 0 || value > 40) return OCHRE_E_INVALID;
+        ctx->test_spin_log2 = (uint32_t)value;
+    } else if (!std::strcmp(name, "test_skip_first_raster")) {
+        if (value < 0 || value > 1) return OCHRE_E_INVALID;
+        ctx->test_skip_first_raster = (uint32_t)value;
     } else {
         return OCHRE_E_INVALID;
     }

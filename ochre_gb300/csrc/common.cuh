@@ -39,7 +39,12 @@ enum : uint32_t {
 constexpr uint32_t FLATTEN_CAP = 1u << 20;   // lines per curve segment
 constexpr uint32_t WALK_CAP = 1u << 20;      // pixel cells per line
 constexpr int CONIC_DEPTH_CAP = 40;          // conic subdivision depth
-constexpr long long SPIN_LIMIT = 1ll << 23;  // polls of a look-back flag (~1 s with backoff)
+constexpr long long SPIN_LIMIT = 1ll << 21;  // polls of a look-back flag (about a second under load)
+// Word index, counted from the run's error word, of the run's poll-limit
+// override (log2 of the limit; 0: SPIN_LIMIT).  Every kernel that waits is
+// given the address of the error word of its run's device scalars, which
+// holds both (internal.h checks the layout).
+constexpr int SPIN_LOG2_WORD = 22;
 
 // The count a kernel works on: its launch-time value, or, when the count is
 // held on the device (launch chains replayed from a CUDA graph), the device
@@ -324,6 +329,43 @@ __device__ __forceinline__ uint64_t ld_relaxed64(const uint64_t* p) {
 __device__ __forceinline__ void st_relaxed64(uint64_t* p, uint64_t v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// ---------------------------------------------------------------------
+// Bounded waits with a run-wide abort.
+// ---------------------------------------------------------------------
+// A wait polls at most spin_limit(err) times.  The first wait that gives up
+// sets ERR_TIMEOUT in the run's error word; every other wait of the run sees
+// that bit within a few polls and gives up too, so a run whose waits cannot
+// finish ends after about one wait's limit, not one limit per wait.
+__device__ __forceinline__ long long spin_limit(const uint32_t* err) {
+    const uint32_t k = ld_relaxed(err + SPIN_LOG2_WORD);
+    return k == 0u ? SPIN_LIMIT : (1ll << min(k, 40u));
+}
+// One more poll by a single thread; true when it must stop waiting.
+__device__ __forceinline__ bool wait_give_up(long long& spins, long long limit, uint32_t* err) {
+    ++spins;
+    if ((spins & 7) == 0 && (ld_relaxed(err) & ERR_TIMEOUT) != 0u) return true;
+    if (spins > limit) {
+        atomicOr(err, ERR_TIMEOUT);
+        return true;
+    }
+    return false;
+}
+// The same for a wait a whole warp makes together: the answer is the same in
+// every lane (every lane calls it with the same spins and limit).
+__device__ __forceinline__ bool wait_give_up_warp(long long& spins, long long limit, uint32_t* err) {
+    ++spins;
+    const bool aborted = (spins & 7) == 0 && (ld_relaxed(err) & ERR_TIMEOUT) != 0u;
+    if (__any_sync(0xffffffffu, aborted)) return true;
+    if (spins > limit) {
+        if ((threadIdx.x & 31) == 0) atomicOr(err, ERR_TIMEOUT);
+        return true;
+    }
+    return false;
+}
+// A kernel that consumes the results of earlier waiting kernels of its run
+// returns at once when one of them gave up (their outputs are not valid).
+__device__ __forceinline__ bool run_aborted(const uint32_t* err) { return (ld_relaxed(err) & ERR_TIMEOUT) != 0u; }
+
 // Look-back slots publish data with relaxed stores followed by a release
 // store of the flag; readers acquire the flag, then read the data relaxed.
 // The release/acquire pair orders the data, so no separate fence is needed.

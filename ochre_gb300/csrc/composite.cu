@@ -168,7 +168,7 @@ extern "C" int ochre_gpu_composite(ochre_gpu_ctx* ctx, const ochre_result* res, 
     const uint64_t S = (uint64_t)T + N;
     OCHRE_CUDA_TRY(ctx->line_ent_off.ensure(S * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(S) * sizeof(ScanStatus<uint32_t>)));
-    OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+    OCHRE_CUDA_TRY(reset_scalars(ctx, s));
     OCHRE_LAUNCH(ctx, "composite_count", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
         S, PieceCount{res->tile_xy, res->span_xy, res->span_width, T, (int)w, (int)h, (int)w8},
         PieceOff{ctx->line_ent_off.as<uint32_t>()}, OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket,

@@ -171,6 +171,7 @@ __device__ __forceinline__ void chain_lookback(uint64_t* slots, uint32_t r, uint
     if (r == 0) return;
     int64_t top = (int64_t)r - 1;   // nearest predecessor not yet summed
     long long spins = 0;
+    const long long limit = spin_limit(err);
     while (top >= 0) {
         uint64_t w[CH_PER_LANE];
 #pragma unroll
@@ -193,10 +194,7 @@ __device__ __forceinline__ void chain_lookback(uint64_t* slots, uint32_t r, uint
             if (__ballot_sync(0xffffffffu, need && (w[k] >> 62) == 0u)) missing = true;
         }
         if (missing) {
-            if (++spins > SPIN_LIMIT) {
-                if (lane == 0) atomicOr(err, ERR_TIMEOUT);
-                break;
-            }
+            if (wait_give_up_warp(spins, limit, err)) break;
             if (spins > 16) __nanosleep(64);
             continue;
         }
@@ -799,7 +797,13 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
         OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
         OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->fused_chain.p, 0, (size_t)R * sizeof(uint64_t), s));
-        OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+        OCHRE_CUDA_TRY(reset_scalars(ctx, s));
+        if (ctx->test_skip_first_raster) {
+            // test hook: raster 0 is never taken, so its successors' output
+            // look-backs cannot finish and must give up
+            static const uint32_t first_ticket = 1u;
+            OCHRE_CUDA_TRY(cudaMemcpyAsync(&ds->ticket, &first_ticket, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        }
         if (n_cmds)
             OCHRE_LAUNCH(ctx, "fused_float_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
                 n_cmds, VerbFloats{in->verbs}, FloatOff{ctx->cmd_foff.as<uint32_t>()}, OpSumU32{}, 0u,

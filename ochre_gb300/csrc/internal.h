@@ -68,7 +68,11 @@ struct DevScalars {
     uint32_t fused_tiles;     // fused path totals
     uint32_t fused_spans;
     uint32_t n_rows;          // tile rows (raster, tile_y) of the general chain
+    uint32_t spin_log2;       // poll limit of the run's bounded waits, log2 (0: SPIN_LIMIT)
 };
+// The waits find spin_log2 from the error word's address (common.cuh).
+static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
+              "spin_log2 must sit SPIN_LOG2_WORD words after err");
 
 // Capacities of a launch chain captured into a CUDA graph.  Every buffer is
 // sized from them once; the counts stay on the device, each kernel reads its
@@ -184,6 +188,13 @@ struct ochre_gpu_ctx {
         sk_pfill_off, sk_first_close, sk_unit_start, sk_out_off, sk_out_foff, sk_unit_fill, sk_overbs, sk_opts,
         sk_ofill_off, sk_oflags, in_fill_width;
 
+    // Test hooks (ochre_gpu_set_tunable "test_*"), used by the next run only:
+    // the poll limit of its bounded waits (log2; 0: the default), and, on the
+    // fused kernel, a first raster that is never taken, so that the waits of
+    // its successors cannot finish.
+    uint32_t test_spin_log2 = 0;
+    uint32_t test_skip_first_raster = 0;
+
     // Launch-shape tunables (ochre_gpu_set_tunable; chosen by the autotuner).
     int tune_fused_threads = 64;
     int tune_fused_chunk = 16;
@@ -242,6 +253,8 @@ cudaError_t launch_plan_cap(ochre_gpu_ctx* ctx, uint32_t* count, uint32_t cap, c
 // (host-batch entry); every stage calls it before its first read of points.
 void wait_inputs(ochre_gpu_ctx* ctx, cudaStream_t s);
 
+// Zeroes the device scalars of a run (and applies the poll-limit test hook).
+cudaError_t reset_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);
 // Read the device scalars into ctx->h_scalars (synchronises the stream).
 int read_scalars(ochre_gpu_ctx* ctx, cudaStream_t s);
 // The same copy, enqueued only.

@@ -14,7 +14,9 @@
 // each stage clears what must start at zero (scan and sort look-back state,
 // tickets, device scalars) before it runs.  Calls that overlap on the GPU
 // (for example on two streams) race on the array; calls from several host
-// threads are serialised by a mutex.
+// threads are serialised by a mutex, and a call that fails waits for the
+// work it already queued before it releases the array, so the next call
+// (on any stream) never meets kernels of a failed one still writing into it.
 #include <mutex>
 
 #include "common.cuh"
@@ -23,15 +25,15 @@
 namespace {
 
 constexpr size_t kScratchBytes = OCHRE_NOALLOC_SCRATCH_BYTES;
-constexpr int kMaxDevices = 64;
 
 // The scratch itself.  Host code must not pass `g_scratch` to a kernel: in
-// host code the name is a host-side stand-in, so the device address is looked
-// up once per device with cudaGetSymbolAddress.
+// host code the name is a host-side stand-in, so every call looks the device
+// address up with cudaGetSymbolAddress, with the calling device current.  The
+// lookup allocates nothing; doing it per call (not once per device) keeps the
+// address right when a context is torn down and created again, which reloads
+// the module and may place the array elsewhere.
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-void* g_scratch_addr[kMaxDevices];
-bool g_scratch_ready[kMaxDevices];
 ochre::DevScalars g_host_scalars;  // host copy of the run's device scalars
 std::mutex g_mutex;
 
@@ -68,21 +70,19 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
     std::lock_guard<std::mutex> lock(g_mutex);
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return OCHRE_E_CUDA;
-    if (dev < 0 || dev >= kMaxDevices) return OCHRE_E_CAPACITY;
-    if (!g_scratch_ready[dev]) {
-        // One-time set-up on this device (the device is current here).
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || p == nullptr) {
+    // The array's device address on the current device.  The first call on a
+    // device loads the library's device code there (placing the array).
+    void* scratch = nullptr;
+    {
+        const cudaError_t e = cudaGetSymbolAddress(&scratch, g_scratch);
+        if (e != cudaSuccess || scratch == nullptr) {
             cudaGetLastError();
             return OCHRE_E_CUDA;
         }
-        g_scratch_addr[dev] = p;
-        g_scratch_ready[dev] = true;
     }
 
     ochre::Arena arena;
-    arena.base = static_cast<char*>(g_scratch_addr[dev]);
+    arena.base = static_cast<char*>(scratch);
     arena.size = kScratchBytes;
 
     ochre_gpu_ctx ctx;
@@ -120,7 +120,14 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
     if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
     ochre_result res;
     int st = ochre::run_device(&ctx, in, &res, ctx.own_stream);
-    if (st != OCHRE_OK && arena.overflow) st = OCHRE_E_CAPACITY;
+    if (st != OCHRE_OK) {
+        // A stage can fail after launching kernels (an intermediate that no
+        // longer fits the array is only found when the next stage sizes its
+        // buffers).  Wait for them while the array is still held.
+        cudaStreamSynchronize(ctx.own_stream);
+        cudaGetLastError();
+        if (arena.overflow) st = OCHRE_E_CAPACITY;
+    }
     if (st == OCHRE_OK) {
         out->n_tiles = res.n_tiles;
         out->n_spans = res.n_spans;

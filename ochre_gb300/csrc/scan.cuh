@@ -4,8 +4,8 @@
 // words), the associative operator, the input functor in(i) -> T and the
 // output functor out(i, exclusive_prefix, own_value).  Tiles are numbered by
 // an atomic ticket taken when a block starts, so a block only ever waits on
-// blocks that are already resident; every wait is bounded (SPIN_LIMIT) and a
-// timeout sets ERR_TIMEOUT instead of hanging.
+// blocks that are already resident; every wait is bounded (wait_give_up_warp)
+// and a timeout sets ERR_TIMEOUT instead of hanging.
 #pragma once
 
 #include "common.cuh"
@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_de
             }
             int64_t top = (int64_t)tile - 1;
             long long spins = 0;
+            const long long limit = spin_limit(err);
             while (top >= 0) {
                 const int64_t j = top - lane;
                 uint32_t f = 2u;   // before tile 0: an inclusive identity
@@ -92,10 +93,7 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_de
                 const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
                 const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
                 if (__ballot_sync(0xffffffffu, f == 0u) & need) {
-                    if (++spins > SPIN_LIMIT) {
-                        if (lane == 0) atomicOr(err, ERR_TIMEOUT);
-                        break;
-                    }
+                    if (wait_give_up_warp(spins, limit, err)) break;
                     if (spins > 64) __nanosleep(64);
                     continue;
                 }

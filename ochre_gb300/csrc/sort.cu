@@ -129,11 +129,12 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
             st_release(my, LB_AGG | run);
             int64_t j = (int64_t)tile - 1;
             long long spins = 0;
+            const long long limit = spin_limit(err);
             while (j >= 0) {
                 const uint32_t v = ld_acquire(lookback + (size_t)j * 256 + d);
                 const uint32_t f = v & ~LB_MASK;
                 if (f == 0u) {
-                    if (++spins > SPIN_LIMIT) { atomicOr(err, ERR_TIMEOUT); break; }
+                    if (wait_give_up(spins, limit, err)) break;
                     if (spins > 64) __nanosleep(64);
                     continue;
                 }

@@ -380,7 +380,7 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     OCHRE_CUDA_TRY(ctx->sk_cmd_mv.ensure(n * 4));
     OCHRE_CUDA_TRY(ctx->sk_cmd_ep.ensure(n * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n) * sizeof(ScanStatus<CmdScan>)));
-    OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->scalars.p, 0, sizeof(DevScalars), s));
+    OCHRE_CUDA_TRY(reset_scalars(ctx, s));
     OCHRE_LAUNCH(ctx, "stroke_cmd_scan", s, OCHRE_CUDA_TRY(launch_scan<CmdScan>(
         n, CmdIn{in->verbs, &ds->err},
         CmdOut{ctx->sk_cmd_foff.as<uint32_t>(), ctx->sk_cmd_mv.as<uint32_t>(), ctx->sk_cmd_ep.as<uint32_t>()},

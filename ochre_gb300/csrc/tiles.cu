@@ -70,10 +70,12 @@ __global__ void k_tile_info(const uint32_t* __restrict__ vals, const BinRec* __r
                             const uint32_t* __restrict__ head, const uint32_t* __restrict__ head_bins,
                             const int32_t* __restrict__ head_wind, const int32_t* __restrict__ raster_wbase,
                             const uint32_t* __restrict__ total_bins, uint32_t n_tiles, const uint32_t* n_dev,
-                            uint32_t n_rasters, TileInfo* __restrict__ info, uint32_t* __restrict__ raster_tile_off) {
+                            uint32_t n_rasters, TileInfo* __restrict__ info, uint32_t* __restrict__ raster_tile_off,
+                            const uint32_t* err) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     n_tiles = (uint32_t)dev_count(n_tiles, n_dev);
-    if (t >= n_tiles) return;
+    // a wait of the sort gave up: the sorted entries are not valid indices
+    if (t >= n_tiles || run_aborted(err)) return;
     const uint32_t h = head[t];
     const BinRec* rec = bins + vals[h];
     const int r = (int)rec->raster;
@@ -120,6 +122,9 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
     constexpr int WARPS = 4;
     // device-held count (graph replays): blocks past it end before publishing
     n_tiles = (uint32_t)dev_count(n_tiles, n_dev);
+    // an earlier wait of the run gave up: the tile data is not valid (the
+    // blocks' own waits then give up at once too)
+    if (run_aborted(err)) return;
     // [tile][area cells | height cells], ACC_STRIDE floats per tile; see acc_idx
     __shared__ __align__(16) float s_acc[WARPS][CH][ACC_STRIDE];
     __shared__ uint32_t s_head[WARPS][CH];
@@ -219,6 +224,7 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
         float c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         int64_t top = (int64_t)blk - 1;
         long long spins = 0;
+        const long long limit = spin_limit(err);
         while (top >= 0) {
             const int64_t j = top - lane;
             uint32_t f = 2u;   // before block 0: an inclusive zero
@@ -227,10 +233,7 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
             const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
             const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
             if (__ballot_sync(0xffffffffu, f == 0u) & need) {
-                if (++spins > SPIN_LIMIT) {
-                    if (lane == 0) atomicOr(err, ERR_TIMEOUT);
-                    break;
-                }
+                if (wait_give_up_warp(spins, limit, err)) break;
                 if (spins > 16) __nanosleep(64);
                 continue;
             }
@@ -349,8 +352,10 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     const TileInfo* __restrict__ info, uint32_t n_tiles, const uint32_t* n_dev, const uint32_t* __restrict__ row_start,
     const uint32_t* __restrict__ n_rows_p, uint32_t* ticket, uint32_t* __restrict__ out_xy,
     uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov, uint32_t* __restrict__ span_flag,
-    uint64_t* __restrict__ span_val, bool cov_signed) {
+    uint64_t* __restrict__ span_val, const uint32_t* err, bool cov_signed) {
     constexpr int WARPS = 4;
+    // an earlier wait of the run gave up: the tile data is not valid
+    if (run_aborted(err)) return;
     __shared__ __align__(16) float s_acc[WARPS][CH][ACC_STRIDE];
     __shared__ uint32_t s_head[WARPS][CH];
     __shared__ TileInfo s_info[WARPS][CH + 1];
@@ -556,7 +561,7 @@ static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, uint32_t n_rows, boo
             ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(),
             T, t_dev, ctx->tile_row_start.as<uint32_t>(), &ds->n_rows, &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
             ctx->out_tile_alpha.as<uint8_t>(), cov, ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(),
-            ctx->cov_signed);
+            &ds->err, ctx->cov_signed);
     } else {
         const uint32_t blocks = (T + TPW - 1) / TPW;
         cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)blocks * sizeof(TileBlockState), s);
@@ -615,7 +620,7 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
                          ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->tile_head.as<uint32_t>(),
                          ctx->tile_head_bins.as<uint32_t>(), ctx->tile_head_wind.as<int32_t>(),
                          ctx->raster_wbase.as<int32_t>(), &ds->n_bins, T, t_dev, R, ctx->tile_info.as<TileInfo>(),
-                         ctx->out_raster_tile_off.as<uint32_t>()));
+                         ctx->out_raster_tile_off.as<uint32_t>(), &ds->err));
     OCHRE_CUDA_TRY(cudaGetLastError());
     if (T) {
         OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(T) * sizeof(ScanStatus<uint32_t>)));

@@ -32,19 +32,28 @@ def compare(gpu: dict, ref: dict, n_rasters: int) -> dict:
         if not np.array_equal(g.astype(np.int64), r.astype(np.int64)):
             bad = int(np.flatnonzero((g != r).reshape(len(g), -1).any(axis=1))[0])
             raise AssertionError(f"{k} differs at span {bad}: gpu {g[bad]} oracle {r[bad]}")
-    ga = gpu["tile_alpha"].astype(np.int16)
-    ra = ref["tile_alpha"].astype(np.int16)
-    d = np.abs(ga - ra)
-    max_lsb = int(d.max()) if d.size else 0
-    if max_lsb > ALPHA_TOL_LSB:
-        t, c = np.unravel_index(int(np.argmax(d)), d.shape)
-        raise AssertionError(f"alpha differs by {max_lsb} LSB at tile {t} cell {c} "
-                             f"(gpu {ga[t, c]} oracle {ra[t, c]}, tile at {ref['tile_xy'][t]})")
+    ga_all, ra_all = gpu["tile_alpha"], ref["tile_alpha"]
+    assert ga_all.shape == ra_all.shape, (ga_all.shape, ra_all.shape)
+    # in slices of tiles, so that full-size results (tens of millions of
+    # tiles) need no second full-size copy
+    max_lsb, n_diff = 0, 0
+    CH = 1 << 22
+    for a in range(0, len(ra_all), CH):
+        ga = ga_all[a:a + CH].astype(np.int16)
+        ra = ra_all[a:a + CH].astype(np.int16)
+        d = np.abs(ga - ra)
+        m = int(d.max()) if d.size else 0
+        if m > ALPHA_TOL_LSB:
+            t, c = np.unravel_index(int(np.argmax(d)), d.shape)
+            raise AssertionError(f"alpha differs by {m} LSB at tile {a + t} cell {c} "
+                                 f"(gpu {ga[t, c]} oracle {ra[t, c]}, tile at {ref['tile_xy'][a + t]})")
+        max_lsb = max(max_lsb, m)
+        n_diff += int(np.count_nonzero(d))
     stats = {
-        "tiles": int(len(ra)),
+        "tiles": int(len(ra_all)),
         "spans": int(len(ref["span_w"])),
         "max_lsb": max_lsb,
-        "diff_fraction": float((d > 0).mean()) if d.size else 0.0,
+        "diff_fraction": n_diff / ra_all.size if ra_all.size else 0.0,
     }
     if "tile_cov" in gpu and "tile_cov" in ref:
         e = np.abs(gpu["tile_cov"].astype(np.float64) - ref["tile_cov"].astype(np.float64))

@@ -274,6 +274,35 @@ def test_every_fused_shape_matches_oracle(shape):
     ctx.close()
 
 
+@pytest.fixture(scope="session")
+def dense_scenes():
+    # the full dense-scenes configuration (4,096 scenes of 512^2, about a
+    # million fills) takes most of a minute to generate: once per session
+    return W.diff_scenes()
+
+
+@pytest.mark.parametrize("name", ["cubic_boxes", "uneven_mix", "stroke_run", "diff_scenes"])
+def test_full_size_configuration_matches_oracle(gpu_ctx, request, name):
+    """Full-size seeded configurations against the oracle: every tile
+    position, per-raster tile and span offset, span position, width and tile
+    index exact; every alpha byte within 1 LSB.  The cubic boxes (1,000
+    paths) are the plain-method configuration compared against the CPU
+    rasterizer; the uneven mix (20,000 paths, 70 M tiles) carries the
+    batched-vs-plain metric; the dense scenes (4,096 rasters) the
+    differentiable one."""
+    import os
+
+    from ochre_gb300 import DeviceBatch
+    b = request.getfixturevalue("dense_scenes") if name == "diff_scenes" else getattr(W, name)()
+    db = DeviceBatch(b)
+    got = gpu_ctx.device_result_to_numpy(gpu_ctx.rasterize_device(db), b.n_rasters)
+    del db
+    ref = oracle.run(b, threads=os.cpu_count() or 1)
+    st = compare(got, ref, b.n_rasters)
+    print(name, st)
+    assert st["diff_fraction"] < 1e-3, st
+
+
 @pytest.mark.parametrize("name,tiles,spans", [
     ("readme_path", 100, 23),
     ("cubic_boxes", 873_599, 170_315),
@@ -281,12 +310,13 @@ def test_every_fused_shape_matches_oracle(shape):
     ("uneven_mix", 70_365_373, 17_974_124),
     ("diff_union", 8_635, 992),
     ("stroke_run", 5_825_432, 81_363),
+    ("diff_scenes", 12_319_083, 784_530),
 ])
-def test_configuration_counts_match_oracle(gpu_ctx, name, tiles, spans):
+def test_configuration_counts_match_oracle(gpu_ctx, request, name, tiles, spans):
     """Full-size seeded configurations: the GPU's tile and span counts equal
     the oracle's (pinned in tests/test_oracle.py)."""
     from ochre_gb300 import DeviceBatch
-    b = getattr(W, name)()
+    b = request.getfixturevalue("dense_scenes") if name == "diff_scenes" else getattr(W, name)()
     gpu_ctx.rasterize_device(DeviceBatch(b))
     st = gpu_ctx.stats()
     assert (st["n_tiles"], st["n_spans"]) == (tiles, spans)
