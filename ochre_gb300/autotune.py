@@ -1,11 +1,15 @@
 """Launch-shape autotuner.
 
-Times every kernel shape the library offers (threads per raster and tiles per
-accumulation pass of the fused small-raster kernel; tiles per warp of the
-general chain's coverage kernel) on a sample of the caller's workload,
-keeps the fastest, and caches the choice per GPU name in
-``ochre_gb300/_build/tune.json``.  Results never depend on the shape (tile
-and span structure is exact, alpha within 1 LSB of the oracle either way).
+Times every kernel shape the library offers on a sample of the caller's
+workload, keeps the fastest, and caches the choice per GPU name in
+``ochre_gb300/_build/tune.json``:
+  * the fused small-raster kernel: one warp per raster with 256, 384 or 512
+    increments held in shared memory (the rest spill to global memory; fewer
+    slots fit more warps on an SM), or one CTA per raster with its threads
+    per raster and tiles per accumulation pass;
+  * tiles per warp of the general chain's coverage kernel.
+Results never depend on the shape (tile and span structure is exact, alpha
+within 1 LSB of the oracle either way).
 """
 from __future__ import annotations
 
@@ -17,7 +21,18 @@ from typing import Optional
 
 from . import _lib, build
 
-FUSED_SHAPES = [(64, 8), (64, 16), (64, 32), (96, 8), (96, 16), (128, 16), (128, 32)]
+FUSED_SHAPES = [(64, 8), (64, 16), (64, 32), (96, 8), (96, 16), (128, 16), (128, 32)]   # CTA form
+WARP_INCS = [256, 384, 512]                                                               # warp form
+
+
+def fused_candidates() -> list:
+    """Every fused shape as the tunables that select it."""
+    return ([{"fused_form": 1, "fused_warp_inc": i} for i in WARP_INCS]
+            + [{"fused_form": 2, "fused_threads": t, "fused_chunk": c} for t, c in FUSED_SHAPES])
+
+
+def shape_name(p: dict) -> str:
+    return f"warp{p['fused_warp_inc']}" if p["fused_form"] == 1 else f"cta{p['fused_threads']}x{p['fused_chunk']}"
 CHAIN_TILES_PER_WARP = [4, 8, 16]
 CACHE = os.path.join(build.BUILD, "tune.json")
 
@@ -85,12 +100,14 @@ def tune(ctx, fused_sample=None, chain_sample=None, reps: int = 3, save: bool = 
     db = DeviceBatch(fused_sample, ctx.device)
     ctx.set_chain_only(False)
     best_f, best_t = None, float("inf")
-    for th, ch in FUSED_SHAPES:
-        apply(ctx, {"fused_threads": th, "fused_chunk": ch})
+    for cand in fused_candidates():
+        apply(ctx, cand)
         ms = _time(ctx, db, reps)
-        report["fused"][f"{th}x{ch}"] = ms
-        if ctx.stats().get("fused") and ms < best_t:
-            best_f, best_t = (th, ch), ms
+        report["fused"][shape_name(cand)] = ms
+        st = ctx.stats()
+        # a shape counts only when its own form handled the sample
+        if st.get("fused") and st.get("fused_form") == cand["fused_form"] and ms < best_t:
+            best_f, best_t = cand, ms
     db = DeviceBatch(chain_sample, ctx.device)
     ctx.set_chain_only(True)
     best_c, best_ct = None, float("inf")
@@ -101,8 +118,8 @@ def tune(ctx, fused_sample=None, chain_sample=None, reps: int = 3, save: bool = 
         if ms < best_ct:
             best_c, best_ct = tpw, ms
     ctx.set_chain_only(old_chain)
-    choice = {"fused_threads": (best_f or (64, 16))[0], "fused_chunk": (best_f or (64, 16))[1],
-              "chain_tiles_per_warp": best_c or 8}
+    choice = dict(best_f or {"fused_form": 1, "fused_warp_inc": 384})
+    choice["chain_tiles_per_warp"] = best_c or 8
     apply(ctx, choice)
     if save:
         cache = load_cache()

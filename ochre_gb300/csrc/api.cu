@@ -387,7 +387,7 @@ std::vector<DevBuf*> device_buffers(ochre_gpu_ctx* ctx) {
                      &ctx->raster_empty, &ctx->raster_wsum, &ctx->raster_wbase, &ctx->tile_head_bins,
                      &ctx->tile_head_wind, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_row_start, &ctx->tile_state,
-                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain, &ctx->fused_stage,
+                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain, &ctx->fused_stage, &ctx->fused_spill,
                      &ctx->grad_g, &ctx->grad_gs, &ctx->grad_left, &ctx->grad_line, &ctx->grad_pts,
                      &ctx->sk_cmd_foff, &ctx->sk_cmd_mv, &ctx->sk_cmd_ep, &ctx->sk_poly_off, &ctx->sk_poly_foff,
                      &ctx->sk_pverbs, &ctx->sk_ppts, &ctx->sk_pfoff, &ctx->sk_pfill_off, &ctx->sk_first_close,
@@ -621,6 +621,12 @@ int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     if (!std::strcmp(name, "fused_threads")) {
         if (value != 64 && value != 96 && value != 128) return OCHRE_E_INVALID;
         ctx->tune_fused_threads = value;
+    } else if (!std::strcmp(name, "fused_form")) {
+        if (value != 1 && value != 2) return OCHRE_E_INVALID;
+        ctx->tune_fused_form = value;
+    } else if (!std::strcmp(name, "fused_warp_inc")) {
+        if (value != 256 && value != 384 && value != 512) return OCHRE_E_INVALID;
+        ctx->tune_fused_warp_inc = value;
     } else if (!std::strcmp(name, "fused_chunk")) {
         if (value != 8 && value != 16 && value != 32) return OCHRE_E_INVALID;
         ctx->tune_fused_chunk = value;
@@ -646,6 +652,8 @@ int ochre_gpu_get_tunable(const ochre_gpu_ctx* ctx, const char* name, int* value
     if (!ctx || !name || !value) return OCHRE_E_INVALID;
     if (!std::strcmp(name, "fused_threads")) *value = ctx->tune_fused_threads;
     else if (!std::strcmp(name, "fused_chunk")) *value = ctx->tune_fused_chunk;
+    else if (!std::strcmp(name, "fused_form")) *value = ctx->tune_fused_form;
+    else if (!std::strcmp(name, "fused_warp_inc")) *value = ctx->tune_fused_warp_inc;
     else if (!std::strcmp(name, "chain_tiles_per_warp")) *value = ctx->tune_chain_tiles_per_warp;
     else if (!std::strcmp(name, "chain_coverage_form")) *value = ctx->tune_chain_coverage_form;
     else return OCHRE_E_INVALID;

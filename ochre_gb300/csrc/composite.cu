@@ -107,11 +107,12 @@ __device__ __forceinline__ uint64_t lower_bound_u64(const uint64_t* a, uint64_t 
 
 __global__ void k_composite(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals, uint64_t E,
                             uint32_t rbits, uint32_t T, const uint8_t* __restrict__ tile_alpha,
-                            const uint32_t* __restrict__ colors, uint32_t w, uint32_t h, uint32_t w8, uint32_t h8,
-                            uint32_t* __restrict__ canvas) {
+                            const uint32_t* __restrict__ colors, uint32_t n_rasters, uint32_t w, uint32_t h,
+                            uint32_t w8, uint32_t h8, uint32_t* __restrict__ canvas, const uint32_t* err) {
     const uint64_t st = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (st >= (uint64_t)w8 * h8) return;
+    // a wait of the sort gave up: the sorted pieces are not valid
+    if (st >= (uint64_t)w8 * h8 || run_aborted(err)) return;
     const uint64_t lo = lower_bound_u64(keys, E, st << rbits);
     const uint64_t hi = lower_bound_u64(keys, E, (st + 1) << rbits);
     if (lo == hi) return;
@@ -131,6 +132,7 @@ __global__ void k_composite(const uint64_t* __restrict__ keys, const uint32_t* _
     for (uint64_t e = lo; e < hi; e++) {
         const uint32_t r = (uint32_t)(keys[e] & rmask);
         const uint32_t v = vals[e];
+        if (r >= n_rasters) continue;
         const uint32_t col = colors[r];
 #pragma unroll
         for (int k = 0; k < 2; k++) {
@@ -175,6 +177,8 @@ extern "C" int ochre_gpu_composite(ochre_gpu_ctx* ctx, const ochre_result* res, 
         &ds->n_line_ent, &ds->err, s)));
     int st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
+    st = check_device_error(ctx);
+    if (st != OCHRE_OK) return st;
     const uint64_t E = host_scalars(ctx)->n_line_ent;
     if (E == 0) return OCHRE_OK;
     if (E > MAX_COUNT) return OCHRE_E_CAPACITY;
@@ -194,7 +198,8 @@ extern "C" int ochre_gpu_composite(ochre_gpu_ctx* ctx, const ochre_result* res, 
     const uint64_t threads = (uint64_t)w8 * h8 * 32;
     OCHRE_LAUNCH(ctx, "composite", s, k_composite<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
         ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(), E, rbits, T, res->tile_alpha,
-        reinterpret_cast<const uint32_t*>(colors), w, h, w8, h8, reinterpret_cast<uint32_t*>(canvas)));
+        reinterpret_cast<const uint32_t*>(colors), n_rasters, w, h, w8, h8, reinterpret_cast<uint32_t*>(canvas),
+        &ds->err));
     OCHRE_CUDA_TRY(cudaGetLastError());
     ctx->stats.n_launches = ctx->launches;
     collect_timings(ctx, s);

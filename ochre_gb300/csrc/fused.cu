@@ -35,6 +35,7 @@
 #include "common.cuh"
 #include "internal.h"
 #include "scan.cuh"
+#include "fused.cuh"
 
 namespace ochre {
 
@@ -74,18 +75,6 @@ struct FusedSmem {
     uint32_t tile_base, span_base;
     int32_t gx0, gy0, gw, gh;
 };
-
-// Per-raster look-back slot: one 64-bit word holding a flag (bits 62-63: 0
-// none, 1 aggregate, 2 inclusive) and two 30-bit counts (tiles in bits 0-29,
-// spans in bits 30-59).  One naturally aligned 64-bit access reads or writes
-// flag and counts together, so readers need no acquire/release pairing.
-// Counts saturate at 2^30 - 1, above every output capacity.
-constexpr uint64_t CH_AGG = 1ull << 62, CH_INC = 2ull << 62;
-constexpr uint32_t CH_MAX = (1u << 30) - 1u;
-__device__ __forceinline__ uint64_t ch_pack(uint64_t flag, uint32_t a0, uint32_t a1) {
-    return flag | ((uint64_t)min(a1, CH_MAX) << 30) | min(a0, CH_MAX);
-}
-constexpr int CH_PER_LANE = 4;   // predecessors one lane reads per look-back round
 
 // ---- block-wide scans over WARPS * 32 threads (one value each) ----
 template <int WARPS>
@@ -151,105 +140,7 @@ __device__ __forceinline__ void block_excl_max2(int a, int b, int& a_ex, int& b_
     b_ex = max(base_b, eb);
 }
 
-// Publish raster r's counts: its aggregate, or, for raster 0, its inclusive
-// value.  One thread.
-__device__ __forceinline__ void chain_publish(uint64_t* slots, uint32_t r, uint32_t a0, uint32_t a1) {
-    st_relaxed64(slots + r, ch_pack(r == 0 ? CH_INC : CH_AGG, a0, a1));
-}
 
-// Resolve raster r's exclusive prefix (its aggregate a0, a1 already
-// published) by a warp-cooperative decoupled look-back over 32 x CH_PER_LANE
-// predecessors per round (independent loads, one latency per round), and
-// publish its inclusive value.  Predecessor q of a round (q = k * 32 + lane,
-// nearest first) is raster top - q.  Called by one full warp; returns the
-// prefix in every lane.  Every wait is bounded.
-__device__ __forceinline__ void chain_lookback(uint64_t* slots, uint32_t r, uint32_t a0, uint32_t a1, uint32_t* err,
-                                               uint32_t& p0, uint32_t& p1) {
-    const int lane = threadIdx.x & 31;
-    p0 = 0;
-    p1 = 0;
-    if (r == 0) return;
-    int64_t top = (int64_t)r - 1;   // nearest predecessor not yet summed
-    long long spins = 0;
-    const long long limit = spin_limit(err);
-    while (top >= 0) {
-        uint64_t w[CH_PER_LANE];
-#pragma unroll
-        for (int k = 0; k < CH_PER_LANE; k++) {
-            const int64_t j = top - (k * 32 + lane);
-            w[k] = j >= 0 ? ld_relaxed64(slots + j) : CH_INC;   // before raster 0: an inclusive zero
-        }
-        // nearest inclusive predecessor of the round: q_inc (32 * CH_PER_LANE if none)
-        int q_inc = 32 * CH_PER_LANE;
-#pragma unroll
-        for (int k = CH_PER_LANE - 1; k >= 0; k--) {
-            const uint32_t m2 = __ballot_sync(0xffffffffu, (w[k] >> 62) == 2u);
-            if (m2) q_inc = k * 32 + __ffs(m2) - 1;
-        }
-        // every predecessor up to it must have published
-        bool missing = false;
-#pragma unroll
-        for (int k = 0; k < CH_PER_LANE; k++) {
-            const bool need = k * 32 + lane <= q_inc;
-            if (__ballot_sync(0xffffffffu, need && (w[k] >> 62) == 0u)) missing = true;
-        }
-        if (missing) {
-            if (wait_give_up_warp(spins, limit, err)) break;
-            if (spins > 16) __nanosleep(64);
-            continue;
-        }
-        uint32_t v0 = 0, v1 = 0;
-#pragma unroll
-        for (int k = 0; k < CH_PER_LANE; k++) {
-            if (k * 32 + lane <= q_inc) {
-                v0 += (uint32_t)(w[k] & CH_MAX);
-                v1 += (uint32_t)((w[k] >> 30) & CH_MAX);
-            }
-        }
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) {
-            v0 += __shfl_xor_sync(0xffffffffu, v0, d);
-            v1 += __shfl_xor_sync(0xffffffffu, v1, d);
-        }
-        p0 += v0;
-        p1 += v1;
-        if (q_inc < 32 * CH_PER_LANE) break;
-        top -= 32 * CH_PER_LANE;
-    }
-    p0 = min(p0, CH_MAX);
-    p1 = min(p1, CH_MAX);
-    if (lane == 0) st_relaxed64(slots + r, ch_pack(CH_INC, p0 + a0, p1 + a1));
-}
-
-struct FusedArgs {
-    const uint8_t* verbs;
-    const float* pts;
-    const uint32_t* cmd_foff;   // float offset of every command (exclusive scan of floats per verb)
-    const uint32_t* fill_off;
-    const float* fill_xf;
-    const uint8_t* fill_flags;
-    const uint32_t* raster_off;
-    uint32_t n_fills, n_rasters;
-    uint64_t n_floats;
-    uint64_t* co;            // look-back slots of the output tiles / spans
-    uint32_t* ticket;
-    uint32_t* fallback;      // any raster did not fit
-    uint32_t* err;
-    uint32_t* totals;        // [0] tiles, [1] spans
-    uint32_t tile_cap, span_cap;
-    uint32_t* out_xy;
-    uint8_t* out_alpha;
-    float* out_cov;
-    uint32_t* span_xy;
-    uint16_t* span_w;
-    uint32_t* span_tile;
-    uint32_t* raster_tile_off;
-    uint32_t* raster_span_off;
-    uint8_t* stage_alpha;    // per CTA: F_TMAX tiles of alpha (and of coverage when out_cov)
-    float* stage_cov;
-};
-
-__device__ __forceinline__ V2 load_pt(const float* p) { return v2(__ldg(p), __ldg(p + 1)); }
 
 template <int THREADS, int CHUNK>
 __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
@@ -258,6 +149,8 @@ __global__ void __launch_bounds__(THREADS) k_raster_fused(FusedArgs A) {
     constexpr int F_CMAX = THREADS;   // commands per raster
     __shared__ FusedSmem<THREADS, CHUNK> S;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    // the command scan before this launch gave up a wait: its offsets are not valid
+    if (run_aborted(A.err)) return;
     for (;;) {
         if (tid == 0) {
             S.raster = atomicAdd(A.ticket, 1u);
@@ -750,24 +643,30 @@ struct FloatOff {
 
 // Runs the fused kernel over the whole batch.  *handled is false when some
 // raster does not fit (the caller then runs the general chain).
-int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
-                uint32_t* n_spans) {
+// One fused form over the whole batch (form 1: one warp per raster, 2: one
+// CTA per raster).  *handled is false when some raster does not fit it.
+static int run_fused_form(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, int form, bool* handled,
+                          uint32_t* n_tiles, uint32_t* n_spans) {
     *handled = false;
     DevScalars* ds = dev_scalars(ctx);
     const uint32_t R = in->n_rasters;
-    if (R == 0) return OCHRE_OK;
     OCHRE_CUDA_TRY(ctx->fused_chain.ensure((size_t)R * sizeof(uint64_t)));
     uint64_t* co = ctx->fused_chain.as<uint64_t>();
-    // no more CTAs than rasters; each CTA stages the coverage of its raster
+    const bool want_cov = (ctx->flags & OCHRE_CTX_WANT_COV) != 0;
+    // no more CTAs (warps) than rasters; each stages the coverage of its raster
     int grid = 0;
-    {
+    size_t stage_tiles = 0;
+    if (form == 1) {
+        const int st = fused_warp_prepare(ctx, R, &grid, want_cov);
+        if (st != OCHRE_OK) return st;
+    } else {
         const int st = fused_shape(ctx, nullptr, &grid, s);
         if (st != OCHRE_OK) return st;
+        grid = (int)std::min<uint32_t>((uint32_t)grid, R);
+        if (ctx->fused_max_warps) grid = std::min<int>(grid, std::max<int>(1, (int)ctx->fused_max_warps));
+        stage_tiles = (size_t)grid * F_TMAX;
+        OCHRE_CUDA_TRY(ctx->fused_stage.ensure(stage_tiles * 64 * (want_cov ? 5 : 1)));
     }
-    grid = (int)std::min<uint32_t>((uint32_t)grid, R);
-    const bool want_cov = (ctx->flags & OCHRE_CTX_WANT_COV) != 0;
-    const size_t stage_tiles = (size_t)grid * F_TMAX;
-    OCHRE_CUDA_TRY(ctx->fused_stage.ensure(stage_tiles * 64 * (want_cov ? 5 : 1)));
     // float offset of every command (the kernel reads its points there)
     const uint64_t n_cmds = in->n_cmds;
     OCHRE_CUDA_TRY(ctx->cmd_foff.ensure((size_t)std::max<uint64_t>(n_cmds, 1) * 4));
@@ -808,12 +707,13 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
             OCHRE_LAUNCH(ctx, "fused_float_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
                 n_cmds, VerbFloats{in->verbs}, FloatOff{ctx->cmd_foff.as<uint32_t>()}, OpSumU32{}, 0u,
                 ctx->scan_status.p, &ds->sort_ticket, &ds->n_floats, &ds->err, s)));
-        FusedArgs a;
+        FusedArgs a{};
         a.verbs = in->verbs;
         a.pts = in->pts;
         a.cmd_foff = ctx->cmd_foff.as<uint32_t>();
         a.stage_alpha = ctx->fused_stage.as<uint8_t>();
         a.stage_cov = want_cov ? reinterpret_cast<float*>(ctx->fused_stage.as<uint8_t>() + stage_tiles * 64) : nullptr;
+        a.frontier = &ds->fused_frontier;
         a.fill_off = in->fill_cmd_off;
         a.fill_xf = in->fill_xf;
         a.fill_flags = in->fill_flags;
@@ -837,7 +737,7 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         a.raster_tile_off = ctx->out_raster_tile_off.as<uint32_t>();
         a.raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
         wait_inputs(ctx, s);   // the kernel reads points
-        const int st0 = fused_shape(ctx, &a, &grid, s);
+        const int st0 = form == 1 ? fused_warp_launch(ctx, &a, grid, want_cov, s) : fused_shape(ctx, &a, &grid, s);
         if (st0 != OCHRE_OK) return st0;
         if (plan) {
             // totals, fallback and errors are read after the replay
@@ -868,6 +768,27 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
         return OCHRE_OK;
     }
     return OCHRE_E_CAPACITY;
+}
+
+// The fused path: the tuned form first (by default one warp per raster), then
+// the CTA-per-raster form for a batch the first does not fit.  Graph replays
+// run the planned form only (a raster that no longer fits it re-plans).
+int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
+                uint32_t* n_spans) {
+    *handled = false;
+    if (in->n_rasters == 0) return OCHRE_OK;
+    const GraphPlan* plan = ctx->plan;
+    const int first = plan ? (int)plan->fused_form : ctx->tune_fused_form;
+    for (int form = first; form <= 2; form++) {
+        const int st = run_fused_form(ctx, in, s, form, handled, n_tiles, n_spans);
+        if (st != OCHRE_OK) return st;
+        if (*handled) {
+            ctx->stats.fused_form = (uint32_t)form;
+            return OCHRE_OK;
+        }
+        if (plan) return OCHRE_OK;
+    }
+    return OCHRE_OK;
 }
 
 }  // namespace ochre

@@ -69,6 +69,7 @@ struct DevScalars {
     uint32_t fused_spans;
     uint32_t n_rows;          // tile rows (raster, tile_y) of the general chain
     uint32_t spin_log2;       // poll limit of the run's bounded waits, log2 (0: SPIN_LIMIT)
+    uint32_t fused_frontier;  // fused warp form: slots below it hold inclusive values
 };
 // The waits find spin_log2 from the error word's address (common.cuh).
 static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
@@ -81,6 +82,7 @@ static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 *
 // so that no later kernel works past a buffer.
 struct GraphPlan {
     bool fused;          // the batch is one fused launch (else the general chain)
+    uint32_t fused_form; // 1: one warp per raster, 2: one CTA per raster
     uint32_t lines;      // general chain: lines, sort entries, tiles
     uint32_t entries;
     uint32_t tiles;      // (fused: output tiles and spans)
@@ -152,7 +154,9 @@ struct ochre_gpu_ctx {
     ochre::DevBuf scan_status;
     ochre::DevBuf scalars;   // DevScalars
     ochre::DevBuf fused_chain;   // fused path: per-raster look-back slots
-    ochre::DevBuf fused_stage;   // fused path: per-CTA staged alpha (and coverage) of its raster
+    ochre::DevBuf fused_stage;   // fused path: per-CTA (warp) staged alpha (and coverage) of its raster
+    ochre::DevBuf fused_spill;   // fused warp form: per-warp increments past the shared-memory slots
+    uint32_t fused_max_warps = 0; // fused path: at most this many persistent warps / CTAs (0: no limit)
     uint32_t fused_tile_cap = 0; // fused path: output capacity guess (tiles)
     // device outputs
     ochre::DevBuf out_tile_xy, out_tile_alpha, out_tile_cov, out_span_xy, out_span_w, out_span_tile,
@@ -196,6 +200,8 @@ struct ochre_gpu_ctx {
     uint32_t test_skip_first_raster = 0;
 
     // Launch-shape tunables (ochre_gpu_set_tunable; chosen by the autotuner).
+    int tune_fused_form = 1;            // 1: one warp per raster, 2: one CTA per raster
+    int tune_fused_warp_inc = 384;      // warp form: increments held in shared memory per raster
     int tune_fused_threads = 64;
     int tune_fused_chunk = 16;
     int tune_chain_tiles_per_warp = 8;
@@ -238,6 +244,11 @@ int stage_tiles(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t n_entries, c
 int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochre_batch* out);
 int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
                 uint32_t* n_spans);
+// The warp-per-raster fused kernel (fused_warp.cu): sizes its staging and
+// spill buffers for a batch of n_rasters (grid in CTAs out), then launches.
+struct FusedArgs;
+int fused_warp_prepare(ochre_gpu_ctx* ctx, uint32_t n_rasters, int* grid_ctas, bool want_cov);
+int fused_warp_launch(ochre_gpu_ctx* ctx, FusedArgs* a, int grid_ctas, bool want_cov, cudaStream_t s);
 
 // The whole chain for one batch (device pointers), results in ctx buffers.
 int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s);

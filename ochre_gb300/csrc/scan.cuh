@@ -32,6 +32,9 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_de
     // capacity n, the scan covers min(*n_dev, n).  Tiles past the count end
     // before publishing anything; no tile that scans waits on them.
     n = dev_count(n, n_dev);
+    // an earlier wait of the run gave up: its outputs (this scan's inputs) are
+    // not valid; every block ends here, before publishing
+    if (run_aborted(err)) return;
     if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
@@ -84,7 +87,7 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_de
             }
             int64_t top = (int64_t)tile - 1;
             long long spins = 0;
-            const long long limit = spin_limit(err);
+            const long long poll_limit = spin_limit(err);
             while (top >= 0) {
                 const int64_t j = top - lane;
                 uint32_t f = 2u;   // before tile 0: an inclusive identity
@@ -93,7 +96,7 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_de
                 const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
                 const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
                 if (__ballot_sync(0xffffffffu, f == 0u) & need) {
-                    if (wait_give_up_warp(spins, limit, err)) break;
+                    if (wait_give_up_warp(spins, poll_limit, err)) break;
                     if (spins > 64) __nanosleep(64);
                     continue;
                 }

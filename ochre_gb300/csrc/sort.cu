@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
     uint32_t* s_misc = s_gbase + 256;                   // [0]: tile id
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (run_aborted(err)) return;   // an earlier wait of the run gave up
     if (threadIdx.x == 0) s_misc[0] = atomicAdd(ticket, 1u);
     for (int i = lane; i < 256; i += 32) s_whist[warp * 256 + i] = 0u;
     __syncthreads();
@@ -129,12 +130,12 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
             st_release(my, LB_AGG | run);
             int64_t j = (int64_t)tile - 1;
             long long spins = 0;
-            const long long limit = spin_limit(err);
+            const long long poll_limit = spin_limit(err);
             while (j >= 0) {
                 const uint32_t v = ld_acquire(lookback + (size_t)j * 256 + d);
                 const uint32_t f = v & ~LB_MASK;
                 if (f == 0u) {
-                    if (wait_give_up(spins, limit, err)) break;
+                    if (wait_give_up(spins, poll_limit, err)) break;
                     if (spins > 64) __nanosleep(64);
                     continue;
                 }

@@ -451,6 +451,8 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
         &ds->n_tiles, &ds->err, s)));
     st = read_scalars(ctx, s);
     if (st != OCHRE_OK) return st;
+    st = check_device_error(ctx);
+    if (st != OCHRE_OK) return st;
     const uint32_t U = host_scalars(ctx)->n_tiles;
     // 4. output sizes and emission
     OCHRE_CUDA_TRY(ctx->sk_out_off.ensure(((size_t)U + 1) * 4));
@@ -472,6 +474,8 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
         OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_lines, 0, 8, s));
     }
     st = read_scalars(ctx, s);
+    if (st != OCHRE_OK) return st;
+    st = check_device_error(ctx);
     if (st != OCHRE_OK) return st;
     const uint32_t ON = host_scalars(ctx)->n_lines, OF = host_scalars(ctx)->n_line_ent;
     if (ON > MAX_COUNT) return OCHRE_E_CAPACITY;

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
         float c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         int64_t top = (int64_t)blk - 1;
         long long spins = 0;
-        const long long limit = spin_limit(err);
+        const long long poll_limit = spin_limit(err);
         while (top >= 0) {
             const int64_t j = top - lane;
             uint32_t f = 2u;   // before block 0: an inclusive zero
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
             const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
             const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
             if (__ballot_sync(0xffffffffu, f == 0u) & need) {
-                if (wait_give_up_warp(spins, limit, err)) break;
+                if (wait_give_up_warp(spins, poll_limit, err)) break;
                 if (spins > 16) __nanosleep(64);
                 continue;
             }
@@ -600,6 +600,8 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
     } else {
         st = read_scalars(ctx, s);
         if (st != OCHRE_OK) return st;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
         T = host_scalars(ctx)->n_tiles;
     }
     *n_tiles_out = T;
@@ -634,6 +636,8 @@ static int tiles_impl(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t E, cud
         n_rows = plan->rows;
     } else {
         st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        st = check_device_error(ctx);
         if (st != OCHRE_OK) return st;
         n_rows = host_scalars(ctx)->n_rows;
     }
