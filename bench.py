@@ -278,6 +278,7 @@ def run_reference(args, ws, rank):
 
 
 L2_RULE = "flushed (256 MiB write) between timed GPU steps, outside the events"
+MASK_EPS = 1e-3   # gradient check: |S| this close to a kink of min(|S|, 1) is left out
 
 
 def bench_config(args, n_paths: int, ws: int) -> dict:
@@ -553,6 +554,26 @@ def bench_differentiable(ctx, stream, flush, steps, n_scenes):
         _, a_dp, a_dx = oracle.adjoint64(sub, w, h, t_np)
         _, r_dp, r_dx = oracle.diff64(sub, w, h, t_np)
         rel = lambda a, r: float(np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-300))
+        # the same against the all-double forward, with the pixels near the
+        # kinks of min(|S|, 1) (|S| within MASK_EPS of 0 or 1, in the f32 or
+        # the double forward) taken out of both gradients: there dL/dS
+        # switches, and the f32 and double forwards fall on different sides
+        S32, T32, _ = oracle._tile_images(sub, w, h)
+        S64 = oracle.forward64(sub, w, h)
+        near = lambda S: (np.abs(np.abs(S) - 1.0) < MASK_EPS) | (np.abs(S) < MASK_EPS)
+        keep = ~((T32 & near(S32.astype(np.float64))) | near(S64))
+        c64 = np.minimum(np.abs(S64), 1.0)
+        g64 = np.where(keep & (np.abs(S64) < 1.0), np.sign(S64) * 2.0 * (c64 - t_np), 0.0)
+        m_dp, m_dx = oracle.backward64(sub, w, h, g64)
+        dl_m = dl.clone()
+        dl_m[:k] *= torch.as_tensor(keep, device=dl.device, dtype=dl.dtype)
+        if k < b.n_rasters:
+            dl_m[k:] = 0
+        gm_dp, gm_dx = ctx.fill_backward(db, w, h, dl_m, stream=sp)
+        torch.cuda.synchronize()
+        gm_dp = gm_dp.cpu().numpy()[:len(sub.pts)].astype(np.float64)
+        gm_dx = gm_dx.cpu().numpy()[:sub.n_fills].astype(np.float64)
+        del dl_m
         out[name] = {
             "scenes": b.n_rasters, "canvas": [w, h], "fills": b.n_fills, "lines": st["n_lines"],
             "fwd_ms": f_ms, "fwd_bwd_ms": fb_ms,
@@ -565,7 +586,11 @@ def bench_differentiable(ctx, stream, flush, steps, n_scenes):
                                       "note": "f32 forward (the reference's arithmetic), adjoint in double"},
                 "vs_fp64_forward": {"points": rel(g_dp, r_dp), "transforms": rel(g_dx, r_dx),
                                     "note": "forward in double too: pixels whose |S| falls on the other "
-                                            "side of 1 in f32 change dL/dS there"}},
+                                            "side of 1 in f32 change dL/dS there"},
+                "vs_fp64_forward_masked": {"points": rel(gm_dp, m_dp), "transforms": rel(gm_dx, m_dx),
+                                           "eps": MASK_EPS, "masked_fraction": float(1.0 - keep.mean()),
+                                           "note": "pixels with |S| within eps of 0 or 1 (f32 or double "
+                                                   "forward) left out of both gradients"}},
             "kernels_backward": _kernel_shares(ctx, lambda: ctx.fill_backward(db, w, h, dl, dpts, dxf,
                                                                               stream=sp))[:6],
         }
@@ -594,9 +619,10 @@ def _diff_roofline(b, w, h, f_ms, fb_ms):
     return out
 
 
-def _fd_check(ctx, sp, n_paths=16, n_params=64, h_px=1e-3):
+def _fd_check(ctx, sp, n_paths=256, n_params=64, h_px=1e-3):
     """GPU gradient against central finite differences (h = 1e-3 px) of the
-    FP64 loss, on 64 random parameters of a union of 16 blobs x 32 cubics."""
+    FP64 loss, on 64 random parameters of the differentiable configuration
+    itself (a union of 256 blobs x 32 cubics on 1024^2)."""
     import copy
 
     import numpy as np
@@ -652,6 +678,12 @@ def run_profile(args):
     from ochre_gb300 import DeviceBatch, GpuContext
     batch = make_workload(args.workload, args.n_paths, args.seed)
     ctx = GpuContext(0, chain_only=args.chain_only)
+    if args.fused_shape:
+        from ochre_gb300 import autotune
+        shape = [p for p in autotune.fused_candidates() if autotune.shape_name(p) == args.fused_shape]
+        if not shape:
+            raise SystemExit(f"unknown fused shape {args.fused_shape}")
+        autotune.apply(ctx, shape[0])
     db = DeviceBatch(batch, 0)
     sp = torch.cuda.current_stream().cuda_stream
     if args.mode == "profile":
@@ -902,6 +934,7 @@ def main():
                     help="profile: run warmup + steps rasterizations of the workload untimed, for ncu; "
                          "profile-diff: the same for render + loss + backward of --workload diff_union|diff_scenes")
     ap.add_argument("--chain-only", action="store_true", help="profile mode: force the general chain")
+    ap.add_argument("--fused-shape", default="", help="profile mode: fused kernel shape, e.g. warp384 or cta96x16")
     args = ap.parse_args()
     if args.mode != "bench":
         from ochre_gb300 import build

@@ -204,11 +204,13 @@ __device__ __forceinline__ void frontier_help(uint64_t* slots, uint32_t* frontie
             }
         }
     }
-    __threadfence();
+    // the run's inclusive values before the frontier move: the warp barrier
+    // orders every lane's stores before lane 0's release (cumulative)
     __syncwarp();
     if (lane == 0) {
-        __threadfence();
-        atomicMax(frontier, f + (uint32_t)m);
+        uint32_t old;
+        asm volatile("atom.release.gpu.global.max.u32 %0, [%1], %2;"
+                     : "=r"(old) : "l"(frontier), "r"(f + (uint32_t)m) : "memory");
     }
 }
 

@@ -14,6 +14,7 @@
 #include "common.cuh"
 #include "internal.h"
 
+#include <algorithm>
 #include <utility>
 
 namespace ochre {
@@ -23,6 +24,7 @@ constexpr int SORT_WARPS = SORT_BLOCK / 32;
 constexpr int SORT_ITEMS = 15;
 constexpr int SORT_TILE = SORT_BLOCK * SORT_ITEMS;
 constexpr uint32_t LB_AGG = 1u << 30, LB_INC = 2u << 30, LB_MASK = (1u << 30) - 1u;
+constexpr int LB_WINDOW = 8;      // predecessor tiles one digit's look-back reads per round
 
 template <class K>
 __global__ void __launch_bounds__(256) k_sort_hist(const K* __restrict__ keys, uint64_t n, const uint32_t* n_dev,
@@ -128,20 +130,40 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
             st_release(my, LB_INC | run);
         } else {
             st_release(my, LB_AGG | run);
-            int64_t j = (int64_t)tile - 1;
+            // windowed look-back: LB_WINDOW predecessors per round, read
+            // together (one latency per round instead of one per tile), up
+            // to the nearest inclusive value
+            int64_t top = (int64_t)tile - 1;
             long long spins = 0;
             const long long poll_limit = spin_limit(err);
-            while (j >= 0) {
-                const uint32_t v = ld_acquire(lookback + (size_t)j * 256 + d);
-                const uint32_t f = v & ~LB_MASK;
-                if (f == 0u) {
+            while (top >= 0) {
+                uint32_t v[LB_WINDOW];
+#pragma unroll
+                for (int k = 0; k < LB_WINDOW; k++) {
+                    const int64_t j = top - k;
+                    v[k] = j >= 0 ? ld_acquire(lookback + (size_t)j * 256 + d) : LB_INC;   // before tile 0: an inclusive 0
+                }
+                int k_inc = LB_WINDOW;
+#pragma unroll
+                for (int k = LB_WINDOW - 1; k >= 0; k--)
+                    if ((v[k] & ~LB_MASK) == LB_INC) k_inc = k;
+                bool missing = false;
+                uint32_t sum = 0;
+#pragma unroll
+                for (int k = 0; k < LB_WINDOW; k++) {
+                    if (k <= k_inc) {
+                        if ((v[k] & ~LB_MASK) == 0u) missing = true;
+                        sum += v[k] & LB_MASK;
+                    }
+                }
+                if (missing) {
                     if (wait_give_up(spins, poll_limit, err)) break;
                     if (spins > 64) __nanosleep(64);
                     continue;
                 }
-                excl += v & LB_MASK;
-                if (f == LB_INC) break;
-                --j;
+                excl += sum;
+                if (k_inc < LB_WINDOW) break;
+                top -= LB_WINDOW;
             }
             st_release(my, LB_INC | (excl + run));
         }
@@ -205,8 +227,9 @@ static int sort_impl(ochre_gpu_ctx* ctx, uint64_t n, uint32_t key_bits, cudaStre
     K* kout = ctx->keys_alt.as<K>();
     uint32_t* vout = ctx->vals_alt.as<uint32_t>();
     {
-        int blocks = (int)((n + 255) / 256);
-        if (blocks > 152 * 8) blocks = 152 * 8;
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        int blocks = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)std::max(sms, 1) * 8);
         OCHRE_LAUNCH(ctx, "sort_hist", s, k_sort_hist<K><<<blocks, 256, 0, s>>>(kin, n, n_dev, passes, hist));
         OCHRE_CUDA_TRY(cudaGetLastError());
         OCHRE_LAUNCH(ctx, "sort_offsets", s, k_sort_offsets<<<passes, 256, 0, s>>>(hist, off));

@@ -91,6 +91,9 @@ def _load():
         lib.ochre_oracle_backward64.argtypes = [ctypes.POINTER(_Batch), ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.ochre_oracle_backward64.restype = ctypes.c_int
+        lib.ochre_oracle_forward64.argtypes = [ctypes.POINTER(_Batch), ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_void_p]
+        lib.ochre_oracle_forward64.restype = ctypes.c_int
         lib.ochre_oracle_stroke.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_float,
                                             ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64),
                                             ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint64)]
@@ -305,6 +308,20 @@ def backward64(batch, w: int, h: int, dl_ds: np.ndarray, counts=None):
     if st:
         raise RuntimeError(f"oracle backward64 failed with status {st}")
     return dpts[:len(batch.pts)], dxf[:6 * (len(batch.fill_cmd_off) - 1)].reshape(-1, 6)
+
+
+def forward64(batch, w: int, h: int, counts=None) -> np.ndarray:
+    """The FP64 model's signed pre-quantisation sums S = accum + area of every
+    pixel, [R, h, w] (the all-double forward of diff64)."""
+    lib = _load()
+    b, keep = _as_batch(batch)
+    counts = seg_counts(batch) if counts is None else np.ascontiguousarray(counts, np.uint32)
+    out = np.zeros(max(batch.n_rasters * w * h, 1), np.float64)
+    st = lib.ochre_oracle_forward64(ctypes.byref(b), counts.ctypes.data if counts.size else None, int(w), int(h),
+                                    out.ctypes.data)
+    if st:
+        raise RuntimeError(f"oracle forward64 failed with status {st}")
+    return out[:batch.n_rasters * w * h].reshape(batch.n_rasters, h, w)
 
 
 def _tile_images(batch, w: int, h: int):

@@ -1249,7 +1249,7 @@ static int push_edge_t(edges_t *E, dv2 a, dv2 b, pref ra, pref rb, double tb) {
 static int push_edge(edges_t *E, dv2 a, dv2 b, pref ra, pref rb) { return push_edge_t(E, a, b, ra, rb, -1.0); }
 
 static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, const double *target,
-                       const double *dl_ds, double *loss_out, double *dpts, double *dxf) {
+                       const double *dl_ds, double *loss_out, double *dpts, double *dxf, double *s_out) {
     uint64_t *off = NULL;
     int st = validate(bt, &off);
     if (st) return st;
@@ -1374,6 +1374,7 @@ static int diff64_impl(const ochre_oracle_batch *bt, const uint32_t *counts, int
                 const size_t i = (size_t)y * W + x;
                 const double S = acc + area[i];
                 acc += hgt[i];
+                if (s_out) s_out[(size_t)ri * npx + i] = S;
                 const double c = fmin(fabs(S), 1.0);
                 loss += (c - tgt[i]) * (c - tgt[i]);
                 const double gc = 2.0 * (c - tgt[i]);
@@ -1566,13 +1567,25 @@ done:
 
 int ochre_oracle_diff64(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, const double *target,
                         double *loss_out, double *dpts, double *dxf) {
-    return diff64_impl(bt, counts, W, H, target, NULL, loss_out, dpts, dxf);
+    return diff64_impl(bt, counts, W, H, target, NULL, loss_out, dpts, dxf, NULL);
 }
 
 int ochre_oracle_backward64(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, const double *dl_ds,
                             double *dpts, double *dxf) {
     double loss;
-    return diff64_impl(bt, counts, W, H, NULL, dl_ds, &loss, dpts, dxf);
+    return diff64_impl(bt, counts, W, H, NULL, dl_ds, &loss, dpts, dxf, NULL);
+}
+
+/* The FP64 model's signed pre-quantisation sums S (accum + area) of every
+ * pixel, [R, H, W]; target = 0, no gradient. */
+int ochre_oracle_forward64(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, double *s_out) {
+    const size_t n = (size_t)bt->n_rasters * (size_t)W * (size_t)H;
+    double *zero = (double *)calloc(n ? n : 1, sizeof(double));
+    if (!zero) return OCHRE_ORACLE_E_NOMEM;
+    double loss;
+    const int st = diff64_impl(bt, counts, W, H, zero, NULL, &loss, NULL, NULL, s_out);
+    free(zero);
+    return st;
 }
 
 /* ------------------------------------------------------------------ */

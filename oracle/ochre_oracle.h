@@ -100,6 +100,9 @@ int ochre_oracle_diff64(const ochre_oracle_batch *batch, const uint32_t *counts,
  * |.| and the clamp), n_rasters * w * h values. */
 int ochre_oracle_backward64(const ochre_oracle_batch *batch, const uint32_t *counts, int w, int h, const double *dl_ds,
                             double *dpts, double *dxf);
+/* The FP64 model's signed sums S = accum + area of every pixel ([R, H, W],
+ * spans included as their running sums), target 0 and no gradient. */
+int ochre_oracle_forward64(const ochre_oracle_batch *bt, const uint32_t *counts, int W, int H, double *s_out);
 
 #ifdef __cplusplus
 }
