@@ -3,10 +3,8 @@
 Times every kernel shape the library offers on a sample of the caller's
 workload, keeps the fastest, and caches the choice per GPU name in
 ``ochre_gb300/_build/tune.json``:
-  * the fused small-raster kernel: one warp per raster with 256, 384 or 512
-    increments held in shared memory (the rest spill to global memory; fewer
-    slots fit more warps on an SM), or one CTA per raster with its threads
-    per raster and tiles per accumulation pass;
+  * the fused small-raster kernel: threads per raster and tiles per
+    accumulation pass;
   * tiles per warp of the general chain's coverage kernel.
 Results never depend on the shape (tile and span structure is exact, alpha
 within 1 LSB of the oracle either way).
@@ -21,18 +19,16 @@ from typing import Optional
 
 from . import _lib, build
 
-FUSED_SHAPES = [(64, 8), (64, 16), (64, 32), (96, 8), (96, 16), (128, 16), (128, 32)]   # CTA form
-WARP_INCS = [256, 384, 512]                                                               # warp form
+FUSED_SHAPES = [(64, 8), (64, 16), (64, 32), (96, 8), (96, 16), (128, 16), (128, 32)]
 
 
 def fused_candidates() -> list:
     """Every fused shape as the tunables that select it."""
-    return ([{"fused_form": 1, "fused_warp_inc": i} for i in WARP_INCS]
-            + [{"fused_form": 2, "fused_threads": t, "fused_chunk": c} for t, c in FUSED_SHAPES])
+    return [{"fused_threads": t, "fused_chunk": c} for t, c in FUSED_SHAPES]
 
 
 def shape_name(p: dict) -> str:
-    return f"warp{p['fused_warp_inc']}" if p["fused_form"] == 1 else f"cta{p['fused_threads']}x{p['fused_chunk']}"
+    return f"{p['fused_threads']}x{p['fused_chunk']}"
 CHAIN_TILES_PER_WARP = [4, 8, 16]
 CACHE = os.path.join(build.BUILD, "tune.json")
 
@@ -104,9 +100,7 @@ def tune(ctx, fused_sample=None, chain_sample=None, reps: int = 3, save: bool = 
         apply(ctx, cand)
         ms = _time(ctx, db, reps)
         report["fused"][shape_name(cand)] = ms
-        st = ctx.stats()
-        # a shape counts only when its own form handled the sample
-        if st.get("fused") and st.get("fused_form") == cand["fused_form"] and ms < best_t:
+        if ctx.stats().get("fused") and ms < best_t:
             best_f, best_t = cand, ms
     db = DeviceBatch(chain_sample, ctx.device)
     ctx.set_chain_only(True)
@@ -118,7 +112,7 @@ def tune(ctx, fused_sample=None, chain_sample=None, reps: int = 3, save: bool = 
         if ms < best_ct:
             best_c, best_ct = tpw, ms
     ctx.set_chain_only(old_chain)
-    choice = dict(best_f or {"fused_form": 1, "fused_warp_inc": 384})
+    choice = dict(best_f or {"fused_threads": 64, "fused_chunk": 16})
     choice["chain_tiles_per_warp"] = best_c or 8
     apply(ctx, choice)
     if save:

@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libochre_gpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["api.cu", "flatten.cu", "dda.cu", "sort.cu", "tiles.cu", "fused.cu", "fused_warp.cu", "grad.cu", "stroke.cu", "composite.cu", "noalloc.cu",
+SOURCES = ["api.cu", "flatten.cu", "dda.cu", "sort.cu", "tiles.cu", "fused.cu", "grad.cu", "stroke.cu", "composite.cu", "noalloc.cu",
            "graph.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",

@@ -108,11 +108,11 @@ __global__ void k_plan_cap(uint32_t* count, uint32_t cap, uint32_t* err) {
     }
 }
 
-__global__ void k_plan_entries(DevScalars* ds, uint32_t cap, uint32_t key_bits) {
-    const uint64_t e = (uint64_t)ds->n_line_ent + ds->n_empty;
+__global__ void k_plan_entries(DevScalars* ds, uint32_t cap, uint32_t key_bits, uint32_t inc_cap) {
+    const uint64_t e = (uint64_t)ds->line_ent_total + ds->n_empty;
     const uint64_t k = ds->keyspace;
     const bool keys_fit = key_bits >= 64 || k == 0 || ((k - 1) >> key_bits) == 0;
-    if (e > cap || !keys_fit) {
+    if (e > cap || !keys_fit || ds->n_incs > inc_cap) {
         ds->n_entries = 0u;
         ds->n_lines = 0u;   // no line emits an entry
         atomicOr(&ds->err, ERR_CAPACITY);
@@ -126,8 +126,9 @@ cudaError_t launch_plan_cap(ochre_gpu_ctx* ctx, uint32_t* count, uint32_t cap, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_bits, cudaStream_t s) {
-    k_plan_entries<<<1, 1, 0, s>>>(dev_scalars(ctx), cap, key_bits);
+cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_bits, uint32_t inc_cap,
+                                cudaStream_t s) {
+    k_plan_entries<<<1, 1, 0, s>>>(dev_scalars(ctx), cap, key_bits, inc_cap);
     return cudaGetLastError();
 }
 
@@ -225,7 +226,7 @@ int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out
         ochre_gpu_ctx* c;
         ~HookReset() {
             c->test_spin_log2 = 0;
-            c->test_skip_first_raster = 0;
+            c->test_skip_first_ticket = 0;
         }
     } hook_reset{ctx};
     std::memset(out, 0, sizeof *out);
@@ -383,11 +384,11 @@ namespace ochre {
 std::vector<DevBuf*> device_buffers(ochre_gpu_ctx* ctx) {
     return {&ctx->in_verbs, &ctx->in_pts, &ctx->in_fill_off, &ctx->in_fill_xf, &ctx->in_fill_flags,
                      &ctx->in_raster_off, &ctx->cmd_foff, &ctx->cmd_mv, &ctx->cmd_ep, &ctx->cmd_line_off,
-                     &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->raster_bbox, &ctx->raster_keybase,
+                     &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->line_inc_off, &ctx->incs, &ctx->raster_bbox, &ctx->raster_keybase,
                      &ctx->raster_empty, &ctx->raster_wsum, &ctx->raster_wbase, &ctx->tile_head_bins,
                      &ctx->tile_head_wind, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_row_start, &ctx->tile_state,
-                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain, &ctx->fused_stage, &ctx->fused_spill,
+                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_u_xy, &ctx->fused_u_alpha, &ctx->fused_u_cov, &ctx->fused_u_span, &ctx->fused_rcount, &ctx->fused_rstart,
                      &ctx->grad_g, &ctx->grad_gs, &ctx->grad_left, &ctx->grad_line, &ctx->grad_pts,
                      &ctx->sk_cmd_foff, &ctx->sk_cmd_mv, &ctx->sk_cmd_ep, &ctx->sk_poly_off, &ctx->sk_poly_foff,
                      &ctx->sk_pverbs, &ctx->sk_ppts, &ctx->sk_pfoff, &ctx->sk_pfill_off, &ctx->sk_first_close,
@@ -621,12 +622,6 @@ int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     if (!std::strcmp(name, "fused_threads")) {
         if (value != 64 && value != 96 && value != 128) return OCHRE_E_INVALID;
         ctx->tune_fused_threads = value;
-    } else if (!std::strcmp(name, "fused_form")) {
-        if (value != 1 && value != 2) return OCHRE_E_INVALID;
-        ctx->tune_fused_form = value;
-    } else if (!std::strcmp(name, "fused_warp_inc")) {
-        if (value != 256 && value != 384 && value != 512) return OCHRE_E_INVALID;
-        ctx->tune_fused_warp_inc = value;
     } else if (!std::strcmp(name, "fused_chunk")) {
         if (value != 8 && value != 16 && value != 32) return OCHRE_E_INVALID;
         ctx->tune_fused_chunk = value;
@@ -639,9 +634,9 @@ int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     } else if (!std::strcmp(name, "test_spin_log2")) {
         if (value < 0 || value > 40) return OCHRE_E_INVALID;
         ctx->test_spin_log2 = (uint32_t)value;
-    } else if (!std::strcmp(name, "test_skip_first_raster")) {
+    } else if (!std::strcmp(name, "test_skip_first_ticket")) {
         if (value < 0 || value > 1) return OCHRE_E_INVALID;
-        ctx->test_skip_first_raster = (uint32_t)value;
+        ctx->test_skip_first_ticket = (uint32_t)value;
     } else {
         return OCHRE_E_INVALID;
     }
@@ -652,8 +647,6 @@ int ochre_gpu_get_tunable(const ochre_gpu_ctx* ctx, const char* name, int* value
     if (!ctx || !name || !value) return OCHRE_E_INVALID;
     if (!std::strcmp(name, "fused_threads")) *value = ctx->tune_fused_threads;
     else if (!std::strcmp(name, "fused_chunk")) *value = ctx->tune_fused_chunk;
-    else if (!std::strcmp(name, "fused_form")) *value = ctx->tune_fused_form;
-    else if (!std::strcmp(name, "fused_warp_inc")) *value = ctx->tune_fused_warp_inc;
     else if (!std::strcmp(name, "chain_tiles_per_warp")) *value = ctx->tune_chain_tiles_per_warp;
     else if (!std::strcmp(name, "chain_coverage_form")) *value = ctx->tune_chain_coverage_form;
     else return OCHRE_E_INVALID;

@@ -9,16 +9,21 @@
 // sets it that way (rasterizer.rs:68) and every walk ends by snapping to
 // floor(point) and updating tile_y_prev for that cell (rasterizer.rs:118-131).
 //
-// A walk produces two kinds of sort entries:
+// A walk stores the increment (area, height) of every cell it visits once,
+// line by line (the count pass gives each line its offset), and produces two
+// kinds of sort entries:
 //   * a *bin* per run of consecutive increment cells in one tile
-//     (value = entry index; the BinRec at that index holds the DDA state at
-//     the run's first cell so the tile kernel can replay it exactly);
+//     (value = entry index; the BinRec at that index holds the run's first
+//     increment, first cell and steps, so the tile kernel finds every cell's
+//     increment without walking again);
 //   * a *crossing* per tile-row change (rasterizer.rs:123-131)
 //     (value = CROSS_TAG | raster << 8 | sign byte).
 // Keys order entries by (raster, tile_y, tile_x, kind) inside a compact key
 // space: key_base[raster] + ((ty - by0) * w + (tx - bx0)) * 2 + kind, with
 // the raster's tile bounding box (bx0, by0)..(bx1, by1) measured in the count
 // pass; kind 0 (crossing) sorts before kind 1 (bin) of the same tile.
+#include <algorithm>
+
 #include "common.cuh"
 #include "internal.h"
 #include "scan.cuh"
@@ -37,19 +42,22 @@ __device__ __forceinline__ void bbox_add(BBoxAcc& b, int x, int y) {
     b.y1 = max(b.y1, ty);
 }
 
-// Count bins and crossings of a line; extend its raster's tile bbox; sum
-// the crossing signs.
-__device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* capped, int* wsum) {
+// Count bins, crossings and increment cells of a line; extend its raster's
+// tile bbox; sum the crossing signs.
+__device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* capped, int* wsum, uint32_t* cells) {
     *wsum = 0;
+    *cells = 0;
     if (veq(a, p)) return 0u;
-    uint32_t nb = 0, nc = 0;
+    uint32_t nb = 0, nc = 0, nx = 0, run = 0;
     int ws = 0;
     int ptx = 0x7fffffff, pty = 0x7fffffff;
     const bool ok = walk_line(
         a, p,
         [&](const Walk&, const WalkState& s) {
             const int tx = div8(s.x), ty = div8(s.y);
-            if (tx != ptx || ty != pty) { nb++; ptx = tx; pty = ty; }
+            if (tx != ptx || ty != pty || run == BIN_MAX_CELLS) { nb++; ptx = tx; pty = ty; run = 0; }
+            run++;
+            nx++;
         },
         [&](int, int, int sign) {
             nc++;
@@ -58,6 +66,7 @@ __device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* ca
         [&](int x, int y) { bbox_add(bb, x, y); });
     if (!ok) *capped = true;
     *wsum = ws;
+    *cells = nx;
     return nb + nc;
 }
 
@@ -116,7 +125,8 @@ __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1
 __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ lines,
                                                     const uint32_t* __restrict__ line_raster, uint32_t n_cap,
                                                     const uint32_t* n_dev, int4* bbox, int* raster_wsum,
-                                                    uint32_t* __restrict__ counts, uint32_t* err) {
+                                                    uint32_t* __restrict__ counts, uint32_t* __restrict__ inc_counts,
+                                                    uint32_t* err) {
     __shared__ int4 s_box[BOX_SLOTS];
     __shared__ int s_ws[BOX_SLOTS];
     __shared__ uint32_t s_r0;
@@ -140,7 +150,9 @@ __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ l
     if (i < n_lines) {
         const float4 l = lines[i];
         bool capped = false;
-        counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped, &ws);
+        uint32_t nc = 0;
+        counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped, &ws, &nc);
+        inc_counts[i] = nc;
         if (capped) atomicOr(err, ERR_LIMIT);
         r = line_raster[i];
     }
@@ -170,13 +182,28 @@ __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ l
         if (s_ws[threadIdx.x]) atomicAdd(raster_wsum + r0 + threadIdx.x, s_ws[threadIdx.x]);
     }
 }
-struct CountIn32 {
-    const uint32_t* counts;
-    __device__ __forceinline__ uint32_t operator()(uint64_t i) const { return counts[i]; }
+// Entry and increment offsets of every line, one scan of the pair (in place:
+// every count is read by the thread that writes its offset).
+struct LinePair {
+    uint32_t ent, inc;
 };
-struct OffOut32 {
-    uint32_t* off;
-    __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
+struct OpLinePair {
+    __device__ __forceinline__ LinePair operator()(LinePair a, LinePair b) const {
+        return LinePair{a.ent + b.ent, a.inc + b.inc};
+    }
+};
+struct LinePairIn {
+    const uint32_t* ent;
+    const uint32_t* inc;
+    __device__ __forceinline__ LinePair operator()(uint64_t i) const { return LinePair{ent[i], inc[i]}; }
+};
+struct LinePairOut {
+    uint32_t* ent;
+    uint32_t* inc;
+    __device__ __forceinline__ void operator()(uint64_t i, LinePair ex, LinePair) const {
+        ent[i] = ex.ent;
+        inc[i] = ex.inc;
+    }
 };
 
 __global__ void k_bbox_init(int4* bbox, int* wsum, uint32_t n) {
@@ -236,9 +263,10 @@ __device__ __forceinline__ K make_key(uint64_t base, const int4& bb, int tx, int
 // (In line order: neighbouring lanes write neighbouring entry ranges.)
 template <class K>
 __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster,
-                            const uint32_t* __restrict__ ent_off, uint64_t n_cap, const uint32_t* n_dev,
-                            const int4* __restrict__ bbox, const uint64_t* __restrict__ key_base,
-                            K* __restrict__ keys, uint32_t* __restrict__ vals, BinRec* __restrict__ bins) {
+                            const uint32_t* __restrict__ ent_off, const uint32_t* __restrict__ inc_off, uint64_t n_cap,
+                            const uint32_t* n_dev, const int4* __restrict__ bbox, const uint64_t* __restrict__ key_base,
+                            K* __restrict__ keys, uint32_t* __restrict__ vals, BinRec* __restrict__ bins,
+                            float2* __restrict__ incs) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= dev_count(n_cap, n_dev)) return;
     const float4 l = lines[i];
@@ -248,40 +276,42 @@ __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __
     const int4 bb = bbox[r];
     const uint64_t base = key_base[r];
     uint32_t e = ent_off[i];
+    uint32_t q = inc_off[i];   // next stored increment
     // open bin
-    int btx = 0x7fffffff, bty = 0x7fffffff;
+    int btx = 0x7fffffff, bty = 0x7fffffff, prev_x = 0;
     uint32_t bcount = 0, bentry = 0;
     BinRec rec;
     auto flush = [&]() {
         if (bcount) {
-            rec.n = bcount;
-            const uint4* s = reinterpret_cast<const uint4*>(&rec);
-            uint4* d = reinterpret_cast<uint4*>(bins + bentry);
-            d[0] = s[0];
-            d[1] = s[1];
+            rec.n = (uint8_t)bcount;
+            *reinterpret_cast<uint4*>(bins + bentry) = *reinterpret_cast<const uint4*>(&rec);
             keys[bentry] = make_key<K>(base, bb, btx, bty, 1u);
             vals[bentry] = bentry;
         }
     };
     walk_line(
         a, p,
-        [&](const Walk&, const WalkState& s) {
+        [&](const Walk& w, const WalkState& s) {
+            float area, height;
+            walk_increment(w, s, area, height);
             const int tx = div8(s.x), ty = div8(s.y);
-            if (tx != btx || ty != bty) {
+            if (tx != btx || ty != bty || bcount == BIN_MAX_CELLS) {
                 flush();
                 btx = tx;
                 bty = ty;
                 bcount = 0;
                 bentry = e++;
-                rec.line = (uint32_t)i;
+                rec.inc = q;
                 rec.raster = r;
                 rec.x = (int16_t)s.x;
                 rec.y = (int16_t)s.y;
-                rec.row_t0 = s.row_t0;
-                rec.row_t1 = s.row_t1;
-                rec.col_t0 = s.col_t0;
-                rec.col_t1 = s.col_t1;
+                rec.steps = 0;
+                rec.dirs = (uint8_t)((w.x_dir < 0 ? 1u : 0u) | (w.y_dir < 0 ? 2u : 0u));
+            } else if (s.x != prev_x) {
+                rec.steps = (uint16_t)(rec.steps | (1u << (bcount - 1)));   // the step into this cell moved in x
             }
+            incs[q++] = make_float2(area, height);
+            prev_x = s.x;
             bcount++;
         },
         [&](int tx, int ty, int sign) {
@@ -308,12 +338,13 @@ __global__ void k_empty_emit(const uint32_t* __restrict__ empty, uint32_t n_rast
     const uint32_t e = first_entry + rank - 1u;
     if (n_ent_dev != nullptr && e >= *n_ent_dev) return;
     BinRec rec;
-    rec.line = 0xffffffffu;
+    rec.inc = 0;
     rec.raster = r;
     rec.x = 0;
     rec.y = 0;
+    rec.steps = 0;
     rec.n = 0;
-    rec.row_t0 = rec.row_t1 = rec.col_t0 = rec.col_t1 = 0.0f;
+    rec.dirs = 0;
     bins[e] = rec;
     keys[e] = (K)(key_base[r] + 1ull);
     vals[e] = e;
@@ -335,21 +366,24 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_LAUNCH(ctx, "bbox_init", s, k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(),
                                                                                  ctx->raster_wsum.as<int>(), R));
     OCHRE_CUDA_TRY(cudaGetLastError());
-    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_line_ent, 0, sizeof(uint32_t), s));
+    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->line_ent_total, 0, 2 * sizeof(uint32_t), s));
     // graph replays: n_lines is the capacity, the count is on the device
     const GraphPlan* plan = ctx->plan;
     const uint32_t* lines_dev = plan ? &ds->n_lines : nullptr;
     if (n_lines) {
         OCHRE_CUDA_TRY(ctx->line_ent_off.ensure((size_t)n_lines * 4));
-        OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<uint32_t>)));
+        OCHRE_CUDA_TRY(ctx->line_inc_off.ensure((size_t)n_lines * 4));
+        OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<LinePair>)));
         OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<(n_lines + 255) / 256, 256, 0, s>>>(
             ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
-            ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), &ds->err));
+            ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>(), &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());
         // in place: every count is read by the thread that writes its offset
-        OCHRE_LAUNCH(ctx, "dda_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
-            n_lines, CountIn32{ctx->line_ent_off.as<uint32_t>()}, OffOut32{ctx->line_ent_off.as<uint32_t>()},
-            OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket, &ds->n_line_ent, &ds->err, s, lines_dev)));
+        OCHRE_LAUNCH(ctx, "dda_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<LinePair>(
+            n_lines, LinePairIn{ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>()},
+            LinePairOut{ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>()}, OpLinePair{},
+            LinePair{0u, 0u}, ctx->scan_status.p, &ds->ticket, reinterpret_cast<LinePair*>(&ds->line_ent_total),
+            &ds->err, s, lines_dev)));
     }
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(R) * sizeof(ScanStatus<RasterScan>)));
     OCHRE_LAUNCH(ctx, "raster_key_scan", s, OCHRE_CUDA_TRY(launch_scan<RasterScan>(
@@ -361,26 +395,31 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     uint64_t E;
     uint32_t bits;
     uint32_t first_entry = 0;
+    uint64_t n_incs;
     bool any_empty = true;
     if (plan) {
-        // entry total and key space checked against the plan on the device
-        OCHRE_LAUNCH(ctx, "plan_entries", s, OCHRE_CUDA_TRY(launch_plan_entries(ctx, plan->entries, plan->key_bits, s)));
+        // entry total, key space and stored increments checked against the plan on the device
+        OCHRE_LAUNCH(ctx, "plan_entries", s, OCHRE_CUDA_TRY(launch_plan_entries(ctx, plan->entries, plan->key_bits,
+                                                                                plan->incs, s)));
         E = plan->entries;
         bits = plan->key_bits;
+        n_incs = plan->incs;
     } else {
         int st = read_scalars(ctx, s);
         if (st != OCHRE_OK) return st;
         st = check_device_error(ctx);
         if (st != OCHRE_OK) return st;
         const DevScalars* hs = host_scalars(ctx);
-        E = (uint64_t)hs->n_line_ent + hs->n_empty;
-        if (E > MAX_COUNT) return OCHRE_E_CAPACITY;
+        E = (uint64_t)hs->line_ent_total + hs->n_empty;
+        n_incs = hs->n_incs;
+        if (E > MAX_COUNT || n_incs > MAX_COUNT) return OCHRE_E_CAPACITY;
         const uint64_t K = hs->keyspace;
         bits = 1;
         while (bits < 64 && (K - 1) >> bits) bits++;
-        first_entry = hs->n_line_ent;
+        first_entry = hs->line_ent_total;
         any_empty = hs->n_empty != 0;
     }
+    OCHRE_CUDA_TRY(ctx->incs.ensure((size_t)std::max<uint64_t>(n_incs, 1) * sizeof(float2)));
     *key_bits = bits;
     *n_entries = E;
     ctx->keys64 = bits > 32;
@@ -394,18 +433,20 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
         const unsigned blocks = (unsigned)((n_lines + 127) / 128);
         if (ctx->keys64)
             OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<blocks, 128, 0, s>>>(
-                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
-                lines_dev, ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(),
-                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
+                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
+                ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
+                ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(),
+                ctx->bins.as<BinRec>(), ctx->incs.as<float2>()));
         else
             OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<blocks, 128, 0, s>>>(
-                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(), n_lines,
-                lines_dev, ctx->raster_bbox.as<int4>(), ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(),
-                ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>()));
+                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
+                ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
+                ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(),
+                ctx->bins.as<BinRec>(), ctx->incs.as<float2>()));
         OCHRE_CUDA_TRY(cudaGetLastError());
     }
     if (any_empty) {
-        const uint32_t* first_dev = plan ? &ds->n_line_ent : nullptr;
+        const uint32_t* first_dev = plan ? &ds->line_ent_total : nullptr;
         const uint32_t* ent_dev = plan ? &ds->n_entries : nullptr;
         if (ctx->keys64)
             OCHRE_LAUNCH(ctx, "empty_emit", s, k_empty_emit<uint64_t><<<(R + 255) / 256, 256, 0, s>>>(

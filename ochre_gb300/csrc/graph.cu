@@ -112,11 +112,11 @@ int build(ochre_graph* g) {
     const ochre_stats& es = ctx->stats;
     GraphPlan p{};
     p.fused = es.fused != 0;
-    p.fused_form = es.fused_form;
     p.tiles = cap_of(es.n_tiles, g->headroom);
     if (!p.fused) {
         p.lines = cap_of(es.n_lines, g->headroom);
         p.entries = cap_of(es.n_entries, g->headroom);
+        p.incs = cap_of(host_scalars(ctx)->n_incs, g->headroom);
         // key bits: the key space (areas of tile boxes) with headroom^2, up
         // to the next digit boundary (no extra sort pass for it), and never
         // into 64-bit keys when 32 hold the planning run
@@ -232,8 +232,6 @@ int ochre_graph_create(ochre_gpu_ctx* ctx, const ochre_batch* in, float headroom
         delete g;
         return st;
     }
-    g->ctx->tune_fused_form = ctx->tune_fused_form;
-    g->ctx->tune_fused_warp_inc = ctx->tune_fused_warp_inc;
     g->ctx->tune_fused_threads = ctx->tune_fused_threads;
     g->ctx->tune_fused_chunk = ctx->tune_fused_chunk;
     g->ctx->tune_chain_tiles_per_warp = ctx->tune_chain_tiles_per_warp;

@@ -69,7 +69,11 @@ struct DevScalars {
     uint32_t fused_spans;
     uint32_t n_rows;          // tile rows (raster, tile_y) of the general chain
     uint32_t spin_log2;       // poll limit of the run's bounded waits, log2 (0: SPIN_LIMIT)
-    uint32_t fused_frontier;  // fused warp form: slots below it hold inclusive values
+    uint32_t pad3;
+    uint32_t line_ent_total;  // chain: sort entries the lines produce   } (line scan
+    uint32_t n_incs;          // chain: pixel-cell increments of the lines } pair total)
+    uint32_t fused_cursor_t;  // fused path: next free tile / span of the unordered output
+    uint32_t fused_cursor_s;
 };
 // The waits find spin_log2 from the error word's address (common.cuh).
 static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
@@ -82,11 +86,11 @@ static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 *
 // so that no later kernel works past a buffer.
 struct GraphPlan {
     bool fused;          // the batch is one fused launch (else the general chain)
-    uint32_t fused_form; // 1: one warp per raster, 2: one CTA per raster
     uint32_t lines;      // general chain: lines, sort entries, tiles
     uint32_t entries;
     uint32_t tiles;      // (fused: output tiles and spans)
     uint32_t key_bits;   // sort key bits; keys are 64-bit above 32
+    uint32_t incs;       // general chain: stored pixel-cell increments
     uint32_t rows;       // tile rows of the planning run (coverage form and grid)
 };
 
@@ -95,16 +99,21 @@ constexpr uint32_t CROSS_TAG = 0x80000000u;
 constexpr uint32_t MAX_RASTERS = 1u << 23;
 constexpr uint64_t MAX_COUNT = (1ull << 30) - 1;   // lines, entries, tiles
 
-// Per-bin replay record: DDA state at the first cell of a run of cells that
-// share one tile (32 bytes).
+// A bin: a run of consecutive pixel cells of one line's walk that share one
+// tile (16 bytes).  Its cells' increments (area, height) were stored by the
+// walk at inc .. inc + n - 1; the cells themselves follow from the first cell
+// and the walk's steps (bit k of `steps`: the step from cell k to cell k + 1
+// moved in x, else in y; `dirs` bit 0 / 1: the x / y step is -1).
 struct alignas(16) BinRec {
-    uint32_t line;       // line index, 0xffffffff for the empty-raster tile
+    uint32_t inc;        // first increment of the run
     uint32_t raster;
-    int16_t x, y;        // first cell of the run
-    uint32_t n;          // cells in the run
-    float row_t0, row_t1, col_t0, col_t1;
+    int16_t x, y;        // first cell of the run (i16 cell coordinates)
+    uint16_t steps;
+    uint8_t n;           // cells in the run (0 for the empty-raster tile)
+    uint8_t dirs;
 };
-static_assert(sizeof(BinRec) == 32, "BinRec must be 32 bytes");
+static_assert(sizeof(BinRec) == 16, "BinRec must be 16 bytes");
+constexpr uint32_t BIN_MAX_CELLS = 16;   // a run longer than this is split (it never is: 15 at most)
 
 // Look-back state of one block of tiles (block-form coverage kernel): the row
 // sums (8 pixel rows) of the block's last row segment.
@@ -137,8 +146,10 @@ struct ochre_gpu_ctx {
     ochre::DevBuf in_verbs, in_pts, in_fill_off, in_fill_xf, in_fill_flags, in_raster_off;
     // per command
     ochre::DevBuf cmd_foff, cmd_mv, cmd_ep, cmd_line_off;
-    // per line
-    ochre::DevBuf lines, line_raster, line_ent_off;
+    // per line (line_inc_off: first stored increment of the line's walk)
+    ochre::DevBuf lines, line_raster, line_ent_off, line_inc_off;
+    // stored pixel-cell increments (area, height) of every walk, line by line
+    ochre::DevBuf incs;
     // per raster
     ochre::DevBuf raster_bbox, raster_keybase, raster_empty;
     // per raster: sum of its tile-row crossing signs, and the sum over earlier rasters
@@ -153,10 +164,10 @@ struct ochre_gpu_ctx {
     // scan workspace
     ochre::DevBuf scan_status;
     ochre::DevBuf scalars;   // DevScalars
-    ochre::DevBuf fused_chain;   // fused path: per-raster look-back slots
-    ochre::DevBuf fused_stage;   // fused path: per-CTA (warp) staged alpha (and coverage) of its raster
-    ochre::DevBuf fused_spill;   // fused warp form: per-warp increments past the shared-memory slots
-    uint32_t fused_max_warps = 0; // fused path: at most this many persistent warps / CTAs (0: no limit)
+    // fused path: the unordered output (tiles and spans in the order the CTAs
+    // finished their rasters) and per raster its counts and first tile / span
+    ochre::DevBuf fused_u_xy, fused_u_alpha, fused_u_cov, fused_u_span, fused_rcount, fused_rstart;
+    uint32_t fused_max_ctas = 0; // fused path: at most this many persistent CTAs (0: no limit)
     uint32_t fused_tile_cap = 0; // fused path: output capacity guess (tiles)
     // device outputs
     ochre::DevBuf out_tile_xy, out_tile_alpha, out_tile_cov, out_span_xy, out_span_w, out_span_tile,
@@ -194,14 +205,12 @@ struct ochre_gpu_ctx {
 
     // Test hooks (ochre_gpu_set_tunable "test_*"), used by the next run only:
     // the poll limit of its bounded waits (log2; 0: the default), and, on the
-    // fused kernel, a first raster that is never taken, so that the waits of
-    // its successors cannot finish.
+    // fused path, a raster-offset scan whose first tile is never taken, so
+    // that the waits of the tiles after it cannot finish.
     uint32_t test_spin_log2 = 0;
-    uint32_t test_skip_first_raster = 0;
+    uint32_t test_skip_first_ticket = 0;
 
     // Launch-shape tunables (ochre_gpu_set_tunable; chosen by the autotuner).
-    int tune_fused_form = 1;            // 1: one warp per raster, 2: one CTA per raster
-    int tune_fused_warp_inc = 384;      // warp form: increments held in shared memory per raster
     int tune_fused_threads = 64;
     int tune_fused_chunk = 16;
     int tune_chain_tiles_per_warp = 8;
@@ -244,20 +253,17 @@ int stage_tiles(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t n_entries, c
 int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochre_batch* out);
 int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
                 uint32_t* n_spans);
-// The warp-per-raster fused kernel (fused_warp.cu): sizes its staging and
-// spill buffers for a batch of n_rasters (grid in CTAs out), then launches.
-struct FusedArgs;
-int fused_warp_prepare(ochre_gpu_ctx* ctx, uint32_t n_rasters, int* grid_ctas, bool want_cov);
-int fused_warp_launch(ochre_gpu_ctx* ctx, FusedArgs* a, int grid_ctas, bool want_cov, cudaStream_t s);
+
 
 // The whole chain for one batch (device pointers), results in ctx buffers.
 int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s);
 
 // Graph replays: device checks of counts against the plan (api.cu).  The
-// entry check sets n_entries = n_line_ent + n_empty and zeroes it, and the
-// line count, when it or the key space exceeds the plan; the other zeroes
-// *count above cap.  Both flag ERR_CAPACITY.
-cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_bits, cudaStream_t s);
+// entry check sets n_entries = line_ent_total + n_empty and zeroes it, and the
+// line count, when it, the key space or the stored increments exceed the
+// plan; the other zeroes *count above cap.  Both flag ERR_CAPACITY.
+cudaError_t launch_plan_entries(ochre_gpu_ctx* ctx, uint32_t cap, uint32_t key_bits, uint32_t inc_cap,
+                                cudaStream_t s);
 cudaError_t launch_plan_cap(ochre_gpu_ctx* ctx, uint32_t* count, uint32_t cap, cudaStream_t s);
 
 // Makes stream s wait for the batch's points if they are still being copied

@@ -146,14 +146,21 @@ constexpr int SCAN_ITEMS = 8;
 inline uint64_t scan_tiles(uint64_t n) { return (n + SCAN_BLOCK * SCAN_ITEMS - 1) / (SCAN_BLOCK * SCAN_ITEMS); }
 
 // `n_dev` (optional): the count lives on the device and `n` is its capacity.
+// `first_ticket` (a test hook, else 0): tiles below it are never taken.
 template <class T, class Op, class In, class Out>
 cudaError_t launch_scan(uint64_t n, In in, Out out, Op op, T identity, void* status, uint32_t* ticket, T* total,
-                        uint32_t* err, cudaStream_t stream, const uint32_t* n_dev = nullptr) {
+                        uint32_t* err, cudaStream_t stream, const uint32_t* n_dev = nullptr,
+                        uint32_t first_ticket = 0u) {
     const uint64_t tiles = scan_tiles(n);
     if (tiles == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(status, 0, tiles * sizeof(ScanStatus<T>), stream);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
+    if (first_ticket == 0u) {
+        e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), stream);
+    } else {
+        static const uint32_t one = 1u;
+        e = cudaMemcpyAsync(ticket, &one, sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
+    }
     if (e != cudaSuccess) return e;
     k_scan<SCAN_BLOCK, SCAN_ITEMS, T, Op, In, Out><<<(unsigned)tiles, SCAN_BLOCK, 0, stream>>>(
         n, n_dev, in, out, op, identity, reinterpret_cast<ScanStatus<T>*>(status), ticket, total, err);

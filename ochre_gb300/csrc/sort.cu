@@ -136,6 +136,14 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
             int64_t top = (int64_t)tile - 1;
             long long spins = 0;
             const long long poll_limit = spin_limit(err);
+            // the nearest predecessor alone first: often it is inclusive already
+            {
+                const uint32_t v = ld_acquire(lookback + (size_t)top * 256 + d);
+                if ((v & ~LB_MASK) == LB_INC) {
+                    excl = v & LB_MASK;
+                    top = -1;
+                }
+            }
             while (top >= 0) {
                 uint32_t v[LB_WINDOW];
 #pragma unroll

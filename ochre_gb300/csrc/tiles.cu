@@ -106,6 +106,80 @@ constexpr int ACC_H = 68;          // offset of the height cells
 constexpr int ACC_STRIDE = 136;    // floats per tile
 __device__ __forceinline__ int acc_idx(int cell) { return cell + ((cell >> 5) << 2); }
 
+// Stage of one batch of a chunk's bins (per warp): first increment, first
+// cell, packed steps / cell count / directions / accumulator slot, and the
+// exclusive prefix of the cell counts.
+struct BinStage {
+    uint32_t inc[32];
+    uint32_t xy[32];     // x (low 16 bits) | y (high 16 bits)
+    uint32_t meta[32];   // steps (bits 0-15) | n (16-20) | dirs (21-22) | slot (23-27)
+    uint32_t pre[33];
+};
+
+// Adds the stored increments of the bins among entries e0 .. e1 - 1 (the
+// entries of the chunk's nt tiles; crossing entries skipped) into the chunk's
+// shared accumulators (rasterizer.rs:223-228).  The bins of a batch of 32
+// entries are staged, then the warp takes their cells 32 at a time, so every
+// lane has a cell whatever the bins' lengths; a cell's position follows from
+// its bin's first cell and steps.
+template <int CH>
+__device__ __forceinline__ void add_chunk_increments(const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins,
+                                                     const float2* __restrict__ incs, uint32_t e0, uint32_t e1,
+                                                     const uint32_t* s_head, int nt, float (*acc)[ACC_STRIDE],
+                                                     BinStage& st) {
+    const int lane = threadIdx.x & 31;
+    for (uint32_t eb = e0; eb < e1; eb += 32) {
+        const uint32_t e = eb + lane;
+        uint32_t n = 0, inc = 0, xy = 0, meta = 0;
+        if (e < e1) {
+            const uint32_t v = vals[e];
+            if (!(v & CROSS_TAG)) {
+                const BinRec rec = bins[v];
+                int slot = 0;
+#pragma unroll
+                for (int i = 1; i < CH; i++)
+                    if (i < nt && s_head[i] <= e) slot = i;
+                n = rec.n;
+                inc = rec.inc;
+                xy = (uint32_t)(uint16_t)rec.x | ((uint32_t)(uint16_t)rec.y << 16);
+                meta = (uint32_t)rec.steps | (n << 16) | ((uint32_t)rec.dirs << 21) | ((uint32_t)slot << 23);
+            }
+        }
+        uint32_t pre = n;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, pre, d);
+            if (lane >= d) pre += o;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+        st.inc[lane] = inc;
+        st.xy[lane] = xy;
+        st.meta[lane] = meta;
+        st.pre[lane] = pre - n;
+        if (lane == 31) st.pre[32] = total;
+        __syncwarp();
+        for (uint32_t c = lane; c < total; c += 32) {
+            // the bin holding cell c: the last b with pre[b] <= c
+            int b = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1)
+                if (st.pre[b + step] <= c) b += step;
+            const uint32_t k = c - st.pre[b];
+            const uint32_t m = st.meta[b], sxy = st.xy[b];
+            const uint32_t steps_before = m & ((1u << k) - 1u) & 0xffffu;
+            const int nx = __popc(steps_before), ny = (int)k - nx;
+            const int cx = (int)(sxy & 0xffffu) + ((m >> 21) & 1u ? -nx : nx);
+            const int cy = (int)(sxy >> 16) + ((m >> 22) & 1u ? -ny : ny);
+            const int cell = ((cy & 7) << 3) | (cx & 7);
+            const float2 ah = incs[st.inc[b] + k];
+            float* a = acc[(m >> 23) & 31u];
+            atomicAdd(a + acc_idx(cell), ah.x);
+            atomicAdd(a + ACC_H + acc_idx(cell), ah.y);
+        }
+        __syncwarp();
+    }
+}
+
 // Coverage, block form: one warp per aligned block of TILES_PER_WARP
 // consecutive tiles (blocks may cross rows).  A block that continues a row
 // from the previous block resolves its carry by decoupled look-back: blocks
@@ -115,7 +189,7 @@ __device__ __forceinline__ int acc_idx(int cell) { return cell + ((cell >> 5) <<
 // and the row form below is used instead.
 template <int CH>
 __global__ void __launch_bounds__(128) k_tile_cov_blocks(
-    const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
+    const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float2* __restrict__ incs,
     const TileInfo* __restrict__ info, uint32_t n_tiles, const uint32_t* n_dev, TileBlockState* state,
     uint32_t* ticket, uint32_t* __restrict__ out_xy, uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov,
     uint32_t* __restrict__ span_flag, uint64_t* __restrict__ span_val, uint32_t* err, bool cov_signed) {
@@ -129,6 +203,7 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
     __shared__ __align__(16) float s_acc[WARPS][CH][ACC_STRIDE];
     __shared__ uint32_t s_head[WARPS][CH];
     __shared__ TileInfo s_info[WARPS][CH + 1];
+    __shared__ BinStage s_stage[WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     uint32_t blk = 0;
     if (lane == 0) blk = atomicAdd(ticket, 1u);
@@ -149,41 +224,12 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
     if (lane < nt) s_head[wid][lane] = s_info[wid][lane].head;
     __syncwarp();
 
-    // Replay every bin of the block (rasterizer.rs:97-106, 223-228).  The
-    // block's entries are contiguous; crossing entries in between are skipped.
+    // The stored increments of every bin of the block (rasterizer.rs:97-106,
+    // 223-228).  The block's entries are contiguous; crossing entries in
+    // between are skipped.
     const uint32_t e0 = s_info[wid][0].head;
     const uint32_t e1 = s_info[wid][nt - 1].head + s_info[wid][nt - 1].nbins;
-    for (uint32_t e = e0 + lane; e < e1; e += 32) {
-        const uint32_t v = vals[e];
-        if (v & CROSS_TAG) continue;
-        int slot = 0;
-#pragma unroll
-        for (int i = 1; i < CH; i++)
-            if (i < nt && s_head[wid][i] <= e) slot = i;
-        const BinRec rec = bins[v];
-        if (rec.n == 0) continue;
-        const float4 l = lines[rec.line];
-        Walk w;
-        WalkState s;
-        walk_setup(v2(l.x, l.y), v2(l.z, l.w), w, s);
-        s.x = rec.x;
-        s.y = rec.y;
-        s.row_t0 = rec.row_t0;
-        s.row_t1 = rec.row_t1;
-        s.col_t0 = rec.col_t0;
-        s.col_t1 = rec.col_t1;
-        float* a = acc[slot];
-        for (uint32_t k = 0;; k++) {
-            float area, height;
-            walk_increment(w, s, area, height);
-            const int cell = ((s.y & 7) << 3) | (s.x & 7);
-            atomicAdd(a + acc_idx(cell), area);
-            atomicAdd(a + ACC_H + acc_idx(cell), height);
-            if (k + 1 >= rec.n) break;
-            walk_step(w, s);
-        }
-    }
-    __syncwarp();
+    add_chunk_increments<CH>(vals, bins, incs, e0, e1, s_head[wid], nt, acc, s_stage[wid]);
 
     // Each lane owns one pixel row of one tile: lane = 8 * g + y, four tiles
     // (g) per pass.
@@ -348,7 +394,7 @@ __global__ void __launch_bounds__(128) k_tile_cov_blocks(
 // Coverage, row form: one warp per tile row (see the file comment).
 template <int CH>
 __global__ void __launch_bounds__(128) k_tile_cov(
-    const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float4* __restrict__ lines,
+    const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins, const float2* __restrict__ incs,
     const TileInfo* __restrict__ info, uint32_t n_tiles, const uint32_t* n_dev, const uint32_t* __restrict__ row_start,
     const uint32_t* __restrict__ n_rows_p, uint32_t* ticket, uint32_t* __restrict__ out_xy,
     uint8_t* __restrict__ out_alpha, float* __restrict__ out_cov, uint32_t* __restrict__ span_flag,
@@ -359,6 +405,7 @@ __global__ void __launch_bounds__(128) k_tile_cov(
     __shared__ __align__(16) float s_acc[WARPS][CH][ACC_STRIDE];
     __shared__ uint32_t s_head[WARPS][CH];
     __shared__ TileInfo s_info[WARPS][CH + 1];
+    __shared__ BinStage s_stage[WARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     // lane = 8 * g + y: pixel row y of the g-th tile of a pass of four
     const int y = lane & 7, g = lane >> 3;
@@ -389,42 +436,12 @@ __global__ void __launch_bounds__(128) k_tile_cov(
             if (lane < nt) s_head[wid][lane] = s_info[wid][lane].head;
             __syncwarp();
 
-            // Replay every bin of the chunk (rasterizer.rs:97-106, 223-228).
-            // The chunk's entries are contiguous; crossing entries in between
-            // are skipped.
+            // The stored increments of every bin of the chunk
+            // (rasterizer.rs:97-106, 223-228).  The chunk's entries are
+            // contiguous; crossing entries in between are skipped.
             const uint32_t e0 = s_info[wid][0].head;
             const uint32_t e1 = s_info[wid][nt - 1].head + s_info[wid][nt - 1].nbins;
-            for (uint32_t e = e0 + lane; e < e1; e += 32) {
-                const uint32_t v = vals[e];
-                if (v & CROSS_TAG) continue;
-                int slot = 0;
-#pragma unroll
-                for (int i = 1; i < CH; i++)
-                    if (i < nt && s_head[wid][i] <= e) slot = i;
-                const BinRec rec = bins[v];
-                if (rec.n == 0) continue;
-                const float4 l = lines[rec.line];
-                Walk w;
-                WalkState st;
-                walk_setup(v2(l.x, l.y), v2(l.z, l.w), w, st);
-                st.x = rec.x;
-                st.y = rec.y;
-                st.row_t0 = rec.row_t0;
-                st.row_t1 = rec.row_t1;
-                st.col_t0 = rec.col_t0;
-                st.col_t1 = rec.col_t1;
-                float* a = acc[slot];
-                for (uint32_t c = 0;; c++) {
-                    float area, height;
-                    walk_increment(w, st, area, height);
-                    const int cell = ((st.y & 7) << 3) | (st.x & 7);
-                    atomicAdd(a + acc_idx(cell), area);
-                    atomicAdd(a + ACC_H + acc_idx(cell), height);
-                    if (c + 1 >= rec.n) break;
-                    walk_step(w, st);
-                }
-            }
-            __syncwarp();
+            add_chunk_increments<CH>(vals, bins, incs, e0, e1, s_head[wid], nt, acc, s_stage[wid]);
 
             // Tiles left to right (rasterizer.rs:232-250): along its row a lane
             // adds the cells in the reference's order; the carry into a tile is
@@ -558,7 +575,7 @@ static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, uint32_t n_rows, boo
         // no more warps than rows, nor than the GPU keeps resident (16 CTAs of 4 warps per SM)
         const uint32_t ctas = (uint32_t)std::min<uint64_t>(((uint64_t)n_rows + 3) / 4, (uint64_t)sms * 16);
         k_tile_cov<TPW><<<ctas, 128, 0, s>>>(
-            ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(),
+            ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), ctx->tile_info.as<TileInfo>(),
             T, t_dev, ctx->tile_row_start.as<uint32_t>(), &ds->n_rows, &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
             ctx->out_tile_alpha.as<uint8_t>(), cov, ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(),
             &ds->err, ctx->cov_signed);
@@ -566,7 +583,7 @@ static void launch_tile_cov(ochre_gpu_ctx* ctx, uint32_t T, uint32_t n_rows, boo
         const uint32_t blocks = (T + TPW - 1) / TPW;
         cudaMemsetAsync(ctx->tile_state.p, 0, (size_t)blocks * sizeof(TileBlockState), s);
         k_tile_cov_blocks<TPW><<<(blocks + 3) / 4, 128, 0, s>>>(
-            ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->lines.as<float4>(), ctx->tile_info.as<TileInfo>(),
+            ctx->vals.as<uint32_t>(), ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), ctx->tile_info.as<TileInfo>(),
             T, t_dev, ctx->tile_state.as<TileBlockState>(), &ds->ticket, ctx->out_tile_xy.as<uint32_t>(),
             ctx->out_tile_alpha.as<uint8_t>(), cov, ctx->span_flag.as<uint32_t>(), ctx->span_val.as<uint64_t>(),
             &ds->err, ctx->cov_signed);
