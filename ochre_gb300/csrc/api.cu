@@ -388,7 +388,7 @@ std::vector<DevBuf*> device_buffers(ochre_gpu_ctx* ctx) {
                      &ctx->raster_empty, &ctx->raster_wsum, &ctx->raster_wbase, &ctx->tile_head_bins,
                      &ctx->tile_head_wind, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_row_start, &ctx->tile_state,
-                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_u_xy, &ctx->fused_u_alpha, &ctx->fused_u_cov, &ctx->fused_u_span, &ctx->fused_rcount, &ctx->fused_rstart,
+                     &ctx->span_flag, &ctx->span_val, &ctx->scan_status, &ctx->scalars, &ctx->fused_chain, &ctx->fused_stage,
                      &ctx->grad_g, &ctx->grad_gs, &ctx->grad_left, &ctx->grad_line, &ctx->grad_pts,
                      &ctx->sk_cmd_foff, &ctx->sk_cmd_mv, &ctx->sk_cmd_ep, &ctx->sk_poly_off, &ctx->sk_poly_foff,
                      &ctx->sk_pverbs, &ctx->sk_ppts, &ctx->sk_pfoff, &ctx->sk_pfill_off, &ctx->sk_first_close,

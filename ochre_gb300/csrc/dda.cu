@@ -277,6 +277,10 @@ __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __
     const uint64_t base = key_base[r];
     uint32_t e = ent_off[i];
     uint32_t q = inc_off[i];   // next stored increment
+    // increments leave in 16-byte pairs (an even index and the next one):
+    // the first of a pair waits in registers
+    float2 pend = make_float2(0.0f, 0.0f);
+    bool has_pend = false;
     // open bin
     int btx = 0x7fffffff, bty = 0x7fffffff, prev_x = 0;
     uint32_t bcount = 0, bentry = 0;
@@ -310,7 +314,17 @@ __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __
             } else if (s.x != prev_x) {
                 rec.steps = (uint16_t)(rec.steps | (1u << (bcount - 1)));   // the step into this cell moved in x
             }
-            incs[q++] = make_float2(area, height);
+            const float2 v = make_float2(area, height);
+            if ((q & 1u) == 0u) {
+                pend = v;
+                has_pend = true;
+            } else if (has_pend) {
+                reinterpret_cast<float4*>(incs)[q >> 1] = make_float4(pend.x, pend.y, v.x, v.y);
+                has_pend = false;
+            } else {
+                incs[q] = v;   // the line's first increment at an odd index
+            }
+            q++;
             prev_x = s.x;
             bcount++;
         },
@@ -321,6 +335,7 @@ __global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __
         },
         [&](int, int) {});
     flush();
+    if (has_pend) incs[q - 1] = pend;
 }
 
 template <class K>

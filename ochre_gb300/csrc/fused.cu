@@ -76,9 +76,7 @@ struct FusedSmem {
     uint32_t raster;
     uint32_t flag;                 // per-raster fallback
     uint32_t n_cross;
-    uint32_t tile_base, span_base; // this raster's first tile / span in the unordered output
-    uint32_t chunk_t, left_t;      // this CTA's current output chunk: next free tile, tiles left
-    uint32_t chunk_s, left_s;      // ... and span
+    uint32_t tile_base, span_base;
     int32_t gx0, gy0, gw, gh;
 };
 
@@ -157,10 +155,6 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     // the command scan before this launch gave up a wait: its offsets are not valid
     if (run_aborted(A.err)) return;
-    if (tid == 0) {
-        S.left_t = 0;
-        S.left_s = 0;
-    }
     for (;;) {
         if (tid == 0) {
             S.raster = atomicAdd(A.ticket, 1u);
@@ -445,43 +439,18 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
 #pragma unroll
             for (int k = 0; k < F_TMAX / 32; k++) n_spans += __popc(S.span_mask[k]);
         }
-        // Output space: the raster's tiles and spans go to this CTA's current
-        // chunk of the unordered output (a new chunk from the device-wide
-        // cursors when it is full); a scan over the rasters' counts and a
-        // reorder pass after the launch put them in raster order.  No raster
-        // waits for another.
-        if (tid == 0) {
-            const uint32_t nt = bail ? 0u : (uint32_t)n_tiles, ns = bail ? 0u : (uint32_t)n_spans;
-            if (nt > S.left_t) {
-                S.chunk_t = atomicAdd(A.u_cursor, (uint32_t)U_CHUNK_TILES);
-                S.left_t = U_CHUNK_TILES;
-            }
-            if (ns > S.left_s) {
-                S.chunk_s = atomicAdd(A.u_cursor + 1, (uint32_t)U_CHUNK_SPANS);
-                S.left_s = U_CHUNK_SPANS;
-            }
-            S.tile_base = S.chunk_t;
-            S.span_base = S.chunk_s;
-            S.chunk_t += nt;
-            S.left_t -= nt;
-            S.chunk_s += ns;
-            S.left_s -= ns;
-            const bool fits = (uint64_t)S.tile_base + nt <= A.u_tile_cap && (uint64_t)S.span_base + ns <= A.u_span_cap;
-            if (!fits && !bail) atomicOr(A.err, ERR_CAPACITY);
-            S.flag = fits ? 0u : 2u;   // 2: counted, not written
-            A.r_count[2 * (size_t)r] = nt;
-            A.r_count[2 * (size_t)r + 1] = ns;
-            A.r_start[2 * (size_t)r] = S.tile_base;
-            A.r_start[2 * (size_t)r + 1] = S.span_base;
-            if (bail) atomicOr(A.fallback, 1u);
-        }
-        __syncthreads();
-        const bool write = !bail && S.flag == 0u;
-        const uint32_t tb = S.tile_base, sb = S.span_base;
+        // The raster's counts go out now; its output offsets are resolved
+        // after the coverage below, when its predecessors have long
+        // published theirs.  A raster that does not fit publishes zeros and
+        // turns the batch over to the general chain.
+        if (wid == 0) lb_publish(A, r, bail ? 0u : (uint32_t)n_tiles, bail ? 0u : (uint32_t)n_spans);
+        if (tid == 0 && bail) atomicOr(A.fallback, 1u);
 
         // ---------------- C. accumulate and shade, CHUNK tiles at a time ----------------
-        // Alpha (and coverage) of tile i go straight to unordered tile tb + i.
-        if (write && n_real > 0) {
+        // Alpha (and coverage) go to this CTA's staging slots: tile i of the
+        // raster at stage + (blockIdx.x * F_TMAX + i) * 64.
+        if (!bail && n_real > 0) {
+            const size_t stage0 = (size_t)blockIdx.x * F_TMAX;
             const int gx0 = S.gx0, gy0 = S.gy0;
             for (int lo = 0; lo < n_real; lo += CHUNK) {
                 const int nch = min(CHUNK, n_real - lo);
@@ -551,29 +520,62 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
                     const float acc0 = S.carry[i][row] + excl;
                     const float cov0 = fabsf(acc0 + a0);
                     const float cov1 = fabsf((acc0 + h0) + a1);
-                    const size_t t = (size_t)tb + lo + i;
+                    const size_t t = stage0 + lo + i;
                     const uint32_t al0 = f2u8(rmin(cov0 * 256.0f, 255.0f));
                     const uint32_t al1 = f2u8(rmin(cov1 * 256.0f, 255.0f));
-                    reinterpret_cast<uint16_t*>(A.u_alpha + t * 64)[lane] = (uint16_t)(al0 | (al1 << 8));
-                    if (A.u_cov) reinterpret_cast<float2*>(A.u_cov + t * 64)[lane] = make_float2(cov0, cov1);
+                    reinterpret_cast<uint16_t*>(A.stage_alpha + t * 64)[lane] = (uint16_t)(al0 | (al1 << 8));
+                    if (A.out_cov) reinterpret_cast<float2*>(A.stage_cov + t * 64)[lane] = make_float2(cov0, cov1);
                 }
                 __syncthreads();
             }
         }
 
-        // ---------------- tile positions and spans of the raster ----------------
-        if (write) {
-            if (n_real == 0) {
+        // ---------------- offsets, then every output of the raster ----------------
+        if (wid == 0) {
+            uint32_t p0, p1;
+            const uint32_t a0 = bail ? 0u : (uint32_t)n_tiles, a1 = bail ? 0u : (uint32_t)n_spans;
+            lb_resolve(A, r, a0, a1, p0, p1);
+            if (lane == 0) {
+                S.tile_base = p0;
+                S.span_base = p1;
+                if (!bail) {
+                    A.raster_tile_off[r] = p0;
+                    A.raster_span_off[r] = p1;
+                    if (r + 1 == A.n_rasters) {
+                        A.raster_tile_off[r + 1] = p0 + n_tiles;
+                        A.raster_span_off[r + 1] = p1 + n_spans;
+                        A.totals[0] = p0 + n_tiles;
+                        A.totals[1] = p1 + n_spans;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (!bail) {
+            const uint32_t tb = S.tile_base, sb = S.span_base;
+            if ((uint64_t)tb + n_tiles > A.tile_cap || (uint64_t)sb + n_spans > A.span_cap) {
+                if (tid == 0) atomicOr(A.err, ERR_CAPACITY);
+            } else if (n_real == 0) {
                 // no increments: one all-zero tile at (0, 0)
-                if (tid < 16) reinterpret_cast<uint32_t*>(A.u_alpha + (size_t)tb * 64)[tid] = 0u;
-                if (A.u_cov && tid < 64) A.u_cov[(size_t)tb * 64 + tid] = 0.0f;
-                if (tid == 0) A.u_xy[tb] = 0u;
+                if (tid < 16) reinterpret_cast<uint32_t*>(A.out_alpha + (size_t)tb * 64)[tid] = 0u;
+                if (A.out_cov && tid < 64) A.out_cov[(size_t)tb * 64 + tid] = 0.0f;
+                if (tid == 0) A.out_xy[tb] = 0u;
             } else {
+                // staged alpha / coverage -> their final place (8-byte pieces)
+                const size_t stage0 = (size_t)blockIdx.x * F_TMAX;
+                const uint2* sa = reinterpret_cast<const uint2*>(A.stage_alpha + stage0 * 64);
+                uint2* da = reinterpret_cast<uint2*>(A.out_alpha + (size_t)tb * 64);
+                for (int q = tid; q < n_real * 8; q += FUSED_THREADS) da[q] = sa[q];
+                if (A.out_cov) {
+                    const float2* sc = reinterpret_cast<const float2*>(A.stage_cov + stage0 * 64);
+                    float2* dc = reinterpret_cast<float2*>(A.out_cov + (size_t)tb * 64);
+                    for (int q = tid; q < n_real * 32; q += FUSED_THREADS) dc[q] = sc[q];
+                }
                 for (int t = tid; t < n_real; t += FUSED_THREADS) {
                     const int g = S.tile_g[t];
                     const int tx = S.gx0 + (g & 31), ty = S.gy0 + (g >> 5);
-                    A.u_xy[tb + t] = (uint32_t)(uint16_t)(int16_t)(tx * 8) |
-                                     ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
+                    A.out_xy[tb + t] = (uint32_t)(uint16_t)(int16_t)(tx * 8) |
+                                       ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
                     const uint32_t m = S.span_mask[t >> 5];
                     if (m >> (t & 31) & 1u) {
                         // span rank: the span tiles before t (tile order = callback order)
@@ -581,10 +583,10 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
                         for (int k = 0; k < (t >> 5); k++) sr += __popc(S.span_mask[k]);
                         const uint32_t right = S.touched[g >> 5] >> ((g & 31) + 1);
                         const int gap = __ffs(right) - 1;
-                        A.u_span_xy[sb + sr] = (uint32_t)(uint16_t)(int16_t)((tx + 1) * 8) |
-                                               ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
-                        A.u_span_w[sb + sr] = (uint16_t)((uint16_t)gap * 8u);
-                        A.u_span_t[sb + sr] = (uint16_t)t;   // tile index within the raster
+                        A.span_xy[sb + sr] = (uint32_t)(uint16_t)(int16_t)((tx + 1) * 8) |
+                                             ((uint32_t)(uint16_t)(int16_t)(ty * 8) << 16);
+                        A.span_w[sb + sr] = (uint16_t)((uint16_t)gap * 8u);
+                        A.span_tile[sb + sr] = tb + t;
                     }
                 }
             }
@@ -641,70 +643,6 @@ struct FloatOff {
     __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
 };
 
-// Raster output offsets: one scan of the rasters' (tile, span) counts.
-struct TS {
-    uint32_t t, s;
-};
-struct OpTS {
-    __device__ __forceinline__ TS operator()(TS a, TS b) const { return TS{a.t + b.t, a.s + b.s}; }
-};
-struct RCountIn {
-    const uint32_t* count;
-    __device__ __forceinline__ TS operator()(uint64_t r) const { return TS{count[2 * r], count[2 * r + 1]}; }
-};
-struct ROffOut {
-    uint32_t* tile_off;
-    uint32_t* span_off;
-    uint64_t n;
-    __device__ __forceinline__ void operator()(uint64_t r, TS ex, TS v) const {
-        tile_off[r] = ex.t;
-        span_off[r] = ex.s;
-        if (r + 1 == n) {
-            tile_off[n] = ex.t + v.t;
-            span_off[n] = ex.s + v.s;
-        }
-    }
-};
-
-// Unordered output -> raster order: one warp per raster (grid-stride).  A
-// total beyond the output capacity flags ERR_CAPACITY and writes nothing; so
-// does a raster whose range would leave the output (which only offsets that
-// are not valid give).
-__global__ void __launch_bounds__(256) k_fused_reorder(
-    const uint32_t* __restrict__ r_count, const uint32_t* __restrict__ r_start, const uint32_t* __restrict__ tile_off,
-    const uint32_t* __restrict__ span_off, uint32_t n_rasters, const uint32_t* totals, uint32_t tile_cap,
-    uint32_t span_cap, const uint32_t* __restrict__ u_xy, const uint2* __restrict__ u_alpha,
-    const float4* __restrict__ u_cov, const uint32_t* __restrict__ u_span_xy, const uint16_t* __restrict__ u_span_w,
-    const uint16_t* __restrict__ u_span_t, uint32_t* __restrict__ out_xy, uint2* __restrict__ out_alpha,
-    float4* __restrict__ out_cov, uint32_t* __restrict__ out_span_xy, uint16_t* __restrict__ out_span_w,
-    uint32_t* __restrict__ out_span_tile, uint32_t* err) {
-    if (run_aborted(err)) return;   // a wait of the offset scan gave up
-    if (totals[0] > tile_cap || totals[1] > span_cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, ERR_CAPACITY);
-        return;
-    }
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    for (uint32_t r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n_rasters; r += warps) {
-        const uint32_t nt = r_count[2 * (size_t)r], ns = r_count[2 * (size_t)r + 1];
-        const uint32_t ut = r_start[2 * (size_t)r], us = r_start[2 * (size_t)r + 1];
-        const uint32_t ft = tile_off[r], fs = span_off[r];
-        if ((uint64_t)ft + nt > tile_cap || (uint64_t)fs + ns > span_cap) {   // offsets not valid
-            if (lane == 0) atomicOr(err, ERR_CAPACITY);
-            continue;
-        }
-        for (uint32_t q = lane; q < nt * 8; q += 32) out_alpha[(size_t)ft * 8 + q] = u_alpha[(size_t)ut * 8 + q];
-        if (out_cov)
-            for (uint32_t q = lane; q < nt * 16; q += 32) out_cov[(size_t)ft * 16 + q] = u_cov[(size_t)ut * 16 + q];
-        for (uint32_t q = lane; q < nt; q += 32) out_xy[ft + q] = u_xy[ut + q];
-        for (uint32_t q = lane; q < ns; q += 32) {
-            out_span_xy[fs + q] = u_span_xy[us + q];
-            out_span_w[fs + q] = u_span_w[us + q];
-            out_span_tile[fs + q] = ft + u_span_t[us + q];
-        }
-    }
-}
-
 // Runs the fused kernel over the whole batch.  *handled is false when some
 // raster does not fit (the caller then runs the general chain).
 static int run_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
@@ -713,7 +651,13 @@ static int run_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, 
     DevScalars* ds = dev_scalars(ctx);
     const uint32_t R = in->n_rasters;
     const bool want_cov = (ctx->flags & OCHRE_CTX_WANT_COV) != 0;
-    // no more CTAs than rasters
+    // look-back words: per raster (aggregate, inclusive), per block
+    // (aggregate, inclusive) and the blocks' publish counters, zeroed per run
+    const size_t nb = ((size_t)R + LB_BLOCK - 1) / LB_BLOCK;
+    const size_t lb_bytes = (2 * (size_t)R + 2 * nb) * sizeof(uint64_t) + nb * sizeof(uint32_t);
+    OCHRE_CUDA_TRY(ctx->fused_chain.ensure(lb_bytes));
+    uint64_t* lb = ctx->fused_chain.as<uint64_t>();
+    // no more CTAs than rasters; each stages the coverage of its raster
     int grid = 0;
     {
         const int st = fused_shape(ctx, nullptr, &grid, s);
@@ -721,15 +665,12 @@ static int run_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, 
     }
     grid = (int)std::min<uint32_t>((uint32_t)grid, R);
     if (ctx->fused_max_ctas) grid = std::min<int>(grid, std::max<int>(1, (int)ctx->fused_max_ctas));
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const size_t stage_tiles = (size_t)grid * F_TMAX;
+    OCHRE_CUDA_TRY(ctx->fused_stage.ensure(stage_tiles * 64 * (want_cov ? 5 : 1)));
     // float offset of every command (the kernel reads its points there)
     const uint64_t n_cmds = in->n_cmds;
     OCHRE_CUDA_TRY(ctx->cmd_foff.ensure((size_t)std::max<uint64_t>(n_cmds, 1) * 4));
-    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(std::max<uint64_t>(n_cmds, R)) *
-                                           std::max(sizeof(ScanStatus<uint32_t>), sizeof(ScanStatus<TS>))));
-    OCHRE_CUDA_TRY(ctx->fused_rcount.ensure((size_t)R * 8));
-    OCHRE_CUDA_TRY(ctx->fused_rstart.ensure((size_t)R * 8));
+    OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_cmds) * sizeof(ScanStatus<uint32_t>)));
     // capacity guess: the last run's totals, else 48 tiles per raster; with
     // caller-provided (fixed) outputs, their capacity
     const bool fixed_out = ctx->out_tile_xy.fixed;
@@ -746,12 +687,6 @@ static int run_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, 
     }
     for (int attempt = 0; attempt < 2; attempt++) {
         const uint32_t span_cap = fixed_out ? span_cap_fixed : tile_cap;
-        // the unordered output holds every tile plus the unused ends of the
-        // CTAs' chunks
-        const uint64_t u_tcap64 = (uint64_t)tile_cap + (uint64_t)grid * U_CHUNK_TILES;
-        const uint64_t u_scap64 = (uint64_t)std::min(span_cap, tile_cap) + (uint64_t)grid * U_CHUNK_SPANS;
-        if (u_tcap64 > MAX_COUNT || u_scap64 > MAX_COUNT) return OCHRE_E_CAPACITY;
-        const uint32_t u_tcap = (uint32_t)u_tcap64, u_scap = (uint32_t)u_scap64;
         OCHRE_CUDA_TRY(ctx->out_tile_xy.ensure((size_t)tile_cap * 4));
         OCHRE_CUDA_TRY(ctx->out_tile_alpha.ensure((size_t)tile_cap * 64));
         if (want_cov) OCHRE_CUDA_TRY(ctx->out_tile_cov.ensure((size_t)tile_cap * 256));
@@ -760,19 +695,19 @@ static int run_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, 
         OCHRE_CUDA_TRY(ctx->out_span_tile.ensure((size_t)span_cap * 4));
         OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
         OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
-        OCHRE_CUDA_TRY(ctx->fused_u_xy.ensure((size_t)u_tcap * 4));
-        OCHRE_CUDA_TRY(ctx->fused_u_alpha.ensure((size_t)u_tcap * 64));
-        if (want_cov) OCHRE_CUDA_TRY(ctx->fused_u_cov.ensure((size_t)u_tcap * 256));
-        OCHRE_CUDA_TRY(ctx->fused_u_span.ensure((size_t)u_scap * 8));
+        OCHRE_CUDA_TRY(cudaMemsetAsync(lb, 0, lb_bytes, s));
         OCHRE_CUDA_TRY(reset_scalars(ctx, s));
         if (n_cmds)
             OCHRE_LAUNCH(ctx, "fused_float_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
                 n_cmds, VerbFloats{in->verbs}, FloatOff{ctx->cmd_foff.as<uint32_t>()}, OpSumU32{}, 0u,
-                ctx->scan_status.p, &ds->sort_ticket, &ds->n_floats, &ds->err, s)));
+                ctx->scan_status.p, &ds->sort_ticket, &ds->n_floats, &ds->err, s, nullptr,
+                ctx->test_skip_first_ticket ? 1u : 0u)));
         FusedArgs a{};
         a.verbs = in->verbs;
         a.pts = in->pts;
         a.cmd_foff = ctx->cmd_foff.as<uint32_t>();
+        a.stage_alpha = ctx->fused_stage.as<uint8_t>();
+        a.stage_cov = want_cov ? reinterpret_cast<float*>(ctx->fused_stage.as<uint8_t>() + stage_tiles * 64) : nullptr;
         a.fill_off = in->fill_cmd_off;
         a.fill_xf = in->fill_xf;
         a.fill_flags = in->fill_flags;
@@ -780,40 +715,28 @@ static int run_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, 
         a.n_fills = in->n_fills;
         a.n_rasters = R;
         a.n_floats = in->n_floats;
+        a.r_agg = lb;
+        a.r_inc = lb + R;
+        a.b_agg = lb + 2 * (size_t)R;
+        a.b_inc = lb + 2 * (size_t)R + nb;
+        a.b_cnt = reinterpret_cast<uint32_t*>(lb + 2 * (size_t)R + 2 * nb);
         a.ticket = &ds->ticket;
         a.fallback = &ds->fused_fallback;
         a.err = &ds->err;
-        a.u_cursor = &ds->fused_cursor_t;
-        a.u_tile_cap = u_tcap;
-        a.u_span_cap = u_scap;
-        a.u_xy = ctx->fused_u_xy.as<uint32_t>();
-        a.u_alpha = ctx->fused_u_alpha.as<uint8_t>();
-        a.u_cov = want_cov ? ctx->fused_u_cov.as<float>() : nullptr;
-        a.u_span_xy = ctx->fused_u_span.as<uint32_t>();
-        a.u_span_w = reinterpret_cast<uint16_t*>(ctx->fused_u_span.as<uint8_t>() + (size_t)u_scap * 4);
-        a.u_span_t = reinterpret_cast<uint16_t*>(ctx->fused_u_span.as<uint8_t>() + (size_t)u_scap * 6);
-        a.r_count = ctx->fused_rcount.as<uint32_t>();
-        a.r_start = ctx->fused_rstart.as<uint32_t>();
+        a.totals = &ds->fused_tiles;
+        a.tile_cap = tile_cap;
+        a.span_cap = span_cap;
+        a.out_xy = ctx->out_tile_xy.as<uint32_t>();
+        a.out_alpha = ctx->out_tile_alpha.as<uint8_t>();
+        a.out_cov = want_cov ? ctx->out_tile_cov.as<float>() : nullptr;
+        a.span_xy = ctx->out_span_xy.as<uint32_t>();
+        a.span_w = ctx->out_span_w.as<uint16_t>();
+        a.span_tile = ctx->out_span_tile.as<uint32_t>();
+        a.raster_tile_off = ctx->out_raster_tile_off.as<uint32_t>();
+        a.raster_span_off = ctx->out_raster_span_off.as<uint32_t>();
         wait_inputs(ctx, s);   // the kernel reads points
         const int st0 = fused_shape(ctx, &a, &grid, s);
         if (st0 != OCHRE_OK) return st0;
-        // raster order: offsets by a scan of the counts, then the reorder
-        OCHRE_LAUNCH(ctx, "fused_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<TS>(
-            R, RCountIn{a.r_count}, ROffOut{ctx->out_raster_tile_off.as<uint32_t>(),
-                                             ctx->out_raster_span_off.as<uint32_t>(), R},
-            OpTS{}, TS{0u, 0u}, ctx->scan_status.p, &ds->sort_ticket, reinterpret_cast<TS*>(&ds->fused_tiles),
-            &ds->err, s, nullptr, ctx->test_skip_first_ticket ? 1u : 0u)));
-        {
-            const uint32_t blocks = (uint32_t)std::min<uint64_t>(((uint64_t)R + 7) / 8, (uint64_t)std::max(sms, 1) * 8);
-            OCHRE_LAUNCH(ctx, "fused_reorder", s, k_fused_reorder<<<blocks, 256, 0, s>>>(
-                a.r_count, a.r_start, ctx->out_raster_tile_off.as<uint32_t>(), ctx->out_raster_span_off.as<uint32_t>(),
-                R, &ds->fused_tiles, tile_cap, span_cap, a.u_xy, reinterpret_cast<const uint2*>(a.u_alpha),
-                reinterpret_cast<const float4*>(a.u_cov), a.u_span_xy, a.u_span_w, a.u_span_t,
-                ctx->out_tile_xy.as<uint32_t>(), ctx->out_tile_alpha.as<uint2>(),
-                want_cov ? ctx->out_tile_cov.as<float4>() : nullptr, ctx->out_span_xy.as<uint32_t>(),
-                ctx->out_span_w.as<uint16_t>(), ctx->out_span_tile.as<uint32_t>(), &ds->err));
-            OCHRE_CUDA_TRY(cudaGetLastError());
-        }
         if (plan) {
             // totals, fallback and errors are read after the replay
             *handled = true;

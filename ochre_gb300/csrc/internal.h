@@ -72,8 +72,6 @@ struct DevScalars {
     uint32_t pad3;
     uint32_t line_ent_total;  // chain: sort entries the lines produce   } (line scan
     uint32_t n_incs;          // chain: pixel-cell increments of the lines } pair total)
-    uint32_t fused_cursor_t;  // fused path: next free tile / span of the unordered output
-    uint32_t fused_cursor_s;
 };
 // The waits find spin_log2 from the error word's address (common.cuh).
 static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
@@ -164,9 +162,8 @@ struct ochre_gpu_ctx {
     // scan workspace
     ochre::DevBuf scan_status;
     ochre::DevBuf scalars;   // DevScalars
-    // fused path: the unordered output (tiles and spans in the order the CTAs
-    // finished their rasters) and per raster its counts and first tile / span
-    ochre::DevBuf fused_u_xy, fused_u_alpha, fused_u_cov, fused_u_span, fused_rcount, fused_rstart;
+    ochre::DevBuf fused_chain;   // fused path: the rasters' and blocks' look-back words
+    ochre::DevBuf fused_stage;   // fused path: per-CTA staged alpha (and coverage) of its raster
     uint32_t fused_max_ctas = 0; // fused path: at most this many persistent CTAs (0: no limit)
     uint32_t fused_tile_cap = 0; // fused path: output capacity guess (tiles)
     // device outputs
@@ -205,8 +202,8 @@ struct ochre_gpu_ctx {
 
     // Test hooks (ochre_gpu_set_tunable "test_*"), used by the next run only:
     // the poll limit of its bounded waits (log2; 0: the default), and, on the
-    // fused path, a raster-offset scan whose first tile is never taken, so
-    // that the waits of the tiles after it cannot finish.
+    // fused path, a command scan whose first tile is never taken, so that
+    // the waits of the tiles after it cannot finish.
     uint32_t test_spin_log2 = 0;
     uint32_t test_skip_first_ticket = 0;
 

@@ -88,10 +88,9 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
     ochre_gpu_ctx ctx;
     ctx.device = dev;
     ctx.flags = 0;
-    // the fused path's unordered output comes from the array too, with room
-    // for the unused end of every CTA's output chunk: a smaller persistent
-    // grid keeps that to a few MB
-    ctx.fused_max_ctas = 128;
+    // the fused path's per-CTA staging comes from the array too: a smaller
+    // persistent grid keeps it to a few MB
+    ctx.fused_max_ctas = 256;
     ctx.own_stream = static_cast<cudaStream_t>(stream);
     ochre::DevBuf* internal[] = {&ctx.in_verbs, &ctx.in_pts, &ctx.in_fill_off, &ctx.in_fill_xf,
                                  &ctx.in_fill_flags, &ctx.in_raster_off, &ctx.cmd_foff, &ctx.cmd_mv, &ctx.cmd_ep,
@@ -100,7 +99,7 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
                                  &ctx.raster_wsum, &ctx.raster_wbase, &ctx.tile_head_bins, &ctx.tile_head_wind, &ctx.keys, &ctx.vals,
                                  &ctx.keys_alt, &ctx.vals_alt, &ctx.bins, &ctx.sort_hist, &ctx.sort_lookback,
                                  &ctx.tile_head, &ctx.tile_info, &ctx.tile_row_start, &ctx.tile_state, &ctx.span_flag, &ctx.span_val,
-                                 &ctx.scan_status, &ctx.scalars, &ctx.fused_u_xy, &ctx.fused_u_alpha, &ctx.fused_u_cov, &ctx.fused_u_span, &ctx.fused_rcount, &ctx.fused_rstart, &ctx.out_tile_cov,
+                                 &ctx.scan_status, &ctx.scalars, &ctx.fused_chain, &ctx.fused_stage, &ctx.out_tile_cov,
                                  &ctx.grad_g, &ctx.grad_gs, &ctx.grad_left, &ctx.grad_line, &ctx.grad_pts,
                                  &ctx.sk_cmd_foff, &ctx.sk_cmd_mv, &ctx.sk_cmd_ep, &ctx.sk_poly_off,
                                  &ctx.sk_poly_foff, &ctx.sk_pverbs, &ctx.sk_ppts, &ctx.sk_pfoff, &ctx.sk_pfill_off,

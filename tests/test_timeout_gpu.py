@@ -4,8 +4,8 @@ Every look-back wait of the chain polls a bounded number of times; the first
 wait that gives up flags ERR_TIMEOUT and every other wait of the run gives up
 as soon as it sees the flag.  The test makes one run's waits impossible to
 finish on the host side: the test hook `test_skip_first_ticket` starts the
-tickets of the fused path's raster-offset scan at 1, so that scan's first
-tile never publishes and every later tile's look-back waits on it;
+tickets of the fused path's command scan at 1, so that scan's first tile
+never publishes and every later tile's look-back waits on it;
 `test_spin_log2` lowers the poll limit to 2^4 for that run.  The call must
 return OCHRE_E_TIMEOUT quickly, and the same context must then reproduce the
 oracle's output.  Nothing here faults or hangs the GPU: the waits end by
@@ -28,7 +28,7 @@ def _set(ctx, name, value):
 
 
 def test_unfinishable_lookback_times_out_and_context_recovers():
-    # 5,000 rasters: three tiles of the raster-offset scan
+    # 5,000 rasters, 140,000 commands: 69 tiles of the command scan
     b = workloads.glyph_run(n_paths=5000, seed=41)
     exp = oracle.run(b, threads=16)
     ctx = GpuContext(0)
@@ -45,8 +45,9 @@ def test_unfinishable_lookback_times_out_and_context_recovers():
         st = _lib.load().ochre_gpu_rasterize_device(ctx.handle, ctypes.byref(db.c), ctypes.byref(r), None)
         dt = time.perf_counter() - t0
         assert st == _lib.E_TIMEOUT, _lib.status_string(st)
-        # two waiting scan tiles of at most 16 polls each: well under a
-        # second (the default limit alone would be about a second)
+        # the first waiting tile gives up after 16 polls and the others see
+        # the abort within 8: well under a second (the default limit alone
+        # would be about a second)
         assert dt < 0.5, dt
 
         # the hooks applied to that run only; the context still works
