@@ -260,15 +260,22 @@ __device__ __forceinline__ K make_key(uint64_t base, const int4& bb, int tx, int
     return (K)(base + (((uint64_t)(ty - bb.y) * w + (uint64_t)(tx - bb.x)) << 1) + kind);
 }
 
-// (In line order: neighbouring lanes write neighbouring entry ranges.)
+// Lines of a block are walked in order of length (order_by_length), so a
+// warp's lanes walk lines of about the same length.
 template <class K>
-__global__ void k_line_emit(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster,
+__global__ void __launch_bounds__(256) k_line_emit(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster,
                             const uint32_t* __restrict__ ent_off, const uint32_t* __restrict__ inc_off, uint64_t n_cap,
                             const uint32_t* n_dev, const int4* __restrict__ bbox, const uint64_t* __restrict__ key_base,
                             K* __restrict__ keys, uint32_t* __restrict__ vals, BinRec* __restrict__ bins,
                             float2* __restrict__ incs) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= dev_count(n_cap, n_dev)) return;
+    __shared__ uint32_t s_cnt[17];
+    __shared__ uint16_t s_item[256];
+    const uint64_t n_lines = dev_count(n_cap, n_dev);
+    const uint64_t i0 = blockIdx.x * (uint64_t)blockDim.x;
+    if (i0 >= n_lines) return;
+    const uint32_t cells = i0 + threadIdx.x < n_lines ? walk_cells(lines[i0 + threadIdx.x]) : 0u;
+    const uint64_t i = i0 + order_by_length<256>(cells, s_cnt, s_item);
+    if (i >= n_lines) return;
     const float4 l = lines[i];
     const V2 a = v2(l.x, l.y), p = v2(l.z, l.w);
     if (veq(a, p)) return;
@@ -445,15 +452,15 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_CUDA_TRY(ctx->vals_alt.ensure(E * 4));
     OCHRE_CUDA_TRY(ctx->bins.ensure(E * sizeof(BinRec)));
     if (n_lines) {
-        const unsigned blocks = (unsigned)((n_lines + 127) / 128);
+        const unsigned blocks = (unsigned)((n_lines + 255) / 256);
         if (ctx->keys64)
-            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<blocks, 128, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<blocks, 256, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
                 ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
                 ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(),
                 ctx->bins.as<BinRec>(), ctx->incs.as<float2>()));
         else
-            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<blocks, 128, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<blocks, 256, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
                 ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
                 ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(),

@@ -9,8 +9,9 @@
 // then ranks a tile of keys in shared memory (per-warp counters with
 // __match_any_sync for stable ranks), publishes its per-digit counts and
 // resolves its global offsets by decoupled look-back over earlier tiles
-// (bounded spins), and scatters through shared memory so that runs of equal
-// digits leave as contiguous writes.
+// (bounded spins; a look-back word holds its flag and count together, so
+// relaxed accesses suffice), and scatters through shared memory so that
+// runs of equal digits leave as contiguous writes.
 #include "common.cuh"
 #include "internal.h"
 
@@ -93,12 +94,18 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
     uint32_t val[SORT_ITEMS];
     uint32_t rank[SORT_ITEMS];
     uint32_t dig[SORT_ITEMS];
+    // every load of the tile first (all in flight together), then the ranking
 #pragma unroll
     for (int k = 0; k < SORT_ITEMS; k++) {
         const uint64_t i = warp_base + (uint64_t)k * 32 + lane;
         const bool valid = i < n;
         key[k] = valid ? keys_in[i] : (K)0;
         val[k] = valid ? vals_in[i] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < SORT_ITEMS; k++) {
+        const uint64_t i = warp_base + (uint64_t)k * 32 + lane;
+        const bool valid = i < n;
         const uint32_t d = valid ? ((uint32_t)(key[k] >> shift) & 255u) : 256u;
         dig[k] = d;
         const uint32_t peers = __match_any_sync(0xffffffffu, d);
@@ -127,9 +134,9 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
         uint32_t* my = lookback + (size_t)tile * 256 + d;
         uint32_t excl = 0;
         if (tile == 0) {
-            st_release(my, LB_INC | run);
+            st_relaxed(my, LB_INC | run);
         } else {
-            st_release(my, LB_AGG | run);
+            st_relaxed(my, LB_AGG | run);
             // windowed look-back: LB_WINDOW predecessors per round, read
             // together (one latency per round instead of one per tile), up
             // to the nearest inclusive value
@@ -138,7 +145,7 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
             const long long poll_limit = spin_limit(err);
             // the nearest predecessor alone first: often it is inclusive already
             {
-                const uint32_t v = ld_acquire(lookback + (size_t)top * 256 + d);
+                const uint32_t v = ld_relaxed(lookback + (size_t)top * 256 + d);
                 if ((v & ~LB_MASK) == LB_INC) {
                     excl = v & LB_MASK;
                     top = -1;
@@ -149,7 +156,7 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
 #pragma unroll
                 for (int k = 0; k < LB_WINDOW; k++) {
                     const int64_t j = top - k;
-                    v[k] = j >= 0 ? ld_acquire(lookback + (size_t)j * 256 + d) : LB_INC;   // before tile 0: an inclusive 0
+                    v[k] = j >= 0 ? ld_relaxed(lookback + (size_t)j * 256 + d) : LB_INC;   // before tile 0: an inclusive 0
                 }
                 int k_inc = LB_WINDOW;
 #pragma unroll
@@ -173,7 +180,7 @@ __global__ void __launch_bounds__(SORT_BLOCK, 3) k_onesweep(const K* __restrict_
                 if (k_inc < LB_WINDOW) break;
                 top -= LB_WINDOW;
             }
-            st_release(my, LB_INC | (excl + run));
+            st_relaxed(my, LB_INC | (excl + run));
         }
         s_gbase[d] = digit_off[d] + excl;
         // block exclusive scan of run over digits -> tile-local digit starts
