@@ -771,14 +771,19 @@ def run_ours(args, ws, rank, local):
     dom_bytes = kernel_bytes(dom["kernel"], st, batch) / max(1, dom["launches"])
     dom_ms = dom["ms"] / max(1, dom["launches"])
     achieved = dom_bytes / (dom_ms / 1000.0) / 1e9 if dom_ms > 0 else 0.0
+    # DRAM traffic per launch and warp instructions per raster of the dominant
+    # kernel, from committed ncu captures, each keyed by the launch shape it
+    # was taken at: used only when that is the shape this run tuned to
+    from ochre_gb300 import autotune
+    shape = autotune.shape_name(tuned["choice"]) if dom["kernel"] == "raster_fused" else "chain"
     traffic = None
-    inst_per_unit = None   # warp instructions per raster of the dominant kernel (ncu capture)
+    inst_per_unit = None
     tfile = os.path.join(ROOT, "profiles", f"traffic_{args.workload}.json")
     if os.path.exists(tfile):
         with open(tfile) as f:
             tj = json.load(f)
-        traffic = tj.get(dom["kernel"])
-        inst_per_unit = tj.get("warp_instructions_per_raster", {}).get(dom["kernel"])
+        traffic = tj.get("dram_bytes_per_launch", {}).get(dom["kernel"], {}).get(shape)
+        inst_per_unit = tj.get("warp_instructions_per_raster", {}).get(dom["kernel"], {}).get(shape)
 
     # ---- e2e: host C-ABI entry, pinned host inputs, H2D + D2H in the timed region ----
     def pinned(a):
@@ -865,11 +870,14 @@ def run_ours(args, ws, rank, local):
             sms = torch.cuda.get_device_properties(local).multi_processor_count
             peak_inst = sms * 4 * mhz * 1e6
             ach_inst = inst_per_unit * batch.n_rasters / (dom_ms / 1e3)
-            issue = {"bound": "issue", "kernel": dom["kernel"], "unit": "warp instructions/s",
+            issue = {"bound": "issue", "kernel": dom["kernel"], "shape": shape, "unit": "warp instructions/s",
                      "achieved": ach_inst, "peak": peak_inst, "frac": ach_inst / peak_inst,
                      "warp_instructions_per_raster": inst_per_unit,
                      "note": f"peak = {sms} SMs x 4 schedulers x {mhz:.0f} MHz; instructions per raster from "
                              "the committed ncu capture, time from this run"}
+        else:
+            issue = {"kernel": dom["kernel"], "shape": shape, "achieved": None,
+                     "note": "no committed ncu capture of this kernel at this launch shape"}
     except (RuntimeError, TypeError, ValueError, ZeroDivisionError) as e:
         issue = {"error": str(e)}
     cpu = cpu_baseline(batch) if ws == 1 else None
