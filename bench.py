@@ -782,8 +782,11 @@ def run_ours(args, ws, rank, local):
     if os.path.exists(tfile):
         with open(tfile) as f:
             tj = json.load(f)
-        traffic = tj.get("dram_bytes_per_launch", {}).get(dom["kernel"], {}).get(shape)
-        inst_per_unit = tj.get("warp_instructions_per_raster", {}).get(dom["kernel"], {}).get(shape)
+        def keyed(table):
+            per_kernel = tj.get(table, {}).get(dom["kernel"], {})
+            return per_kernel.get(shape) if isinstance(per_kernel, dict) else None
+        traffic = keyed("dram_bytes_per_launch")
+        inst_per_unit = keyed("warp_instructions_per_raster")
 
     # ---- e2e: host C-ABI entry, pinned host inputs, H2D + D2H in the timed region ----
     def pinned(a):

@@ -32,8 +32,6 @@
 // runs the general chain for the whole batch.  Every wait is bounded.
 #include <algorithm>
 
-#include <cooperative_groups.h>
-
 #include "common.cuh"
 #include "internal.h"
 #include "scan.cuh"
@@ -48,7 +46,6 @@ constexpr int F_LMAX = 256;             // lines per raster
 constexpr int GDIM = 32;                // grid side in tiles (one bitmap word per row)
 constexpr int F_TMAX = 128;             // touched tiles per raster
 constexpr int F_XMAX = 256;             // tile-row crossings per raster
-constexpr int F_IMAX = 512;             // increments stored per raster (more: the coverage re-walks)
 // Resident CTAs per SM the register budget keeps (the shared memory of the
 // 16-tile chunk shapes allows about 14): 64 threads 14, 96 threads 12, 128
 // threads 9.
@@ -68,9 +65,6 @@ struct FusedSmem {
         Early early;
     } u;
     uint16_t line_g0[F_LMAX], line_g1[F_LMAX];   // grid-tile range of each line's cells
-    float2 inc_ah[F_IMAX];         // the count walk's increments (area, height) ...
-    uint16_t inc_id[F_IMAX];       // ... and their cells: grid tile << 6 | row-major cell
-    uint32_t n_inc;
     uint16_t tile_g[F_TMAX];       // tile slot -> grid tile (row-major order)
     uint32_t touched[GDIM];        // one word per grid row
     uint32_t span_mask[F_TMAX / 32];   // tile slot t is followed by a span
@@ -167,7 +161,6 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
             // batch already falls back: skip the work, keep the output chain moving
             S.flag = ld_relaxed(A.fallback) != 0u ? 1u : 0u;
             S.n_cross = 0;
-            S.n_inc = 0;
         }
         __syncthreads();
         const uint32_t r = S.raster;
@@ -360,25 +353,13 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
                     bool out = false;
                     const bool ok = walk_line(
                         v2(L.x, L.y), v2(L.z, L.w),
-                        [&](const Walk& w, const WalkState& s) {
+                        [&](const Walk&, const WalkState& s) {
                             const int gx = div8(s.x) - gx0, gy = div8(s.y) - gy0;
                             if ((unsigned)gx >= (unsigned)gw || (unsigned)gy >= (unsigned)gh) { out = true; return; }
                             const int g = gy * GDIM + gx;
                             gmin = min(gmin, g);
                             gmax = max(gmax, g);
                             atomicOr(&S.touched[gy], 1u << gx);
-                            // the cell's increment, stored once (rasterizer.rs:97-106): a
-                            // slot per lane from one atomic per group of converged lanes
-                            float area, height;
-                            walk_increment(w, s, area, height);
-                            const cooperative_groups::coalesced_group cg = cooperative_groups::coalesced_threads();
-                            uint32_t base = 0;
-                            if (cg.thread_rank() == 0) base = atomicAdd(&S.n_inc, cg.size());
-                            const uint32_t k = cg.shfl(base, 0) + cg.thread_rank();
-                            if (k < (uint32_t)F_IMAX) {
-                                S.inc_ah[k] = make_float2(area, height);
-                                S.inc_id[k] = (uint16_t)(((uint32_t)g << 6) | (uint32_t)(((s.y & 7) << 3) | (s.x & 7)));
-                            }
                         },
                         [&](int tx, int ty, int sign) {
                             const int gx = tx - gx0, gy = ty - gy0;
@@ -471,28 +452,14 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
         if (!bail && n_real > 0) {
             const size_t stage0 = (size_t)blockIdx.x * F_TMAX;
             const int gx0 = S.gx0, gy0 = S.gy0;
-            const uint32_t n_inc = S.n_inc;
-            const bool stored = n_inc <= (uint32_t)F_IMAX;
             for (int lo = 0; lo < n_real; lo += CHUNK) {
                 const int nch = min(CHUNK, n_real - lo);
                 const int g_lo = S.tile_g[lo], g_hi = S.tile_g[lo + nch - 1];
                 for (int q = tid; q < nch * 128; q += FUSED_THREADS) (&S.u.acc[0][0])[q] = 0.0f;
                 __syncthreads();
-                // scatter-add the increments of the chunk's tiles
-                // (rasterizer.rs:223-228): the stored ones, or, for a raster
-                // with more than F_IMAX, by walking the lines touching the
-                // chunk again (rasterizer.rs:97-106)
-                for (uint32_t k = tid; stored && k < n_inc; k += FUSED_THREADS) {
-                    const uint32_t id = S.inc_id[k];
-                    const int g = (int)(id >> 6);
-                    if (g < g_lo || g > g_hi) continue;
-                    const int gy = g >> 5, gx = g & 31;
-                    const int i = S.row_base[gy] + __popc(S.touched[gy] & ((1u << gx) - 1u)) - lo;
-                    const float2 ah = S.inc_ah[k];
-                    atomicAdd(&S.u.acc[i][id & 63u], ah.x);
-                    atomicAdd(&S.u.acc[i][64 + (id & 63u)], ah.y);
-                }
-                for (int l = tid; !stored && l < n_lines; l += FUSED_THREADS) {
+                // walk the lines touching the chunk again, scatter-adding the
+                // increments of its tiles (rasterizer.rs:97-106, 223-228)
+                for (int l = tid; l < n_lines; l += FUSED_THREADS) {
                     if ((int)S.line_g1[l] < g_lo || (int)S.line_g0[l] > g_hi) continue;
                     const float4 L = S.lines[l];
                     walk_line(
