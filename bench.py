@@ -945,7 +945,7 @@ def main():
                     help="profile: run warmup + steps rasterizations of the workload untimed, for ncu; "
                          "profile-diff: the same for render + loss + backward of --workload diff_union|diff_scenes")
     ap.add_argument("--chain-only", action="store_true", help="profile mode: force the general chain")
-    ap.add_argument("--fused-shape", default="", help="profile mode: fused kernel shape, e.g. warp384 or cta96x16")
+    ap.add_argument("--fused-shape", default="", help="profile mode: fused kernel shape (threads x tiles per chunk), e.g. 96x16")
     args = ap.parse_args()
     if args.mode != "bench":
         from ochre_gb300 import build
