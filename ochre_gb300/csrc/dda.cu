@@ -284,11 +284,10 @@ __global__ void __launch_bounds__(256) k_line_emit(const float4* __restrict__ li
     const uint64_t base = key_base[r];
     uint32_t e = ent_off[i];
     uint32_t q = inc_off[i];   // next stored increment
-    // increments leave in whole 32-byte sectors (4 increments from an index
-    // that is a multiple of 4): the first three of a group wait in registers;
-    // before the line's first such boundary they go out one by one
-    float2 b0 = make_float2(0.0f, 0.0f), b1 = b0, b2 = b0;
-    bool grouped = (q & 3u) == 0u;
+    // increments leave in 16-byte pairs (an even index and the next one):
+    // the first of a pair waits in registers
+    float2 pend = make_float2(0.0f, 0.0f);
+    bool has_pend = false;
     // open bin
     int btx = 0x7fffffff, bty = 0x7fffffff, prev_x = 0;
     uint32_t bcount = 0, bentry = 0;
@@ -323,20 +322,14 @@ __global__ void __launch_bounds__(256) k_line_emit(const float4* __restrict__ li
                 rec.steps = (uint16_t)(rec.steps | (1u << (bcount - 1)));   // the step into this cell moved in x
             }
             const float2 v = make_float2(area, height);
-            if (!grouped) {
-                incs[q] = v;
-                grouped = ((q + 1u) & 3u) == 0u;
+            if ((q & 1u) == 0u) {
+                pend = v;
+                has_pend = true;
+            } else if (has_pend) {
+                reinterpret_cast<float4*>(incs)[q >> 1] = make_float4(pend.x, pend.y, v.x, v.y);
+                has_pend = false;
             } else {
-                switch (q & 3u) {
-                case 0: b0 = v; break;
-                case 1: b1 = v; break;
-                case 2: b2 = v; break;
-                default: {
-                    float4* d = reinterpret_cast<float4*>(incs + (q - 3u));
-                    d[0] = make_float4(b0.x, b0.y, b1.x, b1.y);
-                    d[1] = make_float4(b2.x, b2.y, v.x, v.y);
-                }
-                }
+                incs[q] = v;   // the line's first increment at an odd index
             }
             q++;
             prev_x = s.x;
@@ -349,13 +342,7 @@ __global__ void __launch_bounds__(256) k_line_emit(const float4* __restrict__ li
         },
         [&](int, int) {});
     flush();
-    // the last, partial group
-    if (grouped) {
-        const uint32_t g0 = q & ~3u, left = q & 3u;
-        if (left > 0u) incs[g0] = b0;
-        if (left > 1u) incs[g0 + 1u] = b1;
-        if (left > 2u) incs[g0 + 2u] = b2;
-    }
+    if (has_pend) incs[q - 1] = pend;
 }
 
 template <class K>
