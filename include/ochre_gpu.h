@@ -116,7 +116,7 @@ typedef struct ochre_stats {
     uint32_t pad;
     uint64_t n_bins;       /* sort entries that are tile bins (runs of cells in one tile) */
     uint32_t fused;        /* 1: the fused small-raster kernel handled the batch, 0: the general chain */
-    uint32_t pad2;
+    uint32_t n_incs;       /* general chain: pixel-cell increments the lines stored (at most 2^32 - 1) */
 } ochre_stats;
 
 /* Device time of one kernel launch of the last run (OCHRE_CTX_PROFILE). */

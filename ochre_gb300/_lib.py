@@ -62,7 +62,7 @@ class Stats(ctypes.Structure):
         ("n_lines", ctypes.c_uint64), ("n_entries", ctypes.c_uint64), ("n_tiles", ctypes.c_uint64),
         ("n_spans", ctypes.c_uint64), ("key_bits", ctypes.c_uint32), ("sort_passes", ctypes.c_uint32),
         ("n_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("n_bins", ctypes.c_uint64),
-        ("fused", ctypes.c_uint32), ("pad2", ctypes.c_uint32),
+        ("fused", ctypes.c_uint32), ("n_incs", ctypes.c_uint32),
     ]
 
 

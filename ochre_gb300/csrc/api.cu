@@ -112,7 +112,7 @@ __global__ void k_plan_entries(DevScalars* ds, uint32_t cap, uint32_t key_bits, 
     const uint64_t e = (uint64_t)ds->line_ent_total + ds->n_empty;
     const uint64_t k = ds->keyspace;
     const bool keys_fit = key_bits >= 64 || k == 0 || ((k - 1) >> key_bits) == 0;
-    if (e > cap || !keys_fit || ds->n_incs > inc_cap) {
+    if (e > cap || !keys_fit || ds->inc_total > inc_cap) {
         ds->n_entries = 0u;
         ds->n_lines = 0u;   // no line emits an entry
         atomicOr(&ds->err, ERR_CAPACITY);

@@ -126,12 +126,13 @@ __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ l
                                                     const uint32_t* __restrict__ line_raster, uint32_t n_cap,
                                                     const uint32_t* n_dev, int4* bbox, int* raster_wsum,
                                                     uint32_t* __restrict__ counts, uint32_t* __restrict__ inc_counts,
-                                                    uint32_t* err) {
+                                                    unsigned long long* inc_total, uint32_t* err) {
     __shared__ int4 s_box[BOX_SLOTS];
     __shared__ int s_ws[BOX_SLOTS];
     __shared__ uint32_t s_r0;
     __shared__ uint32_t s_cnt[17];
     __shared__ uint16_t s_item[256];
+    __shared__ uint32_t s_incs;
     const uint32_t n_lines = (uint32_t)dev_count(n_cap, n_dev);
     const uint32_t i0 = blockIdx.x * blockDim.x;
     if (i0 >= n_lines) return;
@@ -141,16 +142,19 @@ __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ l
         s_box[threadIdx.x] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
         s_ws[threadIdx.x] = 0;
     }
-    if (threadIdx.x == 0) s_r0 = line_raster[i0];
+    if (threadIdx.x == 0) {
+        s_r0 = line_raster[i0];
+        s_incs = 0u;
+    }
     __syncthreads();
     const uint32_t r0 = s_r0;
     BBoxAcc bb{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
     uint32_t r = r0;
     int ws = 0;
+    uint32_t nc = 0;
     if (i < n_lines) {
         const float4 l = lines[i];
         bool capped = false;
-        uint32_t nc = 0;
         counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped, &ws, &nc);
         inc_counts[i] = nc;
         if (capped) atomicOr(err, ERR_LIMIT);
@@ -175,7 +179,11 @@ __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ l
             if (wsg) atomicAdd(raster_wsum + r, wsg);
         }
     }
+    // the block's increments (at most 256 lines of a capped walk: 32 bits hold it)
+    const uint32_t wi = __reduce_add_sync(0xffffffffu, nc);
+    if ((threadIdx.x & 31) == 0 && wi) atomicAdd(&s_incs, wi);
     __syncthreads();
+    if (threadIdx.x == 0 && s_incs) atomicAdd(inc_total, (unsigned long long)s_incs);
     if (threadIdx.x < BOX_SLOTS) {
         const int4 b = s_box[threadIdx.x];
         if (b.x <= b.z) box_grow(bbox + r0 + threadIdx.x, b.x, b.y, b.z, b.w);
@@ -388,7 +396,9 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_LAUNCH(ctx, "bbox_init", s, k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(),
                                                                                  ctx->raster_wsum.as<int>(), R));
     OCHRE_CUDA_TRY(cudaGetLastError());
-    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->line_ent_total, 0, 2 * sizeof(uint32_t), s));
+    // the line pair's totals and the 64-bit increment count
+    static_assert(offsetof(DevScalars, inc_total) == offsetof(DevScalars, line_ent_total) + 8, "layout");
+    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->line_ent_total, 0, 16, s));
     // graph replays: n_lines is the capacity, the count is on the device
     const GraphPlan* plan = ctx->plan;
     const uint32_t* lines_dev = plan ? &ds->n_lines : nullptr;
@@ -398,7 +408,8 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
         OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<LinePair>)));
         OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<(n_lines + 255) / 256, 256, 0, s>>>(
             ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
-            ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>(), &ds->err));
+            ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>(),
+            reinterpret_cast<unsigned long long*>(&ds->inc_total), &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());
         // in place: every count is read by the thread that writes its offset
         OCHRE_LAUNCH(ctx, "dda_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<LinePair>(
@@ -433,8 +444,9 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
         if (st != OCHRE_OK) return st;
         const DevScalars* hs = host_scalars(ctx);
         E = (uint64_t)hs->line_ent_total + hs->n_empty;
-        n_incs = hs->n_incs;
-        if (E > MAX_COUNT || n_incs > MAX_COUNT) return OCHRE_E_CAPACITY;
+        n_incs = hs->inc_total;
+        if (E > MAX_COUNT || n_incs > MAX_INCS) return OCHRE_E_CAPACITY;
+        ctx->stats.n_incs = (uint32_t)n_incs;
         const uint64_t K = hs->keyspace;
         bits = 1;
         while (bits < 64 && (K - 1) >> bits) bits++;

@@ -46,9 +46,9 @@ namespace ochre {
 
 namespace {
 
-uint32_t cap_of(uint64_t n, float headroom) {
+uint32_t cap_of(uint64_t n, float headroom, uint64_t limit = MAX_COUNT) {
     const uint64_t c = (uint64_t)((double)n * headroom) + 1024u;
-    return (uint32_t)std::min<uint64_t>(c, MAX_COUNT);
+    return (uint32_t)std::min<uint64_t>(c, limit);
 }
 
 // The planned chain: the stages of run_device with ctx->plan set (no host
@@ -116,7 +116,7 @@ int build(ochre_graph* g) {
     if (!p.fused) {
         p.lines = cap_of(es.n_lines, g->headroom);
         p.entries = cap_of(es.n_entries, g->headroom);
-        p.incs = cap_of(host_scalars(ctx)->n_incs, g->headroom);
+        p.incs = cap_of(host_scalars(ctx)->inc_total, g->headroom, MAX_INCS);
         // key bits: the key space (areas of tile boxes) with headroom^2, up
         // to the next digit boundary (no extra sort pass for it), and never
         // into 64-bit keys when 32 hold the planning run

@@ -72,6 +72,8 @@ struct DevScalars {
     uint32_t pad3;
     uint32_t line_ent_total;  // chain: sort entries the lines produce   } (line scan
     uint32_t n_incs;          // chain: pixel-cell increments of the lines } pair total)
+    uint64_t inc_total;       // the same increment count summed in 64 bits (the pair
+                              // total wraps above 2^32; this one says when it did)
 };
 // The waits find spin_log2 from the error word's address (common.cuh).
 static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
@@ -96,6 +98,7 @@ struct GraphPlan {
 constexpr uint32_t CROSS_TAG = 0x80000000u;
 constexpr uint32_t MAX_RASTERS = 1u << 23;
 constexpr uint64_t MAX_COUNT = (1ull << 30) - 1;   // lines, entries, tiles
+constexpr uint64_t MAX_INCS = 0xffffffffull;        // stored increments (32-bit offsets)
 
 // A bin: a run of consecutive pixel cells of one line's walk that share one
 // tile (16 bytes).  Its cells' increments (area, height) were stored by the

@@ -323,3 +323,56 @@ def test_configuration_counts_match_oracle(gpu_ctx, request, name, tiles, spans)
     gpu_ctx.rasterize_device(DeviceBatch(b))
     st = gpu_ctx.stats()
     assert (st["n_tiles"], st["n_spans"]) == (tiles, spans)
+
+
+class _Dev:
+    """A device array of a result, seen by torch (no copy)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def test_stored_increments_above_2_30(gpu_ctx_chain):
+    # 36,000 copies of one thin diagonal band (two lines of about 16,000
+    # pixel cells each): 1.15e9 stored increments, more than the 2^30 the
+    # chain's other counts allow.  Every copy must equal the oracle's
+    # rasterization of the band, tile for tile.
+    import torch
+    from ochre_gb300 import DeviceBatch
+    from ochre_gb300.batch import Batch, CLOSE, LINE, MOVE
+    R = 36_000
+    verbs = np.array([MOVE, LINE, LINE, LINE, CLOSE], np.uint8)
+    pts = np.array([0.3, 0.7, 7999.6, 7990.2, 7999.6, 7993.1, 0.3, 3.6], np.float32)
+    xf = np.array([1, 0, 0, 1, 0, 0], np.float32)
+    one = Batch(verbs, pts, np.array([0, 5], np.uint32), xf[None], None, None, 1)
+    big = Batch(np.tile(verbs, R), np.tile(pts, R), (np.arange(R + 1) * 5).astype(np.uint32),
+                np.tile(xf, (R, 1)), None, None, R)
+    exp = oracle.run(one)
+    T1, N1 = len(exp["tile_xy"]), len(exp["span_xy"])
+    db = DeviceBatch(big)
+    r = gpu_ctx_chain.rasterize_device(db)
+    st = gpu_ctx_chain.stats()
+    assert st["n_incs"] > (1 << 30), st
+    assert (r.n_tiles, r.n_spans) == (R * T1, R * N1)
+    rto = torch.as_tensor(_Dev(r.raster_tile_off, (R + 1,), "<u4"), device="cuda").long()
+    rso = torch.as_tensor(_Dev(r.raster_span_off, (R + 1,), "<u4"), device="cuda").long()
+    steps = torch.arange(R + 1, device="cuda", dtype=torch.int64)
+    assert torch.equal(rto, steps * T1) and torch.equal(rso, steps * N1)
+    xy = torch.as_tensor(_Dev(r.tile_xy, (R, T1, 2), "<i2"), device="cuda")
+    al = torch.as_tensor(_Dev(r.tile_alpha, (R, T1, 64), "|u1"), device="cuda")
+    for a in range(0, R, 4096):   # every copy against the first, a slab at a time
+        assert torch.equal(xy[a:a + 4096], xy[:1].expand(min(4096, R - a), -1, -1)), a
+        assert torch.equal(al[a:a + 4096], al[:1].expand(min(4096, R - a), -1, -1)), a
+    if N1:
+        sxy = torch.as_tensor(_Dev(r.span_xy, (R, N1, 2), "<i2"), device="cuda")
+        assert torch.equal(sxy, sxy[:1].expand(R, -1, -1))
+    first = {"tile_xy": xy[0].cpu().numpy(), "tile_alpha": al[0].cpu().numpy(),
+             "span_xy": np.zeros((N1, 2), np.int16) if not N1 else
+             torch.as_tensor(_Dev(r.span_xy, (N1, 2), "<i2"), device="cuda").cpu().numpy(),
+             "span_w": np.zeros(0, np.uint16) if not N1 else
+             torch.as_tensor(_Dev(r.span_width, (N1,), "<u2"), device="cuda").cpu().numpy(),
+             "span_tile": np.zeros(0, np.uint32) if not N1 else
+             torch.as_tensor(_Dev(r.span_tile, (N1,), "<u4"), device="cuda").cpu().numpy(),
+             "raster_tile_off": np.array([0, T1], np.uint64), "raster_span_off": np.array([0, N1], np.uint64)}
+    compare(first, exp, 1)
