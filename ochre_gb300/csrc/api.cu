@@ -371,6 +371,12 @@ void ochre_gpu_destroy(ochre_gpu_ctx* ctx) {
         cudaStreamSynchronize(ctx->copy_stream);
         cudaStreamDestroy(ctx->copy_stream);
     }
+    if (ctx->walk_stream) {
+        cudaStreamSynchronize(ctx->walk_stream);
+        cudaStreamDestroy(ctx->walk_stream);
+    }
+    if (ctx->ev_walk_fork) cudaEventDestroy(ctx->ev_walk_fork);
+    if (ctx->ev_walk_join) cudaEventDestroy(ctx->ev_walk_join);
     if (ctx->ev_prior) cudaEventDestroy(ctx->ev_prior);
     if (ctx->ev_pts) cudaEventDestroy(ctx->ev_pts);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -384,7 +390,7 @@ namespace ochre {
 std::vector<DevBuf*> device_buffers(ochre_gpu_ctx* ctx) {
     return {&ctx->in_verbs, &ctx->in_pts, &ctx->in_fill_off, &ctx->in_fill_xf, &ctx->in_fill_flags,
                      &ctx->in_raster_off, &ctx->cmd_foff, &ctx->cmd_mv, &ctx->cmd_ep, &ctx->cmd_line_off,
-                     &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->line_inc_off, &ctx->incs, &ctx->raster_bbox, &ctx->raster_keybase,
+                     &ctx->lines, &ctx->line_raster, &ctx->line_ent_off, &ctx->line_inc_off, &ctx->long_lines, &ctx->incs, &ctx->raster_bbox, &ctx->raster_keybase,
                      &ctx->raster_empty, &ctx->raster_wsum, &ctx->raster_wbase, &ctx->tile_head_bins,
                      &ctx->tile_head_wind, &ctx->keys, &ctx->vals, &ctx->keys_alt, &ctx->vals_alt, &ctx->bins,
                      &ctx->sort_hist, &ctx->sort_lookback, &ctx->tile_head, &ctx->tile_info, &ctx->tile_row_start, &ctx->tile_state,
@@ -631,6 +637,12 @@ int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     } else if (!std::strcmp(name, "chain_coverage_form")) {
         if (value < 0 || value > 2) return OCHRE_E_INVALID;
         ctx->tune_chain_coverage_form = value;
+    } else if (!std::strcmp(name, "chain_long_cells")) {
+        if (value != 0 && (value < 16 || value > 65535)) return OCHRE_E_INVALID;
+        ctx->tune_chain_long_cells = value;
+    } else if (!std::strcmp(name, "chain_walk_refill")) {
+        if (value < 1 || value > 32) return OCHRE_E_INVALID;
+        ctx->tune_chain_walk_refill = value;
     } else if (!std::strcmp(name, "test_spin_log2")) {
         if (value < 0 || value > 40) return OCHRE_E_INVALID;
         ctx->test_spin_log2 = (uint32_t)value;
@@ -649,6 +661,8 @@ int ochre_gpu_get_tunable(const ochre_gpu_ctx* ctx, const char* name, int* value
     else if (!std::strcmp(name, "fused_chunk")) *value = ctx->tune_fused_chunk;
     else if (!std::strcmp(name, "chain_tiles_per_warp")) *value = ctx->tune_chain_tiles_per_warp;
     else if (!std::strcmp(name, "chain_coverage_form")) *value = ctx->tune_chain_coverage_form;
+    else if (!std::strcmp(name, "chain_long_cells")) *value = ctx->tune_chain_long_cells;
+    else if (!std::strcmp(name, "chain_walk_refill")) *value = ctx->tune_chain_walk_refill;
     else return OCHRE_E_INVALID;
     return OCHRE_OK;
 }

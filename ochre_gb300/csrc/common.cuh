@@ -302,6 +302,14 @@ __device__ __forceinline__ bool walk_line(V2 a, V2 p, OnCell on_cell, OnCross on
     }
 }
 
+// Pixel cells a line's walk visits, about: its start cell and one per row
+// or column step (the reference's walk may add a cell at a corner tie).
+__device__ __forceinline__ uint32_t walk_cells(const float4& l) {
+    const float dx = fabsf(floorf(l.z) - floorf(l.x)), dy = fabsf(floorf(l.w) - floorf(l.y));
+    const float c = 1.0f + dx + dy;
+    return c < 65535.0f ? (uint32_t)c : 65535u;   // also NaN -> 65535 (bucketed last)
+}
+
 // ---------------------------------------------------------------------
 // Memory-order helpers for single-pass look-back chains.
 // ---------------------------------------------------------------------

@@ -70,14 +70,6 @@ __device__ __forceinline__ uint32_t count_line(V2 a, V2 p, BBoxAcc& bb, bool* ca
     return nb + nc;
 }
 
-// Pixel cells a line's walk visits, about: its start cell and one per row
-// or column step (the reference's walk may add a cell at a corner tie).
-__device__ __forceinline__ uint32_t walk_cells(const float4& l) {
-    const float dx = fabsf(floorf(l.z) - floorf(l.x)), dy = fabsf(floorf(l.w) - floorf(l.y));
-    const float c = 1.0f + dx + dy;
-    return c < 65535.0f ? (uint32_t)c : 65535u;   // also NaN -> 65535 (bucketed last)
-}
-
 // Block-local work order by walk length: the BLOCK items of a block are
 // grouped by log2 of their cell count (unstable within a group), so each
 // warp walks lines of about the same length and a warp of short lines does
@@ -106,15 +98,7 @@ __device__ __forceinline__ uint32_t order_by_length(uint32_t cells, uint32_t* s_
     return s_item[threadIdx.x];
 }
 
-// Entry counts per line (written in place of the offsets, then scanned)
-// and the raster tile boxes.  Counting is a separate kernel, not folded into
-// the offset scan: a walk's length varies from one cell to thousands, and a
-// single-pass scan would hold every later block behind the slowest walk.
-// Boxes (and the rasters' crossing-sign sums) are reduced before any global
-// atomic: lanes of one raster (lines of a raster are contiguous) by warp
-// reductions, then the block's first BOX_SLOTS rasters in shared memory; the
-// block then updates each global box only where it grows.
-constexpr int BOX_SLOTS = 8;
+// A raster's global tile box grows by atomics only where it grows.
 __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1) {
     const int4 cur = ld_words(d);
     if (x0 < cur.x) atomicMin(&d->x, x0);
@@ -122,11 +106,244 @@ __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1
     if (x1 > cur.z) atomicMax(&d->z, x1);
     if (y1 > cur.w) atomicMax(&d->w, y1);
 }
+
+// ---------------------------------------------------------------------
+// Long lines: persistent walkers with per-lane refill.
+//
+// Walk lengths run from one cell to thousands (a path's long edges).  One
+// thread per line, as the count and emit kernels walk most lines, would give
+// a long line's warp one busy lane for thousands of steps.  The flatten
+// stage queues every line of more than `long_cells` (estimated) cells, and
+// the first blocks of the count and emit kernels walk that queue this way:
+// every lane of a warp makes one DDA step per loop iteration; a lane whose
+// line has ended takes the next line from the warp's pool of WALK_POOL
+// queued lines, and the warp takes a new pool from a global ticket when its
+// pool runs out.  A refill waits until at least `refill` lanes are idle (a
+// refill costs the new lines' set-up loads).  Outputs go to the per-line
+// offsets of the count scan, so they do not depend on which lane walks which
+// line.  (For short lines the per-line set-up, run by the few lanes that
+// refill at a time, costs more than the idle lanes it saves: measured
+// slower on every configuration, so short lines stay one per thread.)
+//
+// Job interface (per lane): bool begin(queue index, Walk&, WalkState&) sets
+// the walk up (false: the line has no walk); cell(w, s) for every increment
+// cell; visit(x, y) for every visited cell; cross(tx, ty, sign) for every
+// tile-row crossing; end(capped) when the line's walk is over.  The step
+// sequence is walk_line's (common.cuh), including its WALK_CAP.
+// ---------------------------------------------------------------------
+constexpr uint32_t WALK_POOL = 32;
+
+template <class Job>
+__device__ __forceinline__ void walk_refill(uint64_t n_lines, const uint32_t* __restrict__ queue, uint32_t* ticket,
+                                            uint32_t refill, Job& job) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t below = (1u << lane) - 1u;
+    uint64_t pool = 0, pool_end = 0;   // warp-uniform
+    bool more = true;                  // warp-uniform
+    bool live = false;
+    Walk w;
+    WalkState s;
+    int ty_prev = 0;
+    uint32_t it = 0;
+    for (;;) {
+        uint32_t idle = __ballot_sync(0xffffffffu, !live);
+        if (more && (uint32_t)__popc(idle) >= refill) {
+            while (idle != 0u) {
+                if (pool == pool_end) {
+                    uint32_t b = 0;
+                    if (lane == 0) b = atomicAdd(ticket, 1u);
+                    const uint64_t first = (uint64_t)__shfl_sync(0xffffffffu, b, 0) * WALK_POOL;
+                    if (first >= n_lines) {
+                        more = false;
+                        break;
+                    }
+                    pool = first;
+                    pool_end = min(first + WALK_POOL, n_lines);
+                }
+                const uint32_t avail = (uint32_t)(pool_end - pool);
+                const uint32_t rank = (uint32_t)__popc(idle & below);
+                if (((idle >> lane) & 1u) && rank < avail) {
+                    live = job.begin(queue[pool + rank], w, s);
+                    if (live) {
+                        ty_prev = div8(s.y);
+                        it = 0;
+                        job.visit(s.x, s.y);
+                    }
+                }
+                pool += min((uint32_t)__popc(idle), avail);
+                idle = __ballot_sync(0xffffffffu, !live);
+            }
+        }
+        if (__ballot_sync(0xffffffffu, live) == 0u) {
+            if (!more) break;
+            continue;
+        }
+        if (live) {
+            job.cell(w, s);
+            bool done = walk_step(w, s);
+            job.visit(s.x, s.y);
+            const int ty = div8(s.y);
+            if (ty != ty_prev) {
+                job.cross(div8(s.x), min(ty_prev, ty), (int)(int8_t)(int16_t)(ty - ty_prev));
+                ty_prev = ty;
+            }
+            bool capped = false;
+            if (!done && ++it >= WALK_CAP) {
+                capped = true;
+                done = true;
+            }
+            if (done) {
+                job.end(capped);
+                live = false;
+            }
+        }
+    }
+}
+
+// The same steps for one line whose walk job.begin has set up (walk_line's
+// loop with the job's callbacks).
+template <class Job>
+__device__ __forceinline__ void walk_one(Walk& w, WalkState& s, Job& job) {
+    int ty_prev = div8(s.y);
+    job.visit(s.x, s.y);
+    bool capped = false;
+    for (uint32_t it = 0;; ++it) {
+        job.cell(w, s);
+        const bool done = walk_step(w, s);
+        job.visit(s.x, s.y);
+        const int ty = div8(s.y);
+        if (ty != ty_prev) {
+            job.cross(div8(s.x), min(ty_prev, ty), (int)(int8_t)(int16_t)(ty - ty_prev));
+            ty_prev = ty;
+        }
+        if (done) break;
+        if (it + 1 >= WALK_CAP) {
+            capped = true;
+            break;
+        }
+    }
+    job.end(capped);
+}
+
+// Counts of the count pass (see k_line_count) for a queued line, per lane.
+// The raster boxes and crossing-sign sums gather over the lane's lines of one
+// raster and go to memory when the lane moves to another raster.
+struct CountJob {
+    const float4* lines;
+    const uint32_t* line_raster;
+    uint32_t* counts;
+    uint32_t* inc_counts;
+    int4* bbox;
+    int* raster_wsum;
+    uint32_t* err;
+    // the line
+    uint32_t line, nb, nc, nx, run;
+    int ptx, pty, ws;
+    // the lane's current raster
+    uint32_t r;
+    BBoxAcc bb;
+    int wsr;
+    uint64_t incs;   // increments of the lane's lines
+
+    __device__ __forceinline__ void flush() {
+        if (r == 0xffffffffu) return;
+        if (bb.x0 <= bb.x1) box_grow(bbox + r, bb.x0, bb.y0, bb.x1, bb.y1);
+        if (wsr) atomicAdd(raster_wsum + r, wsr);
+    }
+    __device__ __forceinline__ bool begin(uint32_t i, Walk& w, WalkState& s) {
+        const float4 l = lines[i];
+        const uint32_t ri = line_raster[i];
+        if (ri != r) {
+            flush();
+            r = ri;
+            bb = BBoxAcc{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
+            wsr = 0;
+        }
+        const V2 a = v2(l.x, l.y), p = v2(l.z, l.w);
+        if (veq(a, p)) {
+            counts[i] = 0u;
+            inc_counts[i] = 0u;
+            return false;
+        }
+        walk_setup(a, p, w, s);
+        line = i;
+        nb = nc = nx = run = 0u;
+        ptx = pty = 0x7fffffff;
+        ws = 0;
+        return true;
+    }
+    __device__ __forceinline__ void cell(const Walk&, const WalkState& s) {
+        const int tx = div8(s.x), ty = div8(s.y);
+        if (tx != ptx || ty != pty || run == BIN_MAX_CELLS) {
+            nb++;
+            ptx = tx;
+            pty = ty;
+            run = 0;
+        }
+        run++;
+        nx++;
+    }
+    __device__ __forceinline__ void visit(int x, int y) { bbox_add(bb, x, y); }
+    __device__ __forceinline__ void cross(int, int, int sign) {
+        nc++;
+        ws += sign;
+    }
+    __device__ __forceinline__ void end(bool capped) {
+        counts[line] = nb + nc;
+        inc_counts[line] = nx;
+        incs += nx;
+        wsr += ws;
+        if (capped) atomicOr(err, ERR_LIMIT);
+    }
+};
+
+// The queued long lines' counts (see k_line_count): persistent blocks of
+// refilled lanes (walk_refill).
+constexpr int LONG_THREADS = 128;
+constexpr uint32_t LONG_BLOCKS_PER_SM = 2;
+__global__ void __launch_bounds__(LONG_THREADS) k_line_count_long(
+    const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster, uint32_t n_cap, const uint32_t* n_dev,
+    int4* bbox, int* raster_wsum, uint32_t* __restrict__ counts, uint32_t* __restrict__ inc_counts,
+    unsigned long long* inc_total, const uint32_t* __restrict__ queue, const uint32_t* n_queue, uint32_t* ticket,
+    uint32_t refill, uint32_t* err) {
+    // (a line count zeroed on the device, after an overflow of a graph's
+    // plan, stops these walks too)
+    if (dev_count(n_cap, n_dev) == 0) return;
+    CountJob job;
+    job.lines = lines;
+    job.line_raster = line_raster;
+    job.counts = counts;
+    job.inc_counts = inc_counts;
+    job.bbox = bbox;
+    job.raster_wsum = raster_wsum;
+    job.err = err;
+    job.r = 0xffffffffu;
+    job.bb = BBoxAcc{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
+    job.wsr = 0;
+    job.incs = 0;
+    walk_refill(*n_queue, queue, ticket, refill, job);
+    job.flush();
+    unsigned long long t = job.incs;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31u) == 0u && t) atomicAdd(inc_total, t);
+}
+
+// Entry counts per line (written in place of the offsets, then scanned)
+// and the raster tile boxes.  Counting is a separate kernel, not folded into
+// the offset scan: a walk's length varies from one cell to thousands, and a
+// single-pass scan would hold every later block behind the slowest walk.
+// Lines of more than long_cells cells are left to k_line_count_long.  Boxes
+// (and the rasters' crossing-sign sums) are reduced before any global
+// atomic: lanes of one raster (lines of a raster are contiguous) by warp
+// reductions, then the block's first BOX_SLOTS rasters in shared memory; the
+// block then updates each global box only where it grows.
+constexpr int BOX_SLOTS = 8;
 __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ lines,
                                                     const uint32_t* __restrict__ line_raster, uint32_t n_cap,
                                                     const uint32_t* n_dev, int4* bbox, int* raster_wsum,
                                                     uint32_t* __restrict__ counts, uint32_t* __restrict__ inc_counts,
-                                                    unsigned long long* inc_total, uint32_t* err) {
+                                                    unsigned long long* inc_total, uint32_t long_cells, uint32_t* err) {
     __shared__ int4 s_box[BOX_SLOTS];
     __shared__ int s_ws[BOX_SLOTS];
     __shared__ uint32_t s_r0;
@@ -152,8 +369,8 @@ __global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ l
     uint32_t r = r0;
     int ws = 0;
     uint32_t nc = 0;
-    if (i < n_lines) {
-        const float4 l = lines[i];
+    const float4 l = i < n_lines ? lines[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (i < n_lines && !(long_cells && walk_cells(l) > long_cells)) {
         bool capped = false;
         counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped, &ws, &nc);
         inc_counts[i] = nc;
@@ -268,14 +485,139 @@ __device__ __forceinline__ K make_key(uint64_t base, const int4& bb, int tx, int
     return (K)(base + (((uint64_t)(ty - bb.y) * w + (uint64_t)(tx - bb.x)) << 1) + kind);
 }
 
-// Lines of a block are walked in order of length (order_by_length), so a
-// warp's lanes walk lines of about the same length.
+// Entries and increments of the emit pass (see k_line_emit) for one line.
+template <class K>
+struct EmitJob {
+    const float4* lines;
+    const uint32_t* line_raster;
+    const uint32_t* ent_off;
+    const uint32_t* inc_off;
+    const int4* bbox;
+    const uint64_t* key_base;
+    K* keys;
+    uint32_t* vals;
+    BinRec* bins;
+    float2* incs;
+    // the line's raster (kept while the lane stays in it)
+    uint32_t r;
+    int4 bb;
+    uint64_t base;
+    // the line
+    uint32_t e, q;   // next entry, next stored increment
+    float2 pend;     // increments leave in 16-byte pairs; the first of a pair waits here
+    bool has_pend;
+    int btx, bty, prev_x;   // open bin
+    uint32_t bcount, bentry;
+    BinRec rec;
+
+    __device__ __forceinline__ void flush_bin() {
+        if (bcount) {
+            rec.n = (uint8_t)bcount;
+            *reinterpret_cast<uint4*>(bins + bentry) = *reinterpret_cast<const uint4*>(&rec);
+            keys[bentry] = make_key<K>(base, bb, btx, bty, 1u);
+            vals[bentry] = bentry;
+        }
+    }
+    __device__ __forceinline__ bool begin(uint32_t i, Walk& w, WalkState& s) {
+        const float4 l = lines[i];
+        const V2 a = v2(l.x, l.y), p = v2(l.z, l.w);
+        if (veq(a, p)) return false;
+        const uint32_t ri = line_raster[i];
+        if (ri != r) {
+            r = ri;
+            bb = bbox[ri];
+            base = key_base[ri];
+        }
+        e = ent_off[i];
+        q = inc_off[i];
+        has_pend = false;
+        btx = bty = 0x7fffffff;
+        prev_x = 0;
+        bcount = 0;
+        walk_setup(a, p, w, s);
+        return true;
+    }
+    __device__ __forceinline__ void cell(const Walk& w, const WalkState& s) {
+        float area, height;
+        walk_increment(w, s, area, height);
+        const int tx = div8(s.x), ty = div8(s.y);
+        if (tx != btx || ty != bty || bcount == BIN_MAX_CELLS) {
+            flush_bin();
+            btx = tx;
+            bty = ty;
+            bcount = 0;
+            bentry = e++;
+            rec.inc = q;
+            rec.raster = r;
+            rec.x = (int16_t)s.x;
+            rec.y = (int16_t)s.y;
+            rec.steps = 0;
+            rec.dirs = (uint8_t)((w.x_dir < 0 ? 1u : 0u) | (w.y_dir < 0 ? 2u : 0u));
+        } else if (s.x != prev_x) {
+            rec.steps = (uint16_t)(rec.steps | (1u << (bcount - 1)));   // the step into this cell moved in x
+        }
+        const float2 v = make_float2(area, height);
+        if ((q & 1u) == 0u) {
+            pend = v;
+            has_pend = true;
+        } else if (has_pend) {
+            reinterpret_cast<float4*>(incs)[q >> 1] = make_float4(pend.x, pend.y, v.x, v.y);
+            has_pend = false;
+        } else {
+            incs[q] = v;   // the line's first increment at an odd index
+        }
+        q++;
+        prev_x = s.x;
+        bcount++;
+    }
+    __device__ __forceinline__ void visit(int, int) {}
+    __device__ __forceinline__ void cross(int tx, int ty, int sign) {
+        const uint32_t c = e++;
+        keys[c] = make_key<K>(base, bb, tx, ty, 0u);
+        vals[c] = CROSS_TAG | (r << 8) | ((uint32_t)sign & 0xffu);
+    }
+    __device__ __forceinline__ void end(bool) {
+        flush_bin();
+        if (has_pend) incs[q - 1] = pend;
+    }
+};
+
+// The queued long lines' entries and increments (see k_line_emit):
+// persistent blocks of refilled lanes (walk_refill).
+template <class K>
+__global__ void __launch_bounds__(LONG_THREADS) k_line_emit_long(
+    const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster, const uint32_t* __restrict__ ent_off,
+    const uint32_t* __restrict__ inc_off, uint64_t n_cap, const uint32_t* n_dev, const int4* __restrict__ bbox,
+    const uint64_t* __restrict__ key_base, K* __restrict__ keys, uint32_t* __restrict__ vals,
+    BinRec* __restrict__ bins, float2* __restrict__ incs, const uint32_t* __restrict__ queue, const uint32_t* n_queue,
+    uint32_t* ticket, uint32_t refill) {
+    // (a line count zeroed on the device, after an overflow of a graph's
+    // plan, stops these walks too: their offsets were not written)
+    if (dev_count(n_cap, n_dev) == 0) return;
+    EmitJob<K> job;
+    job.lines = lines;
+    job.line_raster = line_raster;
+    job.ent_off = ent_off;
+    job.inc_off = inc_off;
+    job.bbox = bbox;
+    job.key_base = key_base;
+    job.keys = keys;
+    job.vals = vals;
+    job.bins = bins;
+    job.incs = incs;
+    job.r = 0xffffffffu;
+    walk_refill(*n_queue, queue, ticket, refill, job);
+}
+
+// Every thread walks one line, the lines of a block in order of length
+// (order_by_length) so a warp's lanes walk lines of about the same length.
+// Lines of more than long_cells cells are left to k_line_emit_long.
 template <class K>
 __global__ void __launch_bounds__(256) k_line_emit(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster,
                             const uint32_t* __restrict__ ent_off, const uint32_t* __restrict__ inc_off, uint64_t n_cap,
                             const uint32_t* n_dev, const int4* __restrict__ bbox, const uint64_t* __restrict__ key_base,
                             K* __restrict__ keys, uint32_t* __restrict__ vals, BinRec* __restrict__ bins,
-                            float2* __restrict__ incs) {
+                            float2* __restrict__ incs, uint32_t long_cells) {
     __shared__ uint32_t s_cnt[17];
     __shared__ uint16_t s_item[256];
     const uint64_t n_lines = dev_count(n_cap, n_dev);
@@ -284,73 +626,22 @@ __global__ void __launch_bounds__(256) k_line_emit(const float4* __restrict__ li
     const uint32_t cells = i0 + threadIdx.x < n_lines ? walk_cells(lines[i0 + threadIdx.x]) : 0u;
     const uint64_t i = i0 + order_by_length<256>(cells, s_cnt, s_item);
     if (i >= n_lines) return;
-    const float4 l = lines[i];
-    const V2 a = v2(l.x, l.y), p = v2(l.z, l.w);
-    if (veq(a, p)) return;
-    const uint32_t r = line_raster[i];
-    const int4 bb = bbox[r];
-    const uint64_t base = key_base[r];
-    uint32_t e = ent_off[i];
-    uint32_t q = inc_off[i];   // next stored increment
-    // increments leave in 16-byte pairs (an even index and the next one):
-    // the first of a pair waits in registers
-    float2 pend = make_float2(0.0f, 0.0f);
-    bool has_pend = false;
-    // open bin
-    int btx = 0x7fffffff, bty = 0x7fffffff, prev_x = 0;
-    uint32_t bcount = 0, bentry = 0;
-    BinRec rec;
-    auto flush = [&]() {
-        if (bcount) {
-            rec.n = (uint8_t)bcount;
-            *reinterpret_cast<uint4*>(bins + bentry) = *reinterpret_cast<const uint4*>(&rec);
-            keys[bentry] = make_key<K>(base, bb, btx, bty, 1u);
-            vals[bentry] = bentry;
-        }
-    };
-    walk_line(
-        a, p,
-        [&](const Walk& w, const WalkState& s) {
-            float area, height;
-            walk_increment(w, s, area, height);
-            const int tx = div8(s.x), ty = div8(s.y);
-            if (tx != btx || ty != bty || bcount == BIN_MAX_CELLS) {
-                flush();
-                btx = tx;
-                bty = ty;
-                bcount = 0;
-                bentry = e++;
-                rec.inc = q;
-                rec.raster = r;
-                rec.x = (int16_t)s.x;
-                rec.y = (int16_t)s.y;
-                rec.steps = 0;
-                rec.dirs = (uint8_t)((w.x_dir < 0 ? 1u : 0u) | (w.y_dir < 0 ? 2u : 0u));
-            } else if (s.x != prev_x) {
-                rec.steps = (uint16_t)(rec.steps | (1u << (bcount - 1)));   // the step into this cell moved in x
-            }
-            const float2 v = make_float2(area, height);
-            if ((q & 1u) == 0u) {
-                pend = v;
-                has_pend = true;
-            } else if (has_pend) {
-                reinterpret_cast<float4*>(incs)[q >> 1] = make_float4(pend.x, pend.y, v.x, v.y);
-                has_pend = false;
-            } else {
-                incs[q] = v;   // the line's first increment at an odd index
-            }
-            q++;
-            prev_x = s.x;
-            bcount++;
-        },
-        [&](int tx, int ty, int sign) {
-            const uint32_t c = e++;
-            keys[c] = make_key<K>(base, bb, tx, ty, 0u);
-            vals[c] = CROSS_TAG | (r << 8) | ((uint32_t)sign & 0xffu);
-        },
-        [&](int, int) {});
-    flush();
-    if (has_pend) incs[q - 1] = pend;
+    if (long_cells && walk_cells(lines[i]) > long_cells) return;
+    EmitJob<K> job;
+    job.lines = lines;
+    job.line_raster = line_raster;
+    job.ent_off = ent_off;
+    job.inc_off = inc_off;
+    job.bbox = bbox;
+    job.key_base = key_base;
+    job.keys = keys;
+    job.vals = vals;
+    job.bins = bins;
+    job.incs = incs;
+    job.r = 0xffffffffu;
+    Walk w;
+    WalkState s;
+    if (job.begin((uint32_t)i, w, s)) walk_one(w, s, job);
 }
 
 template <class K>
@@ -380,6 +671,34 @@ __global__ void k_empty_emit(const uint32_t* __restrict__ empty, uint32_t n_rast
     vals[e] = e;
 }
 
+// The stream the long-line walkers run on: a side stream that waits for
+// the run's stream s here (join_walks makes s wait for it in turn), so that
+// the walkers, whose time is the longest line's serial walk, overlap the
+// per-line kernel.  s itself when the context has no side stream.
+static cudaError_t fork_walks(ochre_gpu_ctx* ctx, cudaStream_t s, cudaStream_t* side) {
+    *side = s;
+    if (ctx->no_side_stream) return cudaSuccess;
+    if (!ctx->walk_stream) {
+        if (cudaStreamCreateWithFlags(&ctx->walk_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_walk_fork, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_walk_join, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->no_side_stream = true;
+            return cudaSuccess;
+        }
+    }
+    cudaError_t e = cudaEventRecord(ctx->ev_walk_fork, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->walk_stream, ctx->ev_walk_fork, 0);
+    if (e == cudaSuccess) *side = ctx->walk_stream;
+    return e;
+}
+static cudaError_t join_walks(ochre_gpu_ctx* ctx, cudaStream_t side, cudaStream_t s) {
+    if (side == s) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(ctx->ev_walk_join, side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, ctx->ev_walk_join, 0);
+    return e;
+}
+
 int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaStream_t s, uint64_t* n_entries,
               uint32_t* key_bits) {
     DevScalars* ds = dev_scalars(ctx);
@@ -396,9 +715,22 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_LAUNCH(ctx, "bbox_init", s, k_bbox_init<<<(R + 255) / 256, 256, 0, s>>>(ctx->raster_bbox.as<int4>(),
                                                                                  ctx->raster_wsum.as<int>(), R));
     OCHRE_CUDA_TRY(cudaGetLastError());
-    // the line pair's totals and the 64-bit increment count
-    static_assert(offsetof(DevScalars, inc_total) == offsetof(DevScalars, line_ent_total) + 8, "layout");
-    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->line_ent_total, 0, 16, s));
+    // the line pair's totals, the 64-bit increment count and the walks' tickets
+    static_assert(offsetof(DevScalars, inc_total) == offsetof(DevScalars, line_ent_total) + 8 &&
+                      offsetof(DevScalars, walk_ticket) == offsetof(DevScalars, line_ent_total) + 16,
+                  "layout");
+    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->line_ent_total, 0, 24, s));
+    // long-line walkers: persistent, LONG_BLOCKS_PER_SM blocks per SM (each
+    // refills its lanes from the queue)
+    const uint32_t long_cells = (uint32_t)ctx->tune_chain_long_cells;
+    const uint32_t refill = (uint32_t)ctx->tune_chain_walk_refill;
+    uint32_t long_blocks = 0;
+    if (long_cells) {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        long_blocks = (uint32_t)sms * LONG_BLOCKS_PER_SM;
+    }
+    const uint32_t* queue = long_cells ? ctx->long_lines.as<uint32_t>() : nullptr;
     // graph replays: n_lines is the capacity, the count is on the device
     const GraphPlan* plan = ctx->plan;
     const uint32_t* lines_dev = plan ? &ds->n_lines : nullptr;
@@ -406,11 +738,22 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
         OCHRE_CUDA_TRY(ctx->line_ent_off.ensure((size_t)n_lines * 4));
         OCHRE_CUDA_TRY(ctx->line_inc_off.ensure((size_t)n_lines * 4));
         OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n_lines) * sizeof(ScanStatus<LinePair>)));
+        cudaStream_t side = s;
+        if (long_blocks) {
+            OCHRE_CUDA_TRY(fork_walks(ctx, s, &side));
+            OCHRE_LAUNCH(ctx, "dda_count_long", side, k_line_count_long<<<long_blocks, LONG_THREADS, 0, side>>>(
+                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, lines_dev,
+                ctx->raster_bbox.as<int4>(), ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(),
+                ctx->line_inc_off.as<uint32_t>(), reinterpret_cast<unsigned long long*>(&ds->inc_total), queue,
+                &ds->n_long, &ds->walk_ticket[0], refill, &ds->err));
+            OCHRE_CUDA_TRY(cudaGetLastError());
+        }
         OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<(n_lines + 255) / 256, 256, 0, s>>>(
             ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
             ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>(),
-            reinterpret_cast<unsigned long long*>(&ds->inc_total), &ds->err));
+            reinterpret_cast<unsigned long long*>(&ds->inc_total), long_cells, &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());
+        OCHRE_CUDA_TRY(join_walks(ctx, side, s));
         // in place: every count is read by the thread that writes its offset
         OCHRE_LAUNCH(ctx, "dda_offset_scan", s, OCHRE_CUDA_TRY(launch_scan<LinePair>(
             n_lines, LinePairIn{ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>()},
@@ -465,19 +808,34 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_CUDA_TRY(ctx->bins.ensure(E * sizeof(BinRec)));
     if (n_lines) {
         const unsigned blocks = (unsigned)((n_lines + 255) / 256);
+        cudaStream_t side = s;
+        if (long_blocks) OCHRE_CUDA_TRY(fork_walks(ctx, s, &side));
+        if (long_blocks && ctx->keys64)
+            OCHRE_LAUNCH(ctx, "dda_emit_long", side, k_line_emit_long<uint64_t><<<long_blocks, LONG_THREADS, 0, side>>>(
+                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
+                ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
+                ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(),
+                ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), queue, &ds->n_long, &ds->walk_ticket[1], refill));
+        else if (long_blocks)
+            OCHRE_LAUNCH(ctx, "dda_emit_long", side, k_line_emit_long<uint32_t><<<long_blocks, LONG_THREADS, 0, side>>>(
+                ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
+                ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
+                ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(),
+                ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), queue, &ds->n_long, &ds->walk_ticket[1], refill));
         if (ctx->keys64)
             OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<blocks, 256, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
                 ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
                 ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(),
-                ctx->bins.as<BinRec>(), ctx->incs.as<float2>()));
+                ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), long_cells));
         else
             OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<blocks, 256, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
                 ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
                 ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(),
-                ctx->bins.as<BinRec>(), ctx->incs.as<float2>()));
+                ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), long_cells));
         OCHRE_CUDA_TRY(cudaGetLastError());
+        OCHRE_CUDA_TRY(join_walks(ctx, side, s));
     }
     if (any_empty) {
         const uint32_t* first_dev = plan ? &ds->line_ent_total : nullptr;

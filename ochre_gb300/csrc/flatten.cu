@@ -130,8 +130,11 @@ __global__ void __launch_bounds__(128) k_count_each(uint64_t n, In in, uint32_t*
 // Below this many scan tiles the counts get their own kernel.
 constexpr uint64_t SPLIT_COUNT_TILES = 256;
 
+// Lines of more than long_cells cells (walk_cells) are also queued for the
+// long-line walkers of the DDA stage (long_cells 0: none are).
 __global__ void k_cmd_emit(BatchView b, const uint32_t* __restrict__ line_off, uint32_t n_lines_cap,
-                           float4* __restrict__ lines, uint32_t* __restrict__ line_raster, uint32_t* err) {
+                           float4* __restrict__ lines, uint32_t* __restrict__ line_raster, uint32_t long_cells,
+                           uint32_t* __restrict__ long_lines, uint32_t* n_long, uint32_t* err) {
     const uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (c >= b.n_cmds) return;
     const CmdCtx k = load_cmd(b, (uint32_t)c);
@@ -139,8 +142,10 @@ __global__ void k_cmd_emit(BatchView b, const uint32_t* __restrict__ line_off, u
     uint32_t o = line_off[c];
     flatten_cmd(k, [&](V2 a, V2 p) {
         if (o < n_lines_cap) {
-            lines[o] = make_float4(a.x, a.y, p.x, p.y);
+            const float4 l = make_float4(a.x, a.y, p.x, p.y);
+            lines[o] = l;
             line_raster[o] = k.raster;
+            if (long_cells && walk_cells(l) > long_cells) long_lines[atomicAdd(n_long, 1u)] = o;
         } else {
             atomicOr(err, ERR_CAPACITY);
         }
@@ -206,9 +211,13 @@ int stage_flatten(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, uin
     if (L > MAX_COUNT) return OCHRE_E_CAPACITY;
     OCHRE_CUDA_TRY(ctx->lines.ensure((size_t)L * sizeof(float4)));
     OCHRE_CUDA_TRY(ctx->line_raster.ensure((size_t)L * 4));
+    const uint32_t long_cells = (uint32_t)ctx->tune_chain_long_cells;
+    if (long_cells) OCHRE_CUDA_TRY(ctx->long_lines.ensure((size_t)L * 4));
+    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_long, 0, 4, s));
     const unsigned blocks = (unsigned)((n + 255) / 256);
-    OCHRE_LAUNCH(ctx, "flatten_emit", s, k_cmd_emit<<<blocks, 256, 0, s>>>(b, ctx->cmd_line_off.as<uint32_t>(), L, ctx->lines.as<float4>(),
-                                      ctx->line_raster.as<uint32_t>(), &ds->err));
+    OCHRE_LAUNCH(ctx, "flatten_emit", s, k_cmd_emit<<<blocks, 256, 0, s>>>(
+        b, ctx->cmd_line_off.as<uint32_t>(), L, ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), long_cells,
+        long_cells ? ctx->long_lines.as<uint32_t>() : nullptr, &ds->n_long, &ds->err));
     OCHRE_CUDA_TRY(cudaGetLastError());
     return OCHRE_OK;
 }

@@ -74,6 +74,9 @@ struct DevScalars {
     uint32_t n_incs;          // chain: pixel-cell increments of the lines } pair total)
     uint64_t inc_total;       // the same increment count summed in 64 bits (the pair
                               // total wraps above 2^32; this one says when it did)
+    uint32_t walk_ticket[2];  // long-line pools handed out in the count and emit walks
+    uint32_t n_long;          // lines queued for the long-line walkers (flatten)
+    uint32_t pad4;
 };
 // The waits find spin_log2 from the error word's address (common.cuh).
 static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
@@ -149,6 +152,7 @@ struct ochre_gpu_ctx {
     ochre::DevBuf cmd_foff, cmd_mv, cmd_ep, cmd_line_off;
     // per line (line_inc_off: first stored increment of the line's walk)
     ochre::DevBuf lines, line_raster, line_ent_off, line_inc_off;
+    ochre::DevBuf long_lines;   // indices of the lines walked by the long-line walkers
     // stored pixel-cell increments (area, height) of every walk, line by line
     ochre::DevBuf incs;
     // per raster
@@ -215,6 +219,8 @@ struct ochre_gpu_ctx {
     int tune_fused_chunk = 16;
     int tune_chain_tiles_per_warp = 8;
     int tune_chain_coverage_form = 0;   // 0: by row count, 1: block form, 2: row form
+    int tune_chain_long_cells = 64;     // lines of more (estimated) cells go to the long-line walkers; 0: none
+    int tune_chain_walk_refill = 8;     // idle lanes of a long-line warp that trigger a refill (1..32)
 
     // Host-batch entry: a large point array is copied on copy_stream while
     // the first stages run; pts_pending until a stage that reads points has
@@ -222,6 +228,12 @@ struct ochre_gpu_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_prior = nullptr, ev_pts = nullptr;
     bool pts_pending = false;
+    // The chain's long-line walkers run on walk_stream beside the per-line
+    // walks (forked from and joined to the run's stream by the two events),
+    // or on the run's stream itself when no_side_stream is set.
+    cudaStream_t walk_stream = nullptr;
+    cudaEvent_t ev_walk_fork = nullptr, ev_walk_join = nullptr;
+    bool no_side_stream = false;
 
     // Set while the chain is planned for (and captured into) a CUDA graph:
     // stages size buffers from it and never read counts back to the host.

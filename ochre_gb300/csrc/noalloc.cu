@@ -91,10 +91,12 @@ extern "C" int ochre_gpu_rasterize_noalloc(const ochre_batch* in, ochre_output_b
     // the fused path's per-CTA staging comes from the array too: a smaller
     // persistent grid keeps it to a few MB
     ctx.fused_max_ctas = 256;
+    ctx.no_side_stream = true;   // creates no stream: every kernel on the caller's
     ctx.own_stream = static_cast<cudaStream_t>(stream);
     ochre::DevBuf* internal[] = {&ctx.in_verbs, &ctx.in_pts, &ctx.in_fill_off, &ctx.in_fill_xf,
                                  &ctx.in_fill_flags, &ctx.in_raster_off, &ctx.cmd_foff, &ctx.cmd_mv, &ctx.cmd_ep,
-                                 &ctx.cmd_line_off, &ctx.lines, &ctx.line_raster, &ctx.line_ent_off, &ctx.line_inc_off, &ctx.incs,
+                                 &ctx.cmd_line_off, &ctx.lines, &ctx.line_raster, &ctx.line_ent_off, &ctx.line_inc_off,
+                                 &ctx.long_lines, &ctx.incs,
                                  &ctx.raster_bbox, &ctx.raster_keybase, &ctx.raster_empty,
                                  &ctx.raster_wsum, &ctx.raster_wbase, &ctx.tile_head_bins, &ctx.tile_head_wind, &ctx.keys, &ctx.vals,
                                  &ctx.keys_alt, &ctx.vals_alt, &ctx.bins, &ctx.sort_hist, &ctx.sort_lookback,

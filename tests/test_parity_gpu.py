@@ -376,3 +376,23 @@ def test_stored_increments_above_2_30(gpu_ctx_chain):
              torch.as_tensor(_Dev(r.span_tile, (N1,), "<u4"), device="cuda").cpu().numpy(),
              "raster_tile_off": np.array([0, T1], np.uint64), "raster_span_off": np.array([0, N1], np.uint64)}
     compare(first, exp, 1)
+
+
+@pytest.mark.parametrize("long_cells,refill", [(0, 8), (16, 1), (16, 8), (16, 32), (64, 8)])
+def test_long_line_walkers_match_oracle(gpu_ctx_chain, long_cells, refill):
+    # Lines of more than long_cells cells are walked by the persistent
+    # refilling walkers beside the one-thread-per-line kernels (0: none are);
+    # a low threshold sends most of a batch's lines there.  The result must
+    # not depend on the split, and must equal the oracle's.
+    from ochre_gb300 import autotune, batch as B
+    b = B.concat([W.uneven_mix(n_paths=120, seed=21), W.cubic_boxes(n_paths=40, seed=22)])
+    ref = oracle.run(b, threads=8)
+    old = {k: autotune.get(gpu_ctx_chain, k) for k in ("chain_long_cells", "chain_walk_refill")}
+    try:
+        autotune.apply(gpu_ctx_chain, {"chain_long_cells": long_cells, "chain_walk_refill": refill})
+        for _ in range(2):
+            got = gpu_ctx_chain.rasterize(b)
+            compare(got, ref, b.n_rasters)
+        assert gpu_ctx_chain.stats()["n_incs"] > 0
+    finally:
+        autotune.apply(gpu_ctx_chain, old)
