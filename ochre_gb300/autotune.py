@@ -5,9 +5,10 @@ workload, keeps the fastest, and caches the choice per GPU name in
 ``ochre_gb300/_build/tune.json``:
   * the fused small-raster kernel: threads per raster and tiles per
     accumulation pass;
-  * tiles per warp of the general chain's coverage kernel.
+  * tiles per warp of the general chain's coverage kernel;
+  * the digit width of the chain's radix sort (8 or 11 bits).
 Results never depend on the shape (tile and span structure is exact, alpha
-within 1 LSB of the oracle either way).
+within 1 LSB of the oracle either way; the sort is stable at any width).
 """
 from __future__ import annotations
 
@@ -30,6 +31,7 @@ def fused_candidates() -> list:
 def shape_name(p: dict) -> str:
     return f"{p['fused_threads']}x{p['fused_chunk']}"
 CHAIN_TILES_PER_WARP = [4, 8, 16]
+SORT_DIGIT_BITS = [8, 11]
 CACHE = os.path.join(build.BUILD, "tune.json")
 
 
@@ -111,9 +113,21 @@ def tune(ctx, fused_sample=None, chain_sample=None, reps: int = 3, save: bool = 
         report["chain"][str(tpw)] = ms
         if ms < best_ct:
             best_c, best_ct = tpw, ms
+    apply(ctx, {"chain_tiles_per_warp": best_c or 8})
+    # radix sort digit width on the same sample (its keys span about 30 bits:
+    # four 8-bit passes or three of at most 11)
+    report["sort_digit_bits"] = {}
+    best_d, best_dt = None, float("inf")
+    for bits in SORT_DIGIT_BITS:
+        apply(ctx, {"sort_digit_bits": bits})
+        ms = _time(ctx, db, reps)
+        report["sort_digit_bits"][str(bits)] = ms
+        if ms < best_dt:
+            best_d, best_dt = bits, ms
     ctx.set_chain_only(old_chain)
     choice = dict(best_f or {"fused_threads": 64, "fused_chunk": 16})
     choice["chain_tiles_per_warp"] = best_c or 8
+    choice["sort_digit_bits"] = best_d or 8
     apply(ctx, choice)
     if save:
         cache = load_cache()

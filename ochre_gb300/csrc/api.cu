@@ -637,6 +637,9 @@ int ochre_gpu_set_tunable(ochre_gpu_ctx* ctx, const char* name, int value) {
     } else if (!std::strcmp(name, "chain_coverage_form")) {
         if (value < 0 || value > 2) return OCHRE_E_INVALID;
         ctx->tune_chain_coverage_form = value;
+    } else if (!std::strcmp(name, "sort_digit_bits")) {
+        if (value != 8 && value != 11) return OCHRE_E_INVALID;
+        ctx->tune_sort_digit_bits = value;
     } else if (!std::strcmp(name, "chain_long_cells")) {
         if (value != 0 && (value < 16 || value > 65535)) return OCHRE_E_INVALID;
         ctx->tune_chain_long_cells = value;
@@ -662,6 +665,7 @@ int ochre_gpu_get_tunable(const ochre_gpu_ctx* ctx, const char* name, int* value
     else if (!std::strcmp(name, "chain_tiles_per_warp")) *value = ctx->tune_chain_tiles_per_warp;
     else if (!std::strcmp(name, "chain_coverage_form")) *value = ctx->tune_chain_coverage_form;
     else if (!std::strcmp(name, "chain_long_cells")) *value = ctx->tune_chain_long_cells;
+    else if (!std::strcmp(name, "sort_digit_bits")) *value = ctx->tune_sort_digit_bits;
     else if (!std::strcmp(name, "chain_walk_refill")) *value = ctx->tune_chain_walk_refill;
     else return OCHRE_E_INVALID;
     return OCHRE_OK;

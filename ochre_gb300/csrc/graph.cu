@@ -237,6 +237,7 @@ int ochre_graph_create(ochre_gpu_ctx* ctx, const ochre_batch* in, float headroom
     g->ctx->tune_chain_tiles_per_warp = ctx->tune_chain_tiles_per_warp;
     g->ctx->tune_chain_coverage_form = ctx->tune_chain_coverage_form;
     g->ctx->tune_chain_long_cells = ctx->tune_chain_long_cells;
+    g->ctx->tune_sort_digit_bits = ctx->tune_sort_digit_bits;
     g->ctx->tune_chain_walk_refill = ctx->tune_chain_walk_refill;
     g->ctx->cov_signed = ctx->cov_signed;
     g->batch = *in;

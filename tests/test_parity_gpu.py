@@ -396,3 +396,56 @@ def test_long_line_walkers_match_oracle(gpu_ctx_chain, long_cells, refill):
         assert gpu_ctx_chain.stats()["n_incs"] > 0
     finally:
         autotune.apply(gpu_ctx_chain, old)
+
+
+def _band_copies(n):
+    from ochre_gb300.batch import Batch, CLOSE, LINE, MOVE
+    verbs = np.array([MOVE, LINE, LINE, LINE, CLOSE], np.uint8)
+    pts = np.array([0.3, 0.7, 7999.6, 7990.2, 7999.6, 7993.1, 0.3, 3.6], np.float32)
+    xf = np.array([1, 0, 0, 1, 0, 0], np.float32)
+    return Batch(np.tile(verbs, n), np.tile(pts, n), (np.arange(n + 1) * 5).astype(np.uint32),
+                 np.tile(xf, (n, 1)), None, None, n)
+
+
+def _result_tensors(r, n_rasters):
+    import torch
+    T, N = r.n_tiles, r.n_spans
+    out = {"rto": torch.as_tensor(_Dev(r.raster_tile_off, (n_rasters + 1,), "<u4"), device="cuda").clone(),
+           "rso": torch.as_tensor(_Dev(r.raster_span_off, (n_rasters + 1,), "<u4"), device="cuda").clone()}
+    if T:
+        out["xy"] = torch.as_tensor(_Dev(r.tile_xy, (T, 2), "<i2"), device="cuda").clone()
+        out["alpha"] = torch.as_tensor(_Dev(r.tile_alpha, (T, 64), "|u1"), device="cuda").clone()
+    if N:
+        out["sxy"] = torch.as_tensor(_Dev(r.span_xy, (N, 2), "<i2"), device="cuda").clone()
+        out["sw"] = torch.as_tensor(_Dev(r.span_width, (N,), "<u2"), device="cuda").clone()
+    return out
+
+
+@pytest.mark.parametrize("case", ["mixed_32bit_keys", "bands_64bit_keys"])
+def test_sort_digit_widths_agree(gpu_ctx_chain, case):
+    # The chain's radix sort with 8- and 11-bit digits (the autotuner picks
+    # one per GPU) gives the same result, with 32-bit keys and with 64-bit
+    # keys (2,400 rasters of 1,000 x 1,000-tile boxes: a key space above 2^32).
+    import torch
+    from ochre_gb300 import DeviceBatch, autotune, batch as B
+    b = (B.concat([W.uneven_mix(n_paths=150, seed=23), W.cubic_boxes(n_paths=40, seed=24)])
+         if case == "mixed_32bit_keys" else _band_copies(2400))
+    db = DeviceBatch(b)
+    old = autotune.get(gpu_ctx_chain, "sort_digit_bits")
+    res = {}
+    try:
+        for bits in (8, 11):
+            autotune.apply(gpu_ctx_chain, {"sort_digit_bits": bits})
+            r = gpu_ctx_chain.rasterize_device(db)
+            st = gpu_ctx_chain.stats()
+            assert (st["key_bits"] > 32) == (case == "bands_64bit_keys"), st
+            assert 0 < st["sort_passes"] <= -(-st["key_bits"] // bits), st
+            res[bits] = _result_tensors(r, b.n_rasters)
+        assert res[8].keys() == res[11].keys()
+        for k in res[8]:
+            assert torch.equal(res[8][k], res[11][k]), k
+        if case == "mixed_32bit_keys":
+            autotune.apply(gpu_ctx_chain, {"sort_digit_bits": 11})
+            compare(gpu_ctx_chain.rasterize(b), oracle.run(b, threads=8), b.n_rasters)
+    finally:
+        autotune.apply(gpu_ctx_chain, {"sort_digit_bits": old})
