@@ -98,6 +98,58 @@ __device__ __forceinline__ uint32_t order_by_length(uint32_t cells, uint32_t* s_
     return s_item[threadIdx.x];
 }
 
+// Persistent count walks of short lines.  A warp takes windows of WIN
+// consecutive lines by ticket and walks each window's lines 32 at a time in
+// order of length (grouped by log2 of their cell count, unstable within a
+// group), so a warp's lanes walk lines of about the same length; no warp
+// waits on another, so an SM stays full until the last window (a block of
+// lines ordered in the block holds its SM slot until its slowest warp ends:
+// count 1.87 -> 1.71 ms on the 20,000-path uneven mix, 0.169 -> 0.143 ms on
+// 100,000 glyphs).  The emit walk keeps the block form: there, each group's
+// set-up loads (line, offsets, raster box and key base) waited behind the
+// previous group of the warp, 9.8 against 7.9 ms.
+constexpr int WIN = 256;
+constexpr int WIN_PER_LANE = WIN / 32;
+constexpr int WALK_BLOCK = 128;
+constexpr int LEN_GROUPS = 17;
+
+// Orders this warp's window: item WIN_PER_LANE * ... of lane k is
+// k + 32 * j (j < WIN_PER_LANE) with `cells[j]` cells; fills s_item[0..WIN)
+// with the items grouped by length.  s_cnt: LEN_GROUPS words of the warp.
+__device__ __forceinline__ void order_window(const uint32_t (&cells)[WIN_PER_LANE], uint32_t* s_cnt,
+                                             uint16_t* s_item) {
+    const uint32_t lane = threadIdx.x & 31u;
+    if (lane < LEN_GROUPS) s_cnt[lane] = 0u;
+    __syncwarp();
+    uint32_t g[WIN_PER_LANE], k[WIN_PER_LANE];
+#pragma unroll
+    for (int j = 0; j < WIN_PER_LANE; j++) {
+        g[j] = min(31u - (uint32_t)__clz(max(cells[j], 1u)), (uint32_t)LEN_GROUPS - 1u);
+        k[j] = atomicAdd(&s_cnt[g[j]], 1u);
+    }
+    __syncwarp();
+    const uint32_t c = lane < LEN_GROUPS ? s_cnt[lane] : 0u;
+    uint32_t inc = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= (uint32_t)o) inc += t;
+    }
+    __syncwarp();
+    if (lane < LEN_GROUPS) s_cnt[lane] = inc - c;
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < WIN_PER_LANE; j++) s_item[s_cnt[g[j]] + k[j]] = (uint16_t)(j * 32 + lane);
+    __syncwarp();
+}
+
+// The next window of a warp (lane 0 takes the ticket); WIN * it is its first line.
+__device__ __forceinline__ uint64_t next_window(uint32_t* ticket) {
+    uint32_t w = 0;
+    if ((threadIdx.x & 31u) == 0u) w = atomicAdd(ticket, 1u);
+    return (uint64_t)__shfl_sync(0xffffffffu, w, 0) * WIN;
+}
+
 // A raster's global tile box grows by atomics only where it grows.
 __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1) {
     const int4 cur = ld_words(d);
@@ -333,79 +385,91 @@ __global__ void __launch_bounds__(LONG_THREADS) k_line_count_long(
 // and the raster tile boxes.  Counting is a separate kernel, not folded into
 // the offset scan: a walk's length varies from one cell to thousands, and a
 // single-pass scan would hold every later block behind the slowest walk.
-// Lines of more than long_cells cells are left to k_line_count_long.  Boxes
-// (and the rasters' crossing-sign sums) are reduced before any global
-// atomic: lanes of one raster (lines of a raster are contiguous) by warp
-// reductions, then the block's first BOX_SLOTS rasters in shared memory; the
-// block then updates each global box only where it grows.
+// Persistent warps over windows (see order_window); lines of more than
+// long_cells cells are left to k_line_count_long.  Boxes (and the rasters'
+// crossing-sign sums) are reduced before any global atomic: lanes of one
+// raster by warp reductions, then the window's first BOX_SLOTS rasters (lines
+// of a raster are contiguous) in the warp's shared slots; each global box is
+// then updated only where it grows.
 constexpr int BOX_SLOTS = 8;
-__global__ void __launch_bounds__(256) k_line_count(const float4* __restrict__ lines,
-                                                    const uint32_t* __restrict__ line_raster, uint32_t n_cap,
-                                                    const uint32_t* n_dev, int4* bbox, int* raster_wsum,
-                                                    uint32_t* __restrict__ counts, uint32_t* __restrict__ inc_counts,
-                                                    unsigned long long* inc_total, uint32_t long_cells, uint32_t* err) {
-    __shared__ int4 s_box[BOX_SLOTS];
-    __shared__ int s_ws[BOX_SLOTS];
-    __shared__ uint32_t s_r0;
-    __shared__ uint32_t s_cnt[17];
-    __shared__ uint16_t s_item[256];
-    __shared__ uint32_t s_incs;
-    const uint32_t n_lines = (uint32_t)dev_count(n_cap, n_dev);
-    const uint32_t i0 = blockIdx.x * blockDim.x;
-    if (i0 >= n_lines) return;
-    const uint32_t cells = i0 + threadIdx.x < n_lines ? walk_cells(lines[i0 + threadIdx.x]) : 0u;
-    const uint32_t i = i0 + order_by_length<256>(cells, s_cnt, s_item);
-    if (threadIdx.x < BOX_SLOTS) {
-        s_box[threadIdx.x] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
-        s_ws[threadIdx.x] = 0;
-    }
-    if (threadIdx.x == 0) {
-        s_r0 = line_raster[i0];
-        s_incs = 0u;
-    }
-    __syncthreads();
-    const uint32_t r0 = s_r0;
-    BBoxAcc bb{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
-    uint32_t r = r0;
-    int ws = 0;
-    uint32_t nc = 0;
-    const float4 l = i < n_lines ? lines[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (i < n_lines && !(long_cells && walk_cells(l) > long_cells)) {
-        bool capped = false;
-        counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped, &ws, &nc);
-        inc_counts[i] = nc;
-        if (capped) atomicOr(err, ERR_LIMIT);
-        r = line_raster[i];
-    }
-    const unsigned grp = __match_any_sync(0xffffffffu, r);
-    const int x0 = __reduce_min_sync(grp, bb.x0), y0 = __reduce_min_sync(grp, bb.y0);
-    const int x1 = __reduce_max_sync(grp, bb.x1), y1 = __reduce_max_sync(grp, bb.y1);
-    const int wsg = __reduce_add_sync(grp, ws);
-    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) {
-        if (r - r0 < (uint32_t)BOX_SLOTS) {
-            if (x0 <= x1) {
-                int4* d = s_box + (r - r0);
-                atomicMin(&d->x, x0);
-                atomicMin(&d->y, y0);
-                atomicMax(&d->z, x1);
-                atomicMax(&d->w, y1);
-            }
-            if (wsg) atomicAdd(s_ws + (r - r0), wsg);
-        } else {
-            if (x0 <= x1) box_grow(bbox + r, x0, y0, x1, y1);
-            if (wsg) atomicAdd(raster_wsum + r, wsg);
+__global__ void __launch_bounds__(WALK_BLOCK) k_line_count(const float4* __restrict__ lines,
+                                                           const uint32_t* __restrict__ line_raster, uint32_t n_cap,
+                                                           const uint32_t* n_dev, int4* bbox, int* raster_wsum,
+                                                           uint32_t* __restrict__ counts,
+                                                           uint32_t* __restrict__ inc_counts,
+                                                           unsigned long long* inc_total, uint32_t long_cells,
+                                                           uint32_t* ticket, uint32_t* err) {
+    constexpr int WARPS = WALK_BLOCK / 32;
+    __shared__ int4 s_box[WARPS][BOX_SLOTS];
+    __shared__ int s_ws[WARPS][BOX_SLOTS];
+    __shared__ uint32_t s_cnt[WARPS][LEN_GROUPS];
+    __shared__ uint16_t s_item[WARPS][WIN];
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    const uint64_t n_lines = dev_count(n_cap, n_dev);
+    unsigned long long incs = 0;   // the warp's increments (lane 0)
+    for (;;) {
+        const uint64_t i0 = next_window(ticket);
+        if (i0 >= n_lines) break;
+        uint32_t cells[WIN_PER_LANE];
+#pragma unroll
+        for (int j = 0; j < WIN_PER_LANE; j++) {
+            const uint64_t i = i0 + j * 32 + lane;
+            cells[j] = i < n_lines ? walk_cells(lines[i]) : 0u;
         }
+        order_window(cells, s_cnt[wid], s_item[wid]);
+        if (lane < BOX_SLOTS) {
+            s_box[wid][lane] = make_int4(0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000);
+            s_ws[wid][lane] = 0;
+        }
+        const uint32_t r0 = line_raster[i0];
+        __syncwarp();
+        for (int j = 0; j < WIN_PER_LANE; j++) {
+            const uint64_t i = i0 + s_item[wid][j * 32 + lane];
+            BBoxAcc bb{0x7fffffff, 0x7fffffff, (int)0x80000000, (int)0x80000000};
+            uint32_t r = r0;
+            int ws = 0;
+            uint32_t nc = 0;
+            if (i < n_lines) {
+                const float4 l = lines[i];
+                if (!(long_cells && walk_cells(l) > long_cells)) {
+                    bool capped = false;
+                    counts[i] = count_line(v2(l.x, l.y), v2(l.z, l.w), bb, &capped, &ws, &nc);
+                    inc_counts[i] = nc;
+                    if (capped) atomicOr(err, ERR_LIMIT);
+                    r = line_raster[i];
+                }
+            }
+            const unsigned grp = __match_any_sync(0xffffffffu, r);
+            const int x0 = __reduce_min_sync(grp, bb.x0), y0 = __reduce_min_sync(grp, bb.y0);
+            const int x1 = __reduce_max_sync(grp, bb.x1), y1 = __reduce_max_sync(grp, bb.y1);
+            const int wsg = __reduce_add_sync(grp, ws);
+            if ((int)lane == __ffs(grp) - 1) {
+                if (r - r0 < (uint32_t)BOX_SLOTS) {
+                    if (x0 <= x1) {
+                        int4* d = &s_box[wid][r - r0];
+                        atomicMin(&d->x, x0);
+                        atomicMin(&d->y, y0);
+                        atomicMax(&d->z, x1);
+                        atomicMax(&d->w, y1);
+                    }
+                    if (wsg) atomicAdd(&s_ws[wid][r - r0], wsg);
+                } else {
+                    if (x0 <= x1) box_grow(bbox + r, x0, y0, x1, y1);
+                    if (wsg) atomicAdd(raster_wsum + r, wsg);
+                }
+            }
+            // (at most 32 capped walks: 32 bits hold it)
+            incs += __reduce_add_sync(0xffffffffu, nc);
+        }
+        __syncwarp();
+        if (lane < BOX_SLOTS) {
+            const int4 b = s_box[wid][lane];
+            if (b.x <= b.z) box_grow(bbox + r0 + lane, b.x, b.y, b.z, b.w);
+            if (s_ws[wid][lane]) atomicAdd(raster_wsum + r0 + lane, s_ws[wid][lane]);
+        }
+        __syncwarp();
     }
-    // the block's increments (at most 256 lines of a capped walk: 32 bits hold it)
-    const uint32_t wi = __reduce_add_sync(0xffffffffu, nc);
-    if ((threadIdx.x & 31) == 0 && wi) atomicAdd(&s_incs, wi);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_incs) atomicAdd(inc_total, (unsigned long long)s_incs);
-    if (threadIdx.x < BOX_SLOTS) {
-        const int4 b = s_box[threadIdx.x];
-        if (b.x <= b.z) box_grow(bbox + r0 + threadIdx.x, b.x, b.y, b.z, b.w);
-        if (s_ws[threadIdx.x]) atomicAdd(raster_wsum + r0 + threadIdx.x, s_ws[threadIdx.x]);
-    }
+    if (lane == 0 && incs) atomicAdd(inc_total, incs);
 }
 // Entry and increment offsets of every line, one scan of the pair (in place:
 // every count is read by the thread that writes its offset).
@@ -699,6 +763,21 @@ static cudaError_t join_walks(ochre_gpu_ctx* ctx, cudaStream_t side, cudaStream_
     return e;
 }
 
+// Persistent grid of a windowed walk kernel: the blocks the GPU keeps
+// resident, or fewer when there are fewer windows than warps.
+template <class Kernel>
+static unsigned window_grid(ochre_gpu_ctx* ctx, Kernel kernel, uint64_t n_lines) {
+    int sms = 152, occ = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, WALK_BLOCK, 0) != cudaSuccess || occ < 1) {
+        cudaGetLastError();
+        occ = 1;
+    }
+    const uint64_t windows = (n_lines + WIN - 1) / WIN;
+    const uint64_t blocks = (windows + WALK_BLOCK / 32 - 1) / (WALK_BLOCK / 32);
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(blocks, (uint64_t)sms * (uint64_t)occ));
+}
+
 int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaStream_t s, uint64_t* n_entries,
               uint32_t* key_bits) {
     DevScalars* ds = dev_scalars(ctx);
@@ -720,6 +799,7 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
                       offsetof(DevScalars, walk_ticket) == offsetof(DevScalars, line_ent_total) + 16,
                   "layout");
     OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->line_ent_total, 0, 24, s));
+    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->line_ticket, 0, 4, s));
     // long-line walkers: persistent, LONG_BLOCKS_PER_SM blocks per SM (each
     // refills its lanes from the queue)
     const uint32_t long_cells = (uint32_t)ctx->tune_chain_long_cells;
@@ -748,10 +828,10 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
                 &ds->n_long, &ds->walk_ticket[0], refill, &ds->err));
             OCHRE_CUDA_TRY(cudaGetLastError());
         }
-        OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<(n_lines + 255) / 256, 256, 0, s>>>(
+        OCHRE_LAUNCH(ctx, "dda_count", s, k_line_count<<<window_grid(ctx, k_line_count, n_lines), WALK_BLOCK, 0, s>>>(
             ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
             ctx->raster_wsum.as<int>(), ctx->line_ent_off.as<uint32_t>(), ctx->line_inc_off.as<uint32_t>(),
-            reinterpret_cast<unsigned long long*>(&ds->inc_total), long_cells, &ds->err));
+            reinterpret_cast<unsigned long long*>(&ds->inc_total), long_cells, &ds->line_ticket, &ds->err));
         OCHRE_CUDA_TRY(cudaGetLastError());
         OCHRE_CUDA_TRY(join_walks(ctx, side, s));
         // in place: every count is read by the thread that writes its offset
@@ -807,7 +887,6 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
     OCHRE_CUDA_TRY(ctx->vals_alt.ensure(E * 4));
     OCHRE_CUDA_TRY(ctx->bins.ensure(E * sizeof(BinRec)));
     if (n_lines) {
-        const unsigned blocks = (unsigned)((n_lines + 255) / 256);
         cudaStream_t side = s;
         if (long_blocks) OCHRE_CUDA_TRY(fork_walks(ctx, s, &side));
         if (long_blocks && ctx->keys64)
@@ -823,13 +902,13 @@ int stage_bin(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t n_lines, cudaS
                 ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(),
                 ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), queue, &ds->n_long, &ds->walk_ticket[1], refill));
         if (ctx->keys64)
-            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<blocks, 256, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint64_t><<<(unsigned)((n_lines + 255) / 256), 256, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
                 ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
                 ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint64_t>(), ctx->vals.as<uint32_t>(),
                 ctx->bins.as<BinRec>(), ctx->incs.as<float2>(), long_cells));
         else
-            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<blocks, 256, 0, s>>>(
+            OCHRE_LAUNCH(ctx, "dda_emit", s, k_line_emit<uint32_t><<<(unsigned)((n_lines + 255) / 256), 256, 0, s>>>(
                 ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(), ctx->line_ent_off.as<uint32_t>(),
                 ctx->line_inc_off.as<uint32_t>(), n_lines, lines_dev, ctx->raster_bbox.as<int4>(),
                 ctx->raster_keybase.as<uint64_t>(), ctx->keys.as<uint32_t>(), ctx->vals.as<uint32_t>(),

@@ -77,6 +77,8 @@ struct DevScalars {
     uint32_t walk_ticket[2];  // long-line pools handed out in the count and emit walks
     uint32_t n_long;          // lines queued for the long-line walkers (flatten)
     uint32_t pad4;
+    uint32_t line_ticket;     // line windows handed out in the count walk
+    uint32_t pad5;
 };
 // The waits find spin_log2 from the error word's address (common.cuh).
 static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
