@@ -121,9 +121,9 @@ constexpr int CELL_UNROLL = 4;
 // Adds the stored increments of the bins among entries e0 .. e1 - 1 (the
 // entries of the chunk's nt tiles; crossing entries skipped) into the chunk's
 // shared accumulators (rasterizer.rs:223-228).  The bins of a batch of 32
-// entries are staged, then the warp takes their cells 32 at a time, so every
-// lane has a cell whatever the bins' lengths; a cell's position follows from
-// its bin's first cell and steps.
+// entries are staged, then the warp's lanes take equal contiguous ranges of
+// their cells, so every lane has cells whatever the bins' lengths; a cell's
+// position follows from its bin's first cell and steps.
 template <int CH>
 __device__ __forceinline__ void add_chunk_increments(const uint32_t* __restrict__ vals, const BinRec* __restrict__ bins,
                                                      const float2* __restrict__ incs, uint32_t e0, uint32_t e1,
@@ -160,39 +160,53 @@ __device__ __forceinline__ void add_chunk_increments(const uint32_t* __restrict_
         st.pre[lane] = pre - n;
         if (lane == 31) st.pre[32] = total;
         __syncwarp();
-        // CELL_UNROLL cells per lane at a time: their increment loads are all
-        // in flight before the first is added
-        for (uint32_t c0 = 0; c0 < total; c0 += 32 * CELL_UNROLL) {
-            float2 ah[CELL_UNROLL];
-            int where[CELL_UNROLL];   // slot << 6 | cell, or -1
+        // Each lane takes a contiguous range of the batch's cells: one search
+        // for the bin of its first cell, then bin after bin; CELL_UNROLL
+        // cells at a time, their increment loads all in flight before the
+        // first is added.
+        const uint32_t per = (total + 31u) >> 5;
+        uint32_t c = lane * per;
+        const uint32_t c_end = min(c + per, total);
+        if (c < c_end) {
+            int b = 0;
 #pragma unroll
-            for (int u = 0; u < CELL_UNROLL; u++) {
-                const uint32_t c = c0 + 32 * u + lane;
-                where[u] = -1;
-                ah[u] = make_float2(0.0f, 0.0f);
-                if (c < total) {
-                    // the bin holding cell c: the last b with pre[b] <= c
-                    int b = 0;
+            for (int step = 16; step > 0; step >>= 1)
+                if (st.pre[b + step] <= c) b += step;
+            uint32_t base = st.pre[b], next = st.pre[b + 1], m = st.meta[b], sxy = st.xy[b], ib = st.inc[b];
+            while (c < c_end) {
+                float2 ah[CELL_UNROLL];
+                int where[CELL_UNROLL];   // slot << 6 | cell, or -1
 #pragma unroll
-                    for (int step = 16; step > 0; step >>= 1)
-                        if (st.pre[b + step] <= c) b += step;
-                    const uint32_t k = c - st.pre[b];
-                    const uint32_t m = st.meta[b], sxy = st.xy[b];
-                    const uint32_t steps_before = m & ((1u << k) - 1u) & 0xffffu;
-                    const int nx = __popc(steps_before), ny = (int)k - nx;
-                    const int cx = (int)(sxy & 0xffffu) + ((m >> 21) & 1u ? -nx : nx);
-                    const int cy = (int)(sxy >> 16) + ((m >> 22) & 1u ? -ny : ny);
-                    where[u] = (int)(((m >> 23) & 31u) << 6) | ((cy & 7) << 3) | (cx & 7);
-                    ah[u] = incs[st.inc[b] + k];
+                for (int u = 0; u < CELL_UNROLL; u++) {
+                    where[u] = -1;
+                    ah[u] = make_float2(0.0f, 0.0f);
+                    if (c < c_end) {
+                        while (c >= next) {   // on to the next bin with cells
+                            b++;
+                            base = next;
+                            next = st.pre[b + 1];
+                            m = st.meta[b];
+                            sxy = st.xy[b];
+                            ib = st.inc[b];
+                        }
+                        const uint32_t k = c - base;
+                        const uint32_t steps_before = m & ((1u << k) - 1u) & 0xffffu;
+                        const int nx = __popc(steps_before), ny = (int)k - nx;
+                        const int cx = (int)(sxy & 0xffffu) + ((m >> 21) & 1u ? -nx : nx);
+                        const int cy = (int)(sxy >> 16) + ((m >> 22) & 1u ? -ny : ny);
+                        where[u] = (int)(((m >> 23) & 31u) << 6) | ((cy & 7) << 3) | (cx & 7);
+                        ah[u] = incs[ib + k];
+                        c++;
+                    }
                 }
-            }
 #pragma unroll
-            for (int u = 0; u < CELL_UNROLL; u++) {
-                if (where[u] < 0) continue;
-                float* a = acc[where[u] >> 6];
-                const int cell = where[u] & 63;
-                atomicAdd(a + acc_idx(cell), ah[u].x);
-                atomicAdd(a + ACC_H + acc_idx(cell), ah[u].y);
+                for (int u = 0; u < CELL_UNROLL; u++) {
+                    if (where[u] < 0) continue;
+                    float* a = acc[where[u] >> 6];
+                    const int cell = where[u] & 63;
+                    atomicAdd(a + acc_idx(cell), ah[u].x);
+                    atomicAdd(a + ACC_H + acc_idx(cell), ah[u].y);
+                }
             }
         }
         __syncwarp();
