@@ -185,6 +185,29 @@ __device__ __forceinline__ void box_grow(int4* d, int x0, int y0, int x1, int y1
 // ---------------------------------------------------------------------
 constexpr uint32_t WALK_POOL = 32;
 
+// The rest of a line's walk from its current state (it steps taken):
+// walk_line's loop with the job's callbacks, then job.end.
+template <class Job>
+__device__ __forceinline__ void walk_rest(const Walk& w, WalkState& s, int ty_prev, uint32_t it, Job& job) {
+    bool capped = false;
+    for (;;) {
+        job.cell(w, s);
+        const bool done = walk_step(w, s);
+        job.visit(s.x, s.y);
+        const int ty = div8(s.y);
+        if (ty != ty_prev) {
+            job.cross(div8(s.x), min(ty_prev, ty), (int)(int8_t)(int16_t)(ty - ty_prev));
+            ty_prev = ty;
+        }
+        if (done) break;
+        if (++it >= WALK_CAP) {
+            capped = true;
+            break;
+        }
+    }
+    job.end(capped);
+}
+
 template <class Job>
 __device__ __forceinline__ void walk_refill(uint64_t n_lines, const uint32_t* __restrict__ queue, uint32_t* ticket,
                                             uint32_t refill, Job& job) {
@@ -226,10 +249,13 @@ __device__ __forceinline__ void walk_refill(uint64_t n_lines, const uint32_t* __
                 idle = __ballot_sync(0xffffffffu, !live);
             }
         }
-        if (__ballot_sync(0xffffffffu, live) == 0u) {
-            if (!more) break;
-            continue;
+        if (!more) {
+            // nothing left to take: the live lanes finish their lines without
+            // the per-step votes (the last, longest walks set the kernel's end)
+            if (live) walk_rest(w, s, ty_prev, it, job);
+            break;
         }
+        if (__ballot_sync(0xffffffffu, live) == 0u) continue;
         if (live) {
             job.cell(w, s);
             bool done = walk_step(w, s);
@@ -252,29 +278,11 @@ __device__ __forceinline__ void walk_refill(uint64_t n_lines, const uint32_t* __
     }
 }
 
-// The same steps for one line whose walk job.begin has set up (walk_line's
-// loop with the job's callbacks).
+// One line whose walk job.begin has set up.
 template <class Job>
 __device__ __forceinline__ void walk_one(Walk& w, WalkState& s, Job& job) {
-    int ty_prev = div8(s.y);
     job.visit(s.x, s.y);
-    bool capped = false;
-    for (uint32_t it = 0;; ++it) {
-        job.cell(w, s);
-        const bool done = walk_step(w, s);
-        job.visit(s.x, s.y);
-        const int ty = div8(s.y);
-        if (ty != ty_prev) {
-            job.cross(div8(s.x), min(ty_prev, ty), (int)(int8_t)(int16_t)(ty - ty_prev));
-            ty_prev = ty;
-        }
-        if (done) break;
-        if (it + 1 >= WALK_CAP) {
-            capped = true;
-            break;
-        }
-    }
-    job.end(capped);
+    walk_rest(w, s, div8(s.y), 0u, job);
 }
 
 // Counts of the count pass (see k_line_count) for a queued line, per lane.
