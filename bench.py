@@ -89,23 +89,30 @@ def kernel_bytes(name: str, st: dict, batch) -> int:
         return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 12 + C * 4
     if name == "flatten_emit":
         return batch.verbs.nbytes + batch.pts.nbytes + 24 * batch.n_fills + C * 16 + L * 20
+    I = st.get("n_incs", 0)
     if name == "dda_count":
-        return L * 20 + L * 4 + R * 16
+        # line + raster read, entry and increment counts written, raster boxes
+        return L * 20 + L * 8 + R * 16
     if name == "dda_offset_scan":
-        return L * 8
+        return L * 16
     if name == "dda_emit":
-        return L * 28 + R * 24 + E * (kb + 4) + B * 32
+        # line, raster, both offsets; raster box and key base; every entry's
+        # key and value, every bin's record (16 B), every increment (8 B)
+        return L * 28 + R * 24 + E * (kb + 4) + B * 16 + I * 8
     if name == "sort_onesweep":
         return 2 * E * (kb + 4)
     if name == "sort_hist":
         return E * kb
     if name == "tile_head_scan":
         return E * (kb + 4) + T * 4
-    if name == "tile_info_wind_scan":
-        return T * 4 + T * (kb + 4 + 32) + T * 32 + R * 4
+    if name == "tile_info":
+        # head, bin count and winding of the tile (and the next tile's bin
+        # count); value and record of its head and its predecessor's; info out
+        return T * 16 + T * 2 * (4 + 16) + T * 32 + R * 8
     if name == "tile_coverage":
-        # bins: value 4 + BinRec 32 + line 16; tiles: info 32 + 68 out + 12 span
-        return B * (4 + 32 + 16) + T * (32 + 68 + 12)
+        # entries: value 4; bins: record 16; increments 8; tiles: info 32 +
+        # 68 out + 12 span slot
+        return E * 4 + B * 16 + I * 8 + T * (32 + 68 + 12)
     if name == "span_scan":
         return T * 4 + T * 8 + N * 10 + R * 4
     if name == "raster_fused":
