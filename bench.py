@@ -473,6 +473,7 @@ def bench_graph(ctx, stream, steps):
         ("glyph run, 1,000 paths", W.glyph_run(n_paths=1000, seed=2)),
         ("union of 256 cubic fills on 1024x1024", W.diff_union()),
         ("uneven mix, 1,000 paths", W.uneven_mix(n_paths=1000, seed=4)),
+        ("stroke run, 1,000 stroked paths", W.stroke_run(n_paths=1000, seed=4)),
     ]
     reps = max(30, 5 * steps)
     out = []

@@ -169,8 +169,11 @@ int ochre_gpu_last_timings(const ochre_gpu_ctx *ctx, ochre_kernel_time *out, uin
  * in the reference, which rasterizes one path per call on the CPU.
  *   - `in` holds device pointers; they and every count in `in` are fixed for
  *     the graph's life.  The values behind them may change between launches
- *     (points, transforms, verbs of the same float layout).  Stroked fills
- *     (fill_width) are not supported (OCHRE_E_INVALID).
+ *     (points, transforms, verbs of the same float layout, stroke widths).
+ *   - Stroked fills (fill_width) are captured too: the stroke stage runs in
+ *     the graph with its counts on the device, and its output is padded
+ *     with Close commands to the planned size; such a graph always runs the
+ *     general chain (results are identical to the fused kernel's).
  *   - Creation runs the batch once eagerly and plans every internal buffer at
  *     `headroom` (1 to 16) times its count.  A launch whose counts outgrow the
  *     plan (or, for a batch planned on the fused kernel, a raster that no

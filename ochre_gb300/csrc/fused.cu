@@ -177,6 +177,7 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
         uint8_t verb = V_CLOSE;
         V2 pt0 = v2(0, 0), pt1 = v2(0, 0), pt2 = v2(0, 0);
         float wgt = 0.0f;
+        float dt = 0.0f;   // a curve's parameter step, kept for the emission
         int n_lines_cmd = 0;
         V2 last = v2(0, 0), first = v2(0, 0);
         bool is_last_cmd = false;
@@ -228,8 +229,14 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
                 switch (verb) {
                 case V_MOVE: n_lines_cmd = veq(last, first) ? 0 : 1; break;
                 case V_LINE: n_lines_cmd = 1; break;
-                case V_QUAD: n_lines_cmd = (int)flatten_steps(quad_dt(last, pt0, pt1), &capped); break;
-                case V_CUBIC: n_lines_cmd = (int)flatten_steps(cubic_dt(last, pt0, pt1, pt2), &capped); break;
+                case V_QUAD:
+                    dt = quad_dt(last, pt0, pt1);
+                    n_lines_cmd = (int)flatten_steps(dt, &capped);
+                    break;
+                case V_CUBIC:
+                    dt = cubic_dt(last, pt0, pt1, pt2);
+                    n_lines_cmd = (int)flatten_steps(dt, &capped);
+                    break;
                 case V_CONIC: {
                     int n = 0;
                     conic_flatten(last, pt0, pt1, wgt, &capped, [&](V2) { n++; });
@@ -264,7 +271,6 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
             case V_MOVE: if (!veq(last, first)) put(last, first); break;
             case V_LINE: to(pt0); break;
             case V_QUAD: {
-                const float dt = quad_dt(last, pt0, pt1);
                 float t = 0.0f;
                 while (t < 1.0f && o < o_end) {
                     t = rmin(__fadd_rn(t, dt), 1.0f);
@@ -273,7 +279,6 @@ __global__ void __launch_bounds__(THREADS, fused_min_ctas(THREADS)) k_raster_fus
                 break;
             }
             case V_CUBIC: {
-                const float dt = cubic_dt(last, pt0, pt1, pt2);
                 float t = 0.0f;
                 while (t < 1.0f && o < o_end) {
                     t = rmin(__fadd_rn(t, dt), 1.0f);

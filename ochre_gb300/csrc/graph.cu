@@ -19,8 +19,18 @@
 // The graph owns a private context: the buffers its nodes point at belong to
 // it alone, so eager calls on the caller's context never move them.  The
 // batch's device pointers and counts are fixed at creation; the values behind
-// them (points, transforms, and verbs of the same float layout) may change
-// between launches.
+// them (points, transforms, verbs of the same float layout, stroke widths)
+// may change between launches.
+//
+// Stroked fills: the stroke stage (stroke.cu) is planned as well (polyline
+// and output command and float capacities, its counts on the device, a check
+// after each of its two scans), and its output is padded with Close commands
+// to the planned command count on the batch's last fill, so the chain after
+// it sees fixed command and float counts.  A trailing Close adds no line and
+// leaves the raster's closing line last, so the padding changes no output.
+// Such a plan always uses the general chain (every pad command sits on the
+// last raster, which the fused kernel's per-raster command limit would
+// refuse).
 #include "common.cuh"
 #include "internal.h"
 
@@ -53,10 +63,20 @@ uint32_t cap_of(uint64_t n, float headroom, uint64_t limit = MAX_COUNT) {
 
 // The planned chain: the stages of run_device with ctx->plan set (no host
 // read-backs), then the scalars copied to the host.
-int planned_body(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s) {
+int planned_body(ochre_gpu_ctx* ctx, const ochre_batch* batch, cudaStream_t s) {
     DevScalars* ds = dev_scalars(ctx);
     ctx->launches = 0;
-    const uint32_t R = in->n_rasters;
+    const uint32_t R = batch->n_rasters;
+    // stroked fills become plain fills first, padded to the planned command
+    // count; the chain below keeps the stroke stage's error bits
+    ochre_batch stroked = *batch;
+    const bool stroke = ctx->plan->stroke;
+    if (stroke) {
+        OCHRE_CUDA_TRY(cudaMemsetAsync(ds, 0, sizeof(DevScalars), s));
+        const int sst = stage_stroke(ctx, batch, s, &stroked);
+        if (sst != OCHRE_OK) return sst;
+    }
+    const ochre_batch* in = &stroked;
     OCHRE_CUDA_TRY(ctx->out_raster_tile_off.ensure((size_t)(R + 1) * 4));
     OCHRE_CUDA_TRY(ctx->out_raster_span_off.ensure((size_t)(R + 1) * 4));
     int st;
@@ -66,7 +86,8 @@ int planned_body(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s) {
         st = stage_fused(ctx, in, s, &handled, &T, &N);
         if (st != OCHRE_OK) return st;
     } else {
-        OCHRE_CUDA_TRY(cudaMemsetAsync(ds, 0, sizeof(DevScalars), s));
+        const size_t keep = stroke ? offsetof(DevScalars, ticket) : 0;
+        OCHRE_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(ds) + keep, 0, sizeof(DevScalars) - keep, s));
         uint32_t L = 0, bits = 0, passes = 0, T = 0, N = 0;
         uint64_t E = 0;
         st = stage_flatten(ctx, in, s, &L);
@@ -127,6 +148,14 @@ int build(ochre_graph* g) {
         if (es.key_bits <= 32 && kb > 32) kb = 32;
         p.key_bits = kb;
         p.rows = std::max<uint32_t>(host_scalars(ctx)->n_rows, 1u);
+    }
+    // stroked fills: the stroke stage's counts of the planning run
+    p.stroke = g->batch.fill_width != nullptr;
+    if (p.stroke) {
+        p.stroke_poly = cap_of(ctx->stroke_counts[0], g->headroom);
+        p.stroke_poly_floats = cap_of(ctx->stroke_counts[1], g->headroom, 0xffffffffull);
+        p.stroke_cmds = cap_of(ctx->stroke_counts[2], g->headroom);
+        p.stroke_floats = cap_of(ctx->stroke_counts[3], g->headroom, 0xffffffffull);
     }
     g->plan = p;
     ctx->plan = &g->plan;
@@ -223,11 +252,13 @@ int ochre_graph_create(ochre_gpu_ctx* ctx, const ochre_batch* in, float headroom
     *out = nullptr;
     if (in->n_rasters == 0 || in->n_rasters > MAX_RASTERS || in->n_cmds > MAX_COUNT) return in->n_rasters ? OCHRE_E_CAPACITY : OCHRE_E_INVALID;
     if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
-    if (in->fill_width != nullptr) return OCHRE_E_INVALID;   // stroked fills: eager only
     if (!(headroom >= 1.0f) || headroom > 16.0f) return OCHRE_E_INVALID;
     ochre_graph* g = new (std::nothrow) ochre_graph();
     if (!g) return OCHRE_E_NOMEM;
-    int st = ochre_gpu_create(&g->ctx, ctx->device, ctx->flags & (OCHRE_CTX_WANT_COV | OCHRE_CTX_CHAIN_ONLY));
+    // stroked fills are planned on the general chain (their padded output
+    // puts every pad command on one raster)
+    const uint32_t chain = in->fill_width != nullptr ? OCHRE_CTX_CHAIN_ONLY : 0u;
+    int st = ochre_gpu_create(&g->ctx, ctx->device, (ctx->flags & (OCHRE_CTX_WANT_COV | OCHRE_CTX_CHAIN_ONLY)) | chain);
     if (st != OCHRE_OK) {
         delete g;
         return st;

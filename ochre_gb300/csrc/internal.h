@@ -97,6 +97,14 @@ struct GraphPlan {
     uint32_t key_bits;   // sort key bits; keys are 64-bit above 32
     uint32_t incs;       // general chain: stored pixel-cell increments
     uint32_t rows;       // tile rows of the planning run (coverage form and grid)
+    // Stroked fills (planned on the general chain): polyline commands and
+    // floats, output commands and floats of the stroke stage.  Its units
+    // never outnumber the polyline commands.  The output is padded to
+    // stroke_cmds with Close commands (no lines) on the batch's last fill,
+    // so the chain after it runs on fixed command and float counts.
+    bool stroke;
+    uint32_t stroke_poly, stroke_poly_floats;
+    uint32_t stroke_cmds, stroke_floats;
 };
 
 // Entry value tag for tile-row crossings: 1 | raster (23 bits) | sign byte.
@@ -208,6 +216,9 @@ struct ochre_gpu_ctx {
     ochre::DevBuf sk_cmd_foff, sk_cmd_mv, sk_cmd_ep, sk_poly_off, sk_poly_foff, sk_pverbs, sk_ppts, sk_pfoff,
         sk_pfill_off, sk_first_close, sk_unit_start, sk_out_off, sk_out_foff, sk_unit_fill, sk_overbs, sk_opts,
         sk_ofill_off, sk_oflags, in_fill_width;
+    // the last eager stroke stage's counts (polyline commands and floats,
+    // output commands and floats): a CUDA graph's plan sizes from them
+    uint32_t stroke_counts[4] = {0, 0, 0, 0};
 
     // Test hooks (ochre_gpu_set_tunable "test_*"), used by the next run only:
     // the poll limit of its bounded waits (log2; 0: the default), and, on the

@@ -96,10 +96,10 @@ struct PairIn {
 // One thread per item: a count functor with a long serial walk per item runs
 // at full occupancy here, and the scan over the stored counts stays light.
 template <class Count>
-__global__ void __launch_bounds__(128) k_pair_count(uint64_t n, Count count, uint32_t* __restrict__ out_n,
-                                                    uint32_t* __restrict__ out_nf) {
+__global__ void __launch_bounds__(128) k_pair_count(uint64_t n, const uint32_t* n_dev, Count count,
+                                                    uint32_t* __restrict__ out_n, uint32_t* __restrict__ out_nf) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= dev_count(n, n_dev)) return;
     const Pair p = count(i);
     out_n[i] = p.n;
     out_nf[i] = p.nf;
@@ -109,7 +109,7 @@ __global__ void k_poly_emit(const uint8_t* __restrict__ verbs, const float* __re
                             const uint32_t* __restrict__ fill_off, uint32_t n_fills, const uint8_t* __restrict__ flags,
                             uint64_t n_cmds, const uint32_t* __restrict__ cmd_foff, const uint32_t* __restrict__ cmd_ep,
                             const uint32_t* __restrict__ poly_off, const uint32_t* __restrict__ poly_foff,
-                            uint8_t* __restrict__ pverbs, float* __restrict__ ppts) {
+                            uint8_t* __restrict__ pverbs, float* __restrict__ ppts, uint32_t p_cap, uint32_t pf_cap) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n_cmds) return;
     const uint32_t c = (uint32_t)i;
@@ -117,25 +117,33 @@ __global__ void k_poly_emit(const uint8_t* __restrict__ verbs, const float* __re
     const uint32_t f = upper_bound_u32(fill_off, n_fills + 1, c) - 1u;
     uint32_t o = poly_off[c], fo = poly_foff[c];
     const float* fp = pts + cmd_foff[c];
+    // writes stay below the buffers' capacities (a planned run whose
+    // polyline outgrew them is flagged by the check after the scan)
+    auto verb = [&](uint32_t at, uint8_t x) {
+        if (at < p_cap) pverbs[at] = x;
+    };
+    auto flt = [&](uint32_t at, float x) {
+        if (at < pf_cap) ppts[at] = x;
+    };
     if (!is_stroke(flags, f)) {
-        pverbs[o] = v;
-        for (uint32_t k = 0; k < floats_per_verb(v); k++) ppts[fo + k] = __ldg(fp + k);
+        verb(o, v);
+        for (uint32_t k = 0; k < floats_per_verb(v); k++) flt(fo + k, __ldg(fp + k));
         return;
     }
     auto line = [&](V2 p) {
-        pverbs[o++] = V_LINE;
-        ppts[fo++] = p.x;
-        ppts[fo++] = p.y;
+        verb(o++, V_LINE);
+        flt(fo++, p.x);
+        flt(fo++, p.y);
     };
     switch (v) {
     case V_MOVE:
     case V_LINE:
-        pverbs[o] = v;
-        ppts[fo] = __ldg(fp);
-        ppts[fo + 1] = __ldg(fp + 1);
+        verb(o, v);
+        flt(fo, __ldg(fp));
+        flt(fo + 1, __ldg(fp + 1));
         break;
     case V_CLOSE:
-        pverbs[o] = V_CLOSE;
+        verb(o, V_CLOSE);
         break;
     case V_QUAD: {
         // path.rs:49-58 in path space
@@ -207,21 +215,23 @@ struct OffOutU32 {
     __device__ __forceinline__ void operator()(uint64_t i, uint32_t ex, uint32_t) const { off[i] = ex; }
 };
 
-__global__ void k_first_close(const uint8_t* __restrict__ pverbs, uint64_t n_poly, const uint32_t* __restrict__ pfill_off,
-                              uint32_t n_fills, const uint8_t* __restrict__ flags, uint32_t* __restrict__ first_close) {
+__global__ void k_first_close(const uint8_t* __restrict__ pverbs, uint64_t n_poly, const uint32_t* n_dev,
+                              const uint32_t* __restrict__ pfill_off, uint32_t n_fills, const uint8_t* __restrict__ flags,
+                              uint32_t* __restrict__ first_close) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n_poly || pverbs[i] != V_CLOSE) return;
+    if (i >= dev_count(n_poly, n_dev) || pverbs[i] != V_CLOSE) return;
     const uint32_t f = upper_bound_u32(pfill_off, n_fills + 1, (uint32_t)i) - 1u;
     if (is_stroke(flags, f)) atomicMin(first_close + f, (uint32_t)i);
 }
 
 __global__ void k_fill_init(uint32_t* __restrict__ first_close, const uint32_t* __restrict__ fill_off,
-                            const uint32_t* __restrict__ poly_off, uint64_t n_cmds, uint32_t n_poly, uint32_t n_fills,
-                            uint32_t* __restrict__ pfill_off) {
+                            const uint32_t* __restrict__ poly_off, uint64_t n_cmds, uint32_t n_poly,
+                            const uint32_t* n_poly_dev, uint32_t n_fills, uint32_t* __restrict__ pfill_off) {
     const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f > n_fills) return;
+    const uint32_t np = (uint32_t)dev_count(n_poly, n_poly_dev);
     const uint32_t c = __ldg(fill_off + f);
-    pfill_off[f] = c < n_cmds ? poly_off[c] : n_poly;
+    pfill_off[f] = c < n_cmds ? min(poly_off[c], np) : np;
     if (f < n_fills) first_close[f] = 0xffffffffu;
 }
 
@@ -312,14 +322,15 @@ struct OutCount {
     }
 };
 
-__global__ void k_out_emit(uint32_t n_units, const uint32_t* __restrict__ unit_start, const uint8_t* __restrict__ pverbs,
+__global__ void k_out_emit(uint32_t n_units, const uint32_t* n_dev, const uint32_t* __restrict__ unit_start,
+                           const uint8_t* __restrict__ pverbs,
                            const float* __restrict__ ppts, const uint32_t* __restrict__ poly_foff_of,
                            const uint32_t* __restrict__ pfill_off, uint32_t n_fills, const uint8_t* __restrict__ flags,
                            const uint32_t* __restrict__ first_close, const float* __restrict__ width,
                            const uint32_t* __restrict__ out_off, const uint32_t* __restrict__ out_foff,
                            uint8_t* __restrict__ overbs, float* __restrict__ opts, uint32_t* __restrict__ unit_fill) {
     const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= n_units) return;
+    if (u >= dev_count(n_units, n_dev)) return;
     const UnitGeom g = unit_geom(u, unit_start, pverbs, pfill_off, n_fills, flags, first_close);
     unit_fill[u] = g.fill;
     uint32_t o = out_off[u], fo = out_foff[u];
@@ -353,52 +364,80 @@ __global__ void k_out_emit(uint32_t n_units, const uint32_t* __restrict__ unit_s
     overbs[o++] = V_CLOSE;
 }
 
-__global__ void k_out_fill_off(const uint32_t* __restrict__ unit_fill, uint32_t n_units, const uint32_t* __restrict__ out_off,
-                               uint32_t total, uint32_t n_fills, uint32_t* __restrict__ ofill_off,
+// A planned run (pad_end > 0) ends the last fill at pad_end: the output
+// commands from the true total up to it are Close commands.
+__global__ void k_out_fill_off(const uint32_t* __restrict__ unit_fill, uint32_t n_units, const uint32_t* units_dev,
+                               const uint32_t* __restrict__ out_off, uint32_t total, const uint32_t* total_dev,
+                               uint32_t pad_end, uint32_t n_fills, uint32_t* __restrict__ ofill_off,
                                const uint8_t* __restrict__ flags, uint8_t* __restrict__ oflags) {
     const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f > n_fills) return;
+    n_units = (uint32_t)dev_count(n_units, units_dev);
+    total = (uint32_t)dev_count(total, total_dev);
     // first unit of fill >= f
     uint32_t lo = 0, hi = n_units;
     while (lo < hi) {
         const uint32_t mid = (lo + hi) >> 1;
         if (unit_fill[mid] < f) lo = mid + 1; else hi = mid;
     }
-    ofill_off[f] = lo < n_units ? out_off[lo] : total;
+    ofill_off[f] = f == n_fills && pad_end ? pad_end : lo < n_units ? min(out_off[lo], total) : total;
     if (f < n_fills) oflags[f] = flags ? (uint8_t)(__ldg(flags + f) & ~OCHRE_FILL_STROKE) : 0u;
 }
 
+// A planned run (CUDA graph): a count pair above its capacities zeroes the
+// pair and the count that bounds the next kernels, and flags ERR_CAPACITY,
+// so no later kernel of the run reads or writes past a buffer (the graph
+// then re-plans).
+__global__ void k_stroke_cap(uint32_t* a, uint32_t cap_a, uint32_t* b, uint32_t cap_b, uint32_t* also,
+                             uint32_t* err) {
+    if (*a > cap_a || *b > cap_b) {
+        *a = 0u;
+        *b = 0u;
+        *also = 0u;
+        atomicOr(err, ERR_CAPACITY);
+    }
+}
+
+// Eager: sizes read back at four points.  Planned (ctx->plan->stroke, inside
+// a CUDA graph): no read-backs; buffers at the plan's capacities, counts on
+// the device, and the output padded with Close commands to the planned
+// command count (the caller zeroed the device scalars).
 int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochre_batch* out) {
     *out = *in;
     out->fill_width = nullptr;
     if (!in->fill_width || !in->fill_flags || in->n_cmds == 0 || in->n_fills == 0) return OCHRE_OK;
+    const GraphPlan* plan = ctx->plan != nullptr && ctx->plan->stroke ? ctx->plan : nullptr;
     DevScalars* ds = dev_scalars(ctx);
     const uint64_t n = in->n_cmds;
     const uint32_t F = in->n_fills;
+    int st = OCHRE_OK;
     // 1. command scan of the input
     OCHRE_CUDA_TRY(ctx->sk_cmd_foff.ensure(n * 4));
     OCHRE_CUDA_TRY(ctx->sk_cmd_mv.ensure(n * 4));
     OCHRE_CUDA_TRY(ctx->sk_cmd_ep.ensure(n * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n) * sizeof(ScanStatus<CmdScan>)));
-    OCHRE_CUDA_TRY(reset_scalars(ctx, s));
+    if (!plan) OCHRE_CUDA_TRY(reset_scalars(ctx, s));
     OCHRE_LAUNCH(ctx, "stroke_cmd_scan", s, OCHRE_CUDA_TRY(launch_scan<CmdScan>(
         n, CmdIn{in->verbs, &ds->err},
         CmdOut{ctx->sk_cmd_foff.as<uint32_t>(), ctx->sk_cmd_mv.as<uint32_t>(), ctx->sk_cmd_ep.as<uint32_t>()},
         OpCmd{}, CmdScan{0, 0, 0}, ctx->scan_status.p, &ds->ticket, reinterpret_cast<CmdScan*>(&ds->n_floats),
         &ds->err, s)));
-    int st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    if (host_scalars(ctx)->n_floats > in->n_floats) return OCHRE_E_INVALID;
-    st = check_device_error(ctx);
-    if (st != OCHRE_OK) return st;
+    if (!plan) {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        if (host_scalars(ctx)->n_floats > in->n_floats) return OCHRE_E_INVALID;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
+    }
     // 2. polyline
     wait_inputs(ctx, s);   // path-space flatten counts read points
     OCHRE_CUDA_TRY(ctx->sk_poly_off.ensure((n + 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_poly_foff.ensure((n + 1) * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(n) * sizeof(ScanStatus<Pair>)));
     OCHRE_LAUNCH(ctx, "stroke_poly_count", s, k_pair_count<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(
-        n, PolyCount{in->verbs, in->pts, in->fill_cmd_off, F, in->fill_flags, ctx->sk_cmd_foff.as<uint32_t>(),
-                     ctx->sk_cmd_ep.as<uint32_t>(), &ds->err},
+        n, nullptr,
+        PolyCount{in->verbs, in->pts, in->fill_cmd_off, F, in->fill_flags, ctx->sk_cmd_foff.as<uint32_t>(),
+                  ctx->sk_cmd_ep.as<uint32_t>(), &ds->err},
         ctx->sk_poly_off.as<uint32_t>(), ctx->sk_poly_foff.as<uint32_t>()));
     OCHRE_CUDA_TRY(cudaGetLastError());
     OCHRE_LAUNCH(ctx, "stroke_poly_scan", s, OCHRE_CUDA_TRY(launch_scan<Pair>(
@@ -406,12 +445,25 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
         PairOut{ctx->sk_poly_off.as<uint32_t>(), ctx->sk_poly_foff.as<uint32_t>()}, OpPair{}, Pair{0u, 0u},
         ctx->scan_status.p, &ds->ticket, reinterpret_cast<Pair*>(&ds->n_lines), &ds->err, s)));
     // (n_lines, n_line_ent) hold the polyline totals here; the fill chain resets them
-    st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    st = check_device_error(ctx);
-    if (st != OCHRE_OK) return st;
-    const uint32_t P = host_scalars(ctx)->n_lines, PF = host_scalars(ctx)->n_line_ent;
-    if (P > MAX_COUNT) return OCHRE_E_CAPACITY;
+    uint32_t P, PF;   // polyline commands and floats (planned: the capacities)
+    if (plan) {
+        P = plan->stroke_poly;
+        PF = plan->stroke_poly_floats;
+        OCHRE_LAUNCH(ctx, "plan_stroke_poly", s,
+                     k_stroke_cap<<<1, 1, 0, s>>>(&ds->n_lines, P, &ds->n_line_ent, PF, &ds->n_tiles, &ds->err));
+        OCHRE_CUDA_TRY(cudaGetLastError());
+    } else {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
+        P = host_scalars(ctx)->n_lines;
+        PF = host_scalars(ctx)->n_line_ent;
+        if (P > MAX_COUNT) return OCHRE_E_CAPACITY;
+        ctx->stroke_counts[0] = P;
+        ctx->stroke_counts[1] = PF;
+    }
+    const uint32_t* p_dev = plan ? &ds->n_lines : nullptr;
     OCHRE_CUDA_TRY(ctx->sk_pverbs.ensure(P ? P : 1));
     OCHRE_CUDA_TRY(ctx->sk_ppts.ensure((size_t)(PF ? PF : 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_pfoff.ensure((size_t)(P ? P : 1) * 4));
@@ -421,12 +473,13 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     OCHRE_LAUNCH(ctx, "stroke_poly_emit", s, k_poly_emit<<<cb, 256, 0, s>>>(
         in->verbs, in->pts, in->fill_cmd_off, F, in->fill_flags, n, ctx->sk_cmd_foff.as<uint32_t>(),
         ctx->sk_cmd_ep.as<uint32_t>(), ctx->sk_poly_off.as<uint32_t>(), ctx->sk_poly_foff.as<uint32_t>(),
-        ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>()));
+        ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(), P, PF));
     OCHRE_LAUNCH(ctx, "stroke_fill_init", s, k_fill_init<<<(F + 256) / 256, 256, 0, s>>>(
-        ctx->sk_first_close.as<uint32_t>(), in->fill_cmd_off, ctx->sk_poly_off.as<uint32_t>(), n, P, F,
+        ctx->sk_first_close.as<uint32_t>(), in->fill_cmd_off, ctx->sk_poly_off.as<uint32_t>(), n, P, p_dev, F,
         ctx->sk_pfill_off.as<uint32_t>()));
     OCHRE_CUDA_TRY(cudaGetLastError());
     if (P == 0) {
+        ctx->stroke_counts[2] = ctx->stroke_counts[3] = 0;
         out->n_cmds = 0;
         out->n_floats = 0;
         OCHRE_CUDA_TRY(ctx->sk_ofill_off.ensure(((size_t)F + 1) * 4));
@@ -438,9 +491,9 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(P) * sizeof(ScanStatus<uint32_t>)));
     OCHRE_LAUNCH(ctx, "stroke_pfoff_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
         P, PolyFloats{ctx->sk_pverbs.as<uint8_t>()}, OffOutU32{ctx->sk_pfoff.as<uint32_t>()}, OpSumU32{}, 0u,
-        ctx->scan_status.p, &ds->ticket, static_cast<uint32_t*>(nullptr), &ds->err, s)));
+        ctx->scan_status.p, &ds->ticket, static_cast<uint32_t*>(nullptr), &ds->err, s, p_dev)));
     OCHRE_LAUNCH(ctx, "stroke_first_close", s, k_first_close<<<(P + 255) / 256, 256, 0, s>>>(
-        ctx->sk_pverbs.as<uint8_t>(), P, ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
+        ctx->sk_pverbs.as<uint8_t>(), P, p_dev, ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
         ctx->sk_first_close.as<uint32_t>()));
     OCHRE_CUDA_TRY(cudaGetLastError());
     // 3. units
@@ -448,51 +501,72 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     OCHRE_LAUNCH(ctx, "stroke_unit_scan", s, OCHRE_CUDA_TRY(launch_scan<uint32_t>(
         P, UnitIn{ctx->sk_pverbs.as<uint8_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags},
         UnitOut{ctx->sk_unit_start.as<uint32_t>()}, OpSumU32{}, 0u, ctx->scan_status.p, &ds->ticket,
-        &ds->n_tiles, &ds->err, s)));
-    st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    st = check_device_error(ctx);
-    if (st != OCHRE_OK) return st;
-    const uint32_t U = host_scalars(ctx)->n_tiles;
+        &ds->n_tiles, &ds->err, s, p_dev)));
+    uint32_t U;   // units (planned: at most P, the count stays on the device)
+    if (plan) {
+        U = P;
+    } else {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
+        U = host_scalars(ctx)->n_tiles;
+    }
+    const uint32_t* u_dev = plan ? &ds->n_tiles : nullptr;
     // 4. output sizes and emission
     OCHRE_CUDA_TRY(ctx->sk_out_off.ensure(((size_t)U + 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_out_foff.ensure(((size_t)U + 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_unit_fill.ensure(((size_t)U + 1) * 4));
     OCHRE_CUDA_TRY(ctx->scan_status.ensure(scan_tiles(U ? U : 1) * sizeof(ScanStatus<Pair>)));
+    // the output totals: a scan that covers no unit writes none
+    OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_lines, 0, 8, s));
     if (U) {
         OCHRE_LAUNCH(ctx, "stroke_out_count", s, k_pair_count<<<(U + 127) / 128, 128, 0, s>>>(
-            U, OutCount{ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
-                        ctx->sk_pfoff.as<uint32_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
-                        ctx->sk_first_close.as<uint32_t>(), in->fill_width},
+            U, u_dev,
+            OutCount{ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
+                     ctx->sk_pfoff.as<uint32_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
+                     ctx->sk_first_close.as<uint32_t>(), in->fill_width},
             ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()));
         OCHRE_CUDA_TRY(cudaGetLastError());
         OCHRE_LAUNCH(ctx, "stroke_out_scan", s, OCHRE_CUDA_TRY(launch_scan<Pair>(
             U, PairIn{ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()},
             PairOut{ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()}, OpPair{}, Pair{0u, 0u},
-            ctx->scan_status.p, &ds->ticket, reinterpret_cast<Pair*>(&ds->n_lines), &ds->err, s)));
-    } else {
-        OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_lines, 0, 8, s));
+            ctx->scan_status.p, &ds->ticket, reinterpret_cast<Pair*>(&ds->n_lines), &ds->err, s, u_dev)));
     }
-    st = read_scalars(ctx, s);
-    if (st != OCHRE_OK) return st;
-    st = check_device_error(ctx);
-    if (st != OCHRE_OK) return st;
-    const uint32_t ON = host_scalars(ctx)->n_lines, OF = host_scalars(ctx)->n_line_ent;
-    if (ON > MAX_COUNT) return OCHRE_E_CAPACITY;
+    uint32_t ON, OF;   // output commands and floats (planned: the capacities)
+    if (plan) {
+        ON = plan->stroke_cmds;
+        OF = plan->stroke_floats;
+        OCHRE_LAUNCH(ctx, "plan_stroke_out", s,
+                     k_stroke_cap<<<1, 1, 0, s>>>(&ds->n_lines, ON, &ds->n_line_ent, OF, &ds->n_tiles, &ds->err));
+        OCHRE_CUDA_TRY(cudaGetLastError());
+    } else {
+        st = read_scalars(ctx, s);
+        if (st != OCHRE_OK) return st;
+        st = check_device_error(ctx);
+        if (st != OCHRE_OK) return st;
+        ON = host_scalars(ctx)->n_lines;
+        OF = host_scalars(ctx)->n_line_ent;
+        if (ON > MAX_COUNT) return OCHRE_E_CAPACITY;
+        ctx->stroke_counts[2] = ON;
+        ctx->stroke_counts[3] = OF;
+    }
     OCHRE_CUDA_TRY(ctx->sk_overbs.ensure(ON ? ON : 1));
     OCHRE_CUDA_TRY(ctx->sk_opts.ensure((size_t)(OF ? OF : 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_ofill_off.ensure(((size_t)F + 1) * 4));
     OCHRE_CUDA_TRY(ctx->sk_oflags.ensure(F));
+    // planned: every output command past the true total is a Close
+    if (plan) OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->sk_overbs.p, V_CLOSE, ON, s));
     if (U)
         OCHRE_LAUNCH(ctx, "stroke_out_emit", s, k_out_emit<<<(U + 127) / 128, 128, 0, s>>>(
-            U, ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
+            U, u_dev, ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
             ctx->sk_pfoff.as<uint32_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
             ctx->sk_first_close.as<uint32_t>(), in->fill_width, ctx->sk_out_off.as<uint32_t>(),
             ctx->sk_out_foff.as<uint32_t>(), ctx->sk_overbs.as<uint8_t>(), ctx->sk_opts.as<float>(),
             ctx->sk_unit_fill.as<uint32_t>()));
     OCHRE_LAUNCH(ctx, "stroke_fill_off", s, k_out_fill_off<<<(F + 256) / 256, 256, 0, s>>>(
-        ctx->sk_unit_fill.as<uint32_t>(), U, ctx->sk_out_off.as<uint32_t>(), ON, F, ctx->sk_ofill_off.as<uint32_t>(),
-        in->fill_flags, ctx->sk_oflags.as<uint8_t>()));
+        ctx->sk_unit_fill.as<uint32_t>(), U, u_dev, ctx->sk_out_off.as<uint32_t>(), ON, plan ? &ds->n_lines : nullptr,
+        plan ? ON : 0u, F, ctx->sk_ofill_off.as<uint32_t>(), in->fill_flags, ctx->sk_oflags.as<uint8_t>()));
     OCHRE_CUDA_TRY(cudaGetLastError());
     out->verbs = ctx->sk_overbs.as<uint8_t>();
     out->n_cmds = ON;

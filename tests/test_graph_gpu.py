@@ -133,11 +133,77 @@ def test_fused_plan_falls_back_to_chain(gpu_ctx):
         g.close()
 
 
-def test_graph_rejects_strokes(gpu_ctx):
-    from ochre_gb300 import DeviceBatch, OchreError
-    b = W.stroke_run(n_paths=10)
-    with pytest.raises(OchreError):
-        gpu_ctx.graph(DeviceBatch(b))
+def _set(dev_tensor, host_array):
+    dev_tensor.copy_(dev_tensor.new_tensor(np.ascontiguousarray(host_array).reshape(-1)))
+
+
+@pytest.mark.parametrize("ctx_name", ["gpu_ctx", "gpu_ctx_chain"])
+def test_stroke_graph_matches_oracle_and_eager(request, ctx_name):
+    """Stroked fills (Rasterizer::stroke) replayed from a graph: the stroke
+    stage runs in the graph with its counts on the device and its output
+    padded with Close commands; results equal the oracle's and the eager
+    call's, on every replay."""
+    from ochre_gb300 import DeviceBatch
+    ctx = request.getfixturevalue(ctx_name)
+    b = W.stroke_run(n_paths=400, seed=11)
+    db = DeviceBatch(b)
+    eager = ctx.device_result_to_numpy(ctx.rasterize_device(db), b.n_rasters)
+    ref = oracle.run(b, threads=8)
+    g = ctx.graph(db)
+    try:
+        assert not g.info()["fused"]
+        for _ in range(3):
+            got = g.rasterize()
+            compare(got, ref, b.n_rasters)
+            _same_as_eager(got, eager)
+        assert g.info()["replans"] == 0
+    finally:
+        g.close()
+
+
+def test_stroke_graph_new_widths_and_points(gpu_ctx_chain):
+    """Stroke widths and points rewritten in place between launches, within
+    the plan's headroom: the same graph strokes and fills the new geometry
+    (the stroke stage's output counts change with the joins)."""
+    from ochre_gb300 import DeviceBatch
+    b = W.stroke_run(n_paths=300, seed=12)
+    db = DeviceBatch(b)
+    g = gpu_ctx_chain.graph(db, headroom=2.0)
+    try:
+        _check(gpu_ctx_chain, g, b)
+        for k in (0.6, 1.4):
+            b2 = dataclasses.replace(b, fill_width=(b.fill_width * np.float32(k)).astype(np.float32))
+            _set(db.fill_width, b2.fill_width)
+            _check(gpu_ctx_chain, g, b2)
+        b3 = dataclasses.replace(b, pts=(b.pts * np.float32(1.2)).astype(np.float32))
+        _set(db.fill_width, b.fill_width)
+        _set(db.pts, b3.pts)
+        _check(gpu_ctx_chain, g, b3)
+        assert g.info()["replans"] == 0
+    finally:
+        g.close()
+
+
+def test_stroke_graph_outgrown_plan_replans(gpu_ctx_chain):
+    """Path-space points scaled up: the curves flatten into more polyline
+    segments than the stroke stage's plan holds (checked on the device after
+    its scans); the launch re-plans from an eager run and replays, exact."""
+    from ochre_gb300 import DeviceBatch
+    b = W.stroke_run(n_paths=300, seed=13)
+    db = DeviceBatch(b)
+    g = gpu_ctx_chain.graph(db, headroom=1.0)
+    try:
+        _check(gpu_ctx_chain, g, b)
+        b2 = dataclasses.replace(b, pts=(b.pts * np.float32(9.0)).astype(np.float32),
+                                 fill_xf=_scaled(b, 1.0 / 9.0).fill_xf)
+        _set(db.pts, b2.pts)
+        _set(db.fill_xf, b2.fill_xf)
+        _check(gpu_ctx_chain, g, b2)
+        assert g.info()["replans"] == 1
+        _check(gpu_ctx_chain, g, b2)
+        assert g.info()["replans"] == 1
+    finally:
+        g.close()
 
 
 def test_graph_with_coverage_output():
