@@ -391,6 +391,77 @@ def bench_uneven(ctx, stream, flush, steps, peak):
     }
 
 
+def bench_configs(ctx, stream, flush, peak, glyphs, scenes):
+    """Every seeded configuration rasterized (fill -> finish: tiles and spans,
+    the reference's output) three ways: on the GPU in one batched call
+    (device-resident inputs, L2 flushed, CUDA events), through the plain
+    general chain once per raster (a sample, host wall clock per call), and
+    by the CPU port (oracle/ochre_oracle.c) on all host cores and on one
+    (bounded samples, stated per row)."""
+    import numpy as np
+    import torch
+    import oracle
+    from ochre_gb300 import DeviceBatch, batch as B, workloads as W
+    sp = stream.cuda_stream
+    cores = os.cpu_count() or 1
+    rows = []
+    cfgs = [
+        ("cubic_boxes", "1,000 closed paths x 16 cubics in 512^2 boxes on 2048^2", W.cubic_boxes(), 200, 200),
+        ("glyph_run", "100,000 glyph-like paths, 8-40 quadratics", glyphs, 1000, 10000),
+        ("uneven_mix", "20,000 paths, lognormal segment counts (median 32, 4-20,000)", W.uneven_mix(), 200, 100),
+        ("diff_union", "256 paths x 32 cubics in one raster, 1024^2", W.diff_union(), 1, 1),
+        ("diff_scenes", f"{scenes.n_rasters:,} scenes of 512^2, 8-512 paths each", scenes, 64, 16),
+    ]
+    rng = np.random.default_rng(0)
+    for name, what, b, n_plain, n_one in cfgs:
+        db = DeviceBatch(b, ctx.device)
+        for _ in range(2):
+            ctx.rasterize_device(db, sp)
+        st = ctx.stats()
+        ms = _event_ms(lambda: ctx.rasterize_device(db, sp), stream, flush, 5)
+        # the plain chain once per raster, on a sample of the rasters
+        idx = np.sort(rng.choice(b.n_rasters, min(n_plain, b.n_rasters), replace=False))
+        subs = [DeviceBatch(B.subset(b, [int(i)]), ctx.device) for i in idx]
+        ctx.set_chain_only(True)
+        for d in subs[:5]:
+            ctx.rasterize_device(d, sp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for d in subs:
+            ctx.rasterize_device(d, sp)
+        torch.cuda.synchronize()
+        plain_s = (time.perf_counter() - t0) / len(subs)
+        ctx.set_chain_only(False)
+        del subs, db
+        # the CPU port: the whole configuration on every core, a prefix on one
+        with np.errstate(all="ignore"):
+            t0 = time.perf_counter()
+            oracle.run(b, threads=cores)
+            cpu_all_s = time.perf_counter() - t0
+            one = B.subset(b, list(range(min(n_one, b.n_rasters))))
+            t0 = time.perf_counter()
+            oracle.run(one, threads=1)
+            cpu_one_s = time.perf_counter() - t0
+        comp = b.input_bytes() + output_bytes(st["n_tiles"], st["n_spans"], b.n_rasters)
+        rows.append({
+            "config": name, "workload": what, "rasters": b.n_rasters, "tiles": st["n_tiles"], "spans": st["n_spans"],
+            "path": "fused" if st.get("fused") else "chain",
+            "gpu_batched": {"rasters_per_s": b.n_rasters / (ms / 1e3), "tiles_per_s": st["n_tiles"] / (ms / 1e3),
+                            "ms_per_call": ms},
+            "gpu_plain_per_raster": {"rasters_per_s": 1.0 / plain_s, "sample_rasters": len(idx)},
+            "batched_over_plain": (b.n_rasters / (ms / 1e3)) * plain_s,
+            "cpu_all_cores": {"rasters_per_s": b.n_rasters / cpu_all_s, "cores": cores,
+                              "sample": f"all {b.n_rasters} rasters, once"},
+            "cpu_one_core": {"rasters_per_s": one.n_rasters / cpu_one_s, "sample": f"the first {one.n_rasters} rasters"},
+            "gpu_over_cpu_all_cores": cpu_all_s / (ms / 1e3),
+            "path_roofline": {"compulsory_bytes": comp, "achieved_gbs": comp / (ms / 1e3) / 1e9,
+                              "frac": comp / (ms / 1e3) / 1e9 / peak},
+        })
+    return {"note": "rasters = paths (scenes for diff_scenes); GPU batched by CUDA events with device-resident "
+                    "inputs and L2 flushed; plain per-raster and CPU by host wall clock; cpu_model "
+                    + _cpu_model(), "rows": rows}
+
+
 def bench_stroke(ctx, stream, flush, steps):
     """Stroked paths (Rasterizer::stroke): 20,000 rasters of 2-24 mixed
     segments, widths 0.5-8 px; the device stroke stage plus the fill path,
@@ -508,7 +579,7 @@ def bench_graph(ctx, stream, steps):
     return {"timing": f"host wall clock, mean of {reps} calls after 3 warm-up calls", "cases": out}
 
 
-def bench_differentiable(ctx, stream, flush, steps, n_scenes):
+def bench_differentiable(ctx, stream, flush, steps, n_scenes, scenes=None):
     """Forward (coverage render + L2 loss) and forward + backward scenes/s on
     the single-raster union (256 paths x 32 cubics, 1024^2) and on batched
     scenes (n_scenes x 512^2), with a gradient check against the FP64
@@ -524,7 +595,7 @@ def bench_differentiable(ctx, stream, flush, steps, n_scenes):
     sp = stream.cuda_stream
     cases = [("diff_union", W.diff_union(), W.diff_union(perturb=2.0), 1024, 1024)]
     t0 = time.time()
-    sc = W.diff_scenes(n_scenes=n_scenes)
+    sc = scenes if scenes is not None else W.diff_scenes(n_scenes=n_scenes)
     pert = copy.copy(sc)
     pert.pts = (sc.pts + np.random.default_rng(4).normal(0, 2.0, sc.pts.shape)).astype(np.float32)
     gen_s = time.time() - t0
@@ -865,7 +936,14 @@ def run_ours(args, ws, rank, local):
     if not args.no_extensions:
         extensions["uneven_mix"] = bench_uneven(ctx, stream, flush, args.steps,
                                                 float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])))
-        extensions["differentiable"] = bench_differentiable(ctx, stream, flush, args.steps, args.diff_scenes)
+        t_gen = time.time()
+        from ochre_gb300 import workloads as W
+        scenes = W.diff_scenes(n_scenes=args.diff_scenes)
+        t_gen = time.time() - t_gen
+        extensions["differentiable"] = bench_differentiable(ctx, stream, flush, args.steps, args.diff_scenes, scenes)
+        extensions["differentiable"]["diff_scenes"]["generation_s"] = t_gen
+        extensions["configs"] = bench_configs(ctx, stream, flush, float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])),
+                                              batch, scenes)
         extensions["stroke"] = bench_stroke(ctx, stream, flush, args.steps)
         extensions["graph"] = bench_graph(ctx, stream, args.steps)
         extensions["composite"] = bench_composite(ctx, stream, flush, args.steps)
@@ -925,6 +1003,7 @@ def run_ours(args, ws, rank, local):
         "stroke": extensions.get("stroke"),
         "graph": extensions.get("graph"),
         "composite": extensions.get("composite"),
+        "configs": extensions.get("configs"),
         "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s,
                 "note": "pinned host inputs: points read by the kernels in place over the host link, the "
