@@ -56,6 +56,9 @@ def compare(gpu: dict, ref: dict, n_rasters: int) -> dict:
         "diff_fraction": n_diff / ra_all.size if ra_all.size else 0.0,
     }
     if "tile_cov" in gpu and "tile_cov" in ref:
-        e = np.abs(gpu["tile_cov"].astype(np.float64) - ref["tile_cov"].astype(np.float64))
+        r = ref["tile_cov"].astype(np.float64)
+        e = np.abs(gpu["tile_cov"].astype(np.float64) - r)
         stats["cov_max_abs_vs_oracle_f32"] = float(e.max()) if e.size else 0.0
+        # relative to |S| where it exceeds 1 (the f32 sums' rounding scales with them)
+        stats["cov_max_rel_vs_oracle_f32"] = float((e / np.maximum(1.0, np.abs(r))).max()) if e.size else 0.0
     return stats

@@ -63,10 +63,36 @@ CASES = {
 }
 
 
-def edge_batch():
+# Rasters at the i16 limits (rasterizer.rs:78-79, 108-116): `floor(p) as i16`
+# saturates at 32767 / -32768 and the walk's `x += x_dir` wraps (release-build
+# integer arithmetic), so a walk that
+# passes 32767 continues at -32768 (tiles at both ends of the i16 range, a span
+# 65,520 px wide, a y wrap covering 16,390 tiles).  A batch of their own: none
+# of them fits the fused kernel's grid, and the dense-canvas tests keep to
+# small coordinates.
+I16_CASES = {
+    "i16_wrap_x": [([MOVE, LINE, LINE, LINE, CLOSE],
+                    [32760.5, 10.5, 32775.5, 14.5, 32775.5, 30.5, 32760.5, 30.5], IDENTITY)],
+    "i16_wrap_neg_x": [([MOVE, LINE, LINE, CLOSE], [-32765.5, 3.5, -32775.0, 9.0, -32760.0, 20.0], IDENTITY)],
+    "i16_wrap_y": [([MOVE, QUADRATIC, LINE, CLOSE],
+                    [100.25, 32758.0, 140.0, 32790.0, 120.0, 32762.5, 90.0, 32750.0], IDENTITY)],
+    "i16_far_both": [([MOVE, LINE, LINE, CLOSE],
+                      [-32766.0, -32766.0, -32760.0, -32771.0, -32770.0, -32760.0], IDENTITY)],
+}
+
+
+def _batch(cases):
     bb = BatchBuilder()
-    for name, fills in CASES.items():
+    for name, fills in cases.items():
         bb.begin_raster()
         for verbs, pts, xf in fills:
             bb.fill(verbs, pts, IDENTITY if xf is None else xf, raw=xf is None)
-    return bb.build(), list(CASES)
+    return bb.build(), list(cases)
+
+
+def edge_batch():
+    return _batch(CASES)
+
+
+def i16_batch():
+    return _batch(I16_CASES)

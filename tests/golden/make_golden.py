@@ -28,9 +28,11 @@ from ochre_gb300.batch import Batch  # noqa: E402
 def cases():
     import edge_cases
     eb, _ = edge_cases.edge_batch()
+    ib, _ = edge_cases.i16_batch()
     return {
         "readme": W.readme_path(),
         "edge_cases": eb,
+        "i16_limits": ib,
         "cubic_boxes_2": W.cubic_boxes(n_paths=2),
         "glyph_run_48": W.glyph_run(n_paths=48),
         "uneven_mix_4": W.uneven_mix(n_paths=4, max_seg=120),
@@ -68,7 +70,7 @@ def load(name: str):
     return b, out
 
 
-NAMES = ["readme", "edge_cases", "cubic_boxes_2", "glyph_run_48", "uneven_mix_4", "diff_union_6", "diff_scenes_1"]
+NAMES = ["readme", "edge_cases", "i16_limits", "cubic_boxes_2", "glyph_run_48", "uneven_mix_4", "diff_union_6", "diff_scenes_1"]
 
 if __name__ == "__main__":
     for name, b in cases().items():

@@ -101,16 +101,18 @@ def test_oracle_matches_python_restatement(gen, kw):
         assert int(r["raster_stats"][i, 1]) == ninc
 
 
-def test_edge_cases_match_python_restatement():
+@pytest.mark.parametrize("which", ["edge_batch", "i16_batch"])
+def test_edge_cases_match_python_restatement(which):
     import edge_cases
-    b, names = edge_cases.edge_batch()
-    r = oracle.run(b)
+    b, names = getattr(edge_cases, which)()
+    with np.errstate(all="ignore"):
+        r = oracle.run(b)
     for i, name in enumerate(names):
         tiles, spans, _ = oracle_py.rasterize(oracle_py.commands_of_batch(b, i))
         xy, alpha, sxy, sw, st = _raster(r, i)
         assert [tuple(t) for t in xy.tolist()] == [t[:2] for t in tiles], name
         assert np.array_equal(alpha, np.array([np.frombuffer(t[2], np.uint8) for t in tiles]).reshape(-1, 64)), name
-        assert len(spans) == len(sw), name
+        assert [(int(a), int(c), int(w), int(t)) for (a, c), w, t in zip(sxy.tolist(), sw, st)] == spans, name
 
 
 def test_oracle_threads_agree():

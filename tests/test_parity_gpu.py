@@ -22,8 +22,10 @@ def test_golden_host_path(any_ctx, name):
     finally:
         any_ctx.set_want_cov(False)
     st = compare(got, exp, b.n_rasters)
-    # pre-quantisation coverage vs the oracle's f32 coverage (summation order only)
-    assert st["cov_max_abs_vs_oracle_f32"] < 1e-3, st
+    # pre-quantisation coverage vs the oracle's f32 coverage (summation order
+    # only): 1e-3 absolute, relative to |S| where |S| > 1 (at the i16 limits a
+    # cell's right edge lies 65,536 px from the line and |S| reaches ~2^17)
+    assert st["cov_max_rel_vs_oracle_f32"] < 1e-3, st
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -150,6 +152,28 @@ def test_invalid_inputs_are_reported(any_ctx):
     # the context stays usable
     got = any_ctx.rasterize(b)
     compare(got, oracle.run(b), 1)
+
+
+@pytest.mark.parametrize("case", ["long_line", "steep_quad"])
+def test_iteration_caps_are_reported(any_ctx, case):
+    """Finite inputs on which the reference would walk millions of pixel
+    cells (a line across 4 million pixel columns: the walk steps on the f32
+    geometry while `as i16` saturates the cells) or flatten one curve into
+    millions of lines: the call returns OCHRE_E_LIMIT (2^20 cells per line,
+    2^20 lines per curve) instead, and the context stays usable.  The oracle
+    has no caps, like the reference, and is not run on them."""
+    from ochre_gb300 import _lib
+    from ochre_gb300.batch import CLOSE, IDENTITY, LINE, MOVE, QUADRATIC, BatchBuilder
+    verbs, pts = {"long_line": ([MOVE, LINE, LINE, CLOSE], [-2.0e6, 0.5, 2.0e6, 0.5, 0.0, 40.0]),
+                  "steep_quad": ([MOVE, QUADRATIC, CLOSE], [0.0, 0.0, 3.0e12, 0.0, 0.0, 1.0])}[case]
+    bb = BatchBuilder()
+    bb.begin_raster()
+    bb.fill(verbs, pts, IDENTITY)
+    with pytest.raises(_lib.OchreError) as e:
+        any_ctx.rasterize(bb.build())
+    assert e.value.status == _lib.E_LIMIT
+    b = W.readme_path()
+    compare(any_ctx.rasterize(b), oracle.run(b), 1)
 
 
 def test_verbs_beyond_the_points_are_reported(any_ctx):
