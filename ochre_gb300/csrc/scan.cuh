@@ -12,13 +12,37 @@
 
 namespace ochre {
 
+// A tile's aggregate and inclusive prefix, every 32-bit word of each in a
+// 64-bit word whose high half is its flag (1: aggregate, 2: inclusive; 0:
+// not yet).  One naturally aligned 64-bit access reads or writes a word with
+// its flag, so a reader takes a value once all its words carry the flag, with
+// relaxed accesses only, and one round of loads reads a predecessor's flags
+// and values together.
 template <class T>
 struct ScanStatus {
-    uint32_t flag;   // 0: nothing yet, 1: aggregate published, 2: inclusive prefix published
-    uint32_t pad;
-    T agg;
-    T inc;
+    static constexpr int W = (int)(sizeof(T) / 4);
+    uint64_t agg[W];
+    uint64_t inc[W];
 };
+template <class T>
+__device__ __forceinline__ void st_flagged(uint64_t* dst, const T& v, uint32_t flag) {
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(&v);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) / 4); i++) st_relaxed64(dst + i, ((uint64_t)flag << 32) | s[i]);
+}
+// True when every word of the value carries `flag`; v receives the words.
+template <class T>
+__device__ __forceinline__ bool ld_flagged(const uint64_t* src, uint32_t flag, T& v) {
+    uint32_t* d = reinterpret_cast<uint32_t*>(&v);
+    bool ok = true;
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(T) / 4); i++) {
+        const uint64_t w = ld_relaxed64(src + i);
+        d[i] = (uint32_t)w;
+        ok = ok && (uint32_t)(w >> 32) == flag;
+    }
+    return ok;
+}
 
 template <int BLOCK, int ITEMS, class T, class Op, class In, class Out>
 __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_dev, In in, Out out, Op op,
@@ -76,32 +100,31 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_de
         T prefix = identity;
         ScanStatus<T>* me = status + tile;
         if (tile == 0) {
-            if (lane == 0) {
-                st_words(&me->inc, tile_agg);
-                st_release(&me->flag, 2u);
-            }
+            if (lane == 0) st_flagged(me->inc, tile_agg, 2u);
         } else {
-            if (lane == 0) {
-                st_words(&me->agg, tile_agg);
-                st_release(&me->flag, 1u);
-            }
+            if (lane == 0) st_flagged(me->agg, tile_agg, 1u);
             int64_t top = (int64_t)tile - 1;
             long long spins = 0;
             const long long poll_limit = spin_limit(err);
             while (top >= 0) {
                 const int64_t j = top - lane;
-                uint32_t f = 2u;   // before tile 0: an inclusive identity
-                if (j >= 0) f = ld_acquire(&status[j].flag);
-                const uint32_t m2 = __ballot_sync(0xffffffffu, f == 2u);
+                // the predecessor's inclusive prefix and aggregate, read together
+                bool has_inc = true, has_agg = true;   // before tile 0: an inclusive identity
+                T vi = identity, va = identity;
+                if (j >= 0) {
+                    has_inc = ld_flagged(status[j].inc, 2u, vi);
+                    has_agg = ld_flagged(status[j].agg, 1u, va);
+                }
+                const uint32_t m2 = __ballot_sync(0xffffffffu, has_inc);
                 const int limit = m2 ? __ffs(m2) - 1 : 31;   // lanes [0, limit] are needed
                 const uint32_t need = limit == 31 ? 0xffffffffu : ((1u << (limit + 1)) - 1u);
-                if (__ballot_sync(0xffffffffu, f == 0u) & need) {
+                if (__ballot_sync(0xffffffffu, !has_inc && !has_agg) & need) {
                     if (wait_give_up_warp(spins, poll_limit, err)) break;
                     if (spins > 64) __nanosleep(64);
                     continue;
                 }
                 T v = identity;
-                if (lane <= limit && j >= 0) v = ld_words(f == 2u ? &status[j].inc : &status[j].agg);
+                if (lane <= limit && j >= 0) v = has_inc ? vi : va;
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
                     const T o = shfl_down_T(v, d);
@@ -111,10 +134,7 @@ __global__ void __launch_bounds__(BLOCK) k_scan(uint64_t n, const uint32_t* n_de
                 if (m2) break;
                 top -= 32;
             }
-            if (lane == 0) {
-                st_words(&me->inc, op(prefix, tile_agg));
-                st_release(&me->flag, 2u);
-            }
+            if (lane == 0) st_flagged(me->inc, op(prefix, tile_agg), 2u);
         }
         if (lane == 0) {
             s_prefix = prefix;
