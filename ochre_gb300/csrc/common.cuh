@@ -374,9 +374,12 @@ __device__ __forceinline__ bool wait_give_up_warp(long long& spins, long long li
 // returns at once when one of them gave up (their outputs are not valid).
 __device__ __forceinline__ bool run_aborted(const uint32_t* err) { return (ld_relaxed(err) & ERR_TIMEOUT) != 0u; }
 
-// Look-back slots publish data with relaxed stores followed by a release
-// store of the flag; readers acquire the flag, then read the data relaxed.
-// The release/acquire pair orders the data, so no separate fence is needed.
+// Look-back slots whose flag is a word of its own (the block-form coverage's
+// row sums) publish data with relaxed stores followed by a release store of
+// the flag; readers acquire the flag, then read the data relaxed.  The
+// release/acquire pair orders the data, so no separate fence is needed.  (The
+// scans, the radix sort and the fused kernel keep a flag in every word
+// instead: one relaxed round reads flags and values together.)
 // Word-wise copies of a trivially copyable T through relaxed accesses.
 template <class T>
 __device__ __forceinline__ void st_words(T* dst, const T& v) {
