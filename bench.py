@@ -547,6 +547,16 @@ def bench_graph(ctx, stream, steps):
         ("stroke run, 1,000 stroked paths", W.stroke_run(n_paths=1000, seed=4)),
     ]
     reps = max(30, 5 * steps)
+
+    def per_call(fn):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        return (time.perf_counter() - t0) / reps * 1e3
+
     out = []
     for name, b in cases:
         db = DeviceBatch(b, ctx.device)
@@ -556,16 +566,6 @@ def bench_graph(ctx, stream, steps):
         try:
             r = g.launch(sp)
             assert r.n_tiles == n_tiles and g.info()["replans"] == 0, (name, r.n_tiles, n_tiles)
-
-            def per_call(fn):
-                for _ in range(3):
-                    fn()
-                torch.cuda.synchronize()
-                t0 = time.perf_counter()
-                for _ in range(reps):
-                    fn()
-                return (time.perf_counter() - t0) / reps * 1e3
-
             eager_ms = per_call(lambda: ctx.rasterize_device(db, sp))
             eager_launches = ctx.stats()["n_launches"]
             graph_ms = per_call(lambda: g.launch(sp))
@@ -576,6 +576,28 @@ def bench_graph(ctx, stream, steps):
                         "eager_launches": eager_launches, "graph_kernels": info["kernels"]})
         finally:
             g.close()
+    # the whole differentiable step (forward with signed coverage, coverage
+    # render, L2 loss, backward) on the 256-path union, 1024^2
+    b, w = W.diff_union(), 1024
+    db = DeviceBatch(b, ctx.device)
+    tgt = ctx.render_coverage(DeviceBatch(W.diff_union(perturb=2.0), ctx.device), w, w, stream=sp).clone()
+    cov, dl = torch.empty_like(tgt), torch.empty_like(tgt)
+
+    def eager_step():
+        ctx.render_coverage(db, w, w, cov, stream=sp)
+        ctx.l2_loss(cov, tgt, dl, stream=sp)
+        ctx.fill_backward(db, w, w, dl, stream=sp)
+        torch.cuda.synchronize()
+
+    g = ctx.graph_diff(db, w, w, tgt)
+    try:
+        eager_ms = per_call(eager_step)
+        graph_ms = per_call(lambda: g.launch(sp))
+        out.append({"batch": "differentiable step: union of 256 cubic fills on 1024x1024 (render, loss, backward)",
+                    "rasters": 1, "form": "chain", "eager_ms_per_call": eager_ms, "graph_ms_per_call": graph_ms,
+                    "speedup": eager_ms / graph_ms, "graph_kernels": g.info()["kernels"]})
+    finally:
+        g.close()
     return {"timing": f"host wall clock, mean of {reps} calls after 3 warm-up calls", "cases": out}
 
 

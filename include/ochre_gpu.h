@@ -191,6 +191,18 @@ int ochre_graph_last_stats(const ochre_graph *g, ochre_stats *out);
 /* Kernels captured, re-plans so far, and 1 when the plan is the fused kernel. */
 int ochre_graph_info(const ochre_graph *g, uint32_t *kernels, uint32_t *replans, uint32_t *fused);
 void ochre_graph_destroy(ochre_graph *g);
+/* One whole differentiable step captured the same way (no counterpart in the
+ * reference): the forward with signed coverage, ochre_gpu_render_coverage
+ * into `cov`, ochre_gpu_l2_loss against `target` (loss and dl_dcov) and
+ * ochre_gpu_fill_backward into dl_dpts / dl_dxf, on the buffers given here
+ * (device pointers, fixed for the graph's life; layouts as in the
+ * differentiable entries below).  ochre_graph_launch replays the step (its
+ * result is the forward's tiles with signed coverage); the values behind the
+ * batch and the target may change between launches.  Stroked fills are not
+ * differentiated (OCHRE_E_INVALID). */
+int ochre_graph_create_diff(ochre_gpu_ctx *ctx, const ochre_batch *in, uint32_t w, uint32_t h, const float *target,
+                            float *cov, float *dl_dcov, double *loss, float *dl_dpts, float *dl_dxf, float headroom,
+                            ochre_graph **out);
 
 /* ---- Differentiable fill -------------------------------------------------
  * Extends the reference's forward model (rasterizer.rs:180-268) with dense

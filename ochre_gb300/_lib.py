@@ -26,6 +26,7 @@ EXPORTS = [
     "ochre_gpu_rasterize_noalloc", "ochre_gpu_set_tunable", "ochre_gpu_get_tunable",
     "ochre_gpu_render_coverage", "ochre_gpu_l2_loss", "ochre_gpu_fill_backward", "ochre_gpu_composite",
     "ochre_graph_create", "ochre_graph_launch", "ochre_graph_last_stats", "ochre_graph_info", "ochre_graph_destroy",
+    "ochre_graph_create_diff",
     "ochre_validate_batch",
 ]
 
@@ -133,6 +134,8 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
         L.ochre_gpu_get_tunable.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
         L.ochre_gpu_composite.argtypes = [vp, ctypes.POINTER(Result), u32, vp, u32, u32, vp, vp]
         L.ochre_graph_create.argtypes = [vp, ctypes.POINTER(Batch), ctypes.c_float, ctypes.POINTER(vp)]
+        L.ochre_graph_create_diff.argtypes = [vp, ctypes.POINTER(Batch), u32, u32, vp, vp, vp, vp, vp, vp,
+                                              ctypes.c_float, ctypes.POINTER(vp)]
         L.ochre_graph_launch.argtypes = [vp, ctypes.POINTER(Result), vp]
         L.ochre_graph_last_stats.argtypes = [vp, ctypes.POINTER(Stats)]
         L.ochre_graph_info.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32)]

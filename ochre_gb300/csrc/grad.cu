@@ -33,19 +33,18 @@
 
 namespace ochre {
 
-// Canvas sides beyond the i16 tile coordinate range hold no pixel a tile can reach.
-constexpr uint32_t MAX_CANVAS = 32768;
-
 __device__ __forceinline__ int tile_x_of(uint32_t xy) { return (int)(int16_t)(xy & 0xffffu); }
 __device__ __forceinline__ int tile_y_of(uint32_t xy) { return (int)(int16_t)(xy >> 16); }
 
 // ---- forward: tiles and spans onto dense canvases ----
+// (t_dev / n_dev / l_dev below: a count held on the device, in CUDA-graph
+// replays; the launch-time count is then its capacity, see dev_count)
 __global__ void k_composite_tiles(const uint32_t* __restrict__ tile_xy, const float* __restrict__ tile_sum,
-                                  uint32_t T, const uint32_t* __restrict__ raster_tile_off, uint32_t R, uint32_t W,
-                                  uint32_t H, float* __restrict__ cov) {
+                                  uint32_t T, const uint32_t* t_dev, const uint32_t* __restrict__ raster_tile_off,
+                                  uint32_t R, uint32_t W, uint32_t H, float* __restrict__ cov) {
     const uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint32_t t = (uint32_t)(idx >> 6), c = (uint32_t)(idx & 63u);
-    if (t >= T) return;
+    if (t >= dev_count(T, t_dev)) return;
     const uint32_t r = upper_bound_u32(raster_tile_off, R + 1, t) - 1u;
     const uint32_t xy = tile_xy[t];
     const int x = tile_x_of(xy) + (int)(c & 7u), y = tile_y_of(xy) + (int)(c >> 3);
@@ -54,11 +53,11 @@ __global__ void k_composite_tiles(const uint32_t* __restrict__ tile_xy, const fl
 }
 
 __global__ void k_composite_spans(const uint32_t* __restrict__ span_xy, const uint16_t* __restrict__ span_w,
-                                  uint32_t N, const uint32_t* __restrict__ raster_span_off, uint32_t R, uint32_t W,
-                                  uint32_t H, float* __restrict__ cov) {
+                                  uint32_t N, const uint32_t* n_dev, const uint32_t* __restrict__ raster_span_off,
+                                  uint32_t R, uint32_t W, uint32_t H, float* __restrict__ cov) {
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
-    if (warp >= N) return;
+    if (warp >= dev_count(N, n_dev)) return;
     const uint32_t s = (uint32_t)warp;
     const uint32_t r = upper_bound_u32(raster_span_off, R + 1, s) - 1u;
     const int x0 = tile_x_of(span_xy[s]), y0 = tile_y_of(span_xy[s]);
@@ -124,11 +123,11 @@ __global__ void k_l2(const float* __restrict__ cov, const float* __restrict__ ta
 
 // ---- backward 1: dL/dS at boundary-tile pixels ----
 __global__ void k_gsigma(const uint32_t* __restrict__ tile_xy, const float* __restrict__ tile_sum, uint32_t T,
-                         const uint32_t* __restrict__ raster_tile_off, uint32_t R, uint32_t W, uint32_t H,
-                         const float* __restrict__ dl_dcov, float* __restrict__ gsig) {
+                         const uint32_t* t_dev, const uint32_t* __restrict__ raster_tile_off, uint32_t R, uint32_t W,
+                         uint32_t H, const float* __restrict__ dl_dcov, float* __restrict__ gsig) {
     const uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     const uint32_t t = (uint32_t)(idx >> 6), c = (uint32_t)(idx & 63u);
-    if (t >= T) return;
+    if (t >= dev_count(T, t_dev)) return;
     const uint32_t r = upper_bound_u32(raster_tile_off, R + 1, t) - 1u;
     const uint32_t xy = tile_xy[t];
     const int x = tile_x_of(xy) + (int)(c & 7u), y = tile_y_of(xy) + (int)(c >> 3);
@@ -220,10 +219,11 @@ __device__ __forceinline__ void cell_grads(int x, int y, uint32_t r, uint32_t W,
 // there; taking both sides of a shared point in the same cell keeps the
 // suffix-sum terms of consecutive lines cancelling.)
 __global__ void k_line_grad(const float4* __restrict__ lines, const uint32_t* __restrict__ line_raster, uint32_t L,
-                            uint32_t W, uint32_t H, const float* __restrict__ gsig, const float* __restrict__ gs,
-                            const float* __restrict__ row_total, LineGrad* __restrict__ out) {
+                            const uint32_t* l_dev, uint32_t W, uint32_t H, const float* __restrict__ gsig,
+                            const float* __restrict__ gs, const float* __restrict__ row_total,
+                            LineGrad* __restrict__ out) {
     const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
-    if (l >= L) return;
+    if (l >= dev_count(L, l_dev)) return;
     const float4 ln = lines[l];
     const V2 A = v2(ln.x, ln.y), B = v2(ln.z, ln.w);
     const uint32_t r = line_raster[l];
@@ -333,12 +333,16 @@ __device__ __forceinline__ int endpoint_index(uint8_t v) {
 __device__ __forceinline__ V2 add2(V2 a, V2 b) { return v2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ V2 mul2(float s, V2 a) { return v2(s * a.x, s * a.y); }
 
-__global__ void k_cmd_grad(BatchView b, const uint32_t* __restrict__ line_off, uint32_t L,
-                           const LineGrad* __restrict__ lg, float* __restrict__ gp, uint32_t W, uint32_t H,
-                           const float* __restrict__ gsig, const float* __restrict__ gs,
+// (`err`: a planned run's error word; when a count of the run outgrew its
+// capacity the lines and offsets are not all there, and nothing is read)
+__global__ void k_cmd_grad(BatchView b, const uint32_t* __restrict__ line_off, uint32_t L, const uint32_t* l_dev,
+                           const uint32_t* err, const LineGrad* __restrict__ lg, float* __restrict__ gp, uint32_t W,
+                           uint32_t H, const float* __restrict__ gsig, const float* __restrict__ gs,
                            const float* __restrict__ row_total) {
     const uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (c >= b.n_cmds) return;
+    if (err != nullptr && (ld_relaxed(err) & ERR_CAPACITY)) return;
+    L = (uint32_t)dev_count(L, l_dev);
     const CmdCtx k = load_cmd(b, (uint32_t)c);
     if (!k.ok) return;
     const uint32_t o0 = line_off[c];
@@ -583,6 +587,72 @@ static BatchView view_of(ochre_gpu_ctx* ctx, const ochre_batch* in) {
                      ctx->cmd_mv.as<uint32_t>(), ctx->cmd_ep.as<uint32_t>(), in->n_floats};
 }
 
+int stage_diff_tail(ochre_gpu_ctx* ctx, const ochre_batch* in, const DiffStep& d, cudaStream_t s) {
+    DevScalars* ds = dev_scalars(ctx);
+    const GraphPlan* plan = ctx->plan;
+    const uint32_t R = in->n_rasters, w = d.w, h = d.h;
+    const size_t npx = (size_t)R * w * h;
+    // capacities; the counts stay on the device (span capacity = tile capacity)
+    const uint32_t T = plan->tiles, L = plan->lines;
+    const uint32_t* t_dev = &ds->n_tiles;
+    const uint32_t* n_dev = &ds->n_spans;
+    const uint32_t* l_dev = &ds->n_lines;
+    const uint32_t* tile_xy = ctx->out_tile_xy.as<uint32_t>();
+    const float* tile_sum = ctx->out_tile_cov.as<float>();
+    const uint32_t* tile_off = ctx->out_raster_tile_off.as<uint32_t>();
+    // coverage render (ochre_gpu_render_coverage)
+    if (npx) OCHRE_CUDA_TRY(cudaMemsetAsync(d.cov, 0, npx * sizeof(float), s));
+    if (npx && T) {
+        OCHRE_LAUNCH(ctx, "composite_tiles", s,
+                     k_composite_tiles<<<(unsigned)(((uint64_t)T * 64 + 255) / 256), 256, 0, s>>>(
+                         tile_xy, tile_sum, T, t_dev, tile_off, R, w, h, d.cov));
+        OCHRE_LAUNCH(ctx, "composite_spans", s,
+                     k_composite_spans<<<(unsigned)(((uint64_t)T * 32 + 255) / 256), 256, 0, s>>>(
+                         ctx->out_span_xy.as<uint32_t>(), ctx->out_span_w.as<uint16_t>(), T, n_dev,
+                         ctx->out_raster_span_off.as<uint32_t>(), R, w, h, d.cov));
+    }
+    // loss and dL/dcov (ochre_gpu_l2_loss)
+    OCHRE_CUDA_TRY(cudaMemsetAsync(d.loss, 0, sizeof(double), s));
+    if (npx) {
+        const int blocks = (int)std::min<uint64_t>((npx + 255) / 256, 152u * 16u);
+        OCHRE_LAUNCH(ctx, "l2_loss", s, k_l2<<<blocks, 256, 0, s>>>(d.cov, d.target, npx, d.loss, d.dl_dcov));
+    }
+    OCHRE_CUDA_TRY(cudaGetLastError());
+    // backward (ochre_gpu_fill_backward) on this run's lines and tiles
+    if (in->n_floats) OCHRE_CUDA_TRY(cudaMemsetAsync(d.dl_dpts, 0, in->n_floats * sizeof(float), s));
+    if (in->n_fills) OCHRE_CUDA_TRY(cudaMemsetAsync(d.dl_dxf, 0, (size_t)in->n_fills * 6 * sizeof(float), s));
+    if (R == 0 || in->n_cmds == 0 || L == 0 || npx == 0) return OCHRE_OK;
+    OCHRE_CUDA_TRY(ctx->grad_g.ensure(npx * 4));
+    OCHRE_CUDA_TRY(ctx->grad_gs.ensure(npx * 4));
+    OCHRE_CUDA_TRY(ctx->grad_left.ensure((size_t)R * h * 4));
+    OCHRE_CUDA_TRY(ctx->grad_line.ensure((size_t)L * sizeof(LineGrad)));
+    OCHRE_CUDA_TRY(ctx->grad_pts.ensure(in->n_floats * 4));
+    float* gsig = ctx->grad_g.as<float>();
+    OCHRE_CUDA_TRY(cudaMemsetAsync(gsig, 0, npx * 4, s));
+    if (T)
+        OCHRE_LAUNCH(ctx, "grad_sigma", s,
+                     k_gsigma<<<(unsigned)(((uint64_t)T * 64 + 255) / 256), 256, 0, s>>>(
+                         tile_xy, tile_sum, T, t_dev, tile_off, R, w, h, d.dl_dcov, gsig));
+    const uint64_t rows = (uint64_t)R * h;
+    OCHRE_LAUNCH(ctx, "grad_row_suffix", s,
+                 k_row_suffix<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, s>>>(
+                     gsig, rows, w, ctx->grad_gs.as<float>(), ctx->grad_left.as<float>()));
+    OCHRE_LAUNCH(ctx, "grad_lines", s,
+                 k_line_grad<<<(L + 127) / 128, 128, 0, s>>>(ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(),
+                                                             L, l_dev, w, h, gsig, ctx->grad_gs.as<float>(),
+                                                             ctx->grad_left.as<float>(), ctx->grad_line.as<LineGrad>()));
+    OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->grad_pts.p, 0, in->n_floats * 4, s));
+    const BatchView b = view_of(ctx, in);
+    const unsigned cb = (unsigned)((in->n_cmds + 127) / 128);
+    OCHRE_LAUNCH(ctx, "grad_commands", s,
+                 k_cmd_grad<<<cb, 128, 0, s>>>(b, ctx->cmd_line_off.as<uint32_t>(), L, l_dev, &ds->err,
+                                               ctx->grad_line.as<LineGrad>(), ctx->grad_pts.as<float>(), w, h, gsig,
+                                               ctx->grad_gs.as<float>(), ctx->grad_left.as<float>()));
+    OCHRE_LAUNCH(ctx, "grad_fills", s, k_fill_grad<<<cb, 128, 0, s>>>(b, ctx->grad_pts.as<float>(), d.dl_dpts, d.dl_dxf));
+    OCHRE_CUDA_TRY(cudaGetLastError());
+    return OCHRE_OK;
+}
+
 }  // namespace ochre
 
 using namespace ochre;
@@ -606,14 +676,14 @@ int ochre_gpu_render_coverage(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_
         const uint64_t threads = (uint64_t)res.n_tiles * 64;
         OCHRE_LAUNCH(ctx, "composite_tiles", s,
                      k_composite_tiles<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-                         reinterpret_cast<const uint32_t*>(res.tile_xy), res.tile_cov, res.n_tiles,
+                         reinterpret_cast<const uint32_t*>(res.tile_xy), res.tile_cov, res.n_tiles, nullptr,
                          res.raster_tile_off, in->n_rasters, w, h, cov));
     }
     if (res.n_spans) {
         const uint64_t threads = (uint64_t)res.n_spans * 32;
         OCHRE_LAUNCH(ctx, "composite_spans", s,
                      k_composite_spans<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-                         reinterpret_cast<const uint32_t*>(res.span_xy), res.span_width, res.n_spans,
+                         reinterpret_cast<const uint32_t*>(res.span_xy), res.span_width, res.n_spans, nullptr,
                          res.raster_span_off, in->n_rasters, w, h, cov));
     }
     OCHRE_CUDA_TRY(cudaGetLastError());
@@ -680,7 +750,7 @@ int ochre_gpu_fill_backward(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t 
         const uint64_t threads = (uint64_t)res.n_tiles * 64;
         OCHRE_LAUNCH(ctx, "grad_sigma", s,
                      k_gsigma<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
-                         reinterpret_cast<const uint32_t*>(res.tile_xy), res.tile_cov, res.n_tiles,
+                         reinterpret_cast<const uint32_t*>(res.tile_xy), res.tile_cov, res.n_tiles, nullptr,
                          res.raster_tile_off, R, w, h, dl_dcov, gsig));
     }
     const uint64_t rows = (uint64_t)R * h;
@@ -689,13 +759,14 @@ int ochre_gpu_fill_backward(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t 
                      gsig, rows, w, ctx->grad_gs.as<float>(), ctx->grad_left.as<float>()));
     OCHRE_LAUNCH(ctx, "grad_lines", s,
                  k_line_grad<<<(L + 127) / 128, 128, 0, s>>>(ctx->lines.as<float4>(), ctx->line_raster.as<uint32_t>(),
-                                                             L, w, h, gsig, ctx->grad_gs.as<float>(),
+                                                             L, nullptr, w, h, gsig, ctx->grad_gs.as<float>(),
                                                              ctx->grad_left.as<float>(), ctx->grad_line.as<LineGrad>()));
     OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->grad_pts.p, 0, in->n_floats * 4, s));
     const BatchView b = view_of(ctx, in);
     const unsigned cb = (unsigned)((in->n_cmds + 127) / 128);
     OCHRE_LAUNCH(ctx, "grad_commands", s,
-                 k_cmd_grad<<<cb, 128, 0, s>>>(b, ctx->cmd_line_off.as<uint32_t>(), L, ctx->grad_line.as<LineGrad>(),
+                 k_cmd_grad<<<cb, 128, 0, s>>>(b, ctx->cmd_line_off.as<uint32_t>(), L, nullptr, nullptr,
+                                               ctx->grad_line.as<LineGrad>(),
                                                ctx->grad_pts.as<float>(), w, h, gsig, ctx->grad_gs.as<float>(),
                                                ctx->grad_left.as<float>()));
     OCHRE_LAUNCH(ctx, "grad_fills", s,

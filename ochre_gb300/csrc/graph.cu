@@ -50,6 +50,8 @@ struct ochre_graph {
     uint32_t kernels = 0;           // kernel launches captured
     uint32_t replans = 0;
     ochre_stats stats{};
+    bool is_diff = false;           // a differentiable step (ochre_graph_create_diff)
+    ochre::DiffStep diff{};
 };
 
 namespace ochre {
@@ -99,6 +101,10 @@ int planned_body(ochre_gpu_ctx* ctx, const ochre_batch* batch, cudaStream_t s) {
         st = stage_tiles(ctx, in, E, s, &T, &N);
         if (st != OCHRE_OK) return st;
         ctx->stats.sort_passes = passes;
+        if (ctx->plan->diff) {
+            st = stage_diff_tail(ctx, in, *ctx->plan->diff, s);
+            if (st != OCHRE_OK) return st;
+        }
     }
     // the scalars to the host: a kernel store into mapped memory, else a copy
     ctx->launches++;
@@ -149,6 +155,7 @@ int build(ochre_graph* g) {
         p.key_bits = kb;
         p.rows = std::max<uint32_t>(host_scalars(ctx)->n_rows, 1u);
     }
+    p.diff = g->is_diff ? &g->diff : nullptr;
     // stroked fills: the stroke stage's counts of the planning run
     p.stroke = g->batch.fill_width != nullptr;
     if (p.stroke) {
@@ -273,6 +280,45 @@ int ochre_graph_create(ochre_gpu_ctx* ctx, const ochre_batch* in, float headroom
     g->ctx->cov_signed = ctx->cov_signed;
     g->batch = *in;
     g->headroom = headroom;
+    st = build(g);
+    if (st != OCHRE_OK) {
+        ochre_graph_destroy(g);
+        return st;
+    }
+    *out = g;
+    return OCHRE_OK;
+}
+
+int ochre_graph_create_diff(ochre_gpu_ctx* ctx, const ochre_batch* in, uint32_t w, uint32_t h, const float* target,
+                            float* cov, float* dl_dcov, double* loss, float* dl_dpts, float* dl_dxf, float headroom,
+                            ochre_graph** out) {
+    if (!ctx || !in || !out || !loss) return OCHRE_E_INVALID;
+    *out = nullptr;
+    if (in->n_rasters == 0 || in->n_rasters > MAX_RASTERS || in->n_cmds > MAX_COUNT) return in->n_rasters ? OCHRE_E_CAPACITY : OCHRE_E_INVALID;
+    if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
+    if (in->fill_width != nullptr) return OCHRE_E_INVALID;   // stroked fills are not differentiated
+    if (w > MAX_CANVAS || h > MAX_CANVAS || !(headroom >= 1.0f) || headroom > 16.0f) return OCHRE_E_INVALID;
+    if (w && h && (!target || !cov || !dl_dcov)) return OCHRE_E_INVALID;
+    if ((in->n_floats && !dl_dpts) || (in->n_fills && !dl_dxf)) return OCHRE_E_INVALID;
+    ochre_graph* g = new (std::nothrow) ochre_graph();
+    if (!g) return OCHRE_E_NOMEM;
+    // the forward with signed tile coverage on the general chain, as the
+    // eager differentiable entries run it
+    int st = ochre_gpu_create(&g->ctx, ctx->device, OCHRE_CTX_WANT_COV | OCHRE_CTX_CHAIN_ONLY);
+    if (st != OCHRE_OK) {
+        delete g;
+        return st;
+    }
+    g->ctx->tune_chain_tiles_per_warp = ctx->tune_chain_tiles_per_warp;
+    g->ctx->tune_chain_coverage_form = ctx->tune_chain_coverage_form;
+    g->ctx->tune_chain_long_cells = ctx->tune_chain_long_cells;
+    g->ctx->tune_sort_digit_bits = ctx->tune_sort_digit_bits;
+    g->ctx->tune_chain_walk_refill = ctx->tune_chain_walk_refill;
+    g->ctx->cov_signed = true;
+    g->batch = *in;
+    g->headroom = headroom;
+    g->is_diff = true;
+    g->diff = DiffStep{w, h, target, cov, dl_dcov, loss, dl_dpts, dl_dxf};
     st = build(g);
     if (st != OCHRE_OK) {
         ochre_graph_destroy(g);

@@ -84,6 +84,22 @@ struct DevScalars {
 static_assert(offsetof(DevScalars, spin_log2) - offsetof(DevScalars, err) == 4 * 22,
               "spin_log2 must sit SPIN_LOG2_WORD words after err");
 
+// Canvas sides of the differentiable entries: beyond the i16 tile
+// coordinate range there is no pixel a tile can reach.
+constexpr uint32_t MAX_CANVAS = 32768;
+
+// The buffers of one differentiable step captured into a CUDA graph
+// (ochre_graph_create_diff): coverage render, L2 loss, backward.
+struct DiffStep {
+    uint32_t w, h;
+    const float* target;
+    float* cov;
+    float* dl_dcov;
+    double* loss;
+    float* dl_dpts;
+    float* dl_dxf;
+};
+
 // Capacities of a launch chain captured into a CUDA graph.  Every buffer is
 // sized from them once; the counts stay on the device, each kernel reads its
 // count there and its grid covers the capacity.  A check kernel at every
@@ -105,6 +121,9 @@ struct GraphPlan {
     bool stroke;
     uint32_t stroke_poly, stroke_poly_floats;
     uint32_t stroke_cmds, stroke_floats;
+    // a differentiable step: after the chain (signed coverage), its render,
+    // loss and backward, their counts on the device
+    const DiffStep* diff;
 };
 
 // Entry value tag for tile-row crossings: 1 | raster (23 bits) | sign byte.
@@ -277,6 +296,10 @@ int stage_tiles(ochre_gpu_ctx* ctx, const ochre_batch* in, uint64_t n_entries, c
                 uint32_t* n_spans);
 // Rewrites stroked fills into plain fills (stroke.cu); *out views device memory.
 int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochre_batch* out);
+// After a planned chain with signed coverage: the coverage render, the L2
+// loss and the backward of one differentiable step, every count read on the
+// device (CUDA graphs; grad.cu).
+int stage_diff_tail(ochre_gpu_ctx* ctx, const ochre_batch* in, const DiffStep& d, cudaStream_t s);
 int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool* handled, uint32_t* n_tiles,
                 uint32_t* n_spans);
 

@@ -258,14 +258,17 @@ class Graph:
     launches).  Owns its buffers; results are device pointers valid until the
     next launch."""
 
-    def __init__(self, ctx: "GpuContext", dbatch: "DeviceBatch", headroom: float = 1.25):
+    def __init__(self, ctx: "GpuContext", dbatch: "DeviceBatch", headroom: float = 1.25, _create=None):
         L = _lib.load()
         h = ctypes.c_void_p()
         self.dbatch = dbatch   # keeps the device storage alive
         self.n_rasters = dbatch.batch.n_rasters
         self._ctx = ctx
-        _lib.check(L.ochre_graph_create(ctx.handle, ctypes.byref(dbatch.c), ctypes.c_float(headroom),
-                                        ctypes.byref(h)), "ochre_graph_create")
+        if _create is None:
+            _lib.check(L.ochre_graph_create(ctx.handle, ctypes.byref(dbatch.c), ctypes.c_float(headroom),
+                                            ctypes.byref(h)), "ochre_graph_create")
+        else:
+            _create(h)
         self.handle = h
 
     def launch(self, stream: Optional[int] = None) -> _lib.Result:
@@ -361,6 +364,32 @@ class DeviceBatch:
         return self.batch.input_bytes()
 
 
+class DiffGraph(Graph):
+    """A captured differentiable step on fixed buffers: ``cov`` [n_rasters, h,
+    w], ``dl_dcov`` (same shape), ``loss`` [1] float64, ``dl_dpts``
+    [n_floats] and ``dl_dxf`` [n_fills, 6] (CUDA tensors), rewritten by every
+    launch.  The values behind the batch and ``target`` may change between
+    launches."""
+
+    def __init__(self, ctx: "GpuContext", dbatch: "DeviceBatch", w: int, h: int, target, headroom: float = 1.25):
+        import torch
+        b = dbatch.batch
+        dev = target.device
+        self.target = target
+        self.cov = torch.empty((b.n_rasters, h, w), dtype=torch.float32, device=dev)
+        self.dl_dcov = torch.empty_like(self.cov)
+        self.loss = torch.empty(1, dtype=torch.float64, device=dev)
+        self.dl_dpts = torch.empty(max(1, len(b.pts)), dtype=torch.float32, device=dev)
+        self.dl_dxf = torch.empty((max(1, b.n_fills), 6), dtype=torch.float32, device=dev)
+
+        def create(hnd):
+            _lib.check(_lib.load().ochre_graph_create_diff(
+                ctx.handle, ctypes.byref(dbatch.c), w, h, target.data_ptr(), self.cov.data_ptr(),
+                self.dl_dcov.data_ptr(), self.loss.data_ptr(), self.dl_dpts.data_ptr(), self.dl_dxf.data_ptr(),
+                ctypes.c_float(headroom), ctypes.byref(hnd)), "ochre_graph_create_diff")
+        super().__init__(ctx, dbatch, headroom, _create=create)
+
+
 def _np_from(ptr, dtype, count):
     if count == 0 or not ptr:
         return np.zeros(0, dtype=dtype)
@@ -450,6 +479,13 @@ class GpuContext:
         """The launch chain of rasterize_device for this batch, captured into a
         CUDA graph (ochre_graph_create)."""
         return Graph(self, dbatch, headroom)
+
+    def graph_diff(self, dbatch: DeviceBatch, w: int, h: int, target, headroom: float = 1.25) -> "DiffGraph":
+        """One differentiable step (render_coverage, l2_loss against ``target``
+        [n_rasters, h, w], fill_backward) captured into a CUDA graph
+        (ochre_graph_create_diff); its output tensors are attributes of the
+        returned graph, rewritten by every launch."""
+        return DiffGraph(self, dbatch, w, h, target, headroom)
 
     def device_result_to_numpy(self, r: _lib.Result, n_rasters: int) -> dict:
         out = {}

@@ -224,3 +224,79 @@ def test_graph_with_coverage_output():
                 g.close()
         finally:
             ctx.close()
+
+
+def _eager_step(ctx, db, w, h, tgt):
+    import torch
+    cov = ctx.render_coverage(db, w, h)
+    dl = torch.empty_like(cov)
+    loss, _ = ctx.l2_loss(cov, tgt, dl)
+    dpts, dxf = ctx.fill_backward(db, w, h, dl)
+    torch.cuda.synchronize()
+    return cov, loss, dpts, dxf
+
+
+def _rel_l2(a, b):
+    """||a - b|| / ||b|| (float64)."""
+    a, b = a.double(), b.double()
+    return ((a - b).norm() / b.norm().clamp_min(1e-30)).item()
+
+
+def _same_step(g, eager):
+    """Coverage within 1e-5, the loss within 1e-5 relative and the gradients
+    within 1e-3 relative (L2, the bound of the differentiable tests): the
+    graph runs the eager step's kernels, and only the order of the atomic
+    sums differs, which moves a tile sum that lands within rounding of 1 to
+    either side of the kink of min(|S|, 1) in either run."""
+    cov, loss, dpts, dxf = eager
+    assert (g.cov - cov).abs().max().item() <= 1e-5
+    assert abs(g.loss.item() - loss.item()) <= 1e-5 * abs(loss.item())
+    assert _rel_l2(g.dl_dpts[:dpts.numel()], dpts) <= 1e-3
+    assert _rel_l2(g.dl_dxf[:dxf.shape[0]], dxf) <= 1e-3
+
+
+@pytest.mark.parametrize("case", ["union", "scenes"])
+def test_differentiable_step_graph_matches_eager(gpu_ctx, case):
+    """The whole differentiable step captured into one graph (forward with
+    signed coverage, coverage render, L2 loss, backward) gives the eager
+    calls' coverage, loss and gradients; points rewritten in place between
+    launches give the new step's; a batch grown past the plan re-plans."""
+    import torch
+    from ochre_gb300 import DeviceBatch
+    if case == "union":
+        b, p, w, h = W.diff_union(n_paths=48), W.diff_union(n_paths=48, perturb=2.0), 1024, 1024
+    else:
+        b, w, h = W.diff_scenes(n_scenes=6, max_paths=48, max_seg=48), 512, 512
+        p = dataclasses.replace(b, pts=(b.pts + np.random.default_rng(4).normal(0, 2.0, b.pts.shape)).astype(np.float32))
+    db = DeviceBatch(b)
+    tgt = gpu_ctx.render_coverage(DeviceBatch(p), w, h).clone()
+    g = gpu_ctx.graph_diff(db, w, h, tgt, headroom=1.5)
+    try:
+        for _ in range(2):
+            g.launch()
+            torch.cuda.synchronize()
+            _same_step(g, _eager_step(gpu_ctx, db, w, h, tgt))
+        # new points, within the plan's headroom
+        moved = (b.pts + np.random.default_rng(9).normal(0, 0.7, b.pts.shape)).astype(np.float32)
+        db.pts.copy_(torch.from_numpy(moved).to(db.pts.device))
+        g.launch()
+        torch.cuda.synchronize()
+        _same_step(g, _eager_step(gpu_ctx, db, w, h, tgt))
+        assert g.info()["replans"] == 0
+        # every transform's matrix scaled up: more lines and tiles than planned
+        db.fill_xf.copy_(db.fill_xf.new_tensor(_scaled(b, 2.0).fill_xf.reshape(-1)))
+        g.launch()
+        torch.cuda.synchronize()
+        assert g.info()["replans"] == 1
+        _same_step(g, _eager_step(gpu_ctx, db, w, h, tgt))
+    finally:
+        g.close()
+
+
+def test_differentiable_graph_rejects_strokes(gpu_ctx):
+    import torch
+    from ochre_gb300 import DeviceBatch, OchreError
+    b = W.stroke_run(n_paths=4)
+    tgt = torch.zeros((b.n_rasters, 64, 64), dtype=torch.float32, device="cuda:0")
+    with pytest.raises(OchreError):
+        gpu_ctx.graph_diff(DeviceBatch(b), 64, 64, tgt)
