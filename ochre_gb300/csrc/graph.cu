@@ -31,6 +31,11 @@
 // Such a plan always uses the general chain (every pad command sits on the
 // last raster, which the fused kernel's per-raster command limit would
 // refuse).
+//
+// A differentiable step (ochre_graph_create_diff) is the chain with signed
+// tile coverage followed by stage_diff_tail (grad.cu): the coverage render,
+// the L2 loss and the backward, on caller buffers fixed at creation, every
+// count read on the device.
 #include "common.cuh"
 #include "internal.h"
 
