@@ -58,3 +58,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "paths/s" and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["cores"] >= 1
+    # the same config keys and values as the GPU arm prints for this workload
+    import argparse
+    import bench
+    assert d["config"] == bench.bench_config(argparse.Namespace(workload="glyph_run", seed=2), 300, 2)
