@@ -236,21 +236,39 @@ __global__ void k_fill_init(uint32_t* __restrict__ first_close, const uint32_t* 
 }
 
 // ---- 4. the offset sides (path.rs:160-212) ----
-// One side of contour [c0, c1) of the polyline (points P(k), 2 floats each);
-// emit(point) once or twice per join.
+// One side of contour [c0, c1) of the polyline (points P(k), 2 floats each),
+// walked by a whole warp, 32 steps at a time.  In the reference's loop the
+// point before step i is always the side's point i - 1 (at i = 0 its first
+// point: a step whose point equals the one before emits nothing and changes
+// nothing), and the normal before step i is that of the last step before i
+// that emitted a join.  So the lanes compute the joins of their steps at
+// once, with the reference's operations in its order, and only the last
+// normal is carried from one round of 32 steps to the next; a scan of the
+// joins' point counts (1 or 2) gives each point its place.  emit(k, point)
+// receives the side's k-th point; every lane returns the side's point count.
 template <class Emit>
-__device__ void stroke_side(const float* __restrict__ P, uint32_t len, bool closed, bool reverse, float width,
-                            Emit emit) {
+__device__ uint32_t stroke_side_warp(const float* __restrict__ P, uint32_t len, bool closed, bool reverse, float width,
+                                     Emit emit) {
+    const uint32_t lane = threadIdx.x & 31u;
     auto pt = [&](uint32_t k) { return v2(P[2 * k], P[2 * k + 1]); };
+    auto side = [&](uint32_t k) { return reverse ? pt(len - k - 1) : pt(k); };   // the side's k-th point
     const V2 first_point = closed == reverse ? pt(0) : pt(len - 1);
-    V2 prev_point = first_point;
-    V2 prev_normal = v2(0.0f, 0.0f);
     const float half = __fmul_rn(0.5f, width);
-    for (uint32_t i = 0;; i++) {
-        const V2 next_point = i < len ? (reverse ? pt(len - i - 1) : pt(i)) : first_point;
-        if (!veq(next_point, prev_point) || i == len) {
-            const V2 tan = vsub(next_point, prev_point);
-            V2 nn = v2(-tan.y, tan.x);
+    float cnx = 0.0f, cny = 0.0f;   // normal of the last join so far
+    uint32_t base = 0;              // points emitted so far
+    for (uint32_t i0 = 0; i0 <= len; i0 += 32) {
+        const uint32_t i = i0 + lane;
+        const bool valid = i <= len;
+        V2 next = v2(0.0f, 0.0f), prev = v2(0.0f, 0.0f);
+        if (valid) {
+            next = i < len ? side(i) : first_point;
+            prev = i == 0 ? first_point : side(i - 1);
+        }
+        const bool join = valid && (!veq(next, prev) || i == len);
+        V2 nn = v2(0.0f, 0.0f);
+        if (join) {
+            const V2 tan = vsub(next, prev);
+            nn = v2(-tan.y, tan.x);
             const float nlen = vlength(nn);
             if (nlen == 0.0f) {
                 nn = v2(0.0f, 0.0f);
@@ -258,20 +276,46 @@ __device__ void stroke_side(const float* __restrict__ P, uint32_t len, bool clos
                 const float r = __fdiv_rn(1.0f, nlen);
                 nn = v2(__fmul_rn(nn.x, r), __fmul_rn(nn.y, r));
             }
+        }
+        // the normal before this step: the nearest join below in this round,
+        // else the one carried from the rounds before
+        const uint32_t jm = __ballot_sync(0xffffffffu, join);
+        const uint32_t below = jm & ((1u << lane) - 1u);
+        const int src = below ? 31 - __clz(below) : (int)lane;
+        const float px = __shfl_sync(0xffffffffu, nn.x, src), py = __shfl_sync(0xffffffffu, nn.y, src);
+        const V2 pn = below ? v2(px, py) : v2(cnx, cny);
+        uint32_t cnt = 0;
+        V2 e0 = v2(0.0f, 0.0f), e1 = v2(0.0f, 0.0f);
+        if (join) {
             // join (path.rs:160-168)
-            const float dot = __fadd_rn(__fmul_rn(prev_normal.x, nn.x), __fmul_rn(prev_normal.y, nn.y));
+            const float dot = __fadd_rn(__fmul_rn(pn.x, nn.x), __fmul_rn(pn.y, nn.y));
             const float offset = __fdiv_rn(1.0f, __fadd_rn(1.0f, dot));
             if (fabsf(offset) > 2.0f) {
-                emit(vadd(prev_point, vscale(half, prev_normal)));
-                emit(vadd(prev_point, vscale(half, nn)));
+                e0 = vadd(prev, vscale(half, pn));
+                e1 = vadd(prev, vscale(half, nn));
+                cnt = 2;
             } else {
-                emit(vadd(prev_point, vscale(__fmul_rn(half, offset), vadd(prev_normal, nn))));
+                e0 = vadd(prev, vscale(__fmul_rn(half, offset), vadd(pn, nn)));
+                cnt = 1;
             }
-            prev_point = next_point;
-            prev_normal = nn;
         }
-        if (i + 1 > len) break;
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t o = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= (uint32_t)d) incl += o;
+        }
+        const uint32_t pos = base + incl - cnt;
+        if (cnt >= 1) emit(pos, e0);
+        if (cnt == 2) emit(pos + 1, e1);
+        base += __shfl_sync(0xffffffffu, incl, 31);
+        if (jm) {
+            const int last = 31 - __clz(jm);
+            cnx = __shfl_sync(0xffffffffu, nn.x, last);
+            cny = __shfl_sync(0xffffffffu, nn.y, last);
+        }
     }
+    return base;
 }
 
 struct UnitGeom {
@@ -280,9 +324,13 @@ struct UnitGeom {
     uint32_t closed;    // 1: closed contour; 2: copied command
 };
 
-__device__ __forceinline__ UnitGeom unit_geom(uint32_t u, const uint32_t* unit_start, const uint8_t* pverbs,
-                                              const uint32_t* pfill_off, uint32_t n_fills, const uint8_t* flags,
-                                              const uint32_t* first_close) {
+// Unit u's contour (every lane of the warp, the same answer).  A contour runs
+// from its start to the first polyline command after it that is not a Line
+// (32 checked per round).
+__device__ __forceinline__ UnitGeom unit_geom_warp(uint32_t u, const uint32_t* unit_start, const uint8_t* pverbs,
+                                                   const uint32_t* pfill_off, uint32_t n_fills, const uint8_t* flags,
+                                                   const uint32_t* first_close) {
+    const uint32_t lane = threadIdx.x & 31u;
     UnitGeom g;
     g.p0 = unit_start[u];
     g.fill = upper_bound_u32(pfill_off, n_fills + 1, g.p0) - 1u;
@@ -293,75 +341,101 @@ __device__ __forceinline__ UnitGeom unit_geom(uint32_t u, const uint32_t* unit_s
     }
     const uint32_t pe = __ldg(pfill_off + g.fill + 1);
     uint32_t e = g.p0 + 1;
-    while (e < pe && pverbs[e] == V_LINE) e++;
+    for (;;) {
+        const uint32_t k = e + lane;
+        const uint32_t stop = __ballot_sync(0xffffffffu, k >= pe || pverbs[k] != V_LINE);
+        if (stop) {
+            e += (uint32_t)__ffs(stop) - 1u;
+            break;
+        }
+        e += 32;
+    }
     g.len = e - g.p0;
     const bool term_close = e < pe && pverbs[e] == V_CLOSE;
     g.closed = (term_close || first_close[g.fill] < g.p0) ? 1u : 0u;
     return g;
 }
 
-struct OutCount {
-    const uint32_t* unit_start;
-    const uint8_t* pverbs;
-    const float* ppts;
-    const uint32_t* poly_foff_of;   // polyline float offset of every polyline command
-    const uint32_t* pfill_off;
-    uint32_t n_fills;
-    const uint8_t* flags;
-    const uint32_t* first_close;
-    const float* width;
-    __device__ Pair operator()(uint64_t i) const {
-        const UnitGeom g = unit_geom((uint32_t)i, unit_start, pverbs, pfill_off, n_fills, flags, first_close);
-        if (g.closed == 2) return Pair{1u, floats_per_verb(pverbs[g.p0])};
-        const float* P = ppts + poly_foff_of[g.p0];
-        const float w = __ldg(width + g.fill);
-        uint32_t n = 0;
-        stroke_side(P, g.len, g.closed != 0, false, w, [&](V2) { n++; });
-        stroke_side(P, g.len, g.closed != 0, true, w, [&](V2) { n++; });
-        return Pair{n + (g.closed ? 2u : 1u), 2u * n};
+// Output commands and floats of every unit, one warp per unit.
+__global__ void __launch_bounds__(128) k_out_count(uint32_t n_units, const uint32_t* n_dev,
+                                                   const uint32_t* __restrict__ unit_start,
+                                                   const uint8_t* __restrict__ pverbs, const float* __restrict__ ppts,
+                                                   const uint32_t* __restrict__ poly_foff_of,
+                                                   const uint32_t* __restrict__ pfill_off, uint32_t n_fills,
+                                                   const uint8_t* __restrict__ flags,
+                                                   const uint32_t* __restrict__ first_close,
+                                                   const float* __restrict__ width, uint32_t* __restrict__ out_n,
+                                                   uint32_t* __restrict__ out_nf) {
+    const uint64_t u = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    if (u >= dev_count(n_units, n_dev)) return;   // whole warps
+    const uint32_t lane = threadIdx.x & 31u;
+    const UnitGeom g = unit_geom_warp((uint32_t)u, unit_start, pverbs, pfill_off, n_fills, flags, first_close);
+    if (g.closed == 2) {
+        if (lane == 0) {
+            out_n[u] = 1u;
+            out_nf[u] = floats_per_verb(pverbs[g.p0]);
+        }
+        return;
     }
-};
+    const float* P = ppts + poly_foff_of[g.p0];
+    const float w = __ldg(width + g.fill);
+    auto none = [](uint32_t, V2) {};
+    const uint32_t n = stroke_side_warp(P, g.len, g.closed != 0, false, w, none) +
+                       stroke_side_warp(P, g.len, g.closed != 0, true, w, none);
+    if (lane == 0) {
+        out_n[u] = n + (g.closed ? 2u : 1u);
+        out_nf[u] = 2u * n;
+    }
+}
 
-__global__ void k_out_emit(uint32_t n_units, const uint32_t* n_dev, const uint32_t* __restrict__ unit_start,
-                           const uint8_t* __restrict__ pverbs,
-                           const float* __restrict__ ppts, const uint32_t* __restrict__ poly_foff_of,
-                           const uint32_t* __restrict__ pfill_off, uint32_t n_fills, const uint8_t* __restrict__ flags,
-                           const uint32_t* __restrict__ first_close, const float* __restrict__ width,
-                           const uint32_t* __restrict__ out_off, const uint32_t* __restrict__ out_foff,
-                           uint8_t* __restrict__ overbs, float* __restrict__ opts, uint32_t* __restrict__ unit_fill) {
-    const uint32_t u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= dev_count(n_units, n_dev)) return;
-    const UnitGeom g = unit_geom(u, unit_start, pverbs, pfill_off, n_fills, flags, first_close);
-    unit_fill[u] = g.fill;
+// Every unit's output commands and points (path.rs:214-274), one warp per unit.
+__global__ void __launch_bounds__(128) k_out_emit(uint32_t n_units, const uint32_t* n_dev,
+                                                  const uint32_t* __restrict__ unit_start,
+                                                  const uint8_t* __restrict__ pverbs, const float* __restrict__ ppts,
+                                                  const uint32_t* __restrict__ poly_foff_of,
+                                                  const uint32_t* __restrict__ pfill_off, uint32_t n_fills,
+                                                  const uint8_t* __restrict__ flags,
+                                                  const uint32_t* __restrict__ first_close,
+                                                  const float* __restrict__ width, const uint32_t* __restrict__ out_off,
+                                                  const uint32_t* __restrict__ out_foff, uint8_t* __restrict__ overbs,
+                                                  float* __restrict__ opts, uint32_t* __restrict__ unit_fill) {
+    const uint64_t u = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+    if (u >= dev_count(n_units, n_dev)) return;   // whole warps
+    const uint32_t lane = threadIdx.x & 31u;
+    const UnitGeom g = unit_geom_warp((uint32_t)u, unit_start, pverbs, pfill_off, n_fills, flags, first_close);
     uint32_t o = out_off[u], fo = out_foff[u];
     const float* P = ppts + poly_foff_of[g.p0];
     if (g.closed == 2) {
-        const uint8_t v = pverbs[g.p0];
-        overbs[o] = v;
-        for (uint32_t k = 0; k < floats_per_verb(v); k++) opts[fo + k] = P[k];
+        if (lane == 0) {
+            unit_fill[u] = g.fill;
+            const uint8_t v = pverbs[g.p0];
+            overbs[o] = v;
+            for (uint32_t k = 0; k < floats_per_verb(v); k++) opts[fo + k] = P[k];
+        }
         return;
     }
+    if (lane == 0) unit_fill[u] = g.fill;
     const float w = __ldg(width + g.fill);
     const bool closed = g.closed != 0;
-    bool first = true;
-    auto put = [&](uint8_t verb, V2 p) {
-        overbs[o++] = verb;
-        opts[fo++] = p.x;
-        opts[fo++] = p.y;
-    };
     // forward side: its first point becomes a Move (path.rs:249-250)
-    stroke_side(P, g.len, closed, false, w, [&](V2 p) {
-        put(first ? V_MOVE : V_LINE, p);
-        first = false;
+    const uint32_t nf = stroke_side_warp(P, g.len, closed, false, w, [&](uint32_t k, V2 p) {
+        overbs[o + k] = k == 0 ? V_MOVE : V_LINE;
+        opts[fo + 2 * k] = p.x;
+        opts[fo + 2 * k + 1] = p.y;
     });
-    if (closed) overbs[o++] = V_CLOSE;
+    o += nf;
+    fo += 2 * nf;
+    if (closed) {
+        if (lane == 0) overbs[o] = V_CLOSE;
+        o++;
+    }
     // backward side: a Move only when closed (path.rs:254-257), then Close
-    first = true;
-    stroke_side(P, g.len, closed, true, w, [&](V2 p) {
-        put(first && closed ? V_MOVE : V_LINE, p);
-        first = false;
+    const uint32_t nb = stroke_side_warp(P, g.len, closed, true, w, [&](uint32_t k, V2 p) {
+        overbs[o + k] = k == 0 && closed ? V_MOVE : V_LINE;
+        opts[fo + 2 * k] = p.x;
+        opts[fo + 2 * k + 1] = p.y;
     });
-    overbs[o++] = V_CLOSE;
+    if (lane == 0) overbs[o + nb] = V_CLOSE;
 }
 
 // A planned run (pad_end > 0) ends the last fill at pad_end: the output
@@ -521,12 +595,11 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     // the output totals: a scan that covers no unit writes none
     OCHRE_CUDA_TRY(cudaMemsetAsync(&ds->n_lines, 0, 8, s));
     if (U) {
-        OCHRE_LAUNCH(ctx, "stroke_out_count", s, k_pair_count<<<(U + 127) / 128, 128, 0, s>>>(
-            U, u_dev,
-            OutCount{ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
-                     ctx->sk_pfoff.as<uint32_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
-                     ctx->sk_first_close.as<uint32_t>(), in->fill_width},
-            ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()));
+        OCHRE_LAUNCH(ctx, "stroke_out_count", s, k_out_count<<<(unsigned)(((uint64_t)U * 32 + 127) / 128), 128, 0, s>>>(
+            U, u_dev, ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
+            ctx->sk_pfoff.as<uint32_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
+            ctx->sk_first_close.as<uint32_t>(), in->fill_width, ctx->sk_out_off.as<uint32_t>(),
+            ctx->sk_out_foff.as<uint32_t>()));
         OCHRE_CUDA_TRY(cudaGetLastError());
         OCHRE_LAUNCH(ctx, "stroke_out_scan", s, OCHRE_CUDA_TRY(launch_scan<Pair>(
             U, PairIn{ctx->sk_out_off.as<uint32_t>(), ctx->sk_out_foff.as<uint32_t>()},
@@ -558,7 +631,7 @@ int stage_stroke(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, ochr
     // planned: every output command past the true total is a Close
     if (plan) OCHRE_CUDA_TRY(cudaMemsetAsync(ctx->sk_overbs.p, V_CLOSE, ON, s));
     if (U)
-        OCHRE_LAUNCH(ctx, "stroke_out_emit", s, k_out_emit<<<(U + 127) / 128, 128, 0, s>>>(
+        OCHRE_LAUNCH(ctx, "stroke_out_emit", s, k_out_emit<<<(unsigned)(((uint64_t)U * 32 + 127) / 128), 128, 0, s>>>(
             U, u_dev, ctx->sk_unit_start.as<uint32_t>(), ctx->sk_pverbs.as<uint8_t>(), ctx->sk_ppts.as<float>(),
             ctx->sk_pfoff.as<uint32_t>(), ctx->sk_pfill_off.as<uint32_t>(), F, in->fill_flags,
             ctx->sk_first_close.as<uint32_t>(), in->fill_width, ctx->sk_out_off.as<uint32_t>(),
