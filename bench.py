@@ -462,6 +462,47 @@ def bench_configs(ctx, stream, flush, peak, glyphs, scenes):
                     + _cpu_model(), "rows": rows}
 
 
+def bench_svg_documents(ctx, stream, flush):
+    """The reference's example documents (examples/res/*.svg, read by this
+    project's SVG reader into the committed fixture tests/golden/svg_docs.npz):
+    every painted path one raster, rasterized in one call and composited onto
+    the document's canvas (CUDA events, L2 flushed), against the CPU port on
+    all host cores."""
+    import numpy as np
+    import torch
+    import oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from golden.make_svg_docs import load
+    from ochre_gb300 import DeviceBatch
+    sp = stream.cuda_stream
+    cores = os.cpu_count() or 1
+    out = []
+    for name in ("tiger", "calabi_yau", "lorem_ipsum"):
+        b, colors, (w, h), _ = load(name)
+        W, H = int(w or 1024), int(h or 1024)
+        db = DeviceBatch(b, ctx.device)
+        for _ in range(2):
+            ctx.rasterize_device(db, sp)
+        st = ctx.stats()
+        ms = _event_ms(lambda: ctx.rasterize_device(db, sp), stream, flush, 5)
+        col = torch.as_tensor(np.ascontiguousarray(colors), device=f"cuda:{ctx.device}")
+        canvas = torch.full((H, W, 4), 255, dtype=torch.uint8, device=col.device)
+        r = ctx.rasterize_device(db, sp)
+        comp_ms = _event_ms(lambda: ctx.composite(r, b.n_rasters, col, canvas, stream=sp), stream, flush, 5)
+        with np.errstate(all="ignore"):
+            oracle.run(b, threads=cores)
+            t0 = time.perf_counter()
+            oracle.run(b, threads=cores)
+            cpu_s = time.perf_counter() - t0
+        out.append({"document": name, "rasters": b.n_rasters, "commands": b.n_cmds, "tiles": st["n_tiles"],
+                    "spans": st["n_spans"], "path": "fused" if st.get("fused") else "chain",
+                    "canvas": [W, H], "rasterize_ms": ms, "composite_ms": comp_ms,
+                    "cpu_rasterize_ms": 1e3 * cpu_s, "cpu_cores": cores,
+                    "gpu_over_cpu": 1e3 * cpu_s / ms})
+    return {"note": "GPU by CUDA events (device-resident inputs, L2 flushed); CPU port by host wall clock, "
+                    "rasterization only", "documents": out}
+
+
 def bench_stroke(ctx, stream, flush, steps):
     """Stroked paths (Rasterizer::stroke): 20,000 rasters of 2-24 mixed
     segments, widths 0.5-8 px; the device stroke stage plus the fill path,
@@ -967,6 +1008,7 @@ def run_ours(args, ws, rank, local):
         extensions["configs"] = bench_configs(ctx, stream, flush, float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"])),
                                               batch, scenes)
         extensions["stroke"] = bench_stroke(ctx, stream, flush, args.steps)
+        extensions["svg_documents"] = bench_svg_documents(ctx, stream, flush)
         extensions["graph"] = bench_graph(ctx, stream, args.steps)
         extensions["composite"] = bench_composite(ctx, stream, flush, args.steps)
     n_paths_all = batch.n_rasters * ws
@@ -1026,6 +1068,7 @@ def run_ours(args, ws, rank, local):
         "graph": extensions.get("graph"),
         "composite": extensions.get("composite"),
         "configs": extensions.get("configs"),
+        "svg_documents": extensions.get("svg_documents"),
         "e2e": {"value": n_paths_all / e2e_s, "unit": "paths/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": 1000 * e2e_s,
                 "note": "pinned host inputs: points read by the kernels in place over the host link, the "
