@@ -380,15 +380,7 @@ __device__ __forceinline__ bool run_aborted(const uint32_t* err) { return (ld_re
 // release/acquire pair orders the data, so no separate fence is needed.  (The
 // scans, the radix sort and the fused kernel keep a flag in every word
 // instead: one relaxed round reads flags and values together.)
-// Word-wise copies of a trivially copyable T through relaxed accesses.
-template <class T>
-__device__ __forceinline__ void st_words(T* dst, const T& v) {
-    static_assert(sizeof(T) % 4 == 0, "T must be a multiple of 4 bytes");
-    const uint32_t* s = reinterpret_cast<const uint32_t*>(&v);
-    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
-#pragma unroll
-    for (int i = 0; i < (int)(sizeof(T) / 4); i++) st_relaxed(d + i, s[i]);
-}
+// Word-wise read of a trivially copyable T through relaxed accesses.
 template <class T>
 __device__ __forceinline__ T ld_words(const T* src) {
     T v;
