@@ -233,3 +233,75 @@ def test_configuration_counts(name, expect):
     from golden.config_counts import counts
     c = counts(getattr(W, name)(), threads=os.cpu_count() or 1)
     assert (c["lines"], c["increments"], c["crossings"], c["tiles"], c["spans"]) == expect
+
+
+def _side_step_local(pts, closed, reverse, width):
+    """One offset side with every step's join computed on its own, the form
+    the device walks 32 steps at a time: the point before step i is the
+    side's point i - 1 (its first point at i = 0), and the normal before it
+    is that of the nearest earlier step with a join."""
+    F, ZERO, ONE = np.float32, np.float32(0.0), np.float32(1.0)
+    half = F(0.5) * F(width)
+    seq = pts[::-1] if reverse else pts
+    first = pts[0] if closed == reverse else pts[-1]
+    n = len(seq)
+    normals = []   # per step: its normal when it has a join, else None
+    for i in range(n + 1):
+        nxt = seq[i] if i < n else first
+        prv = seq[i - 1] if i > 0 else first
+        if i < n and nxt[0] == prv[0] and nxt[1] == prv[1]:
+            normals.append(None)
+            continue
+        tx, ty = nxt[0] - prv[0], nxt[1] - prv[1]
+        nn = (-ty, tx)
+        ln = np.sqrt(nn[0] * nn[0] + nn[1] * nn[1])
+        normals.append((ZERO, ZERO) if ln == ZERO else (nn[0] * (ONE / ln), nn[1] * (ONE / ln)))
+    res = []
+    for i in range(n + 1):
+        nn = normals[i]
+        if nn is None:
+            continue
+        prv = seq[i - 1] if i > 0 else first
+        earlier = [m for m in normals[:i] if m is not None]
+        pn = earlier[-1] if earlier else (ZERO, ZERO)
+        off = ONE / (ONE + (pn[0] * nn[0] + pn[1] * nn[1]))
+        if abs(off) > F(2.0):
+            res.append((prv[0] + half * pn[0], prv[1] + half * pn[1]))
+            res.append((prv[0] + half * nn[0], prv[1] + half * nn[1]))
+        else:
+            k = half * off
+            res.append((prv[0] + k * (pn[0] + nn[0]), prv[1] + k * (pn[1] + nn[1])))
+    return res
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_stroke_joins_are_step_local(seed):
+    """The reference's offset loop (path.rs:160-212) carries the previous
+    distinct point and the previous join's normal; restated with every join
+    computed from the point before its step and the nearest earlier join's
+    normal (the device's 32-steps-per-round walk), it gives the same points
+    bit for bit, on random contours with repeated points, open and closed."""
+    rng = np.random.default_rng(seed)
+    F = np.float32
+    for _ in range(60):
+        n = int(rng.integers(1, 40))
+        raw = rng.normal(0, 30, size=(n, 2)).astype(F)
+        pts = []
+        for p in raw:
+            pts.append((F(p[0]), F(p[1])))
+            if rng.uniform() < 0.3:          # a repeated point
+                pts.append(pts[-1])
+            if rng.uniform() < 0.05 and len(pts) > 2:   # back to an earlier point
+                pts.append(pts[int(rng.integers(0, len(pts) - 1))])
+        closed = bool(rng.uniform() < 0.5)
+        width = F(rng.uniform(0.25, 12.0))
+        poly = [(0, pts[0])] + [(1, p) for p in pts[1:]] + ([(5, None)] if closed else [])
+        want = oracle_py.stroke_polyline(poly, width)
+        fwd = _side_step_local(pts, closed, False, width)
+        bwd = _side_step_local(pts, closed, True, width)
+        got = [(0 if j == 0 else 1, q) for j, q in enumerate(fwd)] + ([(5, None)] if closed else [])
+        got += [(0 if (j == 0 and closed) else 1, q) for j, q in enumerate(bwd)] + [(5, None)]
+        assert [v for v, _ in got] == [v for v, _ in want]
+        for (_, a), (_, b) in zip(got, want):
+            if a is not None:
+                assert a[0] == b[0] and a[1] == b[1]
