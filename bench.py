@@ -65,6 +65,8 @@ def make_workload(name: str, n: int, seed: int):
         return W.cubic_boxes(n_paths=n, seed=seed)
     if name == "uneven_mix":
         return W.uneven_mix(n_paths=n, seed=seed)
+    if name == "stroke_run":
+        return W.stroke_run(n_paths=n, seed=seed)
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -815,7 +817,8 @@ def _fd_check(ctx, sp, n_paths=256, n_params=64, h_px=1e-3):
 
 def run_profile(args):
     """Untimed runs of one workload for an external profiler (ncu): warmup +
-    steps calls of the rasterization (or of render + loss + backward)."""
+    steps calls of the rasterization (or of render + loss + backward, or of
+    the compositing of one rasterization onto a 4096x4096 RGBA8 canvas)."""
     import torch
     from ochre_gb300 import DeviceBatch, GpuContext
     batch = make_workload(args.workload, args.n_paths, args.seed)
@@ -831,6 +834,14 @@ def run_profile(args):
     if args.mode == "profile":
         for _ in range(args.warmup + args.steps):
             ctx.rasterize_device(db, sp)
+    elif args.mode == "profile-composite":
+        import numpy as np
+        rng = np.random.default_rng(9)
+        colors = torch.as_tensor(rng.integers(0, 256, size=(batch.n_rasters, 4), dtype=np.uint8), device="cuda:0")
+        canvas = torch.full((4096, 4096, 4), 255, dtype=torch.uint8, device="cuda:0")
+        r = ctx.rasterize_device(db, sp)
+        for _ in range(args.warmup + args.steps):
+            ctx.composite(r, batch.n_rasters, colors, canvas, sp)
     else:
         w = h = 1024 if args.workload == "diff_union" else 512
         tgt = torch.zeros((batch.n_rasters, h, w), dtype=torch.float32, device="cuda:0")
@@ -1093,9 +1104,10 @@ def main():
                     help="scenes in the batched differentiable workload (512x512 each)")
     ap.add_argument("--no-extensions", action="store_true",
                     help="skip the uneven-mix and differentiable measurements")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "profile-diff"],
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "profile-diff", "profile-composite"],
                     help="profile: run warmup + steps rasterizations of the workload untimed, for ncu; "
-                         "profile-diff: the same for render + loss + backward of --workload diff_union|diff_scenes")
+                         "profile-diff: the same for render + loss + backward of --workload diff_union|diff_scenes; "
+                         "profile-composite: one rasterization, then warmup + steps compositings onto 4096x4096")
     ap.add_argument("--chain-only", action="store_true", help="profile mode: force the general chain")
     ap.add_argument("--fused-shape", default="", help="profile mode: fused kernel shape (threads x tiles per chunk), e.g. 96x16")
     args = ap.parse_args()

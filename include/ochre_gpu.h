@@ -139,7 +139,12 @@ int ochre_gpu_set_flags(ochre_gpu_ctx *ctx, uint32_t flags);
 /* Batched fill+finish of many independent rasterizers (device pointers in
  * `in`, results left in device memory owned by ctx).  `stream` is a
  * cudaStream_t, or NULL for the context's own stream.  Replaces, per raster,
- * Rasterizer::new/fill/finish (rasterizer.rs:50, 161-165, 180-268). */
+ * Rasterizer::new/fill/finish (rasterizer.rs:50, 161-165, 180-268).
+ * A batch with a raster beyond the fused kernel's limits runs on the general
+ * chain; the context remembers the last such batch (its arrays and counts)
+ * and runs it on the chain without a fused attempt while the same arrays and
+ * counts come back.  Both forms give the same tiles and spans (alpha within
+ * 1 LSB). */
 int ochre_gpu_rasterize_device(ochre_gpu_ctx *ctx, const ochre_batch *in, ochre_result *out, void *stream);
 
 /* Same with host buffers: copies the batch to the device, rasterizes and

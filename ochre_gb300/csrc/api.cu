@@ -220,7 +220,7 @@ static bool non_decreasing(const uint32_t* a, uint64_t n) {
     return bad == 0;
 }
 
-int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out, cudaStream_t s) {
+int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out, cudaStream_t s, bool remember_miss) {
     // the test hooks apply to this run only
     struct HookReset {
         ochre_gpu_ctx* c;
@@ -256,9 +256,16 @@ int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in_orig, ochre_result* out
     uint32_t T = 0, N = 0;
     bool handled = false;
     int st = OCHRE_OK;
-    if (!(ctx->flags & OCHRE_CTX_CHAIN_ONLY)) {
+    // a batch that did not fit the fused kernel last time (same arrays and
+    // counts) goes to the chain directly; the results are the same either way
+    const bool known_miss = remember_miss && ctx->fused_miss_valid && same_batch(ctx->fused_miss, *in_orig);
+    if (!(ctx->flags & OCHRE_CTX_CHAIN_ONLY) && !known_miss) {
         st = stage_fused(ctx, in, s, &handled, &T, &N);
         if (st != OCHRE_OK) return st;
+        if (remember_miss) {
+            ctx->fused_miss_valid = !handled;
+            if (!handled) ctx->fused_miss = *in_orig;
+        }
     }
     if (handled) {
         ctx->stats.fused = 1;
@@ -421,7 +428,7 @@ int ochre_gpu_rasterize_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_
     if (in->raster_fill_off == nullptr && in->n_rasters != in->n_fills) return OCHRE_E_INVALID;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return OCHRE_E_CUDA;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
-    return run_device(ctx, in, out, s);
+    return run_device(ctx, in, out, s, true);
 }
 
 int ochre_validate_batch(const ochre_batch* in) {

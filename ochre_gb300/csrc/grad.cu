@@ -574,13 +574,6 @@ static int run_signed_chain(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStrea
     return st;
 }
 
-static bool same_batch(const ochre_batch& a, const ochre_batch& b) {
-    return a.verbs == b.verbs && a.n_cmds == b.n_cmds && a.pts == b.pts && a.n_floats == b.n_floats &&
-           a.fill_cmd_off == b.fill_cmd_off && a.fill_xf == b.fill_xf && a.fill_flags == b.fill_flags &&
-           a.n_fills == b.n_fills && a.raster_fill_off == b.raster_fill_off && a.n_rasters == b.n_rasters &&
-           a.fill_width == b.fill_width;
-}
-
 static BatchView view_of(ochre_gpu_ctx* ctx, const ochre_batch* in) {
     return BatchView{in->verbs, in->pts, in->fill_cmd_off, in->fill_xf, in->fill_flags, in->raster_fill_off,
                      in->n_fills, in->n_rasters, in->n_cmds, ctx->cmd_foff.as<uint32_t>(),

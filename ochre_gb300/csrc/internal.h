@@ -202,6 +202,11 @@ struct ochre_gpu_ctx {
     ochre::DevBuf fused_stage;   // fused path: per-CTA staged alpha (and coverage) of its raster
     uint32_t fused_max_ctas = 0; // fused path: at most this many persistent CTAs (0: no limit)
     uint32_t fused_tile_cap = 0; // fused path: output capacity guess (tiles)
+    // The last batch of the device entry that did not fit the fused kernel
+    // (its arrays and counts): while the same batch comes back, it goes to
+    // the general chain without a fused attempt.
+    ochre_batch fused_miss{};
+    bool fused_miss_valid = false;
     // device outputs
     ochre::DevBuf out_tile_xy, out_tile_alpha, out_tile_cov, out_span_xy, out_span_w, out_span_tile,
         out_raster_tile_off, out_raster_span_off;
@@ -304,8 +309,19 @@ int stage_fused(ochre_gpu_ctx* ctx, const ochre_batch* in, cudaStream_t s, bool*
                 uint32_t* n_spans);
 
 
+// The same arrays and counts.
+inline bool same_batch(const ochre_batch& a, const ochre_batch& b) {
+    return a.verbs == b.verbs && a.n_cmds == b.n_cmds && a.pts == b.pts && a.n_floats == b.n_floats &&
+           a.fill_cmd_off == b.fill_cmd_off && a.fill_xf == b.fill_xf && a.fill_flags == b.fill_flags &&
+           a.n_fills == b.n_fills && a.raster_fill_off == b.raster_fill_off && a.n_rasters == b.n_rasters &&
+           a.fill_width == b.fill_width;
+}
+
 // The whole chain for one batch (device pointers), results in ctx buffers.
-int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s);
+// With remember_miss, a batch that did not fit the fused kernel is noted in
+// the context, and the same batch then skips the fused attempt.
+int run_device(ochre_gpu_ctx* ctx, const ochre_batch* in, ochre_result* out, cudaStream_t s,
+               bool remember_miss = false);
 
 // Graph replays: device checks of counts against the plan (api.cu).  The
 // entry check sets n_entries = line_ent_total + n_empty and zeroes it, and the

@@ -211,6 +211,40 @@ def test_fused_path_taken_for_glyphs_and_chain_for_big_paths(gpu_ctx):
     assert gpu_ctx.stats()["fused"] == 0
 
 
+def test_device_entry_remembers_a_batch_beyond_the_fused_limits():
+    """A device batch that did not fit the fused kernel runs on the chain
+    again without a fused attempt while its arrays and counts stay the same;
+    a batch that fits (or the same arrays with other counts) is tried on the
+    fused kernel again.  Results match the oracle every time."""
+    import dataclasses
+
+    from ochre_gb300 import DeviceBatch, GpuContext
+    b = W.glyph_run(n_paths=400, seed=5)
+    big = b.fill_xf.copy()
+    big[7, :4] *= np.float32(12.0)   # one glyph ~12x larger: past the fused grid
+    b_big = dataclasses.replace(b, fill_xf=big)
+    ref, ref_big = oracle.run(b, threads=8), oracle.run(b_big, threads=8)
+    ctx = GpuContext(0)
+    try:
+        db = DeviceBatch(b_big)
+        for _ in range(2):
+            compare(ctx.device_result_to_numpy(ctx.rasterize_device(db), b.n_rasters), ref_big, b.n_rasters)
+            assert ctx.stats()["fused"] == 0
+        # the same arrays, the glyph back to its size: still the chain (the
+        # context keys on arrays and counts, not values), still exact
+        db.fill_xf.copy_(db.fill_xf.new_tensor(b.fill_xf.reshape(-1)))
+        compare(ctx.device_result_to_numpy(ctx.rasterize_device(db), b.n_rasters), ref, b.n_rasters)
+        assert ctx.stats()["fused"] == 0
+        # another batch fits and clears the note; the first is tried again
+        db2 = DeviceBatch(b)
+        compare(ctx.device_result_to_numpy(ctx.rasterize_device(db2), b.n_rasters), ref, b.n_rasters)
+        assert ctx.stats()["fused"] == 1
+        compare(ctx.device_result_to_numpy(ctx.rasterize_device(db), b.n_rasters), ref, b.n_rasters)
+        assert ctx.stats()["fused"] == 1
+    finally:
+        ctx.close()
+
+
 def test_full_size_glyph_run_matches_oracle(gpu_ctx):
     """The bench workload at full size (100,000 paths), fused path."""
     b = W.glyph_run(n_paths=100_000)
