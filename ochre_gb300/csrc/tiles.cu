@@ -11,11 +11,14 @@
 //
 // Tiles are numbered in sorted order, which is the reference's callback
 // order.  The tile-head scan also counts bins and sums crossing signs, so
-// each tile's metadata and winding follow without a per-tile search.  Coverage runs one warp per aligned
-// whole tile row (raster, tile_y) at a time, taken by ticket: chunk by chunk
-// of TILES_PER_WARP tiles it replays the chunk's bins into shared-memory
+// each tile's metadata and winding follow without a per-tile search.
+// Coverage (row form) runs one warp per whole tile row (raster, tile_y) at a
+// time, taken by ticket: chunk by chunk of TILES_PER_WARP tiles it adds the
+// increments the emit walk stored for the chunk's bins into shared-memory
 // accumulators, then walks the tiles left to right keeping the row carry in
-// registers, so no carry ever crosses warps.
+// registers, so no carry ever crosses warps.  The block form gives each warp
+// an aligned block of tiles and takes the carry from the block before by
+// look-back.
 #include <algorithm>
 
 #include "common.cuh"
