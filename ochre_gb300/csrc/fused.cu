@@ -27,8 +27,8 @@
 //   D. the raster's output offsets are resolved by decoupled look-back (the
 //      predecessors published their counts while this raster ran C), and
 //      the staged alpha, the tile positions and the spans are written out.
-// Any limit exceeded (commands, lines, grid size, tiles, increment slots,
-// crossings, a cell outside the grid) raises the fallback flag: the host then
+// Any limit exceeded (commands, lines, grid size, tiles, crossings, a cell
+// outside the grid) raises the fallback flag: the host then
 // runs the general chain for the whole batch.  Every wait is bounded.
 #include <algorithm>
 

@@ -12,9 +12,11 @@
 //   2. polyline sizes per command (path-space flatten counts), scan, emit;
 //   3. units: one per stroked contour, one per copied command; compaction;
 //   4. output sizes per unit (the offset sides counted join by join, one
-//      thread per unit), scan in place, emit; fill offsets of the output.
-// A contour is walked by one thread (its joins depend on the previous
-// distinct point).  Contours start at a Move or after a Close; `closed` is
+//      warp per unit), scan in place, emit; fill offsets of the output.
+// A side's join at step i needs only the side's point before it (point i - 1)
+// and the normal of the nearest earlier step that emitted a join, so a warp
+// computes 32 joins at a time and carries one normal between rounds.
+// Contours start at a Move or after a Close; `closed` is
 // set by a Close ending the contour or by any earlier Close of the path
 // (the reference never resets it, path.rs:218-256).
 #include "common.cuh"
