@@ -8,7 +8,9 @@
 // quantisation, rasterizer.rs:232-239), 1 inside spans, 0 elsewhere.
 //
 // Backward, with the discrete structure (line counts, visited cells, tiles)
-// held fixed and recomputed by re-running the forward chain:
+// held fixed: the one the last render_coverage of the same batch left in the
+// context while nothing has rewritten it since, else recomputed by running
+// the forward chain again:
 //   dL/dS   = dL/dc * sign(S) * [|S| < 1] at boundary-tile pixels, else 0;
 //   an increment (cell x, y; area a, height h) adds a to S(x, y) and h to
 //   S(x', y) for every x' > x, so dL/da = dL/dS(x, y) and dL/dh = the suffix
