@@ -285,6 +285,12 @@ int ochre_gpu_rasterize_noalloc(const ochre_batch *in, ochre_output_buffers *out
  *   "chain_tiles_per_warp"   tiles per warp in the chain's coverage kernel: 4 | 8 | 16
  *   "chain_coverage_form"    coverage kernel form: 0 by tile-row count (default), 1 one warp
  *                            per block of tiles with a look-back carry, 2 one warp per tile row
+ *   "sort_digit_bits"        radix digit width of the chain's sort: 8 (default) | 11
+ *   "chain_long_cells"       lines of more estimated cells than this are walked by the
+ *                            refilling long-line walkers beside the per-line kernels:
+ *                            0 (none) | 16 .. 65535 (default 192)
+ *   "chain_walk_refill"      idle lanes a long-line warp waits for before it refills: 1 .. 32
+ *                            (default 8)
  * Results do not depend on them (beyond the 1 LSB alpha bound). */
 int ochre_gpu_set_tunable(ochre_gpu_ctx *ctx, const char *name, int value);
 int ochre_gpu_get_tunable(const ochre_gpu_ctx *ctx, const char *name, int *value);

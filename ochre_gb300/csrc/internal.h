@@ -257,7 +257,7 @@ struct ochre_gpu_ctx {
     int tune_chain_tiles_per_warp = 8;
     int tune_chain_coverage_form = 0;   // 0: by row count, 1: block form, 2: row form
     int tune_sort_digit_bits = 8;       // radix sort digit width: 8 or 11
-    int tune_chain_long_cells = 64;     // lines of more (estimated) cells go to the long-line walkers; 0: none
+    int tune_chain_long_cells = 192;    // lines of more (estimated) cells go to the long-line walkers; 0: none
     int tune_chain_walk_refill = 8;     // idle lanes of a long-line warp that trigger a refill (1..32)
 
     // Host-batch entry: a large point array is copied on copy_stream while

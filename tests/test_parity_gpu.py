@@ -436,7 +436,7 @@ def test_stored_increments_above_2_30(gpu_ctx_chain):
     compare(first, exp, 1)
 
 
-@pytest.mark.parametrize("long_cells,refill", [(0, 8), (16, 1), (16, 8), (16, 32), (64, 8)])
+@pytest.mark.parametrize("long_cells,refill", [(0, 8), (16, 1), (16, 8), (16, 32), (64, 8), (192, 8)])
 def test_long_line_walkers_match_oracle(gpu_ctx_chain, long_cells, refill):
     # Lines of more than long_cells cells are walked by the persistent
     # refilling walkers beside the one-thread-per-line kernels (0: none are);
