@@ -82,6 +82,70 @@ def test_known_answer_half_pixel_edge():
     assert np.array_equal(a, np.tile([255, 255, 128, 0, 0, 0, 0, 0], (8, 1)))
 
 
+@pytest.mark.parametrize("verb,ctrl,n_curve", [
+    # Quadratic (path.rs:49-58): |last - 2c + p| = |(0, -200)| = 200, so
+    # dt = sqrt(4 * 0.1 / 200) = 0.04472; 22 steps reach 0.9839 and the 23rd
+    # is clamped to 1: 23 lines.
+    ("quad", [50, 100, 100, 0], 23),
+    # Cubic (path.rs:59-74): a = -last + 3 c1 - 3 c2 + p = (-200, 0),
+    # b = 3 (last - 2 c1 + c2) = (300, -300), conc = max(|b|, |a + b|)
+    # = max(424.26, 316.23); dt = sqrt(sqrt(8) * 0.1 / 424.26) = 0.02582;
+    # 38 steps reach 0.9812 and the 39th is clamped to 1: 39 lines.
+    ("cubic", [0, 100, 100, 100, 100, 0], 39),
+])
+def test_known_answer_flatten_counts(verb, ctrl, n_curve):
+    # Move (0, 0), the curve to (100, 0), Close: the curve's lines plus the
+    # closing line (100, 0) -> (0, 0) that finish adds (rasterizer.rs:181-183),
+    # each line starting where the previous one ended.
+    from ochre_gb300.batch import CLOSE, CUBIC, MOVE, QUADRATIC, BatchBuilder
+    v = {"quad": QUADRATIC, "cubic": CUBIC}[verb]
+    b = BatchBuilder().fill([MOVE, v, CLOSE], [0, 0] + ctrl, raw=True).build()
+    r = oracle.run(b, capture_lines=True)
+    L = r["lines"][int(r["raster_line_off"][0]):int(r["raster_line_off"][1])]
+    assert len(L) == n_curve + 1
+    assert np.array_equal(L[1:, :2], L[:-1, 2:])
+    assert L[0, :2].tolist() == [0, 0] and L[n_curve - 1, 2:].tolist() == [100, 0]
+    assert L[n_curve].tolist() == [100, 0, 0, 0]
+
+
+def test_known_answer_sloped_triangle():
+    # Triangle (0.5, 0.5) -> (2.5, 2.5) -> (0.5, 2.5): the region
+    # 0.5 <= x <= y <= 2.5.  Per pixel (x, y) the covered area is
+    # (0,0) 1/8, (0,1) 1/2, (0,2) 1/4, (1,1) 1/2, (1,2) 1/2, (2,2) 1/8, else 0;
+    # every term of the reference's sums is a multiple of 1/8, so the f32
+    # coverage is exact and alpha = (area * 256) as u8 (rasterizer.rs:232-239).
+    # The diagonal passes through pixel corners, where the walk steps x first
+    # and adds zero-length increments (rasterizer.rs:108-116).
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    b = BatchBuilder().fill([MOVE, LINE, LINE, CLOSE], [0.5, 0.5, 2.5, 2.5, 0.5, 2.5], raw=True).build()
+    r = oracle.run(b)
+    expect = np.zeros((8, 8), np.uint8)
+    for (x, y), a in {(0, 0): 32, (0, 1): 128, (0, 2): 64, (1, 1): 128, (1, 2): 128, (2, 2): 32}.items():
+        expect[y, x] = a
+    assert r["tile_xy"].tolist() == [[0, 0]]
+    assert np.array_equal(r["tile_alpha"][0].reshape(8, 8), expect)
+    assert len(r["span_w"]) == 0
+
+
+def test_known_answer_negative_coordinates():
+    # Square x, y in [-12, -4]: cells and tiles use floor and div_euclid
+    # (rasterizer.rs:66-68, 123-131), so pixel -12 is column 4 of tile -2
+    # (x -16..-9) and pixel -5 column 3 of tile -1 (x -8..-1).  Four tiles in
+    # (tile_y, tile_x) order, each a filled 4 x 4 quadrant; adjacent tiles on
+    # a row leave no gap, so no span.
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    b = BatchBuilder().fill([MOVE, LINE, LINE, LINE, CLOSE], [-12, -12, -4, -12, -4, -4, -12, -4], raw=True).build()
+    r = oracle.run(b)
+    assert r["tile_xy"].tolist() == [[-16, -16], [-8, -16], [-16, -8], [-8, -8]]
+    quads = [(slice(4, 8), slice(4, 8)), (slice(4, 8), slice(0, 4)), (slice(0, 4), slice(4, 8)),
+             (slice(0, 4), slice(0, 4))]
+    for t, (rows, cols) in enumerate(quads):
+        expect = np.zeros((8, 8), np.uint8)
+        expect[rows, cols] = 255
+        assert np.array_equal(r["tile_alpha"][t].reshape(8, 8), expect), t
+    assert len(r["span_w"]) == 0
+
+
 @pytest.mark.parametrize("gen,kw", [
     (W.readme_path, {}),
     (W.cubic_boxes, dict(n_paths=2)),
