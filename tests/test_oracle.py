@@ -108,6 +108,31 @@ def test_known_answer_flatten_counts(verb, ctrl, n_curve):
     assert L[n_curve].tolist() == [100, 0, 0, 0]
 
 
+def test_known_answer_close_and_move_semantics():
+    # Close is a no-op (rasterizer.rs:154): a Line after it starts at the
+    # last point, so Move (0,0), Line (8,0), Line (8,8), Close, Line (0,8)
+    # outlines the whole tile, and finish closes (0,8) -> (0,0); the edges on
+    # x = 8 and y = 8 walk cells of the next tiles (floor(8) = 8), which get
+    # coverage 0 (the right edge's area cancels the carry).  A Move
+    # closes the contour before it when last != first (rasterizer.rs:62-64):
+    # the second raster's Move (16,0) adds (8,8) -> (0,0) first, and its own
+    # contour (16,0) -> (24,0) -> (24,8) is closed by finish.
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    bb = BatchBuilder()
+    bb.begin_raster()
+    bb.fill([MOVE, LINE, LINE, CLOSE, LINE], [0, 0, 8, 0, 8, 8, 0, 8], raw=True)
+    bb.begin_raster()
+    bb.fill([MOVE, LINE, LINE, MOVE, LINE, LINE], [0, 0, 8, 0, 8, 8, 16, 0, 24, 0, 24, 8], raw=True)
+    r = oracle.run(bb.build(), capture_lines=True)
+    lines = [r["lines"][int(r["raster_line_off"][i]):int(r["raster_line_off"][i + 1])].tolist() for i in range(2)]
+    assert lines[0] == [[0, 0, 8, 0], [8, 0, 8, 8], [8, 8, 0, 8], [0, 8, 0, 0]]
+    assert lines[1] == [[0, 0, 8, 0], [8, 0, 8, 8], [8, 8, 0, 0],
+                        [16, 0, 24, 0], [24, 0, 24, 8], [24, 8, 16, 0]]
+    xy, alpha, _, sw, _ = _raster(r, 0)
+    assert xy.tolist() == [[0, 0], [8, 0], [0, 8], [8, 8]] and len(sw) == 0
+    assert (alpha[0] == 255).all() and not alpha[1:].any()
+
+
 def test_known_answer_sloped_triangle():
     # Triangle (0.5, 0.5) -> (2.5, 2.5) -> (0.5, 2.5): the region
     # 0.5 <= x <= y <= 2.5.  Per pixel (x, y) the covered area is
