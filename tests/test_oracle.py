@@ -133,6 +133,33 @@ def test_known_answer_close_and_move_semantics():
     assert (alpha[0] == 255).all() and not alpha[1:].any()
 
 
+def test_known_answer_union_of_fills():
+    # Several fills on one rasterizer add into one accumulation
+    # (rasterizer.rs:161-165).  Raster 0: the square x 0..2.5, y 0..8 twice
+    # in the same direction: coverage 2 in columns 0-1 and 2 * 0.5 = 1 in
+    # column 2, alpha min(|S| * 256, 255) = 255 for all three (the cast
+    # saturates).  Raster 1: the same square and its reverse: S = 0
+    # everywhere, the tiles are still emitted (their cells had increments)
+    # with alpha 0.
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    fwd = [0, 0, 2.5, 0, 2.5, 8, 0, 8]
+    rev = [0, 0, 0, 8, 2.5, 8, 2.5, 0]
+    verbs = [MOVE, LINE, LINE, LINE, CLOSE]
+    bb = BatchBuilder()
+    bb.begin_raster()
+    bb.fill(verbs, fwd, raw=True)
+    bb.fill(verbs, fwd, raw=True)
+    bb.begin_raster()
+    bb.fill(verbs, fwd, raw=True)
+    bb.fill(verbs, rev, raw=True)
+    r = oracle.run(bb.build())
+    xy0, a0, _, _, _ = _raster(r, 0)
+    xy1, a1, _, _, _ = _raster(r, 1)
+    assert xy0.tolist() == [[0, 0], [0, 8]] == xy1.tolist()
+    assert np.array_equal(a0[0].reshape(8, 8), np.tile([255, 255, 255, 0, 0, 0, 0, 0], (8, 1)))
+    assert not a0[1].any() and not a1.any()
+
+
 def test_known_answer_sloped_triangle():
     # Triangle (0.5, 0.5) -> (2.5, 2.5) -> (0.5, 2.5): the region
     # 0.5 <= x <= y <= 2.5.  Per pixel (x, y) the covered area is
