@@ -19,6 +19,23 @@ def test_builder_and_validate():
     assert b.input_bytes() == 5 + 4 * len(b.pts) + 24 * 3
 
 
+def test_compulsory_bytes_of_the_glyph_run():
+    """The roofline numerator of the headline: 1 B per verb, 8 B per point
+    (Move and Line one point, a quadratic two), 24 B per transform in; 68 B
+    per tile (64 alpha + two i16) and 6 B per span out.  The tile and span
+    counts are the oracle's for this workload."""
+    import bench
+    b = W.glyph_run()
+    counts = np.bincount(b.verbs, minlength=6)
+    points = counts[B.MOVE] + counts[B.LINE] + 2 * counts[B.QUADRATIC] + 3 * counts[B.CUBIC]
+    assert counts[B.CUBIC] == 0 and counts[B.CONIC] == 0
+    inp = b.n_cmds + 8 * int(points) + 24 * b.n_fills
+    assert inp == b.input_bytes() == 45_194_436
+    out = bench.output_bytes(2_116_864, 253_952, b.n_rasters)
+    assert out == 68 * 2_116_864 + 6 * 253_952
+    assert inp + out == 190_664_900
+
+
 def test_validate_rejects_bad_input():
     b = W.readme_path()
     bad = B.Batch(b.verbs.copy(), b.pts[:-1].copy(), b.fill_cmd_off, b.fill_xf, None, None, 1)
