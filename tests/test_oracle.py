@@ -289,13 +289,14 @@ def test_stroke_rasters_match_python_restatement():
         assert [(int(a), int(c), int(w), int(t)) for (a, c), w, t in zip(sxy.tolist(), sw, st)] == spans, name
 
 
-@pytest.mark.parametrize("seed,stroke_share", [(11, 0.0), (12, 0.0), (13, 0.5)])
-def test_fuzz_oracle_matches_python_restatement(seed, stroke_share):
+@pytest.mark.parametrize("seed,stroke_share,big_share",
+                         [(11, 0.0, 0.1), (12, 0.0, 0.1), (13, 0.5, 0.1), (14, 0.0, 0.3), (15, 1.0, 0.15)])
+def test_fuzz_oracle_matches_python_restatement(seed, stroke_share, big_share):
     """Random command sequences (every verb, any order, degenerate curves,
-    repeated points, shears, raw commands): both CPU restatements agree bit
-    for bit, alpha included."""
+    repeated points, shears, raw commands, strokes, rasters eight times
+    larger): both CPU restatements agree bit for bit, alpha included."""
     from fuzz_cases import fuzz_batch
-    b = fuzz_batch(90, seed=seed, stroke_share=stroke_share)
+    b = fuzz_batch(90, seed=seed, stroke_share=stroke_share, big_share=big_share)
     r = oracle.run(b)
     for i in range(b.n_rasters):
         tiles, spans, ninc = oracle_py.rasterize(oracle_py.commands_of_batch(b, i))
