@@ -160,6 +160,35 @@ def test_known_answer_union_of_fills():
     assert not a0[1].any() and not a1.any()
 
 
+@pytest.mark.parametrize("hole", [True, False])
+def test_known_answer_nonzero_winding(hole):
+    # Square x, y in [0, 64] with a second contour x, y in [16, 48] in the
+    # same fill, reversed (a hole) or in the same direction (an overlap).
+    # Tile rows 3-5 (y 24..47) hold only vertical edges: cells x = 0, 16, 48
+    # and 64 put tiles at tile x 0, 2, 6 and 8.  Crossings of each tile-row
+    # boundary add -1 at an up edge and +1 at a down edge, so the winding
+    # after tile 0 is -1 (span over tile 1), after tile 2 is 0 for the hole
+    # (no span over tiles 3-5) or -2 for the overlap (a 24-px span), after
+    # tile 6 is -1 (span over tile 7) (rasterizer.rs:252-265).  Coverage:
+    # tile 0 is 1, tile 2 is 0 (hole) or 2 (overlap, saturating to 255),
+    # tile 6 is 1, tile 8 is 0.
+    from ochre_gb300.batch import CLOSE, LINE, MOVE, BatchBuilder
+    outer = [0, 0, 64, 0, 64, 64, 0, 64]
+    inner = [16, 16, 16, 48, 48, 48, 48, 16] if hole else [16, 16, 48, 16, 48, 48, 16, 48]
+    verbs = [MOVE, LINE, LINE, LINE, CLOSE] * 2
+    r = oracle.run(BatchBuilder().fill(verbs, outer + inner, raw=True).build())
+    xy, alpha, sxy, sw, st = _raster(r, 0)
+    for ty in (3, 4, 5):
+        rows = [i for i, (x, y) in enumerate(xy.tolist()) if y == 8 * ty]
+        assert [xy[i][0] for i in rows] == [0, 16, 48, 64], ty
+        full = [255, 0, 255, 0] if hole else [255, 255, 255, 0]
+        for i, a in zip(rows, full):
+            assert (alpha[i] == a).all(), (ty, int(xy[i][0]))
+        spans = [(int(x), int(w), int(t)) for (x, y), w, t in zip(sxy.tolist(), sw, st) if y == 8 * ty]
+        expect = [(8, 8, rows[0]), (56, 8, rows[2])] if hole else [(8, 8, rows[0]), (24, 24, rows[1]), (56, 8, rows[2])]
+        assert spans == expect, ty
+
+
 def test_known_answer_sloped_triangle():
     # Triangle (0.5, 0.5) -> (2.5, 2.5) -> (0.5, 2.5): the region
     # 0.5 <= x <= y <= 2.5.  Per pixel (x, y) the covered area is
